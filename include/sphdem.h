@@ -1,0 +1,237 @@
+/*
+ * sphdem.h -- C ABI of the GB300-native SPH-DEM per-step particle hot path.
+ *
+ * One handle = one simulation (or one ensemble of independent simulations)
+ * resident in the HBM of one GPU.  Every entry point returns an int status
+ * (SPHDEM_OK == 0); no C++ exception crosses this boundary.  Text for the last
+ * failure is available from sphdem_last_error().
+ *
+ * The functions replace the following interfaces of the reference
+ * (martinjrobins/SPH-DEM, paths relative to the project root):
+ *   - CdataLL constructor + reset()          dataLL.cpp:8-40, 140-236
+ *   - CsphIncompress::start/middle/end       sphIncompress.cpp:3-38, 40-165, 167-251
+ *   - the run loop and its hook sequence     run.cpp:102-119
+ *   - the per-particle neighbour lists       dataLL.cpp:1026-1075 (calcNeighbours)
+ *                                            dataLL.cpp:1104-1192 (calcNeighboursCoupling)
+ *   - the bucket index maps                  dataLL.h:303-311 (getCellI, dem_getCellI)
+ *   - the particle container (host AoS)      particle.h:62-316 (Cparticle), here SoA
+ *
+ * Threading contract: one handle per host thread.  All work of a handle is
+ * ordered on that handle's private CUDA stream; calls returning data to the
+ * host synchronise that stream.
+ */
+#ifndef SPHDEM_H
+#define SPHDEM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SPHDEM_OK                 0
+#define SPHDEM_ERR_INVALID        1   /* bad argument or configuration            */
+#define SPHDEM_ERR_CUDA           2   /* a CUDA runtime call failed               */
+#define SPHDEM_ERR_CAPACITY       3   /* a fixed capacity (cells, pairs) exceeded  */
+#define SPHDEM_ERR_OUT_OF_RANGE   4   /* a particle left the binning domain        */
+#define SPHDEM_ERR_NOT_FINITE     5   /* NaN/Inf found in a state field            */
+#define SPHDEM_ERR_UNSUPPORTED    6   /* option not built for this configuration   */
+#define SPHDEM_ERR_TIMEOUT        7   /* a bounded device wait gave up             */
+
+/* ---- particle types: values of iamTypes, particle.h:17 ------------------ */
+#define SPHDEM_SPH            0
+#define SPHDEM_SPH_BOUNDARY   1
+#define SPHDEM_IMMOVABLE      2
+#define SPHDEM_BOUNDARY       3
+#define SPHDEM_GHOST          4
+#define SPHDEM_DEM           11
+#define SPHDEM_DEM_BOUNDARY  12
+#define SPHDEM_IMMERSED_DEM  13
+
+/* ---- viscosity models (customConstants.h #defines; sph.h:579-666) ------ */
+#define SPHDEM_VISC_NONE        0
+#define SPHDEM_VISC_ARTIFICIAL  1   /* VISC_ARTIFICIAL, sph.h:633-646      */
+#define SPHDEM_VISC_MONAGHAN    2   /* VISC_MONAGHAN,   sph.h:606-630      */
+#define SPHDEM_VISC_MORRIS      3   /* VISC_MORRIS,     sph.h:585-597      */
+
+/* ---- feature flags (compile-time #defines of a case's customConstants.h) */
+#define SPHDEM_F_CONST_H          (1u << 0)  /* CONST_H: h never updated        */
+#define SPHDEM_F_NO_ANTICLUMPING  (1u << 1)  /* NO_ANTICLUMPING                 */
+#define SPHDEM_F_VAR_H_CORRECTION (1u << 2)  /* VAR_H_CORRECTION (Omega terms)  */
+#define SPHDEM_F_LIQ_DEM          (1u << 3)  /* LIQ_DEM: DEM + coupling         */
+#define SPHDEM_F_FIXED_DT         (1u << 4)  /* dt == maxdt every step          */
+#define SPHDEM_F_DEM_ONLY_CONTACT (1u << 5)  /* reserved                        */
+
+/* ---- precision of the pair kernels ------------------------------------- */
+#define SPHDEM_PREC_FP64   0   /* everything in FP64                                  */
+#define SPHDEM_PREC_MIXED  1   /* FP32 pair math on FP64-cell-origin + FP32 offsets,
+                                  Kahan-compensated FP32 sums, FP64 integration       */
+
+/* A planar wall acting on DEM particles only: the device built-in form of a
+ * case hook such as sediment3D/customSim.cpp:67-81 (addCustomBoundaries).
+ * overlap = radius - dot(r - point, normal); force along +normal when > 0. */
+typedef struct SphDemWall {
+    double point[3];
+    double normal[3];   /* unit, pointing into the domain */
+} SphDemWall;
+
+#define SPHDEM_MAX_WALLS 6
+
+/* All case constants the reference takes from customConstants.h /
+ * demConstants.h at compile time, passed at run time instead. */
+typedef struct SphDemConfig {
+    int32_t  ndim;                 /* NDIM: 2 or 3                                */
+    int32_t  visc_model;           /* SPHDEM_VISC_*                               */
+    uint32_t flags;                /* SPHDEM_F_*                                  */
+    int32_t  precision;            /* SPHDEM_PREC_*                               */
+    int32_t  periodic[3];          /* PERIODIC[]                                  */
+    int32_t  n_walls;              /* number of DEM walls used                    */
+    double   pi;                   /* PI of the case (reference cases: 3.14159265)*/
+    double   rmin[3], rmax[3];     /* RMIN[], RMAX[]: periodic extents            */
+    double   domain_min[3];        /* globals.procDomain lower corner             */
+    double   domain_max[3];        /* globals.procDomain upper corner             */
+    double   hfac, psep, h;        /* HFAC, PSEP, H                               */
+    double   dens, refd;           /* DENS, REFD                                  */
+    double   gamma, prb, spsound;  /* GAMMA, PRB, SPSOUND                         */
+    double   viscosity;            /* VISCOSITY (kinematic)                       */
+    double   alpha_artificial;     /* ALPHA_ARTIFICIAL                            */
+    double   bfac;                 /* BFAC (repulsive boundary)                   */
+    double   maxdt;                /* globals.maxdt (== dt with SPHDEM_F_FIXED_DT) */
+    double   damptime;             /* DAMPTIME                                    */
+    double   dem_radius;           /* DEM_RADIUS (per-particle radius overrides)   */
+    double   dem_dens;             /* DEM_DENS                                    */
+    double   dem_k, dem_gamma;     /* DEM_K, DEM_GAMMA (LINEAR contact)            */
+    double   dem_search_radius;    /* DEM_SEARCH_RADIUS                           */
+    double   dem_vol;              /* DEM_VOL                                     */
+    double   coupling_radius;      /* LIQ_DEM_COUPLING_RADIUS                     */
+    double   dem_timestep;         /* DEM_TIMESTEP (demConstants.h:159)            */
+    double   liq_dem_timestep;     /* LIQ_DEM_TIMESTEP (demConstants.h:172)        */
+    double   time_drop_particle;   /* TIME_DROP_PARTICLE                          */
+    double   freeze_dem_until;     /* built-in hook: DEM frozen while time <= this */
+    double   gravity_sph[3];       /* built-in beforeMiddle hook, type sph only    */
+    double   gravity_dem[3];       /* built-in beforeEnd hook, type dem only       */
+    SphDemWall walls[SPHDEM_MAX_WALLS];
+} SphDemConfig;
+
+/* Host-side particle arrays (structure of arrays).  Vector fields hold three
+ * doubles per particle whatever ndim is (z unused in 2D).  Any pointer may be
+ * NULL: that field is then not read (set) or not written (get).  Particles are
+ * always presented in tag order (the order they were given to sphdem_create),
+ * never in the device's cell-sorted order. */
+typedef struct SphDemParticles {
+    int64_t  n;
+    int32_t *iam;          /* iamTypes                                           */
+    int32_t *tag;
+    uint8_t *concave;      /* boundary particle: concave corner flag              */
+    double  *r, *v, *vhat; /* [3n]                                                */
+    double  *mass, *dens, *h;
+    double  *radius;       /* DEM radius; 0 or NULL -> cfg.dem_radius            */
+    double  *norm1, *norm2, *norm3;  /* [3n] boundary normals                   */
+    /* outputs (get only) */
+    double  *f, *fp, *fv, *fb;       /* [3n]                                     */
+    double  *dddt, *press, *pdr2;
+    double  *porosity, *dporositydt, *shep_sum, *omega;
+    double  *fdrag, *fvel, *grad_porosity;  /* [3n]                              */
+    double  *v0, *vhat0;             /* [3n] start-of-step velocities            */
+} SphDemParticles;
+
+/* Field-mask bits for get/set. */
+#define SPHDEM_FIELD_R        (1u << 0)
+#define SPHDEM_FIELD_V        (1u << 1)
+#define SPHDEM_FIELD_VHAT     (1u << 2)
+#define SPHDEM_FIELD_MASS     (1u << 3)
+#define SPHDEM_FIELD_DENS     (1u << 4)
+#define SPHDEM_FIELD_H        (1u << 5)
+#define SPHDEM_FIELD_F        (1u << 6)   /* f, fp, fv, fb */
+#define SPHDEM_FIELD_DDDT     (1u << 7)
+#define SPHDEM_FIELD_PRESS    (1u << 8)   /* press, pdr2 */
+#define SPHDEM_FIELD_COUPLING (1u << 9)   /* porosity, dporositydt, shep_sum, fdrag, fvel, grad_porosity */
+#define SPHDEM_FIELD_OMEGA    (1u << 10)
+#define SPHDEM_FIELD_V0       (1u << 11)  /* v0, vhat0 */
+#define SPHDEM_FIELD_IAM      (1u << 12)
+#define SPHDEM_FIELD_ALL      0xffffffffu
+
+/* Step globals: the CglobalVars members of the hot path, globalVars.h:196-220. */
+typedef struct SphDemGlobals {
+    double  time, dt, new_dt, maxdt, dem_dt;
+    int64_t sph_step;
+    int64_t n_deleted;       /* particles removed for leaving the domain (dataLL.cpp:381-386) */
+} SphDemGlobals;
+
+/* Phases and built-in hook points, in the order run.cpp:112-118 calls them. */
+#define SPHDEM_HOOK_BEFORE_START   0
+#define SPHDEM_PHASE_START         1
+#define SPHDEM_HOOK_BEFORE_MIDDLE  2
+#define SPHDEM_PHASE_MIDDLE        3
+#define SPHDEM_HOOK_BEFORE_END     4
+#define SPHDEM_PHASE_END           5
+#define SPHDEM_HOOK_AFTER_END      6
+
+/* Pair lists exported for parity checks. */
+#define SPHDEM_PAIRS_SPH        0  /* calcNeighbours for non-DEM particles       */
+#define SPHDEM_PAIRS_DEM        1  /* calcNeighbours for DEM particles           */
+#define SPHDEM_PAIRS_COUPLE_SD  2  /* calcNeighboursCoupling, SPH -> DEM, r < Rc   */
+#define SPHDEM_PAIRS_COUPLE_DS  3  /* calcNeighboursCoupling, DEM -> SPH          */
+
+typedef struct sphdem_ctx *sphdem_handle;
+
+/* Create a simulation from host particles.  Replaces `new CdataLL(ps,globals,
+ * true)` (run.cpp:80, dataLL.cpp:8-40): copies the particles to HBM, sizes the
+ * bucket grids and performs the first rebuild.  `capacity` is the maximum
+ * particle count the handle will ever hold (>= init->n). */
+int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init,
+                  int64_t capacity, sphdem_handle *out);
+int sphdem_destroy(sphdem_handle h);
+
+/* Run one phase or built-in hook point (SPHDEM_PHASE_* / SPHDEM_HOOK_*).
+ * PHASE_START/MIDDLE/END replace CsphIncompress::start/middle/end
+ * (sphIncompress.cpp:3-251); the HOOK_* points apply the built-in hooks of the
+ * configuration (gravity, DEM walls, DEM freeze) that a case's customSim
+ * would apply at that point.  A host-side hook instead uses get/set_fields. */
+int sphdem_phase(sphdem_handle h, int phase);
+
+/* nsteps full steps: sph_step++, then the seven phases/hooks in run.cpp order.
+ * Consecutive calls replay one captured CUDA graph of a step. */
+int sphdem_step(sphdem_handle h, int nsteps);
+
+int sphdem_get_fields(sphdem_handle h, uint32_t mask, SphDemParticles *out);
+int sphdem_set_fields(sphdem_handle h, uint32_t mask, const SphDemParticles *in);
+int sphdem_get_globals(sphdem_handle h, SphDemGlobals *out);
+int sphdem_set_globals(sphdem_handle h, const SphDemGlobals *in);
+
+/* Rebuild the bucket lists at the current positions (CdataLL::reset,
+ * dataLL.cpp:140-236): periodic wrap, out-of-domain deletion, h_max tracking,
+ * bin, sort by cell, permute. */
+int sphdem_rebuild(sphdem_handle h);
+
+/* Export one neighbour relation as CSR over tag order.  `offsets` has n+1
+ * entries, `idx` holds neighbour tags' positions (tag order index).  Pass
+ * idx == NULL to query the pair count in *n_pairs. */
+int sphdem_pairs(sphdem_handle h, int kind, int64_t *offsets, int32_t *idx,
+                 int64_t idx_capacity, int64_t *n_pairs);
+
+/* Bucket index of every particle (tag order) in the reference's own maps:
+ * getCellI (dataLL.h:303-305) for non-DEM, dem_getCellI (dataLL.h:308-311)
+ * for DEM, as int32 triples (unused z = 0). */
+int sphdem_cell_ids(sphdem_handle h, int32_t *cell_xyz);
+
+/* Per-kernel device time accumulated with CUDA events since the last reset
+ * (names separated by '\n' in `names`, times in ms, launch counts). */
+int sphdem_kernel_times(sphdem_handle h, char *names, size_t names_len,
+                        double *ms, int64_t *launches, int max_kernels,
+                        int *n_kernels);
+int sphdem_kernel_times_reset(sphdem_handle h, int enable);
+
+/* Time `nsteps` full steps on the handle's stream with CUDA events. */
+int sphdem_time_steps(sphdem_handle h, int nsteps, double *ms);
+
+int sphdem_last_error(sphdem_handle h, char *buf, size_t len);
+const char *sphdem_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPHDEM_H */

@@ -1,0 +1,278 @@
+/*
+ * Driver for the reference's own hot path, compiled from the unmodified
+ * reference sources as a CPU checker (test infrastructure only).
+ *
+ * It stands in for the reference's `setup` + `run` executables without VTK:
+ * it reads a seeded initial state (SPDMST01, written by the case generators),
+ * builds CdataLL/CsphIncompress/CcustomSim exactly as run.cpp:80-83 does, runs
+ * the step loop of run.cpp:102-119 and writes every hot-path field, the
+ * neighbour relations and the bucket indices in tag order (SPDMOUT1).
+ *
+ * Usage: ref_driver <in.state> <out.bin> <nsteps> [timing-only(0|1)]
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <list>
+#include <sstream>
+#include <string>
+#include <sys/time.h>
+#include <vector>
+
+/* Internals of CdataLL (bucket maps, cells) are read for the dump only. */
+#define private public
+#include "customConstants.h"
+#include "sphIncompress.h"
+#include "customSim.h"
+#include "misc.h"
+#undef private
+
+/* misc.cpp refers to these two writers; the checker writes no VTK. */
+void Cio_data_vtk::writeAux(int, particleContainer &, vector<double>, const char *, CglobalVars *) {}
+void Cio_data_vtk::writeAuxNoData(int, particleContainer &, const char *, CglobalVars *) {}
+
+static void fail(const char *msg) {
+    fprintf(stderr, "ref_driver: %s\n", msg);
+    exit(2);
+}
+
+template <class T>
+static void rd(std::ifstream &in, T *p, size_t n) {
+    in.read(reinterpret_cast<char *>(p), sizeof(T) * n);
+    if (!in) fail("short read");
+}
+
+struct Field {
+    std::string name;
+    int ncomp;
+    std::vector<double> data;
+};
+
+static void put_name(FILE *f, const std::string &s) {
+    char buf[16];
+    memset(buf, 0, 16);
+    strncpy(buf, s.c_str(), 15);
+    fwrite(buf, 1, 16, f);
+}
+
+int main(int argc, char **argv) {
+    if (argc < 4) fail("usage: ref_driver in out nsteps [timing-only]");
+    const int nsteps = atoi(argv[3]);
+    const bool timing_only = argc > 4 && atoi(argv[4]) != 0;
+
+    std::ifstream in(argv[1], std::ios::binary);
+    if (!in) fail("cannot open input");
+    char magic[8];
+    rd(in, magic, 8);
+    if (memcmp(magic, "SPDMST01", 8) != 0) fail("bad magic");
+    long long n;
+    rd(in, &n, 1);
+    std::vector<int> iam(n), tag(n), concave(n);
+    std::vector<double> r(3 * n), v(3 * n), mass(n), dens(n), h(n), radius(n);
+    std::vector<double> n1(3 * n), n2(3 * n), n3(3 * n);
+    rd(in, iam.data(), n);
+    rd(in, tag.data(), n);
+    rd(in, concave.data(), n);
+    rd(in, r.data(), 3 * n);
+    rd(in, v.data(), 3 * n);
+    rd(in, mass.data(), n);
+    rd(in, dens.data(), n);
+    rd(in, h.data(), n);
+    rd(in, radius.data(), n);
+    rd(in, n1.data(), 3 * n);
+    rd(in, n2.data(), 3 * n);
+    rd(in, n3.data(), 3 * n);
+
+    vector<Cparticle> ps;
+    ps.reserve(std::max<long long>(MAX_NUM_PARTICLES_PER_CPU, n + 64));
+    for (long long i = 0; i < n; i++) {
+        Cparticle p;
+        p.iam = (enum iamTypes)iam[i];
+        p.tag = tag[i];
+        p.concave = concave[i] != 0;
+        for (int d = 0; d < NDIM; d++) {
+            p.r[d] = r[3 * i + d];
+            p.v[d] = v[3 * i + d];
+            p.norm1[d] = n1[3 * i + d];
+            p.norm2[d] = n2[3 * i + d];
+#ifdef _3D_
+            p.norm3[d] = n3[3 * i + d];
+#endif
+        }
+        p.vhat = p.v;
+        p.mass = mass[i];
+        p.dens = dens[i];
+        p.h = h[i];
+        ps.push_back(p);
+    }
+
+    CglobalVars g;
+    Nmisc::setupEntireDomain(g.procDomain, g.procNeighbrs);
+    g.maxdt = ORACLE_MAXDT;
+    g.dt = ORACLE_MAXDT;
+    /* The O(N^2) insertion sort of the initial traverse order
+     * (dataLL.cpp:887-904) only sets the visit order; skip it for big runs. */
+    CdataLL *data = new CdataLL(ps, g, n <= 20000);
+    CsphIncompress solver(data);
+    CcustomSim customSim(data, g.time);
+
+    int dt_changed = 0;
+    timeval t0, t1;
+    gettimeofday(&t0, NULL);
+    for (int k = 0; k < nsteps; k++) {
+        g.sphStep++;
+        customSim.beforeStart(g.time);
+        solver.start();
+        customSim.beforeMiddle(g.time);
+        solver.middle();
+        customSim.beforeEnd(g.time);
+        solver.end();
+        customSim.afterEnd(g.time);
+        if (g.dt != ORACLE_MAXDT) dt_changed++;
+    }
+    gettimeofday(&t1, NULL);
+    const double sec = (t1.tv_sec - t0.tv_sec) + 1e-6 * (t1.tv_usec - t0.tv_usec);
+    fprintf(stderr, "ref_driver: n=%zu steps=%d sec=%.6f particle_steps_per_s=%.6e dt_changed=%d\n",
+            ps.size(), nsteps, sec, ps.size() * (double)nsteps / (sec > 0 ? sec : 1e-30), dt_changed);
+    if (timing_only) return dt_changed ? 3 : 0;
+
+    /* tag -> position in ps (periodic exchange reorders ps) */
+    std::vector<long long> row_of_tag(n + 1, -1);
+    for (size_t i = 0; i < ps.size(); i++) {
+        if (ps[i].tag < 1 || ps[i].tag > n) fail("tag out of range");
+        row_of_tag[ps[i].tag] = i;
+    }
+    for (long long t = 1; t <= n; t++)
+        if (row_of_tag[t] < 0) fail("particle lost (deleted?)");
+
+    std::vector<Field> fields;
+    auto vec_field = [&](const char *name, vect Cparticle::*m) {
+        Field f{name, 3, std::vector<double>(3 * n, 0.0)};
+        for (long long t = 1; t <= n; t++) {
+            const Cparticle &p = ps[row_of_tag[t]];
+            for (int d = 0; d < NDIM; d++) f.data[3 * (t - 1) + d] = (p.*m)[d];
+        }
+        fields.push_back(f);
+    };
+    auto sca_field = [&](const char *name, double Cparticle::*m) {
+        Field f{name, 1, std::vector<double>(n, 0.0)};
+        for (long long t = 1; t <= n; t++) f.data[t - 1] = ps[row_of_tag[t]].*m;
+        fields.push_back(f);
+    };
+    vec_field("r", &Cparticle::r);
+    vec_field("v", &Cparticle::v);
+    vec_field("vhat", &Cparticle::vhat);
+    vec_field("v0", &Cparticle::v0);
+    vec_field("vhat0", &Cparticle::vhat0);
+    vec_field("f", &Cparticle::f);
+    vec_field("fp", &Cparticle::fp);
+    vec_field("fv", &Cparticle::fv);
+    vec_field("fb", &Cparticle::fb);
+    sca_field("dens", &Cparticle::dens);
+    sca_field("dddt", &Cparticle::dddt);
+    sca_field("h", &Cparticle::h);
+    sca_field("press", &Cparticle::press);
+    sca_field("pdr2", &Cparticle::pdr2);
+    sca_field("mass", &Cparticle::mass);
+#ifdef LIQ_DEM
+    sca_field("porosity", &Cparticle::porosity);
+    sca_field("dporositydt", &Cparticle::dporositydt);
+    vec_field("gradPorosity", &Cparticle::gradPorosity);
+    sca_field("shepSum", &Cparticle::shepSum);
+    vec_field("fdrag", &Cparticle::fdrag);
+    vec_field("fvel", &Cparticle::fvel);
+#endif
+#ifdef VAR_H_CORRECTION
+    sca_field("omega", &Cparticle::omega);
+#endif
+
+    /* neighbour relations at the final positions, after one more reset so
+     * that the ghost copies carry the smoothing lengths driftRest just
+     * updated -- exactly the lists the next traversal would build
+     * (dataLL.cpp:1026-1075, 1104-1192) */
+    data->reset();
+    struct Rel { std::string name; std::vector<std::vector<int> > rows; };
+    std::vector<Rel> rels;
+    Rel sphrel{"sph", std::vector<std::vector<int> >(n)};
+    Rel demrel{"dem", std::vector<std::vector<int> >(n)};
+    Rel sdrel{"couple_sd", std::vector<std::vector<int> >(n)};
+    Rel dsrel{"couple_ds", std::vector<std::vector<int> >(n)};
+    int duplicates = 0;
+    for (long long t = 1; t <= n; t++) {
+        Cparticle &p = ps[row_of_tag[t]];
+        std::vector<Cparticle *> nb;
+        data->calcNeighbours(nb, p);
+        std::vector<int> &row = (p.iam == dem) ? demrel.rows[t - 1] : sphrel.rows[t - 1];
+        for (size_t j = 0; j < nb.size(); j++) row.push_back(nb[j]->tag - 1);
+#ifdef LIQ_DEM
+        std::vector<Cparticle *> cn;
+        data->calcNeighboursCoupling(cn, p);
+        if (p.iam == dem) {
+            for (size_t j = 0; j < cn.size(); j++) dsrel.rows[t - 1].push_back(cn[j]->tag - 1);
+        } else if (p.iam == sph || p.iam == sphBoundary) {
+            for (size_t j = 0; j < cn.size(); j++)
+                if (len2(p.r - cn[j]->r) < pow(LIQ_DEM_COUPLING_RADIUS, 2))
+                    sdrel.rows[t - 1].push_back(cn[j]->tag - 1);
+        }
+#endif
+    }
+    rels.push_back(sphrel);
+    rels.push_back(demrel);
+#ifdef LIQ_DEM
+    rels.push_back(sdrel);
+    rels.push_back(dsrel);
+#endif
+    for (size_t k = 0; k < rels.size(); k++)
+        for (long long i = 0; i < n; i++) {
+            std::vector<int> &row = rels[k].rows[i];
+            std::sort(row.begin(), row.end());
+            size_t before = row.size();
+            row.erase(std::unique(row.begin(), row.end()), row.end());
+            duplicates += (int)(before - row.size());
+        }
+    if (duplicates) fprintf(stderr, "ref_driver: warning: %d duplicate neighbour entries (periodic images)\n", duplicates);
+
+    FILE *out = fopen(argv[2], "wb");
+    if (!out) fail("cannot open output");
+    fwrite("SPDMOUT1", 1, 8, out);
+    fwrite(&n, 8, 1, out);
+    long long nf = fields.size();
+    fwrite(&nf, 8, 1, out);
+    for (size_t k = 0; k < fields.size(); k++) {
+        put_name(out, fields[k].name);
+        long long nc = fields[k].ncomp;
+        fwrite(&nc, 8, 1, out);
+        fwrite(fields[k].data.data(), 8, fields[k].data.size(), out);
+    }
+    long long nk = rels.size();
+    fwrite(&nk, 8, 1, out);
+    for (size_t k = 0; k < rels.size(); k++) {
+        put_name(out, rels[k].name);
+        std::vector<long long> offs(n + 1, 0);
+        for (long long i = 0; i < n; i++) offs[i + 1] = offs[i] + rels[k].rows[i].size();
+        long long np = offs[n];
+        fwrite(&np, 8, 1, out);
+        fwrite(offs.data(), 8, n + 1, out);
+        for (long long i = 0; i < n; i++)
+            if (!rels[k].rows[i].empty()) fwrite(rels[k].rows[i].data(), 4, rels[k].rows[i].size(), out);
+    }
+    std::vector<int> cells(3 * n, 0);
+    for (long long t = 1; t <= n; t++) {
+        Cparticle &p = ps[row_of_tag[t]];
+        vectInt c;
+#ifdef LIQ_DEM
+        if (p.iam == dem) c = data->dem_getCellI(p.r); else
+#endif
+        c = data->getCellI(p.r);
+        for (int d = 0; d < NDIM; d++) cells[3 * (t - 1) + d] = c[d];
+    }
+    fwrite(cells.data(), 4, 3 * n, out);
+    double tt[2] = {g.time, g.dt};
+    fwrite(tt, 8, 2, out);
+    fclose(out);
+    return dt_changed ? 3 : 0;
+}

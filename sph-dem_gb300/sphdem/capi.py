@@ -1,0 +1,268 @@
+"""ctypes view of the C ABI in include/sphdem.h.
+
+`SphDemConfig` / `SphDemParticles` mirror the C structs member for member;
+`config_struct` fills one from a case configuration dictionary and
+`ParticleBuffers` owns numpy arrays behind a `SphDemParticles`.  `Library`
+loads ``libsphdem.so`` (the CUDA implementation) and raises on any non-zero
+status with the library's own error text.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "libsphdem.so")
+
+OK = 0
+ERR_NAMES = {1: "INVALID", 2: "CUDA", 3: "CAPACITY", 4: "OUT_OF_RANGE",
+             5: "NOT_FINITE", 6: "UNSUPPORTED", 7: "TIMEOUT"}
+
+HOOK_BEFORE_START, PHASE_START, HOOK_BEFORE_MIDDLE, PHASE_MIDDLE = 0, 1, 2, 3
+HOOK_BEFORE_END, PHASE_END, HOOK_AFTER_END = 4, 5, 6
+PAIRS_SPH, PAIRS_DEM, PAIRS_COUPLE_SD, PAIRS_COUPLE_DS = 0, 1, 2, 3
+PAIR_KIND_NAMES = {PAIRS_SPH: "sph", PAIRS_DEM: "dem",
+                   PAIRS_COUPLE_SD: "couple_sd", PAIRS_COUPLE_DS: "couple_ds"}
+
+FIELD_ALL = 0xFFFFFFFF
+FIELD_R, FIELD_V, FIELD_VHAT, FIELD_MASS = 1 << 0, 1 << 1, 1 << 2, 1 << 3
+FIELD_DENS, FIELD_H, FIELD_F, FIELD_DDDT = 1 << 4, 1 << 5, 1 << 6, 1 << 7
+FIELD_PRESS, FIELD_COUPLING, FIELD_OMEGA, FIELD_V0, FIELD_IAM = 1 << 8, 1 << 9, 1 << 10, 1 << 11, 1 << 12
+
+D3 = C.c_double * 3
+I3 = C.c_int32 * 3
+
+
+class SphDemWall(C.Structure):
+    _fields_ = [("point", D3), ("normal", D3)]
+
+
+class SphDemConfig(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int32), ("visc_model", C.c_int32), ("flags", C.c_uint32),
+        ("precision", C.c_int32), ("periodic", I3), ("n_walls", C.c_int32),
+        ("pi", C.c_double), ("rmin", D3), ("rmax", D3),
+        ("domain_min", D3), ("domain_max", D3),
+        ("hfac", C.c_double), ("psep", C.c_double), ("h", C.c_double),
+        ("dens", C.c_double), ("refd", C.c_double),
+        ("gamma", C.c_double), ("prb", C.c_double), ("spsound", C.c_double),
+        ("viscosity", C.c_double), ("alpha_artificial", C.c_double), ("bfac", C.c_double),
+        ("maxdt", C.c_double), ("damptime", C.c_double),
+        ("dem_radius", C.c_double), ("dem_dens", C.c_double),
+        ("dem_k", C.c_double), ("dem_gamma", C.c_double),
+        ("dem_search_radius", C.c_double), ("dem_vol", C.c_double),
+        ("coupling_radius", C.c_double), ("dem_timestep", C.c_double),
+        ("liq_dem_timestep", C.c_double), ("time_drop_particle", C.c_double),
+        ("freeze_dem_until", C.c_double),
+        ("gravity_sph", D3), ("gravity_dem", D3),
+        ("walls", SphDemWall * 6),
+    ]
+
+
+P_I32 = C.POINTER(C.c_int32)
+P_U8 = C.POINTER(C.c_uint8)
+P_F64 = C.POINTER(C.c_double)
+
+
+class SphDemParticles(C.Structure):
+    _fields_ = [
+        ("n", C.c_int64), ("iam", P_I32), ("tag", P_I32), ("concave", P_U8),
+        ("r", P_F64), ("v", P_F64), ("vhat", P_F64),
+        ("mass", P_F64), ("dens", P_F64), ("h", P_F64), ("radius", P_F64),
+        ("norm1", P_F64), ("norm2", P_F64), ("norm3", P_F64),
+        ("f", P_F64), ("fp", P_F64), ("fv", P_F64), ("fb", P_F64),
+        ("dddt", P_F64), ("press", P_F64), ("pdr2", P_F64),
+        ("porosity", P_F64), ("dporositydt", P_F64), ("shep_sum", P_F64), ("omega", P_F64),
+        ("fdrag", P_F64), ("fvel", P_F64), ("grad_porosity", P_F64),
+        ("v0", P_F64), ("vhat0", P_F64),
+    ]
+
+
+class SphDemGlobals(C.Structure):
+    _fields_ = [("time", C.c_double), ("dt", C.c_double), ("new_dt", C.c_double),
+                ("maxdt", C.c_double), ("dem_dt", C.c_double),
+                ("sph_step", C.c_int64), ("n_deleted", C.c_int64)]
+
+
+VEC_FIELDS = ("r", "v", "vhat", "norm1", "norm2", "norm3", "f", "fp", "fv", "fb",
+              "fdrag", "fvel", "grad_porosity", "v0", "vhat0")
+SCA_FIELDS = ("mass", "dens", "h", "radius", "dddt", "press", "pdr2", "porosity",
+              "dporositydt", "shep_sum", "omega")
+
+
+def config_struct(cfg: dict, precision: int | None = None) -> SphDemConfig:
+    s = SphDemConfig()
+    for name, ctype in SphDemConfig._fields_:
+        if name == "walls":
+            for i, w in enumerate(cfg.get("walls", [])[:6]):
+                s.walls[i].point = D3(*w["point"])
+                s.walls[i].normal = D3(*w["normal"])
+            continue
+        val = cfg[name]
+        if ctype in (D3, I3):
+            setattr(s, name, ctype(*val))
+        else:
+            setattr(s, name, val)
+    if precision is not None:
+        s.precision = precision
+    return s
+
+
+class ParticleBuffers:
+    """numpy storage behind a SphDemParticles (all fields allocated)."""
+
+    def __init__(self, n: int, init: dict | None = None):
+        self.n = n
+        self.arrays: dict[str, np.ndarray] = {
+            "iam": np.zeros(n, np.int32), "tag": np.arange(1, n + 1, dtype=np.int32),
+            "concave": np.ones(n, np.uint8),
+        }
+        for k in VEC_FIELDS:
+            self.arrays[k] = np.zeros((n, 3), np.float64)
+        for k in SCA_FIELDS:
+            self.arrays[k] = np.zeros(n, np.float64)
+        if init is not None:
+            for k, v in init.items():
+                if k in self.arrays:
+                    self.arrays[k][...] = v
+            if "vhat" not in init and "v" in init:
+                self.arrays["vhat"][...] = init["v"]
+        self.struct = SphDemParticles()
+        self.struct.n = n
+        for name, ctype in SphDemParticles._fields_:
+            if name == "n":
+                continue
+            a = self.arrays[name]
+            setattr(self.struct, name, a.ctypes.data_as(ctype))
+
+    def __getitem__(self, k):
+        return self.arrays[k]
+
+    def ref(self):
+        return C.byref(self.struct)
+
+
+class SphDemError(RuntimeError):
+    pass
+
+
+class Library:
+    """Thin loader of libsphdem.so with checked calls."""
+
+    def __init__(self, path: str | None = None):
+        path = path or LIB_PATH
+        if not os.path.exists(path):
+            raise SphDemError(f"CUDA library not built: {path} (run __graft_entry__.build())")
+        self.lib = C.CDLL(path)
+        L = self.lib
+        H = C.c_void_p
+        L.sphdem_create.argtypes = [C.POINTER(SphDemConfig), C.POINTER(SphDemParticles),
+                                    C.c_int64, C.POINTER(H)]
+        L.sphdem_destroy.argtypes = [H]
+        L.sphdem_phase.argtypes = [H, C.c_int]
+        L.sphdem_step.argtypes = [H, C.c_int]
+        L.sphdem_get_fields.argtypes = [H, C.c_uint32, C.POINTER(SphDemParticles)]
+        L.sphdem_set_fields.argtypes = [H, C.c_uint32, C.POINTER(SphDemParticles)]
+        L.sphdem_get_globals.argtypes = [H, C.POINTER(SphDemGlobals)]
+        L.sphdem_set_globals.argtypes = [H, C.POINTER(SphDemGlobals)]
+        L.sphdem_rebuild.argtypes = [H]
+        L.sphdem_pairs.argtypes = [H, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                   C.c_int64, C.POINTER(C.c_int64)]
+        L.sphdem_cell_ids.argtypes = [H, C.POINTER(C.c_int32)]
+        L.sphdem_kernel_times.argtypes = [H, C.c_char_p, C.c_size_t, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_int64), C.c_int, C.POINTER(C.c_int)]
+        L.sphdem_kernel_times_reset.argtypes = [H, C.c_int]
+        L.sphdem_time_steps.argtypes = [H, C.c_int, C.POINTER(C.c_double)]
+        L.sphdem_last_error.argtypes = [H, C.c_char_p, C.c_size_t]
+        L.sphdem_version.restype = C.c_char_p
+
+    def check(self, rc: int, h=None, what: str = ""):
+        if rc != OK:
+            buf = C.create_string_buffer(2048)
+            self.lib.sphdem_last_error(h, buf, 2048)
+            raise SphDemError(f"{what}: {ERR_NAMES.get(rc, rc)}: {buf.value.decode(errors='replace')}")
+
+
+class Simulation:
+    """One handle of the CUDA library, driven with numpy arrays."""
+
+    def __init__(self, lib: Library, cfg: dict, particles: dict, precision: int = 0,
+                 capacity: int | None = None):
+        self.L = lib
+        self.n = int(particles["iam"].shape[0])
+        self.cfg_struct = config_struct(cfg, precision)
+        init = ParticleBuffers(self.n, particles)
+        self.h = C.c_void_p()
+        rc = lib.lib.sphdem_create(C.byref(self.cfg_struct), init.ref(),
+                                   capacity or self.n, C.byref(self.h))
+        lib.check(rc, None, "sphdem_create")
+
+    def close(self):
+        if self.h:
+            self.L.lib.sphdem_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, n: int = 1):
+        self.L.check(self.L.lib.sphdem_step(self.h, n), self.h, "sphdem_step")
+
+    def phase(self, p: int):
+        self.L.check(self.L.lib.sphdem_phase(self.h, p), self.h, "sphdem_phase")
+
+    def rebuild(self):
+        self.L.check(self.L.lib.sphdem_rebuild(self.h), self.h, "sphdem_rebuild")
+
+    def get(self, mask: int = FIELD_ALL) -> ParticleBuffers:
+        out = ParticleBuffers(self.n)
+        self.L.check(self.L.lib.sphdem_get_fields(self.h, mask, out.ref()), self.h, "get_fields")
+        return out
+
+    def set(self, buf: ParticleBuffers, mask: int):
+        self.L.check(self.L.lib.sphdem_set_fields(self.h, mask, buf.ref()), self.h, "set_fields")
+
+    def globals(self) -> SphDemGlobals:
+        g = SphDemGlobals()
+        self.L.check(self.L.lib.sphdem_get_globals(self.h, C.byref(g)), self.h, "get_globals")
+        return g
+
+    def pairs(self, kind: int):
+        offs = np.zeros(self.n + 1, np.int64)
+        npairs = C.c_int64(0)
+        self.L.check(self.L.lib.sphdem_pairs(self.h, kind, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                                             None, 0, C.byref(npairs)), self.h, "pairs")
+        idx = np.zeros(max(1, npairs.value), np.int32)
+        self.L.check(self.L.lib.sphdem_pairs(self.h, kind, offs.ctypes.data_as(C.POINTER(C.c_int64)),
+                                             idx.ctypes.data_as(C.POINTER(C.c_int32)), idx.size,
+                                             C.byref(npairs)), self.h, "pairs")
+        return offs, idx[: npairs.value]
+
+    def cell_ids(self) -> np.ndarray:
+        cells = np.zeros((self.n, 3), np.int32)
+        self.L.check(self.L.lib.sphdem_cell_ids(self.h, cells.ctypes.data_as(C.POINTER(C.c_int32))),
+                     self.h, "cell_ids")
+        return cells
+
+    def time_steps(self, n: int) -> float:
+        ms = C.c_double(0)
+        self.L.check(self.L.lib.sphdem_time_steps(self.h, n, C.byref(ms)), self.h, "time_steps")
+        return ms.value
+
+    def kernel_times_reset(self, enable: bool = True):
+        self.L.check(self.L.lib.sphdem_kernel_times_reset(self.h, int(enable)), self.h, "kt_reset")
+
+    def kernel_times(self) -> dict:
+        names = C.create_string_buffer(16384)
+        ms = (C.c_double * 128)()
+        cnt = (C.c_int64 * 128)()
+        nk = C.c_int(0)
+        self.L.check(self.L.lib.sphdem_kernel_times(self.h, names, 16384, ms, cnt, 128, C.byref(nk)),
+                     self.h, "kernel_times")
+        keys = names.value.decode().split("\n")
+        return {keys[i]: (ms[i], cnt[i]) for i in range(nk.value)}

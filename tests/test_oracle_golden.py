@@ -1,0 +1,86 @@
+"""The CPU oracle port against golden outputs of the reference itself.
+
+tests/golden/*.npz were produced by tests/golden/make_golden.py, which builds
+the unmodified reference sources (oracle/ref/build_ref.py) and runs them from
+the same seeded initial state.  This pins the port: every neighbour relation
+and every bucket index must match exactly; every field must match to 1e-11
+of the field's own scale (the only freedom left is the order in which the
+reference visits periodic ghosts and scatters Shepard sums).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from sphdem import cases
+from sphdem.capi import PAIR_KIND_NAMES
+from sphdem.state import pair_set
+from oracle.port_api import OracleSim
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+WORKLOADS = ["dambreak2d_small", "dambreak2d_monaghan_small", "dem_small", "sediment3d_small"]
+FIELD_MAP = {"r": "r", "v": "v", "vhat": "vhat", "v0": "v0", "vhat0": "vhat0", "f": "f",
+             "fp": "fp", "fv": "fv", "fb": "fb", "dens": "dens", "dddt": "dddt", "h": "h",
+             "press": "press", "pdr2": "pdr2", "porosity": "porosity",
+             "dporositydt": "dporositydt", "gradPorosity": "grad_porosity",
+             "shepSum": "shep_sum", "fdrag": "fdrag", "fvel": "fvel", "omega": "omega",
+             "mass": "mass"}
+RTOL = 1e-11
+
+
+def _load(name):
+    return np.load(os.path.join(GOLDEN, name + ".npz"))
+
+
+@pytest.fixture(scope="module", params=WORKLOADS)
+def ran(request):
+    name = request.param
+    g = _load(name)
+    case = cases.workload(name)
+    assert case.n == int(g["meta_n"])
+    o = OracleSim(case.cfg, case.particles)
+    o.step(int(g["meta_nsteps"]))
+    return name, g, o, o.get(), o.globals()
+
+
+def test_fields_match_reference(ran):
+    name, g, o, got, glob = ran
+    assert glob.time == pytest.approx(float(g["time"]), rel=1e-15)
+    assert glob.dt == float(g["dt"])
+    for k, ours in FIELD_MAP.items():
+        key = "field_" + k
+        if key not in g:
+            continue
+        ref = g[key]
+        a = got[ours]
+        if a.ndim == 2 and ref.ndim == 1:
+            ref = ref.reshape(a.shape)
+        scale = np.abs(ref).max()
+        err = np.abs(a - ref).max()
+        assert err <= RTOL * max(scale, 1e-300), f"{name}:{k} err {err:.3e} scale {scale:.3e}"
+
+
+def test_pairs_and_cells_match_reference(ran):
+    name, g, o, got, glob = ran
+    o.rebuild()
+    for kind, kname in PAIR_KIND_NAMES.items():
+        key = "pairs_" + kname + "_offs"
+        if key not in g:
+            continue
+        po, pi = o.pairs(kind)
+        ref = pair_set(g[key], g["pairs_" + kname + "_idx"])
+        ours = pair_set(po, pi)
+        assert np.array_equal(ours, ref), f"{name}:{kname} {ours.size} vs {ref.size}"
+    assert np.array_equal(o.cells(), g["cells"])
+
+
+def test_golden_cases_are_not_trivial():
+    # every relation the fixtures pin must be exercised by at least one case
+    seen = {k: 0 for k in PAIR_KIND_NAMES.values()}
+    for name in WORKLOADS:
+        g = _load(name)
+        for k in seen:
+            key = "pairs_" + k + "_idx"
+            if key in g:
+                seen[k] += g[key].size
+    assert all(v > 0 for v in seen.values()), seen
