@@ -1,0 +1,674 @@
+/*
+ * extern "C" entry points of include/sphdem.h.
+ *
+ * A handle owns: the particle state (two SoA copies in HBM), the bucket
+ * arrays, the device-resident step globals, a private CUDA stream and, once
+ * a full step has run, a CUDA graph of one step per state parity.  The phase
+ * sequence reproduces CsphIncompress::start/middle/end (sphIncompress.cpp:
+ * 3-251) with the hooks of run.cpp:112-118 in between.
+ */
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "internal.cuh"
+
+using namespace sphdem;
+
+namespace sphdem {
+
+void launch_begin(sphdem_ctx *c, const char *name) {
+    if (!c->timing || c->in_capture) return;
+    TimedLaunch t;
+    t.name = name;
+    cudaEventCreate(&t.ev0);
+    cudaEventCreate(&t.ev1);
+    cudaEventRecord(t.ev0, c->stream);
+    c->launches.push_back(t);
+}
+
+void launch_end(sphdem_ctx *c) {
+    if (!c->timing || c->in_capture) return;
+    cudaEventRecord(c->launches.back().ev1, c->stream);
+}
+
+}  // namespace sphdem
+
+namespace {
+
+void collect_times(sphdem_ctx *c) {
+    if (c->launches.empty()) return;
+    cudaStreamSynchronize(c->stream);
+    for (auto &t : c->launches) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, t.ev0, t.ev1);
+        auto it = std::find(c->kt_names.begin(), c->kt_names.end(), std::string(t.name));
+        size_t k;
+        if (it == c->kt_names.end()) {
+            c->kt_names.push_back(t.name);
+            c->kt_ms.push_back(0.0);
+            c->kt_count.push_back(0);
+            k = c->kt_names.size() - 1;
+        } else {
+            k = it - c->kt_names.begin();
+        }
+        c->kt_ms[k] += ms;
+        c->kt_count[k] += 1;
+        cudaEventDestroy(t.ev0);
+        cudaEventDestroy(t.ev1);
+    }
+    c->launches.clear();
+}
+
+int fail(sphdem_ctx *c, int code, const std::string &msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+/* Read the device error flags (synchronises the stream). */
+int check_device(sphdem_ctx *c) {
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return fail(c, SPHDEM_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(c, SPHDEM_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
+    unsigned int err = 0;
+    int info = 0;
+    cudaMemcpy(&err, &c->g->err, sizeof(err), cudaMemcpyDeviceToHost);
+    if (!err) return SPHDEM_OK;
+    cudaMemcpy(&info, &c->g->err_info, sizeof(info), cudaMemcpyDeviceToHost);
+    for (int code = 1; code < 32; code++)
+        if (err & (1u << code)) {
+            char buf[256];
+            snprintf(buf, sizeof buf, "device reported error %d (info %d): %s", code, info,
+                     code == SPHDEM_ERR_CAPACITY ? "bucket grid capacity exceeded or periodic axis too short"
+                     : code == SPHDEM_ERR_OUT_OF_RANGE ? "particle outside the bucket grid"
+                                                       : "device check failed");
+            return fail(c, code, buf);
+        }
+    return SPHDEM_ERR_CUDA;
+}
+
+void build_devcfg(const SphDemConfig &h, DevCfg &c) {
+    std::memset(&c, 0, sizeof(c));
+    c.nd = h.ndim;
+    c.visc = h.visc_model;
+    c.precision = h.precision;
+    c.flags = h.flags;
+    c.n_walls = h.n_walls;
+    for (int d = 0; d < 3; d++) {
+        c.periodic[d] = d < h.ndim ? h.periodic[d] : 0;
+        c.rmin[d] = h.rmin[d];
+        c.rmax[d] = h.rmax[d];
+        c.dmin[d] = h.domain_min[d];
+        c.dmax[d] = h.domain_max[d];
+        c.g_sph[d] = h.gravity_sph[d];
+        c.g_dem[d] = h.gravity_dem[d];
+    }
+    c.pi = h.pi;
+    c.hfac = h.hfac;
+    c.psep = h.psep;
+    c.h = h.h;
+    c.dens = h.dens;
+    c.refd = h.refd;
+    c.gamma = h.gamma;
+    c.prb = h.prb;
+    c.spsound = h.spsound;
+    c.viscosity = h.viscosity;
+    c.alpha_art = h.alpha_artificial;
+    c.alpha_mon = h.viscosity * (112.0 / 15.0) / (h.spsound * h.h);  /* viscToAlpha, misc.h:41-43 */
+    c.bfac = h.bfac;
+    c.maxdt = h.maxdt;
+    c.damptime = h.damptime;
+    c.dem_radius = h.dem_radius;
+    c.dem_dens = h.dem_dens;
+    c.dem_k = h.dem_k;
+    c.dem_gamma = h.dem_gamma;
+    c.dem_sr = h.dem_search_radius;
+    c.dem_vol = h.dem_vol;
+    c.rc = h.coupling_radius;
+    c.dem_timestep = h.dem_timestep;
+    c.liq_dem_timestep = h.liq_dem_timestep;
+    c.time_drop = h.time_drop_particle;
+    c.freeze_until = h.freeze_dem_until;
+    for (int w = 0; w < SPHDEM_MAX_WALLS; w++)
+        for (int d = 0; d < 3; d++) {
+            c.wall_p[w][d] = h.walls[w].point[d];
+            c.wall_n[w][d] = h.walls[w].normal[d];
+        }
+    c.wcon = h.ndim == 2 ? 7.0 / (64.0 * h.pi) : 21.0 / (256.0 * h.pi);
+    /* migration test extents */
+    for (int d = 0; d < 3; d++) {
+        c.dspace[d] = c.dmax[d] - c.dmin[d];
+        c.rdspace_f[d] = c.dspace[d] > 0 ? (float)(1.0 / c.dspace[d]) : 0.f;
+    }
+    /* DEM search grid and the reference DEM bucket map */
+    const bool liq = h.flags & SPHDEM_F_LIQ_DEM;
+    double cmin = std::max(h.coupling_radius, 2.0 * h.dem_search_radius) * (1.0 + 1e-12);
+    if (!(cmin > 0)) cmin = 1.0;
+    int ndc = 1;
+    for (int d = 0; d < 3; d++) {
+        if (d >= h.ndim || !liq) {
+            c.ddims[d] = 1;
+            c.dcell[d] = 1.0;
+            c.dorig[d] = 0.0;
+            c.rdcell[d] = 1.0;
+            continue;
+        }
+        const double ext = c.dspace[d];
+        if (c.periodic[d]) {
+            int m = (int)std::floor(ext / cmin);
+            if (m < 3) m = 3;
+            c.ddims[d] = m;
+            c.dcell[d] = ext / m;
+            c.dorig[d] = c.dmin[d];
+        } else {
+            c.ddims[d] = (int)std::ceil(ext / cmin) + 2;
+            c.dcell[d] = cmin;
+            c.dorig[d] = c.dmin[d] - cmin;
+        }
+        c.rdcell[d] = 1.0 / c.dcell[d];
+        ndc *= c.ddims[d];
+    }
+    c.n_dem_cells = liq ? ndc : 0;
+    if (liq && h.dem_search_radius > 0) {
+        c.dem_cell_off = 2 * h.coupling_radius / h.dem_search_radius - 1;
+        c.rdem2_f = (float)(1.0 / (2 * h.dem_search_radius));
+        c.couple_num = (int)std::ceil(0.5 * h.coupling_radius / h.dem_search_radius);
+        c.couple_lim = std::pow(0.5 * h.coupling_radius / h.dem_search_radius, 2);
+        for (int d = 0; d < 3; d++) {
+            c.dg_lo[d] = c.dmin[d] + h.coupling_radius;
+            double sp = c.dspace[d] - h.coupling_radius;
+            sp -= h.coupling_radius;
+            c.dg_sp[d] = sp;
+            c.dg_rsp_f[d] = sp != 0 ? (float)(1.0 / sp) : 0.f;
+        }
+    }
+    c.two_over_rc = h.coupling_radius > 0 ? 2.0 / h.coupling_radius : 0.0;
+    c.rc2 = h.coupling_radius * h.coupling_radius;
+    const double hc = h.coupling_radius / 2.0;
+    if (hc > 0) {
+        c.c_ihn = 1 / std::pow(hc, h.ndim);
+        c.c_ihn2 = 1 / std::pow(hc, h.ndim + 2);
+        c.c_hinv = 1 / hc;
+    }
+    c.por_incr = h.ndim == 2 ? (4.0 / 3.0) * h.pi * std::pow(h.dem_radius, 3) / (2.0 * h.dem_radius)
+                             : (4.0 / 3.0) * h.pi * std::pow(h.dem_radius, 3);
+    {
+        const double q = 1.0 / h.hfac;
+        const double t = 2.0 - q;
+        c.k_anti = q <= 2.0 ? c.wcon * std::pow(t, 4) * (1.0 + 2.0 * q) : 0.0;
+    }
+}
+
+std::string validate(const SphDemConfig *cfg, const SphDemParticles *p, int64_t cap) {
+    if (!cfg || !p) return "null config or particles";
+    if (cfg->ndim < 1 || cfg->ndim > 3) return "ndim must be 1, 2 or 3";
+    if (p->n <= 0) return "no particles";
+    if (cap < p->n) return "capacity smaller than the particle count";
+    if (p->n > (int64_t)1 << 30) return "more than 2^30 particles";
+    if (!p->iam || !p->r || !p->mass || !p->dens || !p->h) return "iam, r, mass, dens and h are required";
+    if (!(cfg->h > 0) || !(cfg->maxdt > 0)) return "h and maxdt must be positive";
+    if (cfg->precision != SPHDEM_PREC_FP64 && cfg->precision != SPHDEM_PREC_MIXED) return "unknown precision";
+    if (cfg->n_walls < 0 || cfg->n_walls > SPHDEM_MAX_WALLS) return "n_walls out of range";
+    for (int d = 0; d < cfg->ndim; d++)
+        if (!(cfg->domain_max[d] > cfg->domain_min[d])) return "empty binning domain";
+    if ((cfg->flags & SPHDEM_F_LIQ_DEM) && !(cfg->dem_search_radius > 0 && cfg->coupling_radius > 0))
+        return "LIQ_DEM needs dem_search_radius and coupling_radius";
+    for (int64_t i = 0; i < p->n; i++) {
+        for (int d = 0; d < 3; d++)
+            if (!std::isfinite(p->r[3 * i + d])) return "non-finite position";
+        if (!(p->h[i] > 0) || !(p->mass[i] > 0) || !(p->dens[i] > 0)) return "h, mass and dens must be positive";
+    }
+    return "";
+}
+
+void free_ctx(sphdem_ctx *c) {
+    if (!c) return;
+    cudaFree(c->A.d);
+    cudaFree(c->A.i);
+    cudaFree(c->B.d);
+    cudaFree(c->B.i);
+    cudaFree(c->g);
+    Buffers &b = c->buf;
+    for (int *p : {b.skey, b.perm, b.slot, b.key, b.cnt, b.start, b.fill, b.bsum, b.fields_d, b.fields_i, b.pair_cnt})
+        cudaFree(p);
+    for (int k = 0; k < 2; k++)
+        if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+void run_phase(sphdem_ctx *c, int phase) {
+    const bool liq = c->cfg.liq_dem();
+    switch (phase) {
+        case SPHDEM_HOOK_BEFORE_START:
+            globals_op(c, OP_STEP_INC);
+            break;
+        case SPHDEM_PHASE_START:
+            run_start(c);
+            break;
+        case SPHDEM_HOOK_BEFORE_MIDDLE:
+            run_hook_before_middle(c);
+            break;
+        case SPHDEM_PHASE_MIDDLE:
+            globals_op(c, OP_MIDDLE_BEGIN);
+            rebuild(c);
+            if (liq) {
+                run_porosity(c);
+                run_dem_drag(c);
+            }
+            run_omega_eos(c, c->cfg.var_h(), true);
+            run_force(c);
+            if (liq) run_dem_accel(c);
+            globals_op(c, OP_SET_DT);
+            run_middle_tail(c);
+            break;
+        case SPHDEM_HOOK_BEFORE_END:
+            run_hook_before_end(c);
+            break;
+        case SPHDEM_PHASE_END:
+            run_end_drift(c);
+            rebuild(c);
+            if (c->cfg.var_h()) run_omega_eos(c, true, false);
+            run_dddt(c);
+            if (liq) run_dem_end(c);
+            run_end_tail(c);
+            break;
+        case SPHDEM_HOOK_AFTER_END:
+            run_hook_after_end(c);
+            break;
+    }
+}
+
+void run_full_step(sphdem_ctx *c) {
+    for (int p = SPHDEM_HOOK_BEFORE_START; p <= SPHDEM_HOOK_AFTER_END; p++) run_phase(c, p);
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *sphdem_version(void) { return "sphdem-gb300 0.1 (sm_103a)"; }
+
+int sphdem_last_error(sphdem_handle h, char *buf, size_t len) {
+    if (!buf || !len) return SPHDEM_ERR_INVALID;
+    const std::string &e = h ? h->err : std::string("no handle");
+    std::snprintf(buf, len, "%s", e.c_str());
+    return SPHDEM_OK;
+}
+
+static thread_local std::string g_create_err;
+
+int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t capacity, sphdem_handle *out) {
+    if (!out) return SPHDEM_ERR_INVALID;
+    *out = nullptr;
+    const std::string v = validate(cfg, init, capacity);
+    if (!v.empty()) {
+        g_create_err = v;
+        fprintf(stderr, "sphdem_create: %s\n", v.c_str());
+        return SPHDEM_ERR_INVALID;
+    }
+    sphdem_ctx *c = new sphdem_ctx();
+    try {
+        c->host_cfg = *cfg;
+        build_devcfg(*cfg, c->cfg);
+        c->n = init->n;
+        c->cap = capacity;
+        SPHDEM_CUDA_CHECK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        for (DevState *s : {&c->A, &c->B}) {
+            s->cap = capacity;
+            SPHDEM_CUDA_CHECK(cudaMalloc(&s->d, (size_t)NFD * capacity * sizeof(double)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&s->i, (size_t)NFI * capacity * sizeof(int)));
+            SPHDEM_CUDA_CHECK(cudaMemset(s->d, 0, (size_t)NFD * capacity * sizeof(double)));
+            SPHDEM_CUDA_CHECK(cudaMemset(s->i, 0, (size_t)NFI * capacity * sizeof(int)));
+        }
+        /* upload in tag order */
+        const int64_t n = c->n;
+        std::vector<double> row(n);
+        auto up = [&](int f, const std::vector<double> &v) {
+            SPHDEM_CUDA_CHECK(cudaMemcpy(c->A.row(f), v.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+        };
+        auto vec = [&](int base, const double *src, double dflt, const double *fallback) {
+            for (int d = 0; d < 3; d++) {
+                for (int64_t i = 0; i < n; i++)
+                    row[i] = src ? src[3 * i + d] : (fallback ? fallback[3 * i + d] : dflt);
+                up(base + d, row);
+            }
+        };
+        auto sca = [&](int f, const double *src, double dflt) {
+            for (int64_t i = 0; i < n; i++) row[i] = src ? src[i] : dflt;
+            up(f, row);
+        };
+        vec(FD_R, init->r, 0.0, nullptr);
+        vec(FD_V, init->v, 0.0, nullptr);
+        vec(FD_VHAT, init->vhat, 0.0, init->v);
+        vec(FD_N1, init->norm1, 0.0, nullptr);
+        vec(FD_N2, init->norm2, 0.0, nullptr);
+        vec(FD_N3, init->norm3, 0.0, nullptr);
+        sca(FD_MASS, init->mass, 0.0);
+        sca(FD_DENS, init->dens, 0.0);
+        sca(FD_H, init->h, 0.0);
+        sca(FD_RADIUS, init->radius, 0.0);
+        sca(FD_POR, nullptr, 1.0);  /* Cparticle() sets porosity = 1 (particle.h:82) */
+        std::vector<int> irow(n);
+        for (int64_t i = 0; i < n; i++) irow[i] = init->iam[i];
+        SPHDEM_CUDA_CHECK(cudaMemcpy(c->A.irow(FI_IAM), irow.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        for (int64_t i = 0; i < n; i++) irow[i] = (int)i;
+        SPHDEM_CUDA_CHECK(cudaMemcpy(c->A.irow(FI_TAG), irow.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+        for (int64_t i = 0; i < n; i++) irow[i] = init->concave ? init->concave[i] != 0 : 1;
+        SPHDEM_CUDA_CHECK(cudaMemcpy(c->A.irow(FI_CONCAVE), irow.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+
+        /* bucket grid capacity: SPH grid at half the smallest of H and the
+         * largest initial h (h may shrink until then), DEM grid fixed */
+        double hmax0 = 0;
+        for (int64_t i = 0; i < n; i++) hmax0 = std::max(hmax0, init->h[i]);
+        const double sr_min = 0.5 * std::min(cfg->h, hmax0);
+        long long sc = 1;
+        for (int d = 0; d < cfg->ndim; d++)
+            sc *= (long long)((cfg->domain_max[d] - cfg->domain_min[d]) / (2.0 * sr_min)) + 9;
+        if (sc > (1ll << 30)) throw std::string("bucket grid too large for the domain / smoothing length");
+        c->cfg.sph_cells_cap = (int)sc;
+        Buffers &b = c->buf;
+        b.cells_cap = (int)sc + c->cfg.n_dem_cells + 2;
+        for (int **p : {&b.skey, &b.perm, &b.slot, &b.key})
+            SPHDEM_CUDA_CHECK(cudaMalloc(p, capacity * sizeof(int)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&b.cnt, (size_t)b.cells_cap * sizeof(int)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&b.start, ((size_t)b.cells_cap + 1) * sizeof(int)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&b.fill, (size_t)b.cells_cap * sizeof(int)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&b.bsum, ((size_t)b.cells_cap / 4096 + 2) * sizeof(int)));
+        setup_rebuild_buffers(c);
+
+        /* globals as the CdataLL constructor leaves them (dataLL.cpp:8-40) */
+        DevGlobals hg;
+        std::memset(&hg, 0, sizeof(hg));
+        hg.dt = cfg->maxdt;
+        hg.old_dt = cfg->maxdt;
+        hg.maxdt = cfg->maxdt;
+        hg.new_dt = cfg->maxdt;
+        hg.dem_dt = cfg->maxdt;
+        hg.sr = cfg->h;
+        hg.hmax = cfg->h;
+        for (int k = 0; k < 27; k++) hg.gw[k] = 1.1 * 2.0 * cfg->h;
+        for (int d = 0; d < 3; d++) {
+            hg.ghost_lo[d] = c->cfg.dmin[d] + hg.gw[0];
+            double sp = c->cfg.dspace[d] - hg.gw[0];
+            sp -= hg.gw[0];
+            hg.ghost_sp[d] = sp;
+            hg.ghost_rsp_f[d] = sp != 0 ? (float)(1.0 / sp) : 0.f;
+        }
+        SPHDEM_CUDA_CHECK(cudaMalloc(&c->g, sizeof(DevGlobals)));
+        SPHDEM_CUDA_CHECK(cudaMemcpy(c->g, &hg, sizeof(hg), cudaMemcpyHostToDevice));
+        /* the uploads above ran on the legacy stream; the handle's stream is
+         * non-blocking, so order them explicitly */
+        SPHDEM_CUDA_CHECK(cudaDeviceSynchronize());
+        run_h_derived(c);
+        rebuild(c);
+        int rc = check_device(c);
+        if (rc != SPHDEM_OK) {
+            g_create_err = c->err;
+            fprintf(stderr, "sphdem_create: %s\n", c->err.c_str());
+            free_ctx(c);
+            return rc;
+        }
+    } catch (const std::string &e) {
+        g_create_err = e;
+        fprintf(stderr, "sphdem_create: %s\n", e.c_str());
+        free_ctx(c);
+        return SPHDEM_ERR_CUDA;
+    }
+    *out = c;
+    return SPHDEM_OK;
+}
+
+int sphdem_destroy(sphdem_handle h) {
+    if (!h) return SPHDEM_ERR_INVALID;
+    collect_times(h);
+    free_ctx(h);
+    return SPHDEM_OK;
+}
+
+int sphdem_phase(sphdem_handle h, int phase) {
+    if (!h) return SPHDEM_ERR_INVALID;
+    if (phase < SPHDEM_HOOK_BEFORE_START || phase > SPHDEM_HOOK_AFTER_END)
+        return fail(h, SPHDEM_ERR_INVALID, "unknown phase");
+    try {
+        run_phase(h, phase);
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+    const int rc = check_device(h);
+    collect_times(h);
+    return rc;
+}
+
+int sphdem_step(sphdem_handle h, int nsteps) {
+    if (!h) return SPHDEM_ERR_INVALID;
+    if (nsteps < 0) return fail(h, SPHDEM_ERR_INVALID, "negative step count");
+    try {
+        for (int k = 0; k < nsteps; k++) {
+            if (h->timing) {
+                run_full_step(h);
+                continue;
+            }
+            cudaGraphExec_t &ge = h->graph[h->flipped ? 1 : 0];
+            if (!ge) {
+                cudaGraph_t graph;
+                h->in_capture = true;
+                SPHDEM_CUDA_CHECK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+                const bool flipped0 = h->flipped;
+                run_full_step(h);
+                h->in_capture = false;
+                SPHDEM_CUDA_CHECK(cudaStreamEndCapture(h->stream, &graph));
+                if (h->flipped != flipped0) throw std::string("a step must rebuild an even number of times");
+                SPHDEM_CUDA_CHECK(cudaGraphInstantiate(&ge, graph, 0));
+                cudaGraphDestroy(graph);
+            }
+            SPHDEM_CUDA_CHECK(cudaGraphLaunch(ge, h->stream));
+        }
+    } catch (const std::string &e) {
+        h->in_capture = false;
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+    const int rc = check_device(h);
+    collect_times(h);
+    return rc;
+}
+
+int sphdem_rebuild(sphdem_handle h) {
+    if (!h) return SPHDEM_ERR_INVALID;
+    try {
+        rebuild(h);
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+    return check_device(h);
+}
+
+int sphdem_time_steps(sphdem_handle h, int nsteps, double *ms) {
+    if (!h || !ms) return SPHDEM_ERR_INVALID;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    int rc = sphdem_step(h, 1);  /* make sure the graph exists */
+    if (rc) return rc;
+    cudaEventRecord(e0, h->stream);
+    rc = sphdem_step(h, nsteps);
+    cudaEventRecord(e1, h->stream);
+    cudaEventSynchronize(e1);
+    float t = 0.f;
+    cudaEventElapsedTime(&t, e0, e1);
+    *ms = t;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+int sphdem_get_globals(sphdem_handle h, SphDemGlobals *out) {
+    if (!h || !out) return SPHDEM_ERR_INVALID;
+    DevGlobals hg;
+    cudaStreamSynchronize(h->stream);
+    if (cudaMemcpy(&hg, h->g, sizeof(hg), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return fail(h, SPHDEM_ERR_CUDA, "cannot read globals");
+    out->time = hg.time;
+    out->dt = hg.dt;
+    out->new_dt = hg.new_dt;
+    out->maxdt = hg.maxdt;
+    out->dem_dt = hg.dem_dt;
+    out->sph_step = hg.step;
+    out->n_deleted = hg.n_deleted;
+    return SPHDEM_OK;
+}
+
+int sphdem_set_globals(sphdem_handle h, const SphDemGlobals *in) {
+    if (!h || !in) return SPHDEM_ERR_INVALID;
+    DevGlobals hg;
+    cudaStreamSynchronize(h->stream);
+    cudaMemcpy(&hg, h->g, sizeof(hg), cudaMemcpyDeviceToHost);
+    hg.time = in->time;
+    hg.dt = in->dt;
+    hg.maxdt = in->maxdt;
+    hg.step = in->sph_step;
+    if (cudaMemcpy(h->g, &hg, sizeof(hg), cudaMemcpyHostToDevice) != cudaSuccess)
+        return fail(h, SPHDEM_ERR_CUDA, "cannot write globals");
+    cudaDeviceSynchronize();
+    return SPHDEM_OK;
+}
+
+namespace {
+struct FieldMap {
+    uint32_t bit;
+    int row;
+    int ncomp;
+    double *SphDemParticles::*ptr;
+};
+const FieldMap kFields[] = {
+    {SPHDEM_FIELD_R, FD_R, 3, &SphDemParticles::r},
+    {SPHDEM_FIELD_V, FD_V, 3, &SphDemParticles::v},
+    {SPHDEM_FIELD_VHAT, FD_VHAT, 3, &SphDemParticles::vhat},
+    {SPHDEM_FIELD_MASS, FD_MASS, 1, &SphDemParticles::mass},
+    {SPHDEM_FIELD_DENS, FD_DENS, 1, &SphDemParticles::dens},
+    {SPHDEM_FIELD_H, FD_H, 1, &SphDemParticles::h},
+    {SPHDEM_FIELD_F, FD_F, 3, &SphDemParticles::f},
+    {SPHDEM_FIELD_F, FD_FP, 3, &SphDemParticles::fp},
+    {SPHDEM_FIELD_F, FD_FV, 3, &SphDemParticles::fv},
+    {SPHDEM_FIELD_F, FD_FB, 3, &SphDemParticles::fb},
+    {SPHDEM_FIELD_DDDT, FD_DDDT, 1, &SphDemParticles::dddt},
+    {SPHDEM_FIELD_PRESS, FD_PRESS, 1, &SphDemParticles::press},
+    {SPHDEM_FIELD_PRESS, FD_PDR2, 1, &SphDemParticles::pdr2},
+    {SPHDEM_FIELD_COUPLING, FD_POR, 1, &SphDemParticles::porosity},
+    {SPHDEM_FIELD_COUPLING, FD_DPORDT, 1, &SphDemParticles::dporositydt},
+    {SPHDEM_FIELD_COUPLING, FD_SHEP, 1, &SphDemParticles::shep_sum},
+    {SPHDEM_FIELD_COUPLING, FD_FDRAG, 3, &SphDemParticles::fdrag},
+    {SPHDEM_FIELD_COUPLING, FD_FVEL, 3, &SphDemParticles::fvel},
+    {SPHDEM_FIELD_COUPLING, FD_GPOR, 3, &SphDemParticles::grad_porosity},
+    {SPHDEM_FIELD_OMEGA, FD_OMEGA, 1, &SphDemParticles::omega},
+    {SPHDEM_FIELD_V0, FD_V0, 3, &SphDemParticles::v0},
+    {SPHDEM_FIELD_V0, FD_VHAT0, 3, &SphDemParticles::vhat0},
+};
+}  // namespace
+
+int sphdem_get_fields(sphdem_handle h, uint32_t mask, SphDemParticles *out) {
+    if (!h || !out) return SPHDEM_ERR_INVALID;
+    if (out->n != h->n) return fail(h, SPHDEM_ERR_INVALID, "particle count mismatch");
+    const int64_t n = h->n;
+    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return fail(h, SPHDEM_ERR_CUDA, "stream failed");
+    std::vector<int> tag(n), iam(n);
+    std::vector<double> row(n);
+    cudaMemcpy(tag.data(), h->A.irow(FI_TAG), n * sizeof(int), cudaMemcpyDeviceToHost);
+    cudaMemcpy(iam.data(), h->A.irow(FI_IAM), n * sizeof(int), cudaMemcpyDeviceToHost);
+    if (out->iam && (mask & SPHDEM_FIELD_IAM))
+        for (int64_t k = 0; k < n; k++) out->iam[tag[k]] = iam[k];
+    if (out->tag)
+        for (int64_t k = 0; k < n; k++) out->tag[tag[k]] = tag[k] + 1;
+    for (const FieldMap &fm : kFields) {
+        if (!(mask & fm.bit)) continue;
+        double *dst = out->*fm.ptr;
+        if (!dst) continue;
+        for (int d = 0; d < fm.ncomp; d++) {
+            cudaMemcpy(row.data(), h->A.row(fm.row + d), n * sizeof(double), cudaMemcpyDeviceToHost);
+            if (fm.ncomp == 3)
+                for (int64_t k = 0; k < n; k++) dst[3 * (int64_t)tag[k] + d] = row[k];
+            else
+                for (int64_t k = 0; k < n; k++) dst[tag[k]] = row[k];
+        }
+    }
+    if (cudaGetLastError() != cudaSuccess) return fail(h, SPHDEM_ERR_CUDA, "copy failed");
+    return SPHDEM_OK;
+}
+
+int sphdem_set_fields(sphdem_handle h, uint32_t mask, const SphDemParticles *in) {
+    if (!h || !in) return SPHDEM_ERR_INVALID;
+    if (in->n != h->n) return fail(h, SPHDEM_ERR_INVALID, "particle count mismatch");
+    const int64_t n = h->n;
+    cudaStreamSynchronize(h->stream);
+    std::vector<int> tag(n);
+    std::vector<double> row(n);
+    cudaMemcpy(tag.data(), h->A.irow(FI_TAG), n * sizeof(int), cudaMemcpyDeviceToHost);
+    for (const FieldMap &fm : kFields) {
+        if (!(mask & fm.bit)) continue;
+        const double *src = in->*fm.ptr;
+        if (!src) continue;
+        for (int d = 0; d < fm.ncomp; d++) {
+            if (fm.ncomp == 3)
+                for (int64_t k = 0; k < n; k++) row[k] = src[3 * (int64_t)tag[k] + d];
+            else
+                for (int64_t k = 0; k < n; k++) row[k] = src[tag[k]];
+            cudaMemcpy(h->A.row(fm.row + d), row.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+        }
+    }
+    cudaDeviceSynchronize();
+    if (mask & SPHDEM_FIELD_H) run_h_derived(h);
+    return check_device(h);
+}
+
+int sphdem_pairs(sphdem_handle h, int kind, int64_t *offsets, int32_t *idx, int64_t idx_capacity, int64_t *n_pairs) {
+    if (!h || !n_pairs || kind < 0 || kind > 3) return SPHDEM_ERR_INVALID;
+    try {
+        const int rc = export_pairs(h, kind, offsets, idx, idx_capacity, n_pairs);
+        if (rc) return fail(h, rc, "pair buffer too small");
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+    return SPHDEM_OK;
+}
+
+int sphdem_cell_ids(sphdem_handle h, int32_t *cells) {
+    if (!h || !cells) return SPHDEM_ERR_INVALID;
+    try {
+        return export_cells(h, cells);
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+}
+
+int sphdem_kernel_times_reset(sphdem_handle h, int enable) {
+    if (!h) return SPHDEM_ERR_INVALID;
+    collect_times(h);
+    h->kt_names.clear();
+    h->kt_ms.clear();
+    h->kt_count.clear();
+    h->timing = enable != 0;
+    return SPHDEM_OK;
+}
+
+int sphdem_kernel_times(sphdem_handle h, char *names, size_t names_len, double *ms, int64_t *launches,
+                        int max_kernels, int *n_kernels) {
+    if (!h || !names || !ms || !launches || !n_kernels) return SPHDEM_ERR_INVALID;
+    collect_times(h);
+    std::string all;
+    const int k = std::min<int>(max_kernels, (int)h->kt_names.size());
+    for (int i = 0; i < k; i++) {
+        if (i) all += "\n";
+        all += h->kt_names[i];
+        ms[i] = h->kt_ms[i];
+        launches[i] = h->kt_count[i];
+    }
+    std::snprintf(names, names_len, "%s", all.c_str());
+    *n_kernels = k;
+    return SPHDEM_OK;
+}
+
+}  // extern "C"

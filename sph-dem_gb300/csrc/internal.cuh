@@ -1,0 +1,118 @@
+/*
+ * Host-side context of one handle and the launch entry points each .cu file
+ * provides.  Not part of the public ABI (include/sphdem.h is).
+ */
+#pragma once
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+struct sphdem_ctx;
+
+namespace sphdem {
+
+/* One timed launch (enabled by sphdem_kernel_times_reset(h, 1)). */
+struct TimedLaunch {
+    const char *name;
+    cudaEvent_t ev0, ev1;
+};
+
+struct Buffers {
+    int *skey = nullptr;     /* bucket key of each sorted particle        */
+    int *perm = nullptr;     /* sorted slot -> previous slot              */
+    int *slot = nullptr;     /* scatter scratch                           */
+    int *key = nullptr;      /* bucket key of each particle, previous order */
+    int *cnt = nullptr;      /* bucket counts                             */
+    int *start = nullptr;    /* bucket starts (exclusive scan)            */
+    int *fill = nullptr;     /* scatter cursors                           */
+    int *bsum = nullptr;     /* scan block sums                           */
+    int *fields_d = nullptr; /* FP64 rows to gather at a rebuild          */
+    int *fields_i = nullptr; /* int rows to gather                        */
+    int n_fields_d = 0, n_fields_i = 0;
+    int cells_cap = 0;       /* capacity of cnt/start/fill                */
+    /* export scratch */
+    int *pair_cnt = nullptr;
+};
+
+}  // namespace sphdem
+
+struct sphdem_ctx {
+    SphDemConfig host_cfg;
+    sphdem::DevCfg cfg;
+    int64_t n = 0, cap = 0;
+    sphdem::DevState A, B;   /* B is the gather target of the next rebuild */
+    bool flipped = false;    /* odd number of rebuilds so far              */
+    sphdem::DevGlobals *g = nullptr;
+    sphdem::Buffers buf;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    /* CUDA graph of one full step, per state parity */
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    bool in_capture = false;
+    /* timing */
+    bool timing = false;
+    std::vector<sphdem::TimedLaunch> launches;
+    std::vector<std::string> kt_names;
+    std::vector<double> kt_ms;
+    std::vector<long long> kt_count;
+    /* mixed precision packed inputs */
+    float4 *mx_pos = nullptr, *mx_vel = nullptr, *mx_aux = nullptr;
+    float *mx_out = nullptr;
+};
+
+namespace sphdem {
+
+/* launch bracket: records events around a launch when timing is enabled */
+void launch_begin(sphdem_ctx *c, const char *name);
+void launch_end(sphdem_ctx *c);
+
+/* binning.cu */
+void rebuild(sphdem_ctx *c);
+void setup_rebuild_buffers(sphdem_ctx *c);
+
+/* integrate.cu: elementwise phases and built-in hooks */
+enum GlobalsOp { OP_MIDDLE_BEGIN = 0, OP_SET_DT, OP_END_BEGIN, OP_STEP_INC };
+void globals_op(sphdem_ctx *c, int op);
+void run_start(sphdem_ctx *c);
+void run_hook_before_middle(sphdem_ctx *c);
+void run_middle_tail(sphdem_ctx *c);
+void run_end_drift(sphdem_ctx *c);
+void run_end_tail(sphdem_ctx *c);
+void run_hook_before_end(sphdem_ctx *c);
+void run_hook_after_end(sphdem_ctx *c);
+void run_h_derived(sphdem_ctx *c);
+
+/* pairs64.cu / pairs32.cu: pair passes */
+void run_porosity(sphdem_ctx *c);      /* calcPorosity + calcShepSum        */
+void run_dem_drag(sphdem_ctx *c);      /* calcDEMtoSPHDrag + finalisePorosity */
+void run_omega_eos(sphdem_ctx *c, bool omega, bool eos);
+void run_force(sphdem_ctx *c);         /* calcForce + accelCondition        */
+void run_dem_accel(sphdem_ctx *c);
+void run_dddt(sphdem_ctx *c);          /* calcDddtDudt                      */
+void run_dem_end(sphdem_ctx *c);       /* calcFPI + calcDEMContacts         */
+
+/* export.cu */
+int export_pairs(sphdem_ctx *c, int kind, int64_t *offs, int32_t *idx, int64_t cap, int64_t *np);
+int export_cells(sphdem_ctx *c, int32_t *cells);
+
+inline const DevState &cur(const sphdem_ctx *c) { return c->A; }
+
+inline int grid_for(int64_t n, int block) { return (int)((n + block - 1) / block); }
+
+}  // namespace sphdem
+
+#define SPHDEM_CUDA_CHECK(expr)                                                  \
+    do {                                                                         \
+        cudaError_t e_ = (expr);                                                 \
+        if (e_ != cudaSuccess)                                                   \
+            throw std::string(#expr) + ": " + cudaGetErrorString(e_);            \
+    } while (0)
+
+#define SPHDEM_LAUNCH(ctx, name, kernel, grid, block, smem, ...)                \
+    do {                                                                         \
+        sphdem::launch_begin(ctx, name);                                         \
+        kernel<<<(grid), (block), (smem), (ctx)->stream>>>(__VA_ARGS__);         \
+        sphdem::launch_end(ctx);                                                 \
+    } while (0)

@@ -1,0 +1,51 @@
+"""The C-ABI library loads and exports every entry point include/*.h declares
+(no GPU needed: the library is only dlopen'ed, nothing is called on a device)."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(REPO, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b(sphdem_[a-z0-9_]+)\s*\(", src):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for required in ("sphdem_create", "sphdem_destroy", "sphdem_phase", "sphdem_step",
+                     "sphdem_get_fields", "sphdem_set_fields", "sphdem_pairs", "sphdem_last_error"):
+        assert required in names
+
+
+def test_library_exports_all_declared_symbols():
+    import __graft_entry__  # noqa: F401  (build() compiles the library)
+    from sphdem import capi
+    if not os.path.exists(capi.LIB_PATH):
+        __graft_entry__.build()
+    lib = ctypes.CDLL(capi.LIB_PATH)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    lib.sphdem_version.restype = ctypes.c_char_p
+    assert b"sm_103a" in lib.sphdem_version()
+
+
+def test_config_struct_layout_matches_header():
+    """ctypes mirror of SphDemConfig has every member of the C struct."""
+    from sphdem import capi
+    src = open(os.path.join(REPO, "include", "sphdem.h")).read()
+    body = src[src.index("typedef struct SphDemConfig"):src.index("} SphDemConfig;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    members = re.findall(r"\b([a-z_0-9]+)\s*(?:\[[^\]]*\])?\s*[;,]", body)
+    ours = [f for f, _ in capi.SphDemConfig._fields_]
+    for m in members:
+        assert m in ours, m
