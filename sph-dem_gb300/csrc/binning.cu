@@ -402,7 +402,8 @@ void setup_rebuild_buffers(sphdem_ctx *c) {
     for (int f : {FD_MASS, FD_DENS, FD_DDDT, FD_H, FD_PRESS, FD_PDR2, FD_OMEGA, FD_RADIUS,
                   FD_IH, FD_IHN, FD_IHN2})
         fd.push_back(f);
-    if (liq) for (int f : {FD_POR, FD_DPORDT, FD_SHEP}) fd.push_back(f);
+    fd.push_back(FD_POR);
+    if (liq) for (int f : {FD_DPORDT, FD_SHEP}) fd.push_back(f);
     fi = {FI_IAM, FI_TAG, FI_CONCAVE, FI_GCODE};
     if (liq) for (int f : {FI_RDC0, FI_RDC1, FI_RDC2}) fi.push_back(f);
     SPHDEM_CUDA_CHECK(cudaMalloc(&c->buf.fields_d, fd.size() * sizeof(int)));

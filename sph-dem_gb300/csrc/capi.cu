@@ -208,7 +208,7 @@ std::string validate(const SphDemConfig *cfg, const SphDemParticles *p, int64_t 
     if (cfg->ndim < 1 || cfg->ndim > 3) return "ndim must be 1, 2 or 3";
     if (p->n <= 0) return "no particles";
     if (cap < p->n) return "capacity smaller than the particle count";
-    if (p->n > (int64_t)1 << 30) return "more than 2^30 particles";
+    if (p->n > (int64_t)1 << 26) return "more than 2^26 particles";
     if (!p->iam || !p->r || !p->mass || !p->dens || !p->h) return "iam, r, mass, dens and h are required";
     if (!(cfg->h > 0) || !(cfg->maxdt > 0)) return "h and maxdt must be positive";
     if (cfg->precision != SPHDEM_PREC_FP64 && cfg->precision != SPHDEM_PREC_MIXED) return "unknown precision";
@@ -235,14 +235,62 @@ void free_ctx(sphdem_ctx *c) {
     Buffers &b = c->buf;
     for (int *p : {b.skey, b.perm, b.slot, b.key, b.cnt, b.start, b.fill, b.bsum, b.fields_d, b.fields_i, b.pair_cnt})
         cudaFree(p);
+    cudaFree(c->mx_pos);
+    cudaFree(c->mx_vel);
+    cudaFree(c->mx_aux);
+    cudaFree(c->mx_tg);
+    cudaFree(c->mx_om);
+    cudaFree(c->mx_nbr);
+    cudaFree(c->mx_ncnt);
     for (int k = 0; k < 2; k++)
         if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
 
+void run_phase_mixed(sphdem_ctx *c, int phase) {
+    const bool liq = c->cfg.liq_dem();
+    const bool lists = c->mx_maxn > 0;
+    switch (phase) {
+        case SPHDEM_PHASE_MIDDLE:
+            globals_op(c, OP_MIDDLE_BEGIN);
+            rebuild(c);
+            mixed::pack(c);
+            if (lists) mixed::nlist(c);
+            if (liq) {
+                zero_dem_shep(c);
+                mixed::porosity(c);
+                mixed::dem_drag(c);
+            }
+            if (lists) {
+                mixed::omega_eos(c, c->cfg.var_h(), true);
+                mixed::force(c);
+            }
+            if (liq) run_dem_accel(c);
+            globals_op(c, OP_SET_DT);
+            run_middle_tail(c);
+            break;
+        case SPHDEM_PHASE_END:
+            run_end_drift(c);
+            rebuild(c);
+            mixed::pack(c);
+            if (lists) {
+                mixed::nlist(c);
+                if (c->cfg.var_h()) mixed::omega_eos(c, true, false);
+                mixed::dddt(c);
+            }
+            if (liq) mixed::dem_end(c);
+            run_end_tail(c);
+            break;
+    }
+}
+
 void run_phase(sphdem_ctx *c, int phase) {
     const bool liq = c->cfg.liq_dem();
+    if (c->cfg.precision == SPHDEM_PREC_MIXED && (phase == SPHDEM_PHASE_MIDDLE || phase == SPHDEM_PHASE_END)) {
+        run_phase_mixed(c, phase);
+        return;
+    }
     switch (phase) {
         case SPHDEM_HOOK_BEFORE_START:
             globals_op(c, OP_STEP_INC);
@@ -406,6 +454,27 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
         SPHDEM_CUDA_CHECK(cudaDeviceSynchronize());
         run_h_derived(c);
         rebuild(c);
+        if (cfg->precision == SPHDEM_PREC_MIXED) {
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_pos, capacity * sizeof(float4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_vel, capacity * sizeof(float4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_aux, capacity * sizeof(float4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_tg, capacity * sizeof(int)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_om, capacity * sizeof(float)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_ncnt, capacity * sizeof(int)));
+            SPHDEM_CUDA_CHECK(cudaMemset(c->mx_om, 0, capacity * sizeof(float)));
+            SPHDEM_CUDA_CHECK(cudaMemset(c->mx_ncnt, 0, capacity * sizeof(int)));
+            SPHDEM_CUDA_CHECK(cudaDeviceSynchronize());
+            mixed::pack(c);
+            const int m = mixed::nlist_max_count(c);
+            if (m > 0) {
+                /* headroom for compression; a run that outgrows it stops with
+                 * SPHDEM_ERR_CAPACITY rather than dropping neighbours */
+                int maxn = std::max(32, (int)(1.6 * m) + 16);
+                maxn = (maxn + 31) / 32 * 32;
+                c->mx_maxn = maxn;
+                SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_nbr, (size_t)maxn * capacity * sizeof(int)));
+            }
+        }
         int rc = check_device(c);
         if (rc != SPHDEM_OK) {
             g_create_err = c->err;
@@ -481,6 +550,10 @@ int sphdem_rebuild(sphdem_handle h) {
     if (!h) return SPHDEM_ERR_INVALID;
     try {
         rebuild(h);
+        if (h->mx_maxn > 0) {
+            mixed::pack(h);
+            mixed::nlist(h);
+        }
     } catch (const std::string &e) {
         return fail(h, SPHDEM_ERR_CUDA, e);
     }

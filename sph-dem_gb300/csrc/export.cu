@@ -40,11 +40,12 @@ __device__ __forceinline__ CellCoord cell_dem(const DevCfg &c, const double *r) 
 
 /* mode 0: count, 1: write (tag-order rows at offs[tag]) */
 __global__ void k_pairs(DevCfg c, DevState s, const int *start, const DevGlobals *g, int64_t n, int kind,
-                        int mode, int *cnt, const long long *offs, int *idx) {
+                        int mode, int *cnt, const long long *offs, int *idx, int skip_listed) {
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (a >= n) return;
     const int ta = s.irow(FI_IAM)[a];
     if (ta == T_DEAD) return;
+    if (skip_listed && is_sph_or_sphb(ta)) return;  /* these rows come from the neighbour lists */
     const bool dem = c.liq_dem() && ta == T_DEM;
     const int tag = s.irow(FI_TAG)[a];
     double ra[3] = {0, 0, 0};
@@ -140,8 +141,11 @@ int export_pairs(sphdem_ctx *c, int kind, int64_t *offs, int32_t *idx, int64_t c
     int *didx = nullptr;
     SPHDEM_CUDA_CHECK(cudaMalloc(&dcnt, n * sizeof(int)));
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(dcnt, 0, n * sizeof(int), c->stream));
+    /* mixed precision: sph/sphBoundary rows come from the FP32-built lists */
+    const bool from_list = kind == SPHDEM_PAIRS_SPH && c->mx_maxn > 0;
     k_pairs<<<grid_for(n, BLK), BLK, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->g, n, kind, 0, dcnt, nullptr,
-                                                     nullptr);
+                                                     nullptr, (int)from_list);
+    if (from_list) mixed_list_export(c, dcnt, nullptr, nullptr);
     std::vector<int> hcnt(n);
     SPHDEM_CUDA_CHECK(cudaMemcpyAsync(hcnt.data(), dcnt, n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
@@ -160,7 +164,8 @@ int export_pairs(sphdem_ctx *c, int kind, int64_t *offs, int32_t *idx, int64_t c
             SPHDEM_CUDA_CHECK(cudaMemcpyAsync(doffs, hoffs.data(), (n + 1) * sizeof(long long),
                                               cudaMemcpyHostToDevice, c->stream));
             k_pairs<<<grid_for(n, BLK), BLK, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->g, n, kind, 1, dcnt,
-                                                             doffs, didx);
+                                                             doffs, didx, (int)from_list);
+            if (from_list) mixed_list_export(c, dcnt, doffs, didx);
             SPHDEM_CUDA_CHECK(cudaMemcpyAsync(idx, didx, hoffs[n] * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
             SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
             for (int64_t i = 0; i < n; i++) std::sort(idx + hoffs[i], idx + hoffs[i + 1]);

@@ -57,9 +57,13 @@ struct sphdem_ctx {
     std::vector<std::string> kt_names;
     std::vector<double> kt_ms;
     std::vector<long long> kt_count;
-    /* mixed precision packed inputs */
+    /* mixed precision: packed FP32 particle records and neighbour lists */
     float4 *mx_pos = nullptr, *mx_vel = nullptr, *mx_aux = nullptr;
-    float *mx_out = nullptr;
+    int *mx_tg = nullptr;       /* type | ghost code << 8 */
+    float *mx_om = nullptr;     /* Omega (VAR_H_CORRECTION) */
+    int *mx_nbr = nullptr;      /* column-major lists, mx_maxn x cap */
+    int *mx_ncnt = nullptr;
+    int mx_maxn = 0;
 };
 
 namespace sphdem {
@@ -92,6 +96,22 @@ void run_force(sphdem_ctx *c);         /* calcForce + accelCondition        */
 void run_dem_accel(sphdem_ctx *c);
 void run_dddt(sphdem_ctx *c);          /* calcDddtDudt                      */
 void run_dem_end(sphdem_ctx *c);       /* calcFPI + calcDEMContacts         */
+
+void zero_dem_shep(sphdem_ctx *c);
+void mixed_list_export(sphdem_ctx *c, int *cnt, const long long *offs, int *idx);
+
+/* pairs32.cu: mixed-precision passes */
+namespace mixed {
+void pack(sphdem_ctx *c);
+void nlist(sphdem_ctx *c);
+int nlist_max_count(sphdem_ctx *c);
+void omega_eos(sphdem_ctx *c, bool omega, bool eos);
+void force(sphdem_ctx *c);
+void dddt(sphdem_ctx *c);
+void porosity(sphdem_ctx *c);
+void dem_drag(sphdem_ctx *c);
+void dem_end(sphdem_ctx *c);
+}  // namespace mixed
 
 /* export.cu */
 int export_pairs(sphdem_ctx *c, int kind, int64_t *offs, int32_t *idx, int64_t cap, int64_t *np);

@@ -648,8 +648,11 @@ __global__ void k_dem_end(DevCfg c, DevState s, const int *start, const DevGloba
 
 }  // namespace
 
-void run_porosity(sphdem_ctx *c) {
+void zero_dem_shep(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "zero_dem_shep", k_zero_dem_shep, grid_for(c->n, 256), 256, 0, c->A, c->n);
+}
+void run_porosity(sphdem_ctx *c) {
+    zero_dem_shep(c);
     SPHDEM_LAUNCH(c, "porosity_fp64", k_porosity, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, c->buf.start, c->g, c->n);
 }
 void run_dem_drag(sphdem_ctx *c) {
