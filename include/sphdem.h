@@ -227,6 +227,12 @@ int sphdem_kernel_times_reset(sphdem_handle h, int enable);
 /* Time `nsteps` full steps on the handle's stream with CUDA events. */
 int sphdem_time_steps(sphdem_handle h, int nsteps, double *ms);
 
+/* Page-locked host buffers for get/set_fields: transfers from and to them run
+ * at full link bandwidth.  (No counterpart in the reference, which has no
+ * device; a convenience for callers that stream fields every step.) */
+int sphdem_alloc_host(size_t bytes, void **ptr);
+int sphdem_free_host(void *ptr);
+
 int sphdem_last_error(sphdem_handle h, char *buf, size_t len);
 const char *sphdem_version(void);
 

@@ -242,6 +242,7 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->mx_om);
     cudaFree(c->mx_nbr);
     cudaFree(c->mx_ncnt);
+    cudaFree(c->stage);
     for (int k = 0; k < 2; k++)
         if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -646,55 +647,44 @@ const FieldMap kFields[] = {
 int sphdem_get_fields(sphdem_handle h, uint32_t mask, SphDemParticles *out) {
     if (!h || !out) return SPHDEM_ERR_INVALID;
     if (out->n != h->n) return fail(h, SPHDEM_ERR_INVALID, "particle count mismatch");
-    const int64_t n = h->n;
-    if (cudaStreamSynchronize(h->stream) != cudaSuccess) return fail(h, SPHDEM_ERR_CUDA, "stream failed");
-    std::vector<int> tag(n), iam(n);
-    std::vector<double> row(n);
-    cudaMemcpy(tag.data(), h->A.irow(FI_TAG), n * sizeof(int), cudaMemcpyDeviceToHost);
-    cudaMemcpy(iam.data(), h->A.irow(FI_IAM), n * sizeof(int), cudaMemcpyDeviceToHost);
-    if (out->iam && (mask & SPHDEM_FIELD_IAM))
-        for (int64_t k = 0; k < n; k++) out->iam[tag[k]] = iam[k];
-    if (out->tag)
-        for (int64_t k = 0; k < n; k++) out->tag[tag[k]] = tag[k] + 1;
-    for (const FieldMap &fm : kFields) {
-        if (!(mask & fm.bit)) continue;
-        double *dst = out->*fm.ptr;
-        if (!dst) continue;
-        for (int d = 0; d < fm.ncomp; d++) {
-            cudaMemcpy(row.data(), h->A.row(fm.row + d), n * sizeof(double), cudaMemcpyDeviceToHost);
-            if (fm.ncomp == 3)
-                for (int64_t k = 0; k < n; k++) dst[3 * (int64_t)tag[k] + d] = row[k];
-            else
-                for (int64_t k = 0; k < n; k++) dst[tag[k]] = row[k];
+    try {
+        if (out->iam && (mask & SPHDEM_FIELD_IAM)) field_get_int(h, FI_IAM, out->iam);
+        if (out->tag)
+            for (int64_t k = 0; k < h->n; k++) out->tag[k] = (int32_t)(k + 1);
+        for (const FieldMap &fm : kFields) {
+            if (!(mask & fm.bit)) continue;
+            double *dst = out->*fm.ptr;
+            if (dst) field_get(h, fm.row, fm.ncomp, dst);
         }
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
     }
-    if (cudaGetLastError() != cudaSuccess) return fail(h, SPHDEM_ERR_CUDA, "copy failed");
     return SPHDEM_OK;
 }
 
 int sphdem_set_fields(sphdem_handle h, uint32_t mask, const SphDemParticles *in) {
     if (!h || !in) return SPHDEM_ERR_INVALID;
     if (in->n != h->n) return fail(h, SPHDEM_ERR_INVALID, "particle count mismatch");
-    const int64_t n = h->n;
-    cudaStreamSynchronize(h->stream);
-    std::vector<int> tag(n);
-    std::vector<double> row(n);
-    cudaMemcpy(tag.data(), h->A.irow(FI_TAG), n * sizeof(int), cudaMemcpyDeviceToHost);
-    for (const FieldMap &fm : kFields) {
-        if (!(mask & fm.bit)) continue;
-        const double *src = in->*fm.ptr;
-        if (!src) continue;
-        for (int d = 0; d < fm.ncomp; d++) {
-            if (fm.ncomp == 3)
-                for (int64_t k = 0; k < n; k++) row[k] = src[3 * (int64_t)tag[k] + d];
-            else
-                for (int64_t k = 0; k < n; k++) row[k] = src[tag[k]];
-            cudaMemcpy(h->A.row(fm.row + d), row.data(), n * sizeof(double), cudaMemcpyHostToDevice);
+    try {
+        for (const FieldMap &fm : kFields) {
+            if (!(mask & fm.bit)) continue;
+            const double *src = in->*fm.ptr;
+            if (src) field_set(h, fm.row, fm.ncomp, src);
         }
+        if (mask & SPHDEM_FIELD_H) run_h_derived(h);
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
     }
-    cudaDeviceSynchronize();
-    if (mask & SPHDEM_FIELD_H) run_h_derived(h);
     return check_device(h);
+}
+
+int sphdem_alloc_host(size_t bytes, void **ptr) {
+    if (!ptr) return SPHDEM_ERR_INVALID;
+    return cudaHostAlloc(ptr, bytes, cudaHostAllocDefault) == cudaSuccess ? SPHDEM_OK : SPHDEM_ERR_CUDA;
+}
+
+int sphdem_free_host(void *ptr) {
+    return cudaFreeHost(ptr) == cudaSuccess ? SPHDEM_OK : SPHDEM_ERR_CUDA;
 }
 
 int sphdem_pairs(sphdem_handle h, int kind, int64_t *offsets, int32_t *idx, int64_t idx_capacity, int64_t *n_pairs) {

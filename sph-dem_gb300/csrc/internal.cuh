@@ -64,6 +64,8 @@ struct sphdem_ctx {
     int *mx_nbr = nullptr;      /* column-major lists, mx_maxn x cap */
     int *mx_ncnt = nullptr;
     int mx_maxn = 0;
+    /* staging buffer for field transfers in tag order */
+    double *stage = nullptr;
 };
 
 namespace sphdem {
@@ -112,6 +114,11 @@ void porosity(sphdem_ctx *c);
 void dem_drag(sphdem_ctx *c);
 void dem_end(sphdem_ctx *c);
 }  // namespace mixed
+
+/* fields.cu */
+void field_get(sphdem_ctx *c, int row, int ncomp, double *host);
+void field_set(sphdem_ctx *c, int row, int ncomp, const double *host);
+void field_get_int(sphdem_ctx *c, int row, int *host);
 
 /* export.cu */
 int export_pairs(sphdem_ctx *c, int kind, int64_t *offs, int32_t *idx, int64_t cap, int64_t *np);
