@@ -1,0 +1,337 @@
+"""Benchmark of the SPH-DEM per-step hot path on one GB300 (one JSON line).
+
+Workload: the 3D coupled SPH-DEM sedimentation configuration -- 1,024,000
+fluid particles (dx = 2.5 mm, h = 1.5 dx, periodic x/y box 0.2 x 0.2 x 0.4
+with a bottom wall of 6,400 repulsive boundary particles) and 50,000 DEM
+spheres of radius 0.5 dx seeded in the top half; Wendland C2, Morris
+viscosity, Omega correction, porosity-weighted Tait EOS, Di Felice drag,
+linear spring-dashpot contacts, fixed dt.  Synthetic, seeded inputs.
+
+  value     particle-steps/s of the mixed-precision path, state resident in
+            HBM (1.05M particles x ~1 GB of state, larger than L2), K steps
+            timed with CUDA events around replays of the captured step graph
+  e2e       the same metric through the C ABI with host buffers: create the
+            simulation from pinned host arrays, then every step run it and
+            read positions and densities back into pinned host arrays
+  fp64      the plain-FP64 GPU path on the same input (a few steps)
+  error     mixed vs FP64 after the same steps: max |drho|/rho0 and
+            max |df| / max |f|
+  roofline  the dominant kernel (force pass) from live per-launch CUDA
+            events; HBM fraction of its compulsory bytes and FP32-pipe
+            fraction of its pair FLOPs
+  cpu_baseline  the CPU oracle port (a restatement of the reference's own
+            C++ step) on a 1/16 periodic sub-box of the same workload
+
+  python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "sph-dem_gb300"))
+sys.path.insert(0, REPO)
+
+import numpy as np  # noqa: E402
+
+METRIC = "particle-steps/s (mixed-precision SPH-DEM step, 1 GPU)"
+UNIT = "particle-steps/s"
+SM_COUNT = 152
+FP32_LANES = 128
+# FLOPs per listed pair of the force pass (kernel evaluations for h_a and h_b,
+# Morris viscosity, pressure; counted from k_force32's FP32 instruction mix)
+FORCE_FLOP_PER_PAIR = 80.0
+
+
+def workload_case(small: bool = False):
+    from sphdem import cases
+    if small:
+        # 1/16 periodic sub-box of the same workload: same dx, height, DEM density
+        return cases.sediment3d(nx=20, L=0.05, height=0.4, n_dem=3125, seed=3, nsteps=2)
+    return cases.sediment3d(seed=3)
+
+
+def workload_config(case, nsteps):
+    n = case.n
+    nd = int((case.particles["iam"] == 11).sum())
+    return {
+        "workload": "sediment3d_coupled_1M: 3D SPH-DEM sedimentation, periodic x/y 0.2x0.2x0.4 box",
+        "n_particles": n, "n_fluid": case.notes["n_fluid"], "n_boundary": case.notes["n_boundary"],
+        "n_dem": nd, "dx": case.cfg["psep"], "dt": case.cfg["maxdt"],
+        "dem_radius": case.notes["dem_radius"], "coupling_radius": case.notes["coupling_radius"],
+        "viscosity_kinematic": case.cfg["viscosity"], "steps": nsteps,
+        "precision": "mixed (FP32 pair math on FP64-cell-origin offsets, FP64 integration)",
+        "l2_policy": "inputs larger than L2 (state > 1 GB, L2 129 MB)",
+        "parallelism": "single GPU",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            return json.load(fh), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def force_bytes_per_particle(avg_pairs: float) -> float:
+    """Compulsory bytes of k_force32 per target particle: packed inputs
+    (3 float4 = 48 B), type word, list length, Omega (4 B each), the list
+    itself (4 B per pair), and read+write of f, fp, fv, fb (FP64, 3 comps)."""
+    return 48 + 4 + 4 + 4 + 4.0 * avg_pairs + 4 * 3 * 8 * 2
+
+
+# --------------------------------------------------------------------------
+def cpu_sample_worker(args):
+    """Time the CPU oracle port on the sub-box sample (test infrastructure as
+    the CPU baseline)."""
+    steps, warm = args
+    from oracle.port_api import OracleSim
+    case = workload_case(small=True)
+    o = OracleSim(case.cfg, case.particles)
+    o.step(warm)
+    t0 = time.perf_counter()
+    o.step(steps)
+    t = time.perf_counter() - t0
+    return case.n, steps, t
+
+
+def cpu_baseline(steps=2, warm=1, procs=1):
+    from oracle import build_oracle
+    build_oracle.build()
+    if procs == 1:
+        n, s, t = cpu_sample_worker((steps, warm))
+        return n * s / t, n, s, t
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(procs) as pool:
+        res = pool.map(cpu_sample_worker, [(steps, warm)] * procs)
+    agg = sum(n * s / t for n, s, t in res)
+    return agg, res[0][0], steps, max(t for _, _, t in res)
+
+
+# --------------------------------------------------------------------------
+def run_reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    procs = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 2))
+    value, n, s, t = cpu_baseline(steps=steps, warm=1, procs=procs)
+    sample = (f"CPU oracle port (restatement of the reference's C++ step, single-threaded per "
+              f"process) on a 1/16 periodic sub-box of the workload ({n} particles), "
+              f"{procs} independent processes x {s} steps after 1 warm-up step")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / s,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)", "config": workload_config(workload_case(), args.steps),
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world):
+    import __graft_entry__
+    __graft_entry__.build()
+    from sphdem import capi, cases
+    lib = capi.Library()
+    case = workload_case()
+    n = case.n
+    out_dir = os.path.join(REPO, "gpurun_out")
+    os.makedirs(out_dir, exist_ok=True)
+
+    # ---- mixed precision, device-resident --------------------------------
+    sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    sim.step(args.warmup)
+    with ClockSampler(os.path.join(out_dir, "bench_clocks.csv")) as clk:
+        ms = sim.time_steps(args.steps)
+    clocks = clk.summary()
+    value = n * args.steps / (ms * 1e-3)
+    st = sim.stats()
+
+    # per-kernel device times (CUDA events around each launch), 2 steps
+    sim.kernel_times_reset(True)
+    sim.step(2)
+    kt = sim.kernel_times()
+    sim.kernel_times_reset(False)
+    launches_per_step = sum(c for _, c in kt.values()) / 2.0
+    total_ms = sum(m for m, _ in kt.values())
+    top = sorted(kt.items(), key=lambda kv: -kv[1][0])
+    force_ms, force_launches = kt.get("force32", (float("nan"), 1))
+    force_ms_per_launch = force_ms / max(1, force_launches)
+
+    peaks, peak_kind = measured_peaks()
+    avg_pairs = st.n_list_pairs / max(1, case.notes["n_fluid"] + case.notes["n_boundary"])
+    targets = case.notes["n_fluid"]
+    alg_bytes = force_bytes_per_particle(avg_pairs) * targets
+    achieved_gbs = alg_bytes / (force_ms_per_launch * 1e-3) / 1e9
+    sm_mhz = clocks.get("sm_max_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    fp32_peak = SM_COUNT * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
+    flops = FORCE_FLOP_PER_PAIR * st.n_list_pairs
+    achieved_tf = flops / (force_ms_per_launch * 1e-3) / 1e12
+    traffic = None
+    tpath = os.path.join(REPO, "profiles", "force32_traffic.json")
+    if os.path.exists(tpath):
+        try:
+            traffic = json.load(open(tpath)).get("bytes_per_launch_full")
+        except Exception:
+            traffic = None
+
+    # ---- mixed vs FP64 on the same input ---------------------------------
+    fp64_steps = max(1, min(args.fp64_steps, args.steps))
+    ref = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_FP64)
+    ref.step(1)
+    ms64 = ref.time_steps(fp64_steps)  # steps 2 .. fp64_steps+2 (one more inside for the graph)
+    fp64_value = n * fp64_steps / (ms64 * 1e-3)
+    ref_steps = 2 + fp64_steps
+    cmp = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    cmp.step(ref_steps)
+    a = cmp.get(capi.FIELD_DENS | capi.FIELD_F)
+    b = ref.get(capi.FIELD_DENS | capi.FIELD_F)
+    err_dens = float(np.abs(a["dens"] - b["dens"]).max() / case.cfg["dens"])
+    err_f = float(np.abs(a["f"] - b["f"]).max() / np.abs(b["f"]).max())
+    ref.close()
+    cmp.close()
+
+    # ---- end to end through the C ABI with host buffers -------------------
+    e2e_steps = args.steps
+    init = capi.ParticleBuffers(n, case.particles, pinned=lib)
+    outbuf = capi.ParticleBuffers(n, pinned=lib, fields=("r", "dens"))
+    import ctypes as C
+    cfgs = capi.config_struct(case.cfg, cases.PREC_MIXED)
+    t0 = time.perf_counter()
+    h = C.c_void_p()
+    lib.check(lib.lib.sphdem_create(C.byref(cfgs), init.ref(), n, C.byref(h)), None, "create")
+    for _ in range(e2e_steps):
+        lib.check(lib.lib.sphdem_step(h, 1), h, "step")
+        lib.check(lib.lib.sphdem_get_fields(h, capi.FIELD_R | capi.FIELD_DENS, outbuf.ref()), h, "get")
+    t_e2e = time.perf_counter() - t0
+    lib.lib.sphdem_destroy(h)
+    e2e_value = n * e2e_steps / t_e2e
+    h2d_bytes = n * (4 * 3 * 8 + 4 * 8 + 12)  # r, v, norms x3 (3 comps) + mass, dens, h, radius + ints
+    d2h_bytes = n * (3 * 8 + 8)
+
+    # ---- CPU baseline (oracle port, 1 core, bounded sample) ---------------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cv, cn, cs, ct = cpu_baseline(steps=args.cpu_steps, warm=1, procs=1)
+        cpu = {"value": cv, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"CPU oracle port on a 1/16 periodic sub-box of the workload ({cn} particles, "
+                         f"same dx/physics), {cs} steps after 1 warm-up step, {ct:.1f} s"}
+
+    sim.close()
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic (seeded)",
+        "config": workload_config(case, args.steps),
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d_bytes / e2e_steps),
+                "d2h_bytes_per_step": int(d2h_bytes),
+                "what": "sphdem_create from pinned host arrays + per step sphdem_step + sphdem_get_fields(r, dens) "
+                        "into pinned host arrays, wall clock"},
+        "fp64": {"value": fp64_value, "unit": UNIT, "steps": fp64_steps,
+                 "mixed_over_fp64": value / fp64_value},
+        "error_vs_fp64": {"steps": ref_steps, "max_abs_drho_over_rho0": err_dens,
+                          "max_abs_df_over_max_f": err_f},
+        "adjoint_over_forward": None,
+        "roofline": {
+            "kernel": "force32", "bound": "hbm", "achieved": achieved_gbs, "peak": peaks.get("hbm_gbs"),
+            "unit": "GB/s", "frac": achieved_gbs / peaks.get("hbm_gbs", 6800.0), "traffic": traffic,
+            "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes,
+            "ms_per_launch": force_ms_per_launch, "avg_list_pairs": avg_pairs,
+            "fp32_pipe": {"achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                          "frac": achieved_tf / fp32_peak,
+                          "peak_basis": f"{SM_COUNT} SMs x {FP32_LANES} lanes x 2 x {sm_mhz:.0f} MHz"},
+        },
+        "kernels_ms_per_step": {k: v[0] / 2.0 for k, v in top[:12]},
+        "kernel_share": {k: v[0] / total_ms for k, v in top[:12]},
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    if args.impl == "reference":
+        run_reference_arm(args, rank, world)
+    else:
+        if world > 1:
+            os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

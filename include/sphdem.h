@@ -160,6 +160,15 @@ typedef struct SphDemGlobals {
     int64_t n_deleted;       /* particles removed for leaving the domain (dataLL.cpp:381-386) */
 } SphDemGlobals;
 
+/* Sizes of the current rebuild, for reporting and roofline arithmetic. */
+typedef struct SphDemStats {
+    int64_t n_particles, n_alive;
+    int64_t n_list_pairs;    /* sum of the neighbour-list lengths (mixed precision) */
+    int64_t list_depth;      /* allocated entries per particle                      */
+    int64_t n_sph_cells, n_dem_cells;
+    double  h_max, search_radius;
+} SphDemStats;
+
 /* Phases and built-in hook points, in the order run.cpp:112-118 calls them. */
 #define SPHDEM_HOOK_BEFORE_START   0
 #define SPHDEM_PHASE_START         1
@@ -199,6 +208,7 @@ int sphdem_step(sphdem_handle h, int nsteps);
 int sphdem_get_fields(sphdem_handle h, uint32_t mask, SphDemParticles *out);
 int sphdem_set_fields(sphdem_handle h, uint32_t mask, const SphDemParticles *in);
 int sphdem_get_globals(sphdem_handle h, SphDemGlobals *out);
+int sphdem_get_stats(sphdem_handle h, SphDemStats *out);
 int sphdem_set_globals(sphdem_handle h, const SphDemGlobals *in);
 
 /* Rebuild the bucket lists at the current positions (CdataLL::reset,

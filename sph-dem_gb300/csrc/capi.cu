@@ -596,6 +596,30 @@ int sphdem_get_globals(sphdem_handle h, SphDemGlobals *out) {
     return SPHDEM_OK;
 }
 
+int sphdem_get_stats(sphdem_handle h, SphDemStats *out) {
+    if (!h || !out) return SPHDEM_ERR_INVALID;
+    cudaStreamSynchronize(h->stream);
+    DevGlobals hg;
+    cudaMemcpy(&hg, h->g, sizeof(hg), cudaMemcpyDeviceToHost);
+    std::memset(out, 0, sizeof(*out));
+    out->n_particles = h->n;
+    std::vector<int> iam(h->n);
+    cudaMemcpy(iam.data(), h->A.irow(FI_IAM), h->n * sizeof(int), cudaMemcpyDeviceToHost);
+    for (int t : iam) out->n_alive += t != T_DEAD;
+    if (h->mx_maxn > 0) {
+        std::vector<int> cnt(h->n);
+        cudaMemcpy(cnt.data(), h->mx_ncnt, h->n * sizeof(int), cudaMemcpyDeviceToHost);
+        for (int64_t k = 0; k < h->n; k++)
+            if (sphdem::is_sph_or_sphb(iam[k])) out->n_list_pairs += cnt[k];
+    }
+    out->list_depth = h->mx_maxn;
+    out->n_sph_cells = hg.n_sph_cells;
+    out->n_dem_cells = h->cfg.n_dem_cells;
+    out->h_max = hg.hmax;
+    out->search_radius = hg.sr;
+    return cudaGetLastError() == cudaSuccess ? SPHDEM_OK : SPHDEM_ERR_CUDA;
+}
+
 int sphdem_set_globals(sphdem_handle h, const SphDemGlobals *in) {
     if (!h || !in) return SPHDEM_ERR_INVALID;
     DevGlobals hg;

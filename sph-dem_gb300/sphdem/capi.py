@@ -86,6 +86,12 @@ class SphDemGlobals(C.Structure):
                 ("sph_step", C.c_int64), ("n_deleted", C.c_int64)]
 
 
+class SphDemStats(C.Structure):
+    _fields_ = [("n_particles", C.c_int64), ("n_alive", C.c_int64), ("n_list_pairs", C.c_int64),
+                ("list_depth", C.c_int64), ("n_sph_cells", C.c_int64), ("n_dem_cells", C.c_int64),
+                ("h_max", C.c_double), ("search_radius", C.c_double)]
+
+
 VEC_FIELDS = ("r", "v", "vhat", "norm1", "norm2", "norm3", "f", "fp", "fv", "fb",
               "fdrag", "fvel", "grad_porosity", "v0", "vhat0")
 SCA_FIELDS = ("mass", "dens", "h", "radius", "dddt", "press", "pdr2", "porosity",
@@ -111,18 +117,28 @@ def config_struct(cfg: dict, precision: int | None = None) -> SphDemConfig:
 
 
 class ParticleBuffers:
-    """numpy storage behind a SphDemParticles (all fields allocated)."""
+    """numpy storage behind a SphDemParticles (all fields allocated).
 
-    def __init__(self, n: int, init: dict | None = None):
+    With `pinned` (a Library), the field arrays live in page-locked host
+    memory from sphdem_alloc_host, so get/set_fields run at link bandwidth."""
+
+    def __init__(self, n: int, init: dict | None = None, pinned: "Library | None" = None,
+                 fields: tuple | None = None):
         self.n = n
+        self._pinned = []
+        self._lib = pinned
         self.arrays: dict[str, np.ndarray] = {
             "iam": np.zeros(n, np.int32), "tag": np.arange(1, n + 1, dtype=np.int32),
             "concave": np.ones(n, np.uint8),
         }
         for k in VEC_FIELDS:
-            self.arrays[k] = np.zeros((n, 3), np.float64)
+            if fields is not None and k not in fields:
+                continue
+            self.arrays[k] = self._alloc((n, 3))
         for k in SCA_FIELDS:
-            self.arrays[k] = np.zeros(n, np.float64)
+            if fields is not None and k not in fields:
+                continue
+            self.arrays[k] = self._alloc((n,))
         if init is not None:
             for k, v in init.items():
                 if k in self.arrays:
@@ -132,10 +148,30 @@ class ParticleBuffers:
         self.struct = SphDemParticles()
         self.struct.n = n
         for name, ctype in SphDemParticles._fields_:
-            if name == "n":
+            if name == "n" or name not in self.arrays:
                 continue
             a = self.arrays[name]
             setattr(self.struct, name, a.ctypes.data_as(ctype))
+
+    def _alloc(self, shape):
+        if self._lib is None:
+            return np.zeros(shape, np.float64)
+        nbytes = int(np.prod(shape)) * 8
+        p = C.c_void_p()
+        if self._lib.lib.sphdem_alloc_host(nbytes, C.byref(p)) != 0:
+            raise SphDemError("sphdem_alloc_host failed")
+        self._pinned.append(p)
+        buf = (C.c_double * int(np.prod(shape))).from_address(p.value)
+        a = np.frombuffer(buf, np.float64).reshape(shape)
+        a[...] = 0.0
+        return a
+
+    def __del__(self):
+        for p in getattr(self, "_pinned", []):
+            try:
+                self._lib.lib.sphdem_free_host(p)
+            except Exception:
+                pass
 
     def __getitem__(self, k):
         return self.arrays[k]
@@ -177,6 +213,9 @@ class Library:
         L.sphdem_time_steps.argtypes = [H, C.c_int, C.POINTER(C.c_double)]
         L.sphdem_last_error.argtypes = [H, C.c_char_p, C.c_size_t]
         L.sphdem_version.restype = C.c_char_p
+        L.sphdem_get_stats.argtypes = [H, C.POINTER(SphDemStats)]
+        L.sphdem_alloc_host.argtypes = [C.c_size_t, C.POINTER(C.c_void_p)]
+        L.sphdem_free_host.argtypes = [C.c_void_p]
 
     def check(self, rc: int, h=None, what: str = ""):
         if rc != OK:
@@ -219,8 +258,8 @@ class Simulation:
     def rebuild(self):
         self.L.check(self.L.lib.sphdem_rebuild(self.h), self.h, "sphdem_rebuild")
 
-    def get(self, mask: int = FIELD_ALL) -> ParticleBuffers:
-        out = ParticleBuffers(self.n)
+    def get(self, mask: int = FIELD_ALL, out: ParticleBuffers | None = None) -> ParticleBuffers:
+        out = out or ParticleBuffers(self.n)
         self.L.check(self.L.lib.sphdem_get_fields(self.h, mask, out.ref()), self.h, "get_fields")
         return out
 
@@ -231,6 +270,11 @@ class Simulation:
         g = SphDemGlobals()
         self.L.check(self.L.lib.sphdem_get_globals(self.h, C.byref(g)), self.h, "get_globals")
         return g
+
+    def stats(self) -> SphDemStats:
+        st = SphDemStats()
+        self.L.check(self.L.lib.sphdem_get_stats(self.h, C.byref(st)), self.h, "get_stats")
+        return st
 
     def pairs(self, kind: int):
         offs = np.zeros(self.n + 1, np.int64)
