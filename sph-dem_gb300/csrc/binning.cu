@@ -32,34 +32,45 @@ namespace {
 constexpr int BLK = 256;
 
 __global__ void k_migrate(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
+    __shared__ unsigned long long bmax;
+    if (threadIdx.x == 0) bmax = 0ull;
+    __syncthreads();
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    int *iam = s.irow(FI_IAM);
-    if (iam[i] == T_DEAD) return;
-    int oc[3] = {1, 1, 1};
-    bool lost = false, out = false;
-    for (int d = 0; d < c.nd; d++) {
-        const double r = s.row(FD_R + d)[i];
-        oc[d] = trunc_index(r, c.dmin[d], c.dspace[d], c.rdspace_f[d], 1.0);
-        if (oc[d] > 2 || oc[d] < 0) lost = true;
-        if (oc[d] != 1) {
-            out = true;
-            if (!c.periodic[d]) lost = true;
+    double h = -1.0;
+    if (i < n) {
+        int *iam = s.irow(FI_IAM);
+        if (iam[i] != T_DEAD) {
+            int oc[3] = {1, 1, 1};
+            bool lost = false, out = false;
+            for (int d = 0; d < c.nd; d++) {
+                const double r = s.row(FD_R + d)[i];
+                oc[d] = trunc_index(r, c.dmin[d], c.dspace[d], c.rdspace_f[d], 1.0);
+                if (oc[d] > 2 || oc[d] < 0) lost = true;
+                if (oc[d] != 1) {
+                    out = true;
+                    if (!c.periodic[d]) lost = true;
+                }
+            }
+            if (lost) {
+                iam[i] = T_DEAD;
+                atomicAdd((unsigned long long *)&g->n_deleted, 1ull);
+            } else {
+                if (out) {
+                    for (int d = 0; d < c.nd; d++) {
+                        double *r = s.row(FD_R + d);
+                        if (oc[d] == 2) r[i] = dadd(dsub(c.rmin[d], c.rmax[d]), r[i]);
+                        else if (oc[d] == 0) r[i] = dadd(dsub(c.rmax[d], c.rmin[d]), r[i]);
+                    }
+                }
+                h = s.row(FD_H)[i];
+            }
         }
     }
-    if (lost) {
-        iam[i] = T_DEAD;
-        atomicAdd((unsigned long long *)&g->n_deleted, 1ull);
-        return;
-    }
-    if (out) {
-        for (int d = 0; d < c.nd; d++) {
-            double *r = s.row(FD_R + d);
-            if (oc[d] == 2) r[i] = dadd(dsub(c.rmin[d], c.rmax[d]), r[i]);
-            else if (oc[d] == 0) r[i] = dadd(dsub(c.rmax[d], c.rmin[d]), r[i]);
-        }
-    }
-    atomic_max_pos(&g->hmax_bits, s.row(FD_H)[i]);
+    /* block maximum of h, then one atomic per block */
+    for (int o = 16; o > 0; o >>= 1) h = fmax(h, __shfl_xor_sync(0xffffffffu, h, o));
+    if ((threadIdx.x & 31) == 0 && h >= 0.0) atomicMax(&bmax, dbits(h));
+    __syncthreads();
+    if (threadIdx.x == 0 && bmax) atomicMax(&g->hmax_bits, bmax);
 }
 
 __device__ __forceinline__ int slot_index(const int *co, int nd) {

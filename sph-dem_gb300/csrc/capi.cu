@@ -243,6 +243,10 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->mx_nbr);
     cudaFree(c->mx_ncnt);
     cudaFree(c->stage);
+    cudaFree(c->mx_q0);
+    cudaFree(c->mx_q1);
+    cudaFree(c->mx_q2);
+    cudaFree(c->dcfg);
     for (int k = 0; k < 2; k++)
         if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -448,6 +452,8 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
             hg.ghost_sp[d] = sp;
             hg.ghost_rsp_f[d] = sp != 0 ? (float)(1.0 / sp) : 0.f;
         }
+        SPHDEM_CUDA_CHECK(cudaMalloc(&c->dcfg, sizeof(DevCfg)));
+        SPHDEM_CUDA_CHECK(cudaMemcpy(c->dcfg, &c->cfg, sizeof(DevCfg), cudaMemcpyHostToDevice));
         SPHDEM_CUDA_CHECK(cudaMalloc(&c->g, sizeof(DevGlobals)));
         SPHDEM_CUDA_CHECK(cudaMemcpy(c->g, &hg, sizeof(hg), cudaMemcpyHostToDevice));
         /* the uploads above ran on the legacy stream; the handle's stream is
@@ -462,6 +468,9 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_tg, capacity * sizeof(int)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_om, capacity * sizeof(float)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_ncnt, capacity * sizeof(int)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_q0, capacity * sizeof(float4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_q1, capacity * sizeof(float4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_q2, capacity * sizeof(float4)));
             SPHDEM_CUDA_CHECK(cudaMemset(c->mx_om, 0, capacity * sizeof(float)));
             SPHDEM_CUDA_CHECK(cudaMemset(c->mx_ncnt, 0, capacity * sizeof(int)));
             SPHDEM_CUDA_CHECK(cudaDeviceSynchronize());

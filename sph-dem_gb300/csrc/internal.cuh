@@ -64,6 +64,8 @@ struct sphdem_ctx {
     int *mx_nbr = nullptr;      /* column-major lists, mx_maxn x cap */
     int *mx_ncnt = nullptr;
     int mx_maxn = 0;
+    float4 *mx_q0 = nullptr, *mx_q1 = nullptr, *mx_q2 = nullptr;  /* FPI fields of fluid particles */
+    sphdem::DevCfg *dcfg = nullptr;  /* device copy of cfg for out-of-line helpers */
     /* staging buffer for field transfers in tag order */
     double *stage = nullptr;
 };
@@ -105,6 +107,7 @@ void mixed_list_export(sphdem_ctx *c, int *cnt, const long long *offs, int *idx)
 /* pairs32.cu: mixed-precision passes */
 namespace mixed {
 void pack(sphdem_ctx *c);
+void pack_fpi(sphdem_ctx *c);
 void nlist(sphdem_ctx *c);
 int nlist_max_count(sphdem_ctx *c);
 void omega_eos(sphdem_ctx *c, bool omega, bool eos);
