@@ -51,12 +51,32 @@ FP32_LANES = 128
 FORCE_FLOP_PER_PAIR = 80.0
 
 
-def workload_case(small: bool = False):
+def workload_case(small: bool = False, quarter: bool = False):
     from sphdem import cases
     if small:
         # 1/16 periodic sub-box of the same workload: same dx, height, DEM density
         return cases.sediment3d(nx=20, L=0.05, height=0.4, n_dem=3125, seed=3, nsteps=2)
+    if quarter:
+        # 1/4 periodic sub-box (270k particles): profiler captures
+        return cases.sediment3d(nx=40, L=0.1, height=0.4, n_dem=12500, seed=3, nsteps=2)
     return cases.sediment3d(seed=3)
+
+
+def run_profile(args):
+    """Mixed path only: warm-up steps then `steps` graph replays; the command
+    the ncu captures under profiles/ run."""
+    import __graft_entry__
+    __graft_entry__.build()
+    from sphdem import capi, cases
+    lib = capi.Library()
+    case = workload_case(quarter=args.quarter)
+    sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    sim.step(args.warmup)
+    ms = sim.time_steps(args.steps)
+    st = sim.stats()
+    print(json.dumps({"profile": True, "n": case.n, "ms_per_step": ms / args.steps,
+                      "list_pairs": st.n_list_pairs, "h_max": st.h_max,
+                      "search_radius": st.search_radius, "n_sph_cells": st.n_sph_cells}))
 
 
 def workload_config(case, nsteps):
@@ -297,6 +317,7 @@ def run_ours(args, rank, world):
             "unit": "GB/s", "frac": achieved_gbs / peaks.get("hbm_gbs", 6800.0), "traffic": traffic,
             "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes,
             "ms_per_launch": force_ms_per_launch, "avg_list_pairs": avg_pairs,
+            "h_max": st.h_max, "search_radius": st.search_radius, "n_sph_cells": st.n_sph_cells,
             "fp32_pipe": {"achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                           "frac": achieved_tf / fp32_peak,
                           "peak_basis": f"{SM_COUNT} SMs x {FP32_LANES} lanes x 2 x {sm_mhz:.0f} MHz"},
@@ -320,12 +341,16 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="mixed path only (for profiler captures)")
+    ap.add_argument("--quarter", action="store_true", help="with --profile: 1/4 sub-box of the workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference_arm(args, rank, world)
     else:
         if world > 1:

@@ -246,6 +246,9 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->mx_q0);
     cudaFree(c->mx_q1);
     cudaFree(c->mx_q2);
+    cudaFree(c->mx_dp);
+    cudaFree(c->mx_bandq);
+    cudaFree(c->mx_bandq_n);
     cudaFree(c->dcfg);
     for (int k = 0; k < 2; k++)
         if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
@@ -471,6 +474,10 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_q0, capacity * sizeof(float4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_q1, capacity * sizeof(float4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_q2, capacity * sizeof(float4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_dp, capacity * sizeof(float4)));
+            c->mx_bandq_cap = std::max<long long>(1 << 20, 8 * capacity);
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_bandq, c->mx_bandq_cap * sizeof(int4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_bandq_n, sizeof(unsigned long long)));
             SPHDEM_CUDA_CHECK(cudaMemset(c->mx_om, 0, capacity * sizeof(float)));
             SPHDEM_CUDA_CHECK(cudaMemset(c->mx_ncnt, 0, capacity * sizeof(int)));
             SPHDEM_CUDA_CHECK(cudaDeviceSynchronize());

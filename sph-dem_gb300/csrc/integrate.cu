@@ -45,9 +45,33 @@ __global__ void k_globals_op(DevCfg c, DevGlobals *g, int op) {
     }
 }
 
+/* h = HFAC (m/rho)^(1/NDIM) (sphIncompress.h:698-700).  The FP64 path calls
+ * pow like the reference; the mixed path takes an FP32 estimate of
+ * x^(-1/NDIM) and one FP64 Newton step (relative error ~1e-14), because FP64
+ * pow costs hundreds of FP64 operations on this GPU. */
+__device__ __forceinline__ double smoothing_length(const DevCfg &c, double x) {
+    if (c.precision != SPHDEM_PREC_MIXED) return c.hfac * pow(x, 1.0 / c.nd);
+    if (c.nd == 1) return c.hfac * x;
+    if (c.nd == 2) {
+        double z = (double)rsqrtf((float)x);
+        z = z * (1.5 - 0.5 * x * z * z);
+        return c.hfac * x * z;
+    }
+    double z = (double)(1.0f / cbrtf((float)x));
+    z = z * (4.0 - x * z * z * z) * (1.0 / 3.0);
+    return c.hfac * x * z * z;
+}
+
+/* 1/h by an FP32 estimate and one FP64 Newton step in the mixed path */
+__device__ __forceinline__ double recip(const DevCfg &c, double h) {
+    if (c.precision != SPHDEM_PREC_MIXED) return 1.0 / h;
+    double y = (double)(1.0f / (float)h);
+    return y * (2.0 - h * y);
+}
+
 __device__ __forceinline__ void h_derived(const DevCfg &c, const DevState &s, int64_t i) {
     const double h = s.row(FD_H)[i];
-    const double ih = 1.0 / h;
+    const double ih = recip(c, h);
     double ihn = ih;
     for (int d = 1; d < c.nd; d++) ihn *= ih;
     s.row(FD_IH)[i] = ih;
@@ -59,7 +83,7 @@ __device__ __forceinline__ void eos(const DevCfg &c, const DevState &s, int64_t 
     const double dens = s.row(FD_DENS)[i];
     double press;
     if (c.liq_dem()) {
-        const double x = dens / (c.refd * s.row(FD_POR)[i]);
+        const double x = dens * recip(c, c.refd * s.row(FD_POR)[i]);
         double xg;
         if (c.gamma == 7.0) {
             const double x2 = x * x;
@@ -73,8 +97,9 @@ __device__ __forceinline__ void eos(const DevCfg &c, const DevState &s, int64_t 
         const double x2 = x * x;
         press = c.prb * (x2 * x2 * x2 * x - 1.0);
     }
+    const double rd = recip(c, dens);
     s.row(FD_PRESS)[i] = press;
-    s.row(FD_PDR2)[i] = press / (dens * dens);
+    s.row(FD_PDR2)[i] = press * (rd * rd);
 }
 
 /* start(): driftRAndKick + driftRest + initSumsMiddle for sph/sphBoundary,
@@ -101,7 +126,7 @@ __global__ void k_start(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
         double *dens = s.row(FD_DENS);
         dens[i] += hd * s.row(FD_DDDT)[i];
         if (!(c.flags & SPHDEM_F_CONST_H)) {
-            s.row(FD_H)[i] = c.hfac * pow(s.row(FD_MASS)[i] / dens[i], 1.0 / c.nd);
+            s.row(FD_H)[i] = smoothing_length(c, s.row(FD_MASS)[i] * recip(c, dens[i]));
             h_derived(c, s, i);
         }
         for (int d = 0; d < 3; d++) {
@@ -207,7 +232,7 @@ __global__ void k_end_tail(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
         double *dens = s.row(FD_DENS);
         dens[i] += (dt / 2) * s.row(FD_DDDT)[i];
         if (!(c.flags & SPHDEM_F_CONST_H)) {
-            s.row(FD_H)[i] = c.hfac * pow(s.row(FD_MASS)[i] / dens[i], 1.0 / c.nd);
+            s.row(FD_H)[i] = smoothing_length(c, s.row(FD_MASS)[i] * recip(c, dens[i]));
             h_derived(c, s, i);
         }
         eos(c, s, i);

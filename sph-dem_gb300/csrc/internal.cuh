@@ -65,6 +65,10 @@ struct sphdem_ctx {
     int *mx_ncnt = nullptr;
     int mx_maxn = 0;
     float4 *mx_q0 = nullptr, *mx_q1 = nullptr, *mx_q2 = nullptr;  /* FPI fields of fluid particles */
+    float4 *mx_dp = nullptr;    /* (m/shep, fdrag) of DEM particles */
+    int4 *mx_bandq = nullptr;   /* neighbour candidates within the FP32 band */
+    unsigned long long *mx_bandq_n = nullptr;
+    long long mx_bandq_cap = 0;
     sphdem::DevCfg *dcfg = nullptr;  /* device copy of cfg for out-of-line helpers */
     /* staging buffer for field transfers in tag order */
     double *stage = nullptr;

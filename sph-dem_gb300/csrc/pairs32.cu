@@ -44,7 +44,10 @@ namespace {
 constexpr int BLK = 128;
 constexpr int B_BITS = 26;
 constexpr int B_MASK = (1 << B_BITS) - 1;
-constexpr float BAND = 4e-6f;
+/* FP32 error of r^2 from bucket offsets is below 6e-7 relative (offsets <
+ * one bucket, each rounded once; r^2 and (2h)^2 a few ulps); pairs within
+ * BAND of the cut-off are decided by the reference's FP64 predicate. */
+constexpr float BAND = 1e-6f;
 
 struct Kahan {
     float s, c;
@@ -227,7 +230,9 @@ template <int ND>
 __global__ void __launch_bounds__(BLK) k_nlist(DevCfg c, const DevCfg *__restrict__ cp, DevState s, const int *__restrict__ start,
                                                DevGlobals *__restrict__ g, const float4 *__restrict__ P0,
                                                const int *__restrict__ tg, int *__restrict__ nbr,
-                                               int *__restrict__ ncnt, int maxn, int64_t ld, int count_only) {
+                                               int *__restrict__ ncnt, int maxn, int64_t ld, int count_only,
+                                               int4 *__restrict__ bandq, unsigned long long *__restrict__ bandq_n,
+                                               long long bandq_cap) {
     const int lane = threadIdx.x & 31;
     const int warps = (blockDim.x >> 5) * gridDim.x;
     const int nsc = g->n_sph_cells;
@@ -268,12 +273,23 @@ __global__ void __launch_bounds__(BLK) k_nlist(DevCfg c, const DevCfg *__restric
                             const float T = t * t;
                             if (r2 > T * (1.f + BAND)) continue;
                             if (b == a && !shifted) continue;
-                            bool in = r2 < T * (1.f - BAND) || exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], 0.0, 0);
-                            if (in && shifted) in = img_ok<ND>(tg[b] >> 8, sh);
-                            if (in) {
-                                if (cnt < maxn) nbr[(int64_t)cnt * ld + a] = b | code;
-                                cnt++;
+                            if (shifted && !img_ok<ND>(tg[b] >> 8, sh)) continue;
+                            const bool band = r2 >= T * (1.f - BAND);
+                            if (cnt < maxn) {
+                                int e = b | code;
+                                if (band && !count_only) {
+                                    /* decided later, in one coalesced FP64 pass */
+                                    const unsigned long long slot = atomicAdd(bandq_n, 1ull);
+                                    if (slot < (unsigned long long)bandq_cap) {
+                                        bandq[slot] = make_int4(a, b, (sh[0] + 1) | ((sh[1] + 1) << 2) | ((sh[2] + 1) << 4), cnt);
+                                        e |= (int)0x80000000u;
+                                    } else {
+                                        set_err(g, SPHDEM_ERR_CAPACITY, -2);
+                                    }
+                                }
+                                if (!count_only) nbr[(int64_t)cnt * ld + a] = e;
                             }
+                            cnt++;
                         }
                     }
             if (act) {
@@ -282,6 +298,30 @@ __global__ void __launch_bounds__(BLK) k_nlist(DevCfg c, const DevCfg *__restric
                 if (cnt > maxn && !count_only) set_err(g, SPHDEM_ERR_CAPACITY, cnt);
             }
         }
+    }
+}
+
+/* Decide the queued band candidates with the reference's FP64 predicate:
+ * keep (clear the pending bit) or mark the list slot invalid (all ones). */
+template <int ND>
+__global__ void k_band_fix(DevCfg c, DevState s, const int4 *__restrict__ bandq,
+                           const unsigned long long *__restrict__ bandq_n, long long bandq_cap,
+                           int *__restrict__ nbr, int64_t ld) {
+    const unsigned long long nq = min(*bandq_n, (unsigned long long)bandq_cap);
+    for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < nq;
+         q += (unsigned long long)gridDim.x * blockDim.x) {
+        const int4 it = bandq[q];
+        const int a = it.x, b = it.y;
+        const int sh[3] = {(it.z & 3) - 1, ((it.z >> 2) & 3) - 1, ((it.z >> 4) & 3) - 1};
+        double dx[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < ND; d++)
+            dx[d] = dsub(s.row(FD_R + d)[a], image_pos(s.row(FD_R + d)[b], sh[d], c.rmin[d], c.rmax[d]));
+        const double r2 = exact_len2(dx, ND);
+        const double ha = s.row(FD_H)[a], hb = s.row(FD_H)[b];
+        const double t = 2.0 * (ha > hb ? ha : hb);
+        int *slot = &nbr[(int64_t)it.w * ld + a];
+        *slot = r2 <= dmul(t, t) ? (*slot & 0x7fffffff) : -1;
     }
 }
 
@@ -324,6 +364,7 @@ __global__ void __launch_bounds__(BLK) k_omega_eos(DevCfg c, DevState s, const D
 #pragma unroll 2
         for (int j = 0; j < cnt; j++) {
             const int e = nbr[(int64_t)j * ld + a];
+            if (e < 0) continue;
             const int b = e & B_MASK;
             const float4 pb = P0[b];
             const float mb = P1[b].w;
@@ -334,13 +375,19 @@ __global__ void __launch_bounds__(BLK) k_omega_eos(DevCfg c, DevState s, const D
             const float pdkh = -q * wdK32(q, wcon) * iha;
             if (is_sph_or_sphb(tb)) om.add(mb * (ihna * pdkh - pd_coef * wK32(q, wcon)));
         }
-        const double omega = 1 + s.row(FD_H)[a] * om.value() / (s.row(FD_DENS)[a] * ND);
+        /* Omega = 1 + h*sum/(rho*NDIM): an O(1) number, FP32 is ample */
+        const float omega = 1.f + pa.w * om.s / (P2[a].x * ND);
         s.row(FD_OMEGA)[a] = omega;
-        om32[a] = (float)omega;
+        om32[a] = omega;
     }
     if (do_eos) {
+        /* FP64: p = PRB((rho/rho0)^7 - 1) cancels; one FP64 reciprocal by
+         * an FP32 estimate and a Newton step, integer powers */
         const double densa = s.row(FD_DENS)[a];
-        const double x = c.liq_dem() ? densa / (c.refd * s.row(FD_POR)[a]) : densa / c.refd;
+        const double rho0 = c.liq_dem() ? c.refd * s.row(FD_POR)[a] : c.refd;
+        double r0 = (double)(1.0f / (float)rho0);
+        r0 = r0 * (2.0 - rho0 * r0);
+        const double x = densa * r0;
         double xg;
         if (!c.liq_dem() || c.gamma == 7.0) {
             const double x2 = x * x;
@@ -348,8 +395,10 @@ __global__ void __launch_bounds__(BLK) k_omega_eos(DevCfg c, DevState s, const D
         } else {
             xg = pow(x, c.gamma);
         }
+        double rd = (double)(1.0f / (float)densa);
+        rd = rd * (2.0 - densa * rd);
         const double press = c.prb * (xg - 1.0);
-        const double pdr2 = press / (densa * densa);
+        const double pdr2 = press * (rd * rd);
         s.row(FD_PRESS)[a] = press;
         s.row(FD_PDR2)[a] = pdr2;
         float4 p2 = P2[a];
@@ -469,6 +518,7 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
 #pragma unroll 2
         for (int j = 0; j < cnt; j++) {
             const int e = nbr[(int64_t)j * ld + a];
+            if (e < 0) continue;
             const int b = e & B_MASK;
             const float4 pb = P0[b], vb = P1[b], xb = P2[b];
             const int tb = tg[b] & 0xff;
@@ -541,19 +591,20 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
                 for (int k = 0; k < ND; k++) fp[k].add(-mb * (pc * d[k] + antic));
             }
         }
-        double fsum2 = 0.0;
+        float fsum2 = 0.f;
 #pragma unroll
         for (int k = 0; k < ND; k++) {
-            const double fpk = fp[k].value(), fvk = fv[k].value(), fbk = fb[k].value(), fak = fa[k].value();
-            s.row(FD_FP + k)[a] += fpk;
-            s.row(FD_FV + k)[a] += fvk;
-            s.row(FD_FB + k)[a] += fbk;
+            s.row(FD_FP + k)[a] += fp[k].s;
+            s.row(FD_FV + k)[a] += fv[k].s;
+            s.row(FD_FB + k)[a] += fb[k].s;
             double *f = s.row(FD_F + k);
-            const double fk = f[a] + fak + fvk + fbk + fpk;
+            const double fk = f[a] + (double)((fa[k].s + fv[k].s) + (fb[k].s + fp[k].s));
             f[a] = fk;
-            fsum2 += fk * fk;
+            const float fkf = (float)fk;
+            fsum2 += fkf * fkf;
         }
-        ndt = fminf(ndt, (float)(0.25 * sqrt((double)ha / sqrt(fsum2))));
+        /* accelCondition (sph.h:566-568), a dt bound: FP32 */
+        ndt = fminf(ndt, 0.25f * sqrtf(ha * rsqrtf(fsum2)));
     }
     block_min_atomic(ndt, &g->new_dt_bits);
 }
@@ -580,6 +631,7 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
 #pragma unroll 2
     for (int j = 0; j < cnt; j++) {
         const int e = nbr[(int64_t)j * ld + a];
+        if (e < 0) continue;
         const int b = e & B_MASK;
         const int tb = tg[b] & 0xff;
         const float4 pb = P0[b], vb = P1[b];
@@ -602,7 +654,7 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
         const float vdr = (va.x - vb.x) * d[0] + (va.y - vb.y) * d[1] + (va.z - vb.z) * d[2];
         if (!(is_boundary(tb) || tb == T_DEM)) acc.add(vb.w * vdr * F);
     }
-    s.row(FD_DDDT)[a] += acc.value();
+    s.row(FD_DDDT)[a] += (double)acc.s;
 }
 
 /* ---------------------------------------------------------------------- */
@@ -611,7 +663,8 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
 template <int ND, int MODE>
 __global__ void __launch_bounds__(BLK) k_couple(DevCfg c, const DevCfg *__restrict__ cp, DevState s, const int *__restrict__ start,
                                                 const DevGlobals *__restrict__ g, const float4 *__restrict__ P0,
-                                                const float4 *__restrict__ P1, const int *__restrict__ tg) {
+                                                const float4 *__restrict__ P1, const float4 *__restrict__ P2,
+                                                const float4 *__restrict__ DP, const int *__restrict__ tg) {
     const int lane = threadIdx.x & 31;
     const int warps = (blockDim.x >> 5) * gridDim.x;
     const int nsc = g->n_sph_cells;
@@ -625,19 +678,24 @@ __global__ void __launch_bounds__(BLK) k_couple(DevCfg c, const DevCfg *__restri
         if (s0 == s1) continue;
         int cc[3] = {0, 0, 0};
         decode<ND>(ci, sdims, cc);
-        double orig[3] = {0, 0, 0};
         int klo[3] = {0, 0, 0}, khi[3] = {0, 0, 0};
+        /* delta(k) = origin(SPH bucket) - origin(DEM bucket k) = base - (k - klo)*dcell:
+         * one FP64 difference per warp, the rest in FP32 (periodic wrap of
+         * k changes the origin by a multiple of L, i.e. nothing) */
+        float obase[3] = {0.f, 0.f, 0.f}, dcf[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int d = 0; d < ND; d++) {
-            orig[d] = sph_origin(c, g, d, cc[d]);
-            klo[d] = (int)floor((orig[d] - c.rc - c.dorig[d]) * c.rdcell[d]);
-            khi[d] = (int)floor((orig[d] + sph_width(c, g, d) + c.rc - c.dorig[d]) * c.rdcell[d]);
+            const double orig = sph_origin(c, g, d, cc[d]);
+            klo[d] = (int)floor((orig - c.rc - c.dorig[d]) * c.rdcell[d]);
+            khi[d] = (int)floor((orig + sph_width(c, g, d) + c.rc - c.dorig[d]) * c.rdcell[d]);
             if (!c.periodic[d]) {
                 klo[d] = max(klo[d], 0);
                 khi[d] = min(khi[d], c.ddims[d] - 1);
             } else if (khi[d] - klo[d] + 1 > c.ddims[d]) {
                 khi[d] = klo[d] + c.ddims[d] - 1;
             }
+            obase[d] = (float)(orig - (c.dorig[d] + klo[d] * c.dcell[d]));
+            dcf[d] = (float)c.dcell[d];
         }
         for (int base = s0; base < s1; base += 32) {
             const int a = base + lane;
@@ -652,9 +710,9 @@ __global__ void __launch_bounds__(BLK) k_couple(DevCfg c, const DevCfg *__restri
                 va = P1[a];
 #pragma unroll
                 for (int d = 0; d < ND; d++) cs[d] = ref_dem_cell(s.row(FD_R + d)[a], c, d);
-                const double densa = s.row(FD_DENS)[a];
-                dvol = (float)(s.row(FD_MASS)[a] / densa);
-                rdens = (float)(ND == 2 ? (1.0 / (2.0 * c.dem_radius)) / densa : 1.0 / densa);
+                const float densa = P2[a].x;
+                dvol = va.w / densa;
+                rdens = ND == 2 ? (float)(1.0 / (2.0 * c.dem_radius)) / densa : 1.f / densa;
             }
             Kahan por, dpd, acc[ND];
             por.init(0.f);
@@ -684,8 +742,7 @@ __global__ void __launch_bounds__(BLK) k_couple(DevCfg c, const DevCfg *__restri
                         const bool shifted = any_shift<ND>(sh);
                         float delta[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-                        for (int d = 0; d < ND; d++)
-                            delta[d] = (float)(orig[d] - (dem_origin(c, d, t[d]) + sh[d] * (c.rmax[d] - c.rmin[d])));
+                        for (int d = 0; d < ND; d++) delta[d] = obase[d] - (float)(k3[d] - klo[d]) * dcf[d];
                         for (int b = b0; b < b1; b++) {
                             const int tgb = tg[b];
                             if ((tgb & 0xff) != T_DEM) continue;
@@ -723,10 +780,11 @@ __global__ void __launch_bounds__(BLK) k_couple(DevCfg c, const DevCfg *__restri
                                             for (int k = 0; k < ND; k++) acc[k].add(dem_vol * dd[k] * Fq);
                                         }
                                     } else {
-                                        const float sc =
-                                            (float)(s.row(FD_MASS)[b] / s.row(FD_SHEP)[b]) * rdens * w;
+                                        const float4 dp = DP[b];  /* (m/shep, fdrag) of the DEM particle */
+                                        const float sc = dp.x * rdens * w;
+                                        const float fdb[3] = {dp.y, dp.z, dp.w};
 #pragma unroll
-                                        for (int k = 0; k < ND; k++) acc[k].add(-sc * (float)s.row(FD_FDRAG + k)[b]);
+                                        for (int k = 0; k < ND; k++) acc[k].add(-sc * fdb[k]);
                                     }
                                 }
                             }
@@ -738,14 +796,14 @@ __global__ void __launch_bounds__(BLK) k_couple(DevCfg c, const DevCfg *__restri
                     }
             if (!act) continue;
             if (MODE == 0) {
-                s.row(FD_POR)[a] = por.value();
-                s.row(FD_DPORDT)[a] = dpd.value();
+                s.row(FD_POR)[a] = por.s;
+                s.row(FD_DPORDT)[a] = dpd.s;
 #pragma unroll
-                for (int k = 0; k < ND; k++) s.row(FD_GPOR + k)[a] = acc[k].value();
+                for (int k = 0; k < ND; k++) s.row(FD_GPOR + k)[a] = acc[k].s;
             } else {
 #pragma unroll
                 for (int k = 0; k < ND; k++) {
-                    const double v = acc[k].value();
+                    const double v = acc[k].s;
                     s.row(FD_FDRAG + k)[a] = v;
                     s.row(FD_F + k)[a] += v;
                 }
@@ -759,6 +817,16 @@ __global__ void __launch_bounds__(BLK) k_couple(DevCfg c, const DevCfg *__restri
             }
         }
     }
+}
+
+/* (m/shep, fdrag) of every DEM particle for the DEM->SPH drag (sph.h:1359) */
+__global__ void k_pack_dem_drag(DevState s, float4 *__restrict__ DP, int64_t n) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (s.irow(FI_IAM)[i] != T_DEM) return;
+    const double sh = s.row(FD_SHEP)[i];
+    DP[i] = make_float4(sh != 0.0 ? (float)(s.row(FD_MASS)[i] / sh) : 0.f, (float)s.row(FD_FDRAG)[i],
+                        (float)s.row(FD_FDRAG + 1)[i], (float)s.row(FD_FDRAG + 2)[i]);
 }
 
 /* ---------------------------------------------------------------------- */
@@ -980,10 +1048,16 @@ __global__ void k_list_export(DevState s, const int *tg, const int *nbr, const i
     const int tag = s.irow(FI_TAG)[a];
     const int m = ncnt[a];
     if (!idx) {
-        cnt[tag] = m;
+        int v = 0;
+        for (int j = 0; j < m; j++) v += nbr[(int64_t)j * ld + a] >= 0;
+        cnt[tag] = v;
         return;
     }
-    for (int j = 0; j < m; j++) idx[offs[tag] + j] = s.irow(FI_TAG)[nbr[(int64_t)j * ld + a] & B_MASK];
+    int k = 0;
+    for (int j = 0; j < m; j++) {
+        const int e = nbr[(int64_t)j * ld + a];
+        if (e >= 0) idx[offs[tag] + k++] = s.irow(FI_TAG)[e & B_MASK];
+    }
 }
 
 int warp_blocks(int items) { return std::max(1, std::min(1 << 16, (items + (BLK / 32) - 1) / (BLK / 32))); }
@@ -1023,9 +1097,15 @@ void pack_fpi(sphdem_ctx *c) {
 
 void nlist(sphdem_ctx *c) {
     const int blocks = warp_blocks(c->cfg.sph_cells_cap);
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(c->mx_bandq_n, 0, sizeof(unsigned long long), c->stream));
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "nlist32", k_nlist<ND>, blocks, BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->g, c->mx_pos,         \
-                  c->mx_tg, c->mx_nbr, c->mx_ncnt, c->mx_maxn, c->cap, 0)
+                  c->mx_tg, c->mx_nbr, c->mx_ncnt, c->mx_maxn, c->cap, 0, c->mx_bandq, c->mx_bandq_n, c->mx_bandq_cap)
+    SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
+#undef L_
+#define L_(ND)                                                                                                  \
+    SPHDEM_LAUNCH(c, "band_fix64", k_band_fix<ND>, 4 * 152, 256, 0, c->cfg, c->A, c->mx_bandq, c->mx_bandq_n,        \
+                  c->mx_bandq_cap, c->mx_nbr, c->cap)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
@@ -1036,7 +1116,7 @@ int nlist_max_count(sphdem_ctx *c) {
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(c->mx_ncnt, 0, c->n * sizeof(int), c->stream));
 #define L_(ND)                                                                                                    \
     k_nlist<ND><<<blocks, BLK, 0, c->stream>>>(c->cfg, c->dcfg, c->A, c->buf.start, c->g, c->mx_pos, c->mx_tg, c->mx_nbr, \
-                                               c->mx_ncnt, 0, c->cap, 1)
+                                               c->mx_ncnt, 0, c->cap, 1, nullptr, nullptr, 0)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
     std::vector<int> h(c->n);
@@ -1076,16 +1156,17 @@ void porosity(sphdem_ctx *c) {
     const int blocks = warp_blocks(c->cfg.sph_cells_cap);
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "porosity32", (k_couple<ND, 0>), blocks, BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->g,          \
-                  c->mx_pos, c->mx_vel, c->mx_tg)
+                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
 
 void dem_drag(sphdem_ctx *c) {
     const int blocks = warp_blocks(c->cfg.sph_cells_cap);
+    SPHDEM_LAUNCH(c, "pack_dem_drag32", k_pack_dem_drag, grid_for(c->n, 256), 256, 0, c->A, c->mx_dp, c->n);
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "dem_drag32", (k_couple<ND, 1>), blocks, BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->g,          \
-                  c->mx_pos, c->mx_vel, c->mx_tg)
+                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
