@@ -247,6 +247,7 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->mx_q1);
     cudaFree(c->mx_q2);
     cudaFree(c->mx_dp);
+    cudaFree(c->mx_poslo);
     cudaFree(c->mx_bandq);
     cudaFree(c->mx_bandq_n);
     cudaFree(c->dcfg);
@@ -475,6 +476,9 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_q1, capacity * sizeof(float4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_q2, capacity * sizeof(float4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_dp, capacity * sizeof(float4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_poslo, capacity * sizeof(float4)));
+            /* near-exact FP64 ties (a perfect lattice at rest density) go to the
+             * band queue; candidates beyond its size are decided inline */
             c->mx_bandq_cap = std::max<long long>(1 << 20, 8 * capacity);
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_bandq, c->mx_bandq_cap * sizeof(int4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_bandq_n, sizeof(unsigned long long)));
@@ -579,11 +583,11 @@ int sphdem_rebuild(sphdem_handle h) {
 
 int sphdem_time_steps(sphdem_handle h, int nsteps, double *ms) {
     if (!h || !ms) return SPHDEM_ERR_INVALID;
+    int rc = sphdem_step(h, 1);  /* make sure the graph exists */
+    if (rc) return rc;
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    int rc = sphdem_step(h, 1);  /* make sure the graph exists */
-    if (rc) return rc;
     cudaEventRecord(e0, h->stream);
     rc = sphdem_step(h, nsteps);
     cudaEventRecord(e1, h->stream);

@@ -66,6 +66,7 @@ struct sphdem_ctx {
     int mx_maxn = 0;
     float4 *mx_q0 = nullptr, *mx_q1 = nullptr, *mx_q2 = nullptr;  /* FPI fields of fluid particles */
     float4 *mx_dp = nullptr;    /* (m/shep, fdrag) of DEM particles */
+    float4 *mx_poslo = nullptr; /* low FP32 halves of offsets and h (double-float) */
     int4 *mx_bandq = nullptr;   /* neighbour candidates within the FP32 band */
     unsigned long long *mx_bandq_n = nullptr;
     long long mx_bandq_cap = 0;

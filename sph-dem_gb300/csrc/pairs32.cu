@@ -75,6 +75,17 @@ __device__ __forceinline__ float wdK32(float q, float wcon) {
     return wcon * (-4.f * (t2 * t) * (1.f + 2.f * q) + 2.f * (t2 * t2));
 }
 
+/* error-free transforms for the double-float (hi + lo FP32) refinement */
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = a + b;
+    const float bb = s - a;
+    e = (a - (s - bb)) + (b - bb);
+}
+__device__ __forceinline__ void two_prod(float a, float b, float &p, float &e) {
+    p = a * b;
+    e = fmaf(a, b, -p);
+}
+
 template <int ND>
 __device__ __forceinline__ float powi(float x) {
     float r = x;
@@ -178,24 +189,31 @@ __device__ __noinline__ bool exact_pair(const DevCfg *__restrict__ cp, const Dev
 template <int ND>
 __global__ void k_pack(DevCfg c, DevState s, const int *__restrict__ skey, const DevGlobals *__restrict__ g,
                        float4 *__restrict__ P0, float4 *__restrict__ P1, float4 *__restrict__ P2,
-                       int *__restrict__ tg, int64_t n) {
+                       float4 *__restrict__ P0lo, int *__restrict__ tg, int64_t n) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int t = s.irow(FI_IAM)[i];
     tg[i] = (t & 0xff) | (s.irow(FI_GCODE)[i] << 8);
     if (t == T_DEAD) return;
     const int key = skey[i];
-    float off[3] = {0.f, 0.f, 0.f};
+    float off[3] = {0.f, 0.f, 0.f}, lo[3] = {0.f, 0.f, 0.f};
     int cc[3] = {0, 0, 0};
-    if (c.liq_dem() && t == T_DEM) {
+    const bool dem = c.liq_dem() && t == T_DEM;
+    if (dem) {
         decode<ND>(key - g->n_sph_cells, c.ddims, cc);
-#pragma unroll
-        for (int d = 0; d < ND; d++) off[d] = (float)(s.row(FD_R + d)[i] - dem_origin(c, d, cc[d]));
     } else {
         const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
         decode<ND>(key, dims, cc);
+    }
 #pragma unroll
-        for (int d = 0; d < ND; d++) off[d] = (float)(s.row(FD_R + d)[i] - sph_origin(c, g, d, cc[d]));
+    for (int d = 0; d < ND; d++) {
+        const double o = s.row(FD_R + d)[i] - (dem ? dem_origin(c, d, cc[d]) : sph_origin(c, g, d, cc[d]));
+        off[d] = (float)o;
+        lo[d] = (float)(o - (double)off[d]);
+    }
+    {
+        const double h = s.row(FD_H)[i];
+        P0lo[i] = make_float4(lo[0], lo[1], lo[2], (float)(h - (double)(float)h));
     }
     float vh[3] = {0.f, 0.f, 0.f};
 #pragma unroll
@@ -225,6 +243,20 @@ __global__ void k_pack_fpi(DevState s, float4 *__restrict__ Q0, float4 *__restri
     Q2[i] = make_float4(v[8], v[9], v[10], v[11]);
 }
 
+/* the reference's FP64 neighbour predicate, len2(ra - image(rb)) <= (2 max(ha, hb))^2
+ * (dataLL.h neighbour traversal), evaluated without contraction */
+template <int ND>
+__device__ __forceinline__ bool exact_neighbour(const DevCfg &c, const DevState &s, int a, int b, const int *sh) {
+    double dx[3] = {0, 0, 0};
+#pragma unroll
+    for (int d = 0; d < ND; d++)
+        dx[d] = dsub(s.row(FD_R + d)[a], image_pos(s.row(FD_R + d)[b], sh[d], c.rmin[d], c.rmax[d]));
+    const double r2 = exact_len2(dx, ND);
+    const double ha = s.row(FD_H)[a], hb = s.row(FD_H)[b];
+    const double t = 2.0 * (ha > hb ? ha : hb);
+    return r2 <= dmul(t, t);
+}
+
 /* ---------------------------------------------------------------------- */
 template <int ND>
 __global__ void __launch_bounds__(BLK) k_nlist(DevCfg c, const DevCfg *__restrict__ cp, DevState s, const int *__restrict__ start,
@@ -232,14 +264,18 @@ __global__ void __launch_bounds__(BLK) k_nlist(DevCfg c, const DevCfg *__restric
                                                const int *__restrict__ tg, int *__restrict__ nbr,
                                                int *__restrict__ ncnt, int maxn, int64_t ld, int count_only,
                                                int4 *__restrict__ bandq, unsigned long long *__restrict__ bandq_n,
-                                               long long bandq_cap) {
+                                               long long bandq_cap, const float4 *__restrict__ P0lo) {
     const int lane = threadIdx.x & 31;
     const int warps = (blockDim.x >> 5) * gridDim.x;
     const int nsc = g->n_sph_cells;
     const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
-    float cell[3];
+    float cell[3], cell_lo[3];
 #pragma unroll
-    for (int d = 0; d < 3; d++) cell[d] = (float)(c.periodic[d] ? g->scell[d] : g->sr2);
+    for (int d = 0; d < 3; d++) {
+        const double cw = c.periodic[d] ? g->scell[d] : g->sr2;
+        cell[d] = (float)cw;
+        cell_lo[d] = (float)(cw - (double)cell[d]);
+    }
     for (int ci = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; ci < nsc; ci += warps) {
         const int s0 = start[ci], s1 = start[ci + 1];
         if (s0 == s1) continue;
@@ -274,17 +310,53 @@ __global__ void __launch_bounds__(BLK) k_nlist(DevCfg c, const DevCfg *__restric
                             if (r2 > T * (1.f + BAND)) continue;
                             if (b == a && !shifted) continue;
                             if (shifted && !img_ok<ND>(tg[b] >> 8, sh)) continue;
-                            const bool band = r2 >= T * (1.f - BAND);
+                            bool band = r2 >= T * (1.f - BAND);
+                            if (band) {
+                                /* double-float refinement: offsets, bucket size and h as
+                                 * hi + lo FP32 pairs carry ~48 bits, so |r^2 - (2h)^2| is
+                                 * known to ~1e-13 relative; only closer ties need FP64 */
+                                const float4 al = P0lo[a], bl = P0lo[b];
+                                const float ah[3] = {pa.x, pa.y, pa.z}, bh[3] = {pb.x, pb.y, pb.z};
+                                const float alo[3] = {al.x, al.y, al.z}, blo[3] = {bl.x, bl.y, bl.z};
+                                float r2h = 0.f, r2l = 0.f;
+#pragma unroll
+                                for (int d = 0; d < ND; d++) {
+                                    float s1v, e1, s2v, e2;
+                                    two_sum(ah[d], -bh[d], s1v, e1);
+                                    two_sum(s1v, -o[d] * cell[d], s2v, e2);
+                                    const float lo = e1 + e2 + (alo[d] - blo[d]) - o[d] * cell_lo[d];
+                                    float dh, dl;
+                                    two_sum(s2v, lo, dh, dl);
+                                    float p, pe;
+                                    two_prod(dh, dh, p, pe);
+                                    float t1, te;
+                                    two_sum(r2h, p, t1, te);
+                                    r2h = t1;
+                                    r2l += te + pe + 2.f * dh * dl;
+                                }
+                                /* (2 max h)^2 with h = hi + lo */
+                                const bool amax = pa.w > pb.w || (pa.w == pb.w && al.w >= bl.w);
+                                const float hh = 2.f * (amax ? pa.w : pb.w), hl = 2.f * (amax ? al.w : bl.w);
+                                float Th, Te;
+                                two_prod(hh, hh, Th, Te);
+                                const float Tl = Te + 2.f * hh * hl;
+                                const float diff = (r2h - Th) + (r2l - Tl);
+                                if (fabsf(diff) > 1e-12f * Th) {
+                                    band = false;
+                                    if (diff > 0.f) continue;
+                                }
+                            }
                             if (cnt < maxn) {
                                 int e = b | code;
                                 if (band && !count_only) {
-                                    /* decided later, in one coalesced FP64 pass */
+                                    /* decided later, in one coalesced FP64 pass; when the
+                                     * queue is full, decided here (slow but exact) */
                                     const unsigned long long slot = atomicAdd(bandq_n, 1ull);
                                     if (slot < (unsigned long long)bandq_cap) {
                                         bandq[slot] = make_int4(a, b, (sh[0] + 1) | ((sh[1] + 1) << 2) | ((sh[2] + 1) << 4), cnt);
                                         e |= (int)0x80000000u;
-                                    } else {
-                                        set_err(g, SPHDEM_ERR_CAPACITY, -2);
+                                    } else if (!exact_neighbour<ND>(c, s, a, b, sh)) {
+                                        e = -1;
                                     }
                                 }
                                 if (!count_only) nbr[(int64_t)cnt * ld + a] = e;
@@ -313,15 +385,8 @@ __global__ void k_band_fix(DevCfg c, DevState s, const int4 *__restrict__ bandq,
         const int4 it = bandq[q];
         const int a = it.x, b = it.y;
         const int sh[3] = {(it.z & 3) - 1, ((it.z >> 2) & 3) - 1, ((it.z >> 4) & 3) - 1};
-        double dx[3] = {0, 0, 0};
-#pragma unroll
-        for (int d = 0; d < ND; d++)
-            dx[d] = dsub(s.row(FD_R + d)[a], image_pos(s.row(FD_R + d)[b], sh[d], c.rmin[d], c.rmax[d]));
-        const double r2 = exact_len2(dx, ND);
-        const double ha = s.row(FD_H)[a], hb = s.row(FD_H)[b];
-        const double t = 2.0 * (ha > hb ? ha : hb);
         int *slot = &nbr[(int64_t)it.w * ld + a];
-        *slot = r2 <= dmul(t, t) ? (*slot & 0x7fffffff) : -1;
+        *slot = exact_neighbour<ND>(c, s, a, b, sh) ? (*slot & 0x7fffffff) : -1;
     }
 }
 
@@ -1086,7 +1151,7 @@ namespace mixed {
 void pack(sphdem_ctx *c) {
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "pack32", k_pack<ND>, grid_for(c->n, 256), 256, 0, c->cfg, c->A, c->buf.skey, c->g,         \
-                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_tg, c->n)
+                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_poslo, c->mx_tg, c->n)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
@@ -1100,7 +1165,8 @@ void nlist(sphdem_ctx *c) {
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(c->mx_bandq_n, 0, sizeof(unsigned long long), c->stream));
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "nlist32", k_nlist<ND>, blocks, BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->g, c->mx_pos,         \
-                  c->mx_tg, c->mx_nbr, c->mx_ncnt, c->mx_maxn, c->cap, 0, c->mx_bandq, c->mx_bandq_n, c->mx_bandq_cap)
+                  c->mx_tg, c->mx_nbr, c->mx_ncnt, c->mx_maxn, c->cap, 0, c->mx_bandq, c->mx_bandq_n, c->mx_bandq_cap, \
+                  c->mx_poslo)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 #define L_(ND)                                                                                                  \
@@ -1116,7 +1182,7 @@ int nlist_max_count(sphdem_ctx *c) {
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(c->mx_ncnt, 0, c->n * sizeof(int), c->stream));
 #define L_(ND)                                                                                                    \
     k_nlist<ND><<<blocks, BLK, 0, c->stream>>>(c->cfg, c->dcfg, c->A, c->buf.start, c->g, c->mx_pos, c->mx_tg, c->mx_nbr, \
-                                               c->mx_ncnt, 0, c->cap, 1, nullptr, nullptr, 0)
+                                               c->mx_ncnt, 0, c->cap, 1, nullptr, nullptr, 0, c->mx_poslo)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
     std::vector<int> h(c->n);
