@@ -227,6 +227,21 @@ int sphdem_pairs(sphdem_handle h, int kind, int64_t *offsets, int32_t *idx,
  * for DEM, as int32 triples (unused z = 0). */
 int sphdem_cell_ids(sphdem_handle h, int32_t *cell_xyz);
 
+/* Largest particle count sphdem_cell_ids_noalloc accepts. */
+#define SPHDEM_CELL_IDS_NOALLOC_MAX 262144
+
+/* sphdem_cell_ids without any device allocation: no counterpart in the
+ * reference (whose cell indices are host arrays).  For callers that must not
+ * allocate device memory, e.g. a diagnostics hook after an out-of-memory
+ * failure, or a loop that cannot take the device-wide synchronisation of
+ * cudaFree.  It stages through one static device array of
+ * SPHDEM_CELL_IDS_NOALLOC_MAX x 3 int32 per device, shared by every call on
+ * that device: calls that overlap in time race on it.  Larger simulations
+ * return SPHDEM_ERR_CAPACITY.  The first call on a device sets up the array's
+ * address (and may load the module there): make it before any stream capture
+ * on that device.  Same output as sphdem_cell_ids. */
+int sphdem_cell_ids_noalloc(sphdem_handle h, int32_t *cell_xyz);
+
 /* Per-kernel device time accumulated with CUDA events since the last reset
  * (names separated by '\n' in `names`, times in ms, launch counts). */
 int sphdem_kernel_times(sphdem_handle h, char *names, size_t names_len,

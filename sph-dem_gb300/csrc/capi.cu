@@ -751,6 +751,15 @@ int sphdem_cell_ids(sphdem_handle h, int32_t *cells) {
     }
 }
 
+int sphdem_cell_ids_noalloc(sphdem_handle h, int32_t *cells) {
+    if (!h || !cells) return SPHDEM_ERR_INVALID;
+    try {
+        return export_cells_noalloc(h, cells);
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+}
+
 int sphdem_kernel_times_reset(sphdem_handle h, int enable) {
     if (!h) return SPHDEM_ERR_INVALID;
     collect_times(h);

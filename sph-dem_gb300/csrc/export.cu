@@ -6,6 +6,7 @@
  * lists after a reset.
  */
 #include <algorithm>
+#include <mutex>
 
 #include "internal.cuh"
 
@@ -187,6 +188,80 @@ int export_cells(sphdem_ctx *c, int32_t *cells) {
     SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
     SPHDEM_CUDA_CHECK(cudaGetLastError());
     cudaFree(d);
+    return SPHDEM_OK;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Allocation-free bucket-index export.
+ *
+ * Same kernel and result as export_cells, but the 3n-int device staging
+ * buffer is a fixed file-scope array instead of a cudaMalloc/cudaFree pair,
+ * for callers that must not allocate device memory (a diagnostics hook that
+ * runs after an out-of-memory failure, or a loop that cannot take the
+ * device-wide synchronisation cudaFree implies).
+ *
+ * - Capacity: SPHDEM_CELL_IDS_NOALLOC_MAX particles (3 int32 each, 3 MiB of
+ *   static device memory per device that loads this module); larger
+ *   simulations are rejected with SPHDEM_ERR_CAPACITY.
+ * - The first call on a device looks the array's device address up with
+ *   cudaGetSymbolAddress (this can load the module on that device); make that
+ *   first call before any stream capture on the device.
+ * - Every call on a device shares the one array: calls that overlap in time
+ *   (from several threads, or several handles on one device) race on it.
+ *   Nothing in it needs to start at zero: k_cells writes all 3n entries
+ *   (tags are a permutation of 0..n-1) before the copy-out reads them.
+ */
+namespace {
+
+static __device__ __align__(256) int32_t g_cells_scratch[3 * SPHDEM_CELL_IDS_NOALLOC_MAX];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+int32_t *g_scratch_ptr[kMaxDevices] = {};
+
+}  // namespace
+
+int export_cells_noalloc(sphdem_ctx *c, int32_t *cells) {
+    const int64_t n = c->n;
+    if (n > SPHDEM_CELL_IDS_NOALLOC_MAX) {
+        c->err = "sphdem_cell_ids_noalloc: " + std::to_string(n) + " particles exceed the static buffer of " +
+                 std::to_string(SPHDEM_CELL_IDS_NOALLOC_MAX) + " (use sphdem_cell_ids)";
+        return SPHDEM_ERR_CAPACITY;
+    }
+    /* the handle's device: the one that owns its globals block */
+    cudaPointerAttributes attr{};
+    SPHDEM_CUDA_CHECK(cudaPointerGetAttributes(&attr, c->g));
+    const int dev = attr.device;
+    if (dev < 0 || dev >= kMaxDevices) {
+        c->err = "sphdem_cell_ids_noalloc: device index out of range";
+        return SPHDEM_ERR_UNSUPPORTED;
+    }
+    int prev = -1;
+    SPHDEM_CUDA_CHECK(cudaGetDevice(&prev));
+    if (prev != dev) SPHDEM_CUDA_CHECK(cudaSetDevice(dev));
+    int32_t *scratch = nullptr;
+    cudaError_t e = cudaSuccess;
+    {
+        std::lock_guard<std::mutex> lock(g_scratch_mu);
+        if (!g_scratch_ptr[dev]) {
+            void *p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_cells_scratch);
+            if (e == cudaSuccess) g_scratch_ptr[dev] = static_cast<int32_t *>(p);
+        }
+        scratch = g_scratch_ptr[dev];
+    }
+    if (e == cudaSuccess && n > 0) {
+        k_cells<<<grid_for(n, BLK), BLK, 0, c->stream>>>(c->cfg, c->A, c->g, n, scratch);
+        e = cudaGetLastError();
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(cells, scratch, 3 * n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    }
+    if (prev != dev) cudaSetDevice(prev);
+    if (e != cudaSuccess) {
+        c->err = std::string("sphdem_cell_ids_noalloc: ") + cudaGetErrorString(e);
+        return SPHDEM_ERR_CUDA;
+    }
     return SPHDEM_OK;
 }
 

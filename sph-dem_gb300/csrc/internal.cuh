@@ -131,6 +131,7 @@ void field_get_int(sphdem_ctx *c, int row, int *host);
 /* export.cu */
 int export_pairs(sphdem_ctx *c, int kind, int64_t *offs, int32_t *idx, int64_t cap, int64_t *np);
 int export_cells(sphdem_ctx *c, int32_t *cells);
+int export_cells_noalloc(sphdem_ctx *c, int32_t *cells);
 
 inline const DevState &cur(const sphdem_ctx *c) { return c->A; }
 

@@ -207,6 +207,7 @@ class Library:
         L.sphdem_pairs.argtypes = [H, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                    C.c_int64, C.POINTER(C.c_int64)]
         L.sphdem_cell_ids.argtypes = [H, C.POINTER(C.c_int32)]
+        L.sphdem_cell_ids_noalloc.argtypes = [H, C.POINTER(C.c_int32)]
         L.sphdem_kernel_times.argtypes = [H, C.c_char_p, C.c_size_t, C.POINTER(C.c_double),
                                           C.POINTER(C.c_int64), C.c_int, C.POINTER(C.c_int)]
         L.sphdem_kernel_times_reset.argtypes = [H, C.c_int]
@@ -291,6 +292,14 @@ class Simulation:
         cells = np.zeros((self.n, 3), np.int32)
         self.L.check(self.L.lib.sphdem_cell_ids(self.h, cells.ctypes.data_as(C.POINTER(C.c_int32))),
                      self.h, "cell_ids")
+        return cells
+
+    def cell_ids_noalloc(self) -> np.ndarray:
+        """cell_ids through the allocation-free entry point (static device
+        staging array of SPHDEM_CELL_IDS_NOALLOC_MAX particles)."""
+        cells = np.zeros((self.n, 3), np.int32)
+        self.L.check(self.L.lib.sphdem_cell_ids_noalloc(self.h, cells.ctypes.data_as(C.POINTER(C.c_int32))),
+                     self.h, "cell_ids_noalloc")
         return cells
 
     def time_steps(self, n: int) -> float:
