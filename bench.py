@@ -74,9 +74,14 @@ def run_profile(args):
     sim.step(args.warmup)
     ms = sim.time_steps(args.steps)
     st = sim.stats()
-    print(json.dumps({"profile": True, "n": case.n, "ms_per_step": ms / args.steps,
+    sim.kernel_times_reset(True)
+    sim.step(2)
+    kt = {k: round(m / 2, 4) for k, (m, _) in sorted(sim.kernel_times().items(), key=lambda kv: -kv[1][0])}
+    sim.kernel_times_reset(False)
+    print(json.dumps({"profile": True, "n": case.n, "ms_per_step": ms / args.steps, "kernel_ms_per_step": kt,
                       "list_pairs": st.n_list_pairs, "h_max": st.h_max,
-                      "search_radius": st.search_radius, "n_sph_cells": st.n_sph_cells}))
+                      "search_radius": st.search_radius, "n_sph_cells": st.n_sph_cells,
+                      "band_candidates": st.n_band_candidates, "band_queue_capacity": st.band_queue_capacity}))
 
 
 def workload_config(case, nsteps):
@@ -150,6 +155,9 @@ def measured_peaks():
             return json.load(fh), "measured"
     except Exception:
         return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+FORCE32_DRAM_BYTES_PER_PARTICLE = (163.309824e6 + 12.316928e6) / 270100
 
 
 def force_bytes_per_particle(avg_pairs: float) -> float:
@@ -247,13 +255,10 @@ def run_ours(args, rank, world):
     fp32_peak = SM_COUNT * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
     flops = FORCE_FLOP_PER_PAIR * st.n_list_pairs
     achieved_tf = flops / (force_ms_per_launch * 1e-3) / 1e12
-    traffic = None
-    tpath = os.path.join(REPO, "profiles", "force32_traffic.json")
-    if os.path.exists(tpath):
-        try:
-            traffic = json.load(open(tpath)).get("bytes_per_launch_full")
-        except Exception:
-            traffic = None
+    # DRAM bytes of one force32 launch from an ncu capture, per particle of the
+    # whole state (traffic grows in proportion to the particle count at fixed
+    # density; the capture is the 270k sub-box, profiles/force32_sediment3d_quarter.md)
+    traffic = FORCE32_DRAM_BYTES_PER_PARTICLE * n
 
     # ---- mixed vs FP64 on the same input ---------------------------------
     fp64_steps = max(1, min(args.fp64_steps, args.steps))
@@ -318,6 +323,7 @@ def run_ours(args, rank, world):
             "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes,
             "ms_per_launch": force_ms_per_launch, "avg_list_pairs": avg_pairs,
             "h_max": st.h_max, "search_radius": st.search_radius, "n_sph_cells": st.n_sph_cells,
+            "band_candidates": st.n_band_candidates,
             "fp32_pipe": {"achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
                           "frac": achieved_tf / fp32_peak,
                           "peak_basis": f"{SM_COUNT} SMs x {FP32_LANES} lanes x 2 x {sm_mhz:.0f} MHz"},

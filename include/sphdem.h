@@ -167,6 +167,8 @@ typedef struct SphDemStats {
     int64_t list_depth;      /* allocated entries per particle                      */
     int64_t n_sph_cells, n_dem_cells;
     double  h_max, search_radius;
+    int64_t n_band_candidates; /* pairs of the last list build decided in FP64 (mixed) */
+    int64_t band_queue_capacity;
 } SphDemStats;
 
 /* Phases and built-in hook points, in the order run.cpp:112-118 calls them. */

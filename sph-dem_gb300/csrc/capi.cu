@@ -249,7 +249,7 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->mx_dp);
     cudaFree(c->mx_poslo);
     cudaFree(c->mx_bandq);
-    cudaFree(c->mx_bandq_n);
+    cudaFree(c->mx_bandn);
     cudaFree(c->dcfg);
     for (int k = 0; k < 2; k++)
         if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
@@ -477,11 +477,13 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_q2, capacity * sizeof(float4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_dp, capacity * sizeof(float4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_poslo, capacity * sizeof(float4)));
-            /* near-exact FP64 ties (a perfect lattice at rest density) go to the
-             * band queue; candidates beyond its size are decided inline */
-            c->mx_bandq_cap = std::max<long long>(1 << 20, 8 * capacity);
-            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_bandq, c->mx_bandq_cap * sizeof(int4)));
-            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_bandq_n, sizeof(unsigned long long)));
+            /* list entries that FP32 cannot decide (mostly FP64 ties: a staggered
+             * lattice at rest density has 20 neighbours per particle at exactly
+             * 2h) are recorded per particle for the FP64 fix-up pass */
+            c->mx_band_per_particle = sphdem::mixed::band_records_per_particle();
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_bandq, capacity * c->mx_band_per_particle * sizeof(int2)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_bandn, capacity * sizeof(int)));
+            SPHDEM_CUDA_CHECK(cudaMemset(c->mx_bandn, 0, capacity * sizeof(int)));
             SPHDEM_CUDA_CHECK(cudaMemset(c->mx_om, 0, capacity * sizeof(float)));
             SPHDEM_CUDA_CHECK(cudaMemset(c->mx_ncnt, 0, capacity * sizeof(int)));
             SPHDEM_CUDA_CHECK(cudaDeviceSynchronize());
@@ -637,6 +639,13 @@ int sphdem_get_stats(sphdem_handle h, SphDemStats *out) {
     out->n_dem_cells = h->cfg.n_dem_cells;
     out->h_max = hg.hmax;
     out->search_radius = hg.sr;
+    if (h->mx_bandn) {
+        std::vector<int> nb(h->n);
+        cudaMemcpy(nb.data(), h->mx_bandn, h->n * sizeof(int), cudaMemcpyDeviceToHost);
+        for (int64_t k = 0; k < h->n; k++)
+            if (sphdem::is_sph_or_sphb(iam[k])) out->n_band_candidates += nb[k];
+        out->band_queue_capacity = (int64_t)h->cap * h->mx_band_per_particle;
+    }
     return cudaGetLastError() == cudaSuccess ? SPHDEM_OK : SPHDEM_ERR_CUDA;
 }
 

@@ -67,9 +67,9 @@ struct sphdem_ctx {
     float4 *mx_q0 = nullptr, *mx_q1 = nullptr, *mx_q2 = nullptr;  /* FPI fields of fluid particles */
     float4 *mx_dp = nullptr;    /* (m/shep, fdrag) of DEM particles */
     float4 *mx_poslo = nullptr; /* low FP32 halves of offsets and h (double-float) */
-    int4 *mx_bandq = nullptr;   /* neighbour candidates within the FP32 band */
-    unsigned long long *mx_bandq_n = nullptr;
-    long long mx_bandq_cap = 0;
+    int2 *mx_bandq = nullptr;   /* per particle: list entries within the FP32 band */
+    int *mx_bandn = nullptr;    /* per particle: how many are recorded */
+    int mx_band_per_particle = 0;
     sphdem::DevCfg *dcfg = nullptr;  /* device copy of cfg for out-of-line helpers */
     /* staging buffer for field transfers in tag order */
     double *stage = nullptr;
@@ -115,6 +115,7 @@ void pack(sphdem_ctx *c);
 void pack_fpi(sphdem_ctx *c);
 void nlist(sphdem_ctx *c);
 int nlist_max_count(sphdem_ctx *c);
+int band_records_per_particle();
 void omega_eos(sphdem_ctx *c, bool omega, bool eos);
 void force(sphdem_ctx *c);
 void dddt(sphdem_ctx *c);

@@ -9,12 +9,14 @@
  * the dimension so per-axis arrays live in registers.
  *
  *   k_nlist      after each rebuild, the exact neighbour list of every
- *                sph/sphBoundary particle: one warp per SPH bucket walks the
- *                3^d stencil with warp-uniform loads, FP32 distance test, and
- *                the reference's FP64 predicate (particle.h:236-238) inside a
- *                4e-6 relative band around the cut-off; periodic images only
- *                where the reference holds a ghost.  Column-major storage
- *                (entry j of all particles contiguous): b | stencil code << 26.
+ *                sph/sphBoundary particle: one warp per SPH bucket stages the
+ *                3^d stencil's candidates in shared memory and tests them in
+ *                FP32 with a proven error bound; candidates inside the bound
+ *                go to k_band_fix (double-float, then the reference's FP64
+ *                predicate, particle.h:236-238, for true ties).  Periodic
+ *                images only where the reference holds a ghost.  Column-major
+ *                storage (entry j of all particles contiguous):
+ *                b | stencil code << 26.
  *   k_omega_eos  calcOmega over the list + the FP64 EOS (its (rho/rho0)^7-1
  *                cancels too much for FP32)
  *   k_force      calcForce + the Courant/viscous/accel dt conditions
@@ -44,10 +46,6 @@ namespace {
 constexpr int BLK = 128;
 constexpr int B_BITS = 26;
 constexpr int B_MASK = (1 << B_BITS) - 1;
-/* FP32 error of r^2 from bucket offsets is below 6e-7 relative (offsets <
- * one bucket, each rounded once; r^2 and (2h)^2 a few ulps); pairs within
- * BAND of the cut-off are decided by the reference's FP64 predicate. */
-constexpr float BAND = 1e-6f;
 
 struct Kahan {
     float s, c;
@@ -258,135 +256,369 @@ __device__ __forceinline__ bool exact_neighbour(const DevCfg &c, const DevState 
 }
 
 /* ---------------------------------------------------------------------- */
+/* Half-width of the band around a cut-off T = R^2 inside which an FP32 r^2
+ * built from bucket offsets cannot decide: each displacement component is
+ * off by < 6 * 2^-24 L when L bounds the magnitudes of the offset terms, so
+ * r^2 by < 1.25e-6 L max(L, R) + 1.8e-7 r^2, and T by < 1.8e-7 T. */
+__device__ __forceinline__ float fp32_band(float T, float L2) { return fmaf(5e-7f, T, 1.5e-6f * fmaxf(L2, T)); }
+
+constexpr int CENTER_CODE = 13 << B_BITS;
+
+__device__ __forceinline__ void nl_decode_code(int code, int *o) {
+    o[0] = code / 9 - 1;
+    o[1] = (code / 3) % 3 - 1;
+    o[2] = code % 3 - 1;
+}
+
+/* Double-float (hi + lo FP32) decision for one candidate near the cut-off:
+ * +1 inside, -1 outside, 0 an FP64 tie.  Offsets, bucket size and h as hi+lo
+ * pairs carry ~48 bits, so r^2 - (2h)^2 is known to ~1e-13 of (2h)^2 plus
+ * ~1e-14 c^2 (c the bucket size); within 1e-12 of (2h)^2 + tol_abs only the
+ * FP64 predicate decides. */
 template <int ND>
-__global__ void __launch_bounds__(BLK) k_nlist(DevCfg c, const DevCfg *__restrict__ cp, DevState s, const int *__restrict__ start,
-                                               DevGlobals *__restrict__ g, const float4 *__restrict__ P0,
-                                               const int *__restrict__ tg, int *__restrict__ nbr,
-                                               int *__restrict__ ncnt, int maxn, int64_t ld, int count_only,
-                                               int4 *__restrict__ bandq, unsigned long long *__restrict__ bandq_n,
-                                               long long bandq_cap, const float4 *__restrict__ P0lo) {
-    const int lane = threadIdx.x & 31;
-    const int warps = (blockDim.x >> 5) * gridDim.x;
-    const int nsc = g->n_sph_cells;
+__device__ __forceinline__ int nl_refine(const float4 pa, const float4 al, const float4 pb, const float4 bl,
+                                         const int *o, const float *cell, const float *cell_lo, float tol_abs) {
+    const float ah[3] = {pa.x, pa.y, pa.z}, bh[3] = {pb.x, pb.y, pb.z};
+    const float alo[3] = {al.x, al.y, al.z}, blo[3] = {bl.x, bl.y, bl.z};
+    float r2h = 0.f, r2l = 0.f;
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        float s1v, e1, s2v, e2;
+        two_sum(ah[d], -bh[d], s1v, e1);
+        two_sum(s1v, -o[d] * cell[d], s2v, e2);
+        const float lo = e1 + e2 + (alo[d] - blo[d]) - o[d] * cell_lo[d];
+        float dh, dl;
+        two_sum(s2v, lo, dh, dl);
+        float p, pe;
+        two_prod(dh, dh, p, pe);
+        float t1, te;
+        two_sum(r2h, p, t1, te);
+        r2h = t1;
+        r2l += te + pe + 2.f * dh * dl;
+    }
+    const bool amax = pa.w > pb.w || (pa.w == pb.w && al.w >= bl.w);
+    const float hh = 2.f * (amax ? pa.w : pb.w), hl = 2.f * (amax ? al.w : bl.w);
+    float Th, Te;
+    two_prod(hh, hh, Th, Te);
+    const float Tl = Te + 2.f * hh * hl;
+    const float diff = (r2h - Th) + (r2l - Tl);
+    if (fabsf(diff) <= 1e-12f * Th + tol_abs) return 0;
+    return diff < 0.f ? 1 : -1;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Neighbour-list build.
+ *
+ * A warp takes 32 consecutive particles of the bucket order.  Buckets are
+ * numbered with the last axis fastest, so those particles lie in one or two
+ * runs of consecutive buckets along that axis (a "column").  For each run
+ * the warp stages the candidates of the union of the runs' 3^d stencils --
+ * 3^(d-1) neighbour columns x the run's z-range +-1 -- in shared memory,
+ * with positions moved into the run's frame (coalesced loads; the periodic
+ * image filter is applied once per candidate), then every lane tests all
+ * staged candidates with broadcast shared-memory reads.  Sharing the stencil
+ * across a run keeps all 32 lanes busy whatever the bucket occupancy.
+ *
+ * FP32 error bound of the test (L = largest offset magnitude in the frame,
+ * R = 2 max(ha, hb)): each displacement component carries < 6 * 2^-24 L, so
+ * r^2 is off by < 1.25e-6 L max(L, R) + 1.8e-7 r^2 and the cut-off
+ * 4 max(ha^2, hb^2) by < 1.8e-7 of itself.  Candidates closer than
+ * fp32_band(T, L^2) to the cut-off are recorded per particle (up to NL_QB)
+ * and decided by k_band_fix; beyond that they are decided inline in FP64. */
+constexpr int NL_WARPS = 8;
+constexpr int NL_CAP = 256;   /* staged candidates per warp before a flush */
+constexpr int NL_QB = 32;     /* band candidates recorded per particle */
+
+__device__ __forceinline__ int code_stride(int d) { return d == 0 ? 9 : (d == 1 ? 3 : 1); }
+
+/* FP64 decision of list entry e of particle a (bucket cc), out of line */
+template <int ND>
+__device__ __noinline__ bool exact_from_code(const DevCfg &c, const DevState &s, const DevGlobals *g, int a, int e,
+                                             const int *cc) {
+    int o[3], sh[3] = {0, 0, 0};
+    nl_decode_code(e >> B_BITS, o);
     const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        const int t = cc[d] + o[d];
+        sh[d] = t < 0 ? -1 : (t >= dims[d] ? 1 : 0);
+    }
+    return exact_neighbour<ND>(c, s, a, e & B_MASK, sh);
+}
+
+template <int ND, bool COUNT>
+__global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s, const int *__restrict__ start,
+                                                         const int *__restrict__ skey, DevGlobals *__restrict__ g,
+                                                         const float4 *__restrict__ P0, const int *__restrict__ tg,
+                                                         int *__restrict__ nbr, int *__restrict__ ncnt, int maxn,
+                                                         int64_t ld, int2 *__restrict__ bandq,
+                                                         int *__restrict__ bandn) {
+    constexpr int Z = ND - 1;
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ float4 s_pos[NL_WARPS][NL_CAP];
+    __shared__ int s_ent[NL_WARPS][NL_CAP];
+    __shared__ unsigned char s_zr[NL_WARPS][NL_CAP];
+    const int lane = threadIdx.x & 31;
+    const int w = threadIdx.x >> 5;
+    float4 *cpos = s_pos[w];
+    int *cent = s_ent[w];
+    unsigned char *czr = s_zr[w];
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int nsc = g->n_sph_cells;
+    const int n_t = start[nsc];
+    const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
+    const int zdim = dims[Z];
+    float cell[3];
+    float l_other = 0.f;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        cell[d] = (float)(c.periodic[d] ? g->scell[d] : g->sr2);
+        if (d < Z) l_other = fmaxf(l_other, 2.f * cell[d]);
+    }
+    const float cz = cell[Z];
+    int code_fixed = 0;
+#pragma unroll
+    for (int d = ND; d < 3; d++) code_fixed += code_stride(d);
+    const int zstride = code_stride(Z) << B_BITS;
+    const int self_e = CENTER_CODE;
+    const float K_HI = 4.f * (1.f + 5e-7f), K_LO = 4.f * (1.f - 5e-7f);
+
+    for (int t0 = (blockIdx.x * NL_WARPS + w) * 32; t0 < n_t; t0 += NL_WARPS * gridDim.x * 32) {
+        const int a = t0 + lane;
+        bool act = false;
+        int key = 0;
+        if (a < n_t) {
+            key = skey[a];
+            act = is_sph_or_sphb(tg[a] & 0xff);
+        }
+        int cc[3] = {0, 0, 0};
+        decode<ND>(key, dims, cc);
+        const int col = key / zdim;
+        float4 pa0 = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (act) pa0 = P0[a];
+        int cnt = 0, nb = 0;
+        int *outp = nbr + a;
+        unsigned pending = __ballot_sync(FULL, act);
+        while (pending) {
+            /* a run: lanes in the leader's column within 3 buckets of it */
+            const int leader = __ffs(pending) - 1;
+            const int lcol = __shfl_sync(FULL, col, leader);
+            const int zmin = __shfl_sync(FULL, cc[Z], leader);
+            const unsigned gmask = __ballot_sync(FULL, act && col == lcol && cc[Z] <= zmin + 2) & pending;
+            pending &= ~gmask;
+            const int zmax = __shfl_sync(FULL, cc[Z], 31 - __clz(gmask));
+            int ccol[3] = {0, 0, 0};
+#pragma unroll
+            for (int d = 0; d < Z; d++) ccol[d] = __shfl_sync(FULL, cc[d], leader);
+            const bool mine = (gmask >> lane) & 1u;
+            /* this lane's particle in the run's frame; others sit far away */
+            float pv[3] = {1e30f, 1e30f, 1e30f};
+            float ha2 = 0.f;
+            if (mine) {
+                pv[0] = pa0.x;
+                pv[1] = pa0.y;
+                pv[2] = pa0.z;
+                pv[Z] += (float)(cc[Z] - zmin) * cz;
+                ha2 = pa0.w * pa0.w;
+            }
+            const int lane_zr = cc[Z] - zmin + 1;
+            const float L = fmaxf(l_other, (float)(zmax - zmin + 2) * cz);
+            const float EPS = 1.5e-6f * L * L;
+            int nst = 0;
+
+            auto evaluate = [&]() {
+                __syncwarp();
+#pragma unroll 4
+                for (int j = 0; j < nst; j++) {
+                    const float4 q = cpos[j];
+                    const float dx = pv[0] - q.x;
+                    const float dy = ND > 1 ? pv[1] - q.y : 0.f;
+                    const float dz = ND > 2 ? pv[2] - q.z : 0.f;
+                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                    const float m2 = fmaxf(ha2, q.w);
+                    if (!(r2 <= fmaf(m2, K_HI, EPS))) continue;
+                    const int dzc = (int)czr[j] - lane_zr;
+                    int e = cent[j] + (dzc + 1) * zstride;
+                    if ((e ^ a) == self_e) continue; /* the particle itself */
+                    if (COUNT) {
+                        cnt++;
+                        continue;
+                    }
+                    if (r2 >= fmaf(m2, K_LO, -EPS)) {
+                        /* buckets are at least 2h wide, so a candidate outside this
+                         * particle's own 3^d stencil is at least 2h away: it can only
+                         * pass the FP32 test inside the band, and is no neighbour */
+                        if ((unsigned)(dzc + 1) > 2u) continue;
+                        if (cnt < maxn) {
+                            if (nb < NL_QB) {
+                                bandq[(int64_t)a * NL_QB + nb] = make_int2(e, cnt);
+                                e |= (int)0x80000000u;
+                            } else if (!exact_from_code<ND>(c, s, g, a, e, cc)) {
+                                continue; /* record full: decided here (slow but exact) */
+                            }
+                            nb++;
+                        }
+                    }
+                    if (cnt < maxn) *outp = e;
+                    outp += ld;
+                    cnt++;
+                }
+                __syncwarp();
+                nst = 0;
+            };
+
+            /* candidate cursor: the 3^(d-1) neighbour columns, each cut into
+             * pieces of consecutive buckets (zmin-1 .. zmax+1, split at a
+             * periodic seam) */
+            constexpr int NCOL = Z == 2 ? 9 : (Z == 1 ? 3 : 1);
+            const int zhi = zmax + 1;
+            int colidx = -1, zs_next = zhi + 1, zs_cur = 0, lin_s = 0, k_cur = 0, k_end = 0;
+            int col_lin = 0, code_o = 0;
+            int sh[3] = {0, 0, 0};
+            float off[3] = {0.f, 0.f, 0.f};
+            bool shifted = false;
+            auto next_piece = [&]() -> bool {
+                for (;;) {
+                    if (zs_next <= zhi) {
+                        const int zs = zs_next;
+                        int wz = 0, tz = zs;
+                        if (tz < 0) {
+                            if (!c.periodic[Z]) {
+                                zs_next = 0;
+                                continue;
+                            }
+                            wz = -1;
+                            tz += zdim;
+                        } else if (tz >= zdim) {
+                            if (!c.periodic[Z]) {
+                                zs_next = zhi + 1;
+                                continue;
+                            }
+                            wz = 1;
+                            tz -= zdim;
+                        }
+                        const int pe = min(zhi, (wz + 1) * zdim - 1);
+                        zs_next = pe + 1;
+                        zs_cur = zs;
+                        lin_s = col_lin * zdim + tz;
+                        k_cur = start[lin_s];
+                        k_end = start[lin_s + (pe - zs) + 1];
+                        sh[Z] = wz;
+                        shifted = any_shift<ND>(sh);
+                        if (k_cur < k_end) return true;
+                        continue;
+                    }
+                    if (++colidx >= NCOL) return false;
+                    /* column colidx: offsets o[d] in -1..1 on the axes before Z */
+                    int o[2] = {0, 0};
+                    if (Z == 2) {
+                        o[0] = colidx / 3 - 1;
+                        o[1] = colidx % 3 - 1;
+                    } else if (Z == 1) {
+                        o[0] = colidx - 1;
+                    }
+                    bool ok = true;
+                    col_lin = 0;
+                    code_o = code_fixed;
+#pragma unroll
+                    for (int d = 0; d < Z; d++) {
+                        int t = ccol[d] + o[d];
+                        sh[d] = 0;
+                        if (t < 0) {
+                            ok = ok && c.periodic[d];
+                            t += dims[d];
+                            sh[d] = -1;
+                        } else if (t >= dims[d]) {
+                            ok = ok && c.periodic[d];
+                            t -= dims[d];
+                            sh[d] = 1;
+                        }
+                        col_lin = col_lin * dims[d] + t;
+                        code_o += (o[d] + 1) * code_stride(d);
+                        off[d] = (float)o[d] * cell[d];
+                    }
+                    code_o <<= B_BITS;
+                    zs_next = ok ? zmin - 1 : zhi + 1;
+                }
+            };
+
+            bool more = next_piece();
+            while (more) {
+                /* fill the stage, then test it */
+                while (more && nst + 32 <= NL_CAP) {
+                    const int k = k_cur + lane;
+                    bool valid = k < k_end;
+                    float4 pb = make_float4(0.f, 0.f, 0.f, 0.f);
+                    int zrel = 0;
+                    if (valid) {
+                        pb = P0[k];
+                        zrel = zs_cur - zmin + (skey[k] - lin_s);
+                        if (shifted) valid = img_ok<ND>(tg[k] >> 8, sh);
+                    }
+                    const unsigned m = __ballot_sync(FULL, valid);
+                    if (valid) {
+                        const int pos = nst + __popc(m & lt_mask);
+                        float qv[3] = {pb.x + off[0], pb.y + off[1], pb.z + off[2]};
+                        qv[Z] = (Z == 0 ? pb.x : (Z == 1 ? pb.y : pb.z)) + (float)zrel * cz;
+                        cpos[pos] = make_float4(qv[0], qv[1], qv[2], pb.w * pb.w);
+                        cent[pos] = k | code_o;
+                        czr[pos] = (unsigned char)(zrel + 1);
+                    }
+                    nst += __popc(m);
+                    k_cur += 32;
+                    if (k_cur >= k_end) more = next_piece();
+                }
+                evaluate();
+            }
+        }
+        if (act) {
+            ncnt[a] = COUNT ? cnt : min(cnt, maxn);
+            if (!COUNT) {
+                bandn[a] = min(nb, NL_QB);
+                /* stored counts never exceed the list depth; an overflow is an error */
+                if (cnt > maxn) set_err(g, SPHDEM_ERR_CAPACITY, cnt);
+            }
+        } else if (!COUNT && a < n_t) {
+            bandn[a] = 0;
+        }
+    }
+}
+
+/* Decide the recorded band candidates of every particle: the double-float
+ * refinement settles all but FP64 ties, which take the reference's FP64
+ * predicate.  Keep (clear the pending bit) or mark the list slot invalid (-1). */
+template <int ND>
+__global__ void k_band_fix(DevCfg c, DevState s, const DevGlobals *__restrict__ g, const int *__restrict__ start,
+                           const int *__restrict__ skey, const float4 *__restrict__ P0,
+                           const float4 *__restrict__ P0lo, const int2 *__restrict__ bandq,
+                           const int *__restrict__ bandn, int *__restrict__ nbr, int64_t ld) {
+    const int n_t = start[g->n_sph_cells];
     float cell[3], cell_lo[3];
+    float cmax = 0.f;
 #pragma unroll
     for (int d = 0; d < 3; d++) {
         const double cw = c.periodic[d] ? g->scell[d] : g->sr2;
         cell[d] = (float)cw;
         cell_lo[d] = (float)(cw - (double)cell[d]);
+        if (d < ND) cmax = fmaxf(cmax, cell[d]);
     }
-    for (int ci = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; ci < nsc; ci += warps) {
-        const int s0 = start[ci], s1 = start[ci + 1];
-        if (s0 == s1) continue;
+    const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
+    for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < n_t; a += gridDim.x * blockDim.x) {
+        const int nb = bandn[a];
+        if (nb == 0) continue;
         int cc[3] = {0, 0, 0};
-        decode<ND>(ci, dims, cc);
-        for (int base = s0; base < s1; base += 32) {
-            const int a = base + lane;
-            const bool act = a < s1 && is_sph_or_sphb(tg[a] & 0xff);
-            float4 pa = make_float4(0.f, 0.f, 0.f, 0.f);
-            if (act) pa = P0[a];
-            int cnt = 0;
-            int o[3] = {0, 0, 0};
-            for (o[0] = -1; o[0] <= 1; o[0]++)
-                for (o[1] = (ND > 1 ? -1 : 0); o[1] <= (ND > 1 ? 1 : 0); o[1]++)
-                    for (o[2] = (ND > 2 ? -1 : 0); o[2] <= (ND > 2 ? 1 : 0); o[2]++) {
-                        int sh[3] = {0, 0, 0};
-                        const int lin = nb_cell<ND>(cc, o, dims, c.periodic, sh);
-                        if (lin < 0) continue;
-                        const int b0 = start[lin], b1 = start[lin + 1];
-                        const float dx0 = -o[0] * cell[0], dy0 = -o[1] * cell[1], dz0 = -o[2] * cell[2];
-                        const bool shifted = any_shift<ND>(sh);
-                        const int code = ((o[0] + 1) * 9 + (o[1] + 1) * 3 + (o[2] + 1)) << B_BITS;
-                        for (int b = b0; b < b1; b++) {
-                            const float4 pb = P0[b];
-                            if (!act) continue;
-                            const float dx = pa.x - pb.x + dx0;
-                            const float dy = ND > 1 ? pa.y - pb.y + dy0 : 0.f;
-                            const float dz = ND > 2 ? pa.z - pb.z + dz0 : 0.f;
-                            const float r2 = dx * dx + dy * dy + dz * dz;
-                            const float t = 2.f * fmaxf(pa.w, pb.w);
-                            const float T = t * t;
-                            if (r2 > T * (1.f + BAND)) continue;
-                            if (b == a && !shifted) continue;
-                            if (shifted && !img_ok<ND>(tg[b] >> 8, sh)) continue;
-                            bool band = r2 >= T * (1.f - BAND);
-                            if (band) {
-                                /* double-float refinement: offsets, bucket size and h as
-                                 * hi + lo FP32 pairs carry ~48 bits, so |r^2 - (2h)^2| is
-                                 * known to ~1e-13 relative; only closer ties need FP64 */
-                                const float4 al = P0lo[a], bl = P0lo[b];
-                                const float ah[3] = {pa.x, pa.y, pa.z}, bh[3] = {pb.x, pb.y, pb.z};
-                                const float alo[3] = {al.x, al.y, al.z}, blo[3] = {bl.x, bl.y, bl.z};
-                                float r2h = 0.f, r2l = 0.f;
-#pragma unroll
-                                for (int d = 0; d < ND; d++) {
-                                    float s1v, e1, s2v, e2;
-                                    two_sum(ah[d], -bh[d], s1v, e1);
-                                    two_sum(s1v, -o[d] * cell[d], s2v, e2);
-                                    const float lo = e1 + e2 + (alo[d] - blo[d]) - o[d] * cell_lo[d];
-                                    float dh, dl;
-                                    two_sum(s2v, lo, dh, dl);
-                                    float p, pe;
-                                    two_prod(dh, dh, p, pe);
-                                    float t1, te;
-                                    two_sum(r2h, p, t1, te);
-                                    r2h = t1;
-                                    r2l += te + pe + 2.f * dh * dl;
-                                }
-                                /* (2 max h)^2 with h = hi + lo */
-                                const bool amax = pa.w > pb.w || (pa.w == pb.w && al.w >= bl.w);
-                                const float hh = 2.f * (amax ? pa.w : pb.w), hl = 2.f * (amax ? al.w : bl.w);
-                                float Th, Te;
-                                two_prod(hh, hh, Th, Te);
-                                const float Tl = Te + 2.f * hh * hl;
-                                const float diff = (r2h - Th) + (r2l - Tl);
-                                if (fabsf(diff) > 1e-12f * Th) {
-                                    band = false;
-                                    if (diff > 0.f) continue;
-                                }
-                            }
-                            if (cnt < maxn) {
-                                int e = b | code;
-                                if (band && !count_only) {
-                                    /* decided later, in one coalesced FP64 pass; when the
-                                     * queue is full, decided here (slow but exact) */
-                                    const unsigned long long slot = atomicAdd(bandq_n, 1ull);
-                                    if (slot < (unsigned long long)bandq_cap) {
-                                        bandq[slot] = make_int4(a, b, (sh[0] + 1) | ((sh[1] + 1) << 2) | ((sh[2] + 1) << 4), cnt);
-                                        e |= (int)0x80000000u;
-                                    } else if (!exact_neighbour<ND>(c, s, a, b, sh)) {
-                                        e = -1;
-                                    }
-                                }
-                                if (!count_only) nbr[(int64_t)cnt * ld + a] = e;
-                            }
-                            cnt++;
-                        }
-                    }
-            if (act) {
-                /* stored counts never exceed the list depth; an overflow is an error */
-                ncnt[a] = count_only ? cnt : min(cnt, maxn);
-                if (cnt > maxn && !count_only) set_err(g, SPHDEM_ERR_CAPACITY, cnt);
-            }
+        decode<ND>(skey[a], dims, cc);
+        const float4 pa = P0[a], al = P0lo[a];
+        for (int k = 0; k < nb; k++) {
+            const int2 it = bandq[(int64_t)a * NL_QB + k];
+            const int e = it.x, b = e & B_MASK;
+            int o[3];
+            nl_decode_code(e >> B_BITS, o);
+            int dec = nl_refine<ND>(pa, al, P0[b], P0lo[b], o, cell, cell_lo, 1e-13f * cmax * cmax);
+            /* an FP64 tie: the reference's predicate on the periodic image */
+            if (dec == 0) dec = exact_from_code<ND>(c, s, g, a, e, cc) ? 1 : -1;
+            nbr[(int64_t)it.y * ld + a] = dec > 0 ? e : -1;
         }
-    }
-}
-
-/* Decide the queued band candidates with the reference's FP64 predicate:
- * keep (clear the pending bit) or mark the list slot invalid (all ones). */
-template <int ND>
-__global__ void k_band_fix(DevCfg c, DevState s, const int4 *__restrict__ bandq,
-                           const unsigned long long *__restrict__ bandq_n, long long bandq_cap,
-                           int *__restrict__ nbr, int64_t ld) {
-    const unsigned long long nq = min(*bandq_n, (unsigned long long)bandq_cap);
-    for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < nq;
-         q += (unsigned long long)gridDim.x * blockDim.x) {
-        const int4 it = bandq[q];
-        const int a = it.x, b = it.y;
-        const int sh[3] = {(it.z & 3) - 1, ((it.z >> 2) & 3) - 1, ((it.z >> 4) & 3) - 1};
-        int *slot = &nbr[(int64_t)it.w * ld + a];
-        *slot = exact_neighbour<ND>(c, s, a, b, sh) ? (*slot & 0x7fffffff) : -1;
     }
 }
 
@@ -762,6 +994,12 @@ __global__ void __launch_bounds__(BLK) k_couple(DevCfg c, const DevCfg *__restri
             obase[d] = (float)(orig - (c.dorig[d] + klo[d] * c.dcell[d]));
             dcf[d] = (float)c.dcell[d];
         }
+        /* offset terms reach one SPH bucket + 2 Rc + 2 DEM buckets */
+        float lmax = 0.f;
+#pragma unroll
+        for (int d = 0; d < ND; d++)
+            lmax = fmaxf(lmax, (float)(sph_width(c, g, d) + 2.0 * c.rc + 2.0 * c.dcell[d]));
+        const float band_c = fp32_band(rc2, lmax * lmax);
         for (int base = s0; base < s1; base += 32) {
             const int a = base + lane;
             const int ta = a < s1 ? (tg[a] & 0xff) : -1;
@@ -825,8 +1063,8 @@ __global__ void __launch_bounds__(BLK) k_couple(DevCfg c, const DevCfg *__restri
                                 if (ND > 1) dd[1] = pa.y - pb.y + delta[1];
                                 if (ND > 2) dd[2] = pa.z - pb.z + delta[2];
                                 const float r2 = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
-                                bool in = r2 < rc2 * (1.f + BAND);
-                                if (in && r2 >= rc2 * (1.f - BAND))
+                                bool in = r2 < rc2 + band_c;
+                                if (in && r2 >= rc2 - band_c)
                                     in = exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], c.rc2, 1);
                                 if (in) in = coupling_rule(cs, cd, c) != 0;
                                 if (in) {
@@ -909,6 +1147,12 @@ __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restr
     const int sdims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
     float cell[3];
     load_cell32(c, g, cell);
+    float cs2 = 0.f, cd2 = 0.f;
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        cs2 = fmaxf(cs2, cell[d] * cell[d]);
+        cd2 = fmaxf(cd2, (float)(c.dcell[d] * c.dcell[d]));
+    }
     const float wcon = (float)c.wcon;
     for (int a = dem0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < dem1; a += warps) {
         if ((tg[a] & 0xff) != T_DEM) continue;
@@ -947,8 +1191,9 @@ __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restr
                         const float r2 = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
                         const float tt = 2.f * fmaxf(ha, pb.w);
                         const float T = tt * tt;
-                        if (r2 > T * (1.f + BAND)) continue;
-                        if (r2 >= T * (1.f - BAND) && !exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], 0.0, 0))
+                        const float band = fp32_band(T, cs2);
+                        if (r2 > T + band) continue;
+                        if (r2 >= T - band && !exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], 0.0, 0))
                             continue;
                         if (shifted && !img_ok<ND>(tgb >> 8, sh)) continue;
                         if ((tgb & 0xff) == T_BOUNDARY) continue;
@@ -1013,8 +1258,10 @@ __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restr
                         if (ND > 2) dd[2] = od[2] - pb.z - o[2] * (float)c.dcell[2];
                         const float r2 = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
                         const float tt = 2.f * fmaxf(ha, pb.w);
-                        if (r2 > tt * tt * (1.f + BAND)) continue;
-                        if (r2 >= tt * tt * (1.f - BAND) && !exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], 0.0, 0))
+                        const float T = tt * tt;
+                        const float band = fp32_band(T, cd2);
+                        if (r2 > T + band) continue;
+                        if (r2 >= T - band && !exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], 0.0, 0))
                             continue;
                         if (shifted && !img_ok<ND>(tgb >> 8, sh)) continue;
                         const double Rb = s.row(FD_RADIUS)[b] > 0 ? s.row(FD_RADIUS)[b] : c.dem_radius;
@@ -1126,6 +1373,20 @@ __global__ void k_list_export(DevState s, const int *tg, const int *nbr, const i
 }
 
 int warp_blocks(int items) { return std::max(1, std::min(1 << 16, (items + (BLK / 32) - 1) / (BLK / 32))); }
+/* list build: grid-stride over 32-particle slices, one wave of resident blocks */
+template <int ND, bool COUNT>
+int nlist_blocks(int64_t particles) {
+    static int resident = 0;
+    if (!resident) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_nlist<ND, COUNT>, NL_WARPS * 32, 0);
+        resident = std::max(1, sms * per_sm);
+    }
+    const int64_t need = (particles + 32 * NL_WARPS - 1) / (32 * NL_WARPS);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(resident, need));
+}
 
 }  // namespace
 
@@ -1160,31 +1421,33 @@ void pack_fpi(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "pack_fpi32", k_pack_fpi, grid_for(c->n, 256), 256, 0, c->A, c->mx_q0, c->mx_q1, c->mx_q2, c->n);
 }
 
+int band_records_per_particle() { return NL_QB; }
+
 void nlist(sphdem_ctx *c) {
-    const int blocks = warp_blocks(c->cfg.sph_cells_cap);
-    SPHDEM_CUDA_CHECK(cudaMemsetAsync(c->mx_bandq_n, 0, sizeof(unsigned long long), c->stream));
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "nlist32", k_nlist<ND>, blocks, BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->g, c->mx_pos,         \
-                  c->mx_tg, c->mx_nbr, c->mx_ncnt, c->mx_maxn, c->cap, 0, c->mx_bandq, c->mx_bandq_n, c->mx_bandq_cap, \
-                  c->mx_poslo)
+    SPHDEM_LAUNCH(c, "nlist32", (k_nlist<ND, false>), (nlist_blocks<ND, false>(c->n)), NL_WARPS * 32, 0, c->cfg,  \
+                  c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->mx_maxn,  \
+                  c->cap, c->mx_bandq, c->mx_bandn)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "band_fix64", k_band_fix<ND>, 4 * 152, 256, 0, c->cfg, c->A, c->mx_bandq, c->mx_bandq_n,        \
-                  c->mx_bandq_cap, c->mx_nbr, c->cap)
+    SPHDEM_LAUNCH(c, "band_fix", k_band_fix<ND>, grid_for(c->n, 256), 256, 0, c->cfg, c->A, c->g, c->buf.start,  \
+                  c->buf.skey, c->mx_pos, c->mx_poslo, c->mx_bandq, c->mx_bandn, c->mx_nbr, c->cap)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
 
-/* largest neighbour count at the current positions (sizes the lists) */
+/* largest neighbour count at the current positions (sizes the lists); band
+ * candidates count as neighbours, so this is an upper bound */
 int nlist_max_count(sphdem_ctx *c) {
-    const int blocks = warp_blocks(c->cfg.sph_cells_cap);
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(c->mx_ncnt, 0, c->n * sizeof(int), c->stream));
 #define L_(ND)                                                                                                    \
-    k_nlist<ND><<<blocks, BLK, 0, c->stream>>>(c->cfg, c->dcfg, c->A, c->buf.start, c->g, c->mx_pos, c->mx_tg, c->mx_nbr, \
-                                               c->mx_ncnt, 0, c->cap, 1, nullptr, nullptr, 0, c->mx_poslo)
+    k_nlist<ND, true><<<nlist_blocks<ND, true>(c->n), NL_WARPS * 32, 0, c->stream>>>(                           \
+        c->cfg, c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_tg, c->mx_nbr, c->mx_ncnt, 0, c->cap,     \
+        nullptr, nullptr)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
+    SPHDEM_CUDA_CHECK(cudaGetLastError());
     std::vector<int> h(c->n);
     SPHDEM_CUDA_CHECK(cudaMemcpyAsync(h.data(), c->mx_ncnt, c->n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));

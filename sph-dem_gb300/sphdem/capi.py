@@ -89,7 +89,8 @@ class SphDemGlobals(C.Structure):
 class SphDemStats(C.Structure):
     _fields_ = [("n_particles", C.c_int64), ("n_alive", C.c_int64), ("n_list_pairs", C.c_int64),
                 ("list_depth", C.c_int64), ("n_sph_cells", C.c_int64), ("n_dem_cells", C.c_int64),
-                ("h_max", C.c_double), ("search_radius", C.c_double)]
+                ("h_max", C.c_double), ("search_radius", C.c_double),
+                ("n_band_candidates", C.c_int64), ("band_queue_capacity", C.c_int64)]
 
 
 VEC_FIELDS = ("r", "v", "vhat", "norm1", "norm2", "norm3", "f", "fp", "fv", "fb",
