@@ -217,6 +217,19 @@ std::string validate(const SphDemConfig *cfg, const SphDemParticles *p, int64_t 
         if (!(cfg->domain_max[d] > cfg->domain_min[d])) return "empty binning domain";
     if ((cfg->flags & SPHDEM_F_LIQ_DEM) && !(cfg->dem_search_radius > 0 && cfg->coupling_radius > 0))
         return "LIQ_DEM needs dem_search_radius and coupling_radius";
+    if ((cfg->flags & SPHDEM_F_LIQ_DEM) && cfg->precision == SPHDEM_PREC_MIXED) {
+        /* the mixed coupling pass packs reference DEM bucket indices (of
+         * particles and their periodic images) into 10 bits per axis */
+        for (int d = 0; d < cfg->ndim; d++) {
+            const double w = 2 * cfg->dem_search_radius;
+            const double off = 2 * cfg->coupling_radius / cfg->dem_search_radius - 1;
+            const double period = cfg->periodic[d] ? cfg->rmax[d] - cfg->rmin[d] : 0.0;
+            const double kmax = (cfg->domain_max[d] - cfg->domain_min[d] + period) / w + off + 2;
+            const double kmin = -period / w + off - 2;
+            if (kmax > 511 || kmin < -512)
+                return "mixed precision: reference DEM bucket indices outside [-512, 511] along an axis";
+        }
+    }
     for (int64_t i = 0; i < p->n; i++) {
         for (int d = 0; d < 3; d++)
             if (!std::isfinite(p->r[3 * i + d])) return "non-finite position";
@@ -248,6 +261,9 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->mx_q2);
     cudaFree(c->mx_dp);
     cudaFree(c->mx_poslo);
+    cudaFree(c->mx_rc4);
+    cudaFree(c->mx_shep32);
+    cudaFree(c->mx_win);
     cudaFree(c->mx_bandq);
     cudaFree(c->mx_bandn);
     cudaFree(c->dcfg);
@@ -267,7 +283,7 @@ void run_phase_mixed(sphdem_ctx *c, int phase) {
             mixed::pack(c);
             if (lists) mixed::nlist(c);
             if (liq) {
-                zero_dem_shep(c);
+                mixed::zero_shep(c);
                 mixed::porosity(c);
                 mixed::dem_drag(c);
             }
@@ -282,7 +298,7 @@ void run_phase_mixed(sphdem_ctx *c, int phase) {
         case SPHDEM_PHASE_END:
             run_end_drift(c);
             rebuild(c);
-            mixed::pack(c);
+            mixed::pack(c, false);
             if (lists) {
                 mixed::nlist(c);
                 if (c->cfg.var_h()) mixed::omega_eos(c, true, false);
@@ -424,8 +440,12 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
         for (int64_t i = 0; i < n; i++) hmax0 = std::max(hmax0, init->h[i]);
         const double sr_min = 0.5 * std::min(cfg->h, hmax0);
         long long sc = 1;
-        for (int d = 0; d < cfg->ndim; d++)
-            sc *= (long long)((cfg->domain_max[d] - cfg->domain_min[d]) / (2.0 * sr_min)) + 9;
+        int win_cap = 1; /* bucket indices along any one axis */
+        for (int d = 0; d < cfg->ndim; d++) {
+            const long long nd = (long long)((cfg->domain_max[d] - cfg->domain_min[d]) / (2.0 * sr_min)) + 9;
+            sc *= nd;
+            win_cap = (int)std::max<long long>(win_cap, std::min<long long>(nd, 1ll << 30));
+        }
         if (sc > (1ll << 30)) throw std::string("bucket grid too large for the domain / smoothing length");
         c->cfg.sph_cells_cap = (int)sc;
         Buffers &b = c->buf;
@@ -477,6 +497,10 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_q2, capacity * sizeof(float4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_dp, capacity * sizeof(float4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_poslo, capacity * sizeof(float4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_rc4, capacity * sizeof(int4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_shep32, capacity * sizeof(float)));
+            c->mx_win_cap = win_cap;
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_win, 3 * (size_t)win_cap * sizeof(int4)));
             /* list entries that FP32 cannot decide (mostly FP64 ties: a staggered
              * lattice at rest density has 20 neighbours per particle at exactly
              * 2h) are recorded per particle for the FP64 fix-up pass */

@@ -67,6 +67,10 @@ struct sphdem_ctx {
     float4 *mx_q0 = nullptr, *mx_q1 = nullptr, *mx_q2 = nullptr;  /* FPI fields of fluid particles */
     float4 *mx_dp = nullptr;    /* (m/shep, fdrag) of DEM particles */
     float4 *mx_poslo = nullptr; /* low FP32 halves of offsets and h (double-float) */
+    int4 *mx_rc4 = nullptr;     /* packed reference DEM buckets (own, image -L, image +L) */
+    int4 *mx_win = nullptr;     /* coupling windows per SPH bucket index and axis */
+    int mx_win_cap = 0;         /* entries per axis */
+    float *mx_shep32 = nullptr; /* FP32 Shepard sums of DEM particles */
     int2 *mx_bandq = nullptr;   /* per particle: list entries within the FP32 band */
     int *mx_bandn = nullptr;    /* per particle: how many are recorded */
     int mx_band_per_particle = 0;
@@ -111,9 +115,12 @@ void mixed_list_export(sphdem_ctx *c, int *cnt, const long long *offs, int *idx)
 
 /* pairs32.cu: mixed-precision passes */
 namespace mixed {
-void pack(sphdem_ctx *c);
+/* pack the FP32 records; `coupling` also packs the reference DEM buckets and
+ * the coupling windows the SPH-DEM passes need */
+void pack(sphdem_ctx *c, bool coupling = true);
 void pack_fpi(sphdem_ctx *c);
 void nlist(sphdem_ctx *c);
+void zero_shep(sphdem_ctx *c);
 int nlist_max_count(sphdem_ctx *c);
 int band_records_per_particle();
 void omega_eos(sphdem_ctx *c, bool omega, bool eos);

@@ -22,9 +22,9 @@
  *   k_force      calcForce + the Courant/viscous/accel dt conditions
  *   k_dddt       calcDddtDudt
  *   k_couple     calcPorosity + calcShepSum (mode 0) and calcDEMtoSPHDrag +
- *                finalisePorosity (mode 1): one warp per SPH bucket walks the
- *                DEM buckets that can hold a partner within Rc, warp-uniform,
- *                with the reference's asymmetric bucket rule
+ *                finalisePorosity (mode 1): 32-particle slices stage the DEM
+ *                particles of the DEM buckets within Rc in shared memory and
+ *                test them with the reference's asymmetric bucket rule
  *                (dataLL.cpp:1154-1190); the Shepard scatter is reduced over
  *                the warp and lands as one FP64 atomic per (warp, DEM particle)
  *   k_dem_end    calcFPI + calcParticleDrag + calcDEMContacts: one warp per
@@ -184,10 +184,20 @@ __device__ __noinline__ bool exact_pair(const DevCfg *__restrict__ cp, const Dev
 /* ---------------------------------------------------------------------- */
 /* P0 = (offset from own bucket origin, h), P1 = (vhat, mass),
  * P2 = (dens, pdr2, porosity, 1/h), tg = type | gcode << 8 */
+/* reference DEM bucket indices packed 10 bits per axis (biased by 512) */
+constexpr int CP_BIAS = 512;
+
+__device__ __forceinline__ int pack_cells(const int *k, int nd) {
+    int p = 0;
+    for (int d = 0; d < nd; d++) p |= ((k[d] + CP_BIAS) & 1023) << (10 * d);
+    return p;
+}
+
 template <int ND>
 __global__ void k_pack(DevCfg c, DevState s, const int *__restrict__ skey, const DevGlobals *__restrict__ g,
                        float4 *__restrict__ P0, float4 *__restrict__ P1, float4 *__restrict__ P2,
-                       float4 *__restrict__ P0lo, int *__restrict__ tg, int64_t n) {
+                       float4 *__restrict__ P0lo, int *__restrict__ tg, int4 *__restrict__ RC4, int with_rc,
+                       int64_t n) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int t = s.irow(FI_IAM)[i];
@@ -220,6 +230,40 @@ __global__ void k_pack(DevCfg c, DevState s, const int *__restrict__ skey, const
     P1[i] = make_float4(vh[0], vh[1], vh[2], (float)s.row(FD_MASS)[i]);
     P2[i] = make_float4((float)s.row(FD_DENS)[i], (float)s.row(FD_PDR2)[i], (float)s.row(FD_POR)[i],
                         (float)s.row(FD_IH)[i]);
+    if (with_rc) {
+        /* reference DEM buckets (dem_getCellI) of the particle and, for DEM
+         * particles, of its periodic images one period below / above */
+        int k[3] = {0, 0, 0}, km[3] = {0, 0, 0}, kp[3] = {0, 0, 0};
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            const double r = s.row(FD_R + d)[i];
+            k[d] = ref_dem_cell(r, c, d);
+            if (dem && c.periodic[d]) {
+                km[d] = ref_dem_cell(image_pos(r, -1, c.rmin[d], c.rmax[d]), c, d);
+                kp[d] = ref_dem_cell(image_pos(r, 1, c.rmin[d], c.rmax[d]), c, d);
+            }
+        }
+        RC4[i] = make_int4(pack_cells(k, ND), pack_cells(km, ND), pack_cells(kp, ND), 0);
+    }
+}
+
+/* Coupling windows: for SPH bucket index i on axis d, the DEM buckets
+ * [klo, khi] within Rc of it and the FP32 offset of its origin from the
+ * origin of DEM bucket klo (one FP64 evaluation per bucket per rebuild). */
+template <int ND>
+__global__ void k_win(DevCfg c, const DevGlobals *__restrict__ g, int4 *__restrict__ win, int win_cap) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int d = t / win_cap, i = t - d * win_cap;
+    if (d >= ND || i >= g->sdims[d]) return;
+    const double lo = sph_origin(c, g, d, i);
+    const double hi = lo + sph_width(c, g, d);
+    int klo = (int)floor((lo - c.rc - c.dorig[d]) * c.rdcell[d]);
+    int khi = (int)floor((hi + c.rc - c.dorig[d]) * c.rdcell[d]);
+    if (!c.periodic[d]) {
+        klo = max(klo, 0);
+        khi = min(khi, c.ddims[d] - 1);
+    }
+    win[t] = make_int4(klo, khi, __float_as_int((float)(lo - (c.dorig[d] + klo * c.dcell[d]))), 0);
 }
 
 /* fields the DEM side gathers from fluid neighbours in calcFPI (sph.h:1708-1792):
@@ -467,108 +511,109 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
                 nst = 0;
             };
 
-            /* candidate cursor: the 3^(d-1) neighbour columns, each cut into
-             * pieces of consecutive buckets (zmin-1 .. zmax+1, split at a
-             * periodic seam) */
+            /* Range table, one lane per (neighbour column, period piece): the
+             * column's buckets zmin-1 .. zmax+1 cut at the periodic seam into at
+             * most 3 runs of consecutive keys.  All lanes load their bucket range
+             * at once; the candidates of all ranges are then gathered flat. */
             constexpr int NCOL = Z == 2 ? 9 : (Z == 1 ? 3 : 1);
-            const int zhi = zmax + 1;
-            int colidx = -1, zs_next = zhi + 1, zs_cur = 0, lin_s = 0, k_cur = 0, k_end = 0;
-            int col_lin = 0, code_o = 0;
-            int sh[3] = {0, 0, 0};
-            float off[3] = {0.f, 0.f, 0.f};
-            bool shifted = false;
-            auto next_piece = [&]() -> bool {
-                for (;;) {
-                    if (zs_next <= zhi) {
-                        const int zs = zs_next;
-                        int wz = 0, tz = zs;
-                        if (tz < 0) {
-                            if (!c.periodic[Z]) {
-                                zs_next = 0;
-                                continue;
-                            }
-                            wz = -1;
-                            tz += zdim;
-                        } else if (tz >= zdim) {
-                            if (!c.periodic[Z]) {
-                                zs_next = zhi + 1;
-                                continue;
-                            }
-                            wz = 1;
-                            tz -= zdim;
-                        }
-                        const int pe = min(zhi, (wz + 1) * zdim - 1);
-                        zs_next = pe + 1;
-                        zs_cur = zs;
-                        lin_s = col_lin * zdim + tz;
-                        k_cur = start[lin_s];
-                        k_end = start[lin_s + (pe - zs) + 1];
-                        sh[Z] = wz;
-                        shifted = any_shift<ND>(sh);
-                        if (k_cur < k_end) return true;
-                        continue;
-                    }
-                    if (++colidx >= NCOL) return false;
-                    /* column colidx: offsets o[d] in -1..1 on the axes before Z */
-                    int o[2] = {0, 0};
-                    if (Z == 2) {
-                        o[0] = colidx / 3 - 1;
-                        o[1] = colidx % 3 - 1;
-                    } else if (Z == 1) {
-                        o[0] = colidx - 1;
-                    }
-                    bool ok = true;
-                    col_lin = 0;
-                    code_o = code_fixed;
+            int r_b0 = 0, r_cnt = 0, r_lin = 0, r_zoff = 0, r_code = 0, r_sh = 0;
+            float r_ox = 0.f, r_oy = 0.f;
+            if (lane < 3 * NCOL) {
+                const int colidx = lane / 3, wz = lane % 3 - 1;
+                int o[2] = {0, 0};
+                if (Z == 2) {
+                    o[0] = colidx / 3 - 1;
+                    o[1] = colidx % 3 - 1;
+                } else if (Z == 1) {
+                    o[0] = colidx - 1;
+                }
+                bool ok = wz == 0 || c.periodic[Z];
+                int col_lin = 0, code_o = code_fixed, shp = 0;
 #pragma unroll
-                    for (int d = 0; d < Z; d++) {
-                        int t = ccol[d] + o[d];
-                        sh[d] = 0;
-                        if (t < 0) {
-                            ok = ok && c.periodic[d];
-                            t += dims[d];
-                            sh[d] = -1;
-                        } else if (t >= dims[d]) {
-                            ok = ok && c.periodic[d];
-                            t -= dims[d];
-                            sh[d] = 1;
-                        }
-                        col_lin = col_lin * dims[d] + t;
-                        code_o += (o[d] + 1) * code_stride(d);
-                        off[d] = (float)o[d] * cell[d];
+                for (int d = ND; d < 3; d++) shp |= 1 << (2 * d); /* unused axes: no shift */
+                float off[2] = {0.f, 0.f};
+#pragma unroll
+                for (int d = 0; d < Z; d++) {
+                    int t = ccol[d] + o[d], shd = 0;
+                    if (t < 0) {
+                        ok = ok && c.periodic[d];
+                        t += dims[d];
+                        shd = -1;
+                    } else if (t >= dims[d]) {
+                        ok = ok && c.periodic[d];
+                        t -= dims[d];
+                        shd = 1;
                     }
-                    code_o <<= B_BITS;
-                    zs_next = ok ? zmin - 1 : zhi + 1;
+                    col_lin = col_lin * dims[d] + t;
+                    code_o += (o[d] + 1) * code_stride(d);
+                    off[d] = (float)o[d] * cell[d];
+                    shp |= (shd + 1) << (2 * d);
                 }
-            };
+                shp |= (wz + 1) << (2 * Z);
+                /* unwrapped z range of this piece */
+                const int zlo = max(zmin - 1, wz * zdim), zhi = min(zmax + 1, (wz + 1) * zdim - 1);
+                if (ok && zlo <= zhi) {
+                    r_lin = col_lin * zdim + (zlo - wz * zdim);
+                    r_b0 = start[r_lin];
+                    r_cnt = start[r_lin + (zhi - zlo) + 1] - r_b0;
+                    r_zoff = zlo - zmin;
+                    r_code = code_o << B_BITS;
+                    r_sh = shp;
+                    r_ox = off[0];
+                    r_oy = off[1];
+                }
+            }
+            /* exclusive prefix of the range sizes over the lanes */
+            int r_excl = r_cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int v = __shfl_up_sync(FULL, r_excl, o);
+                if (lane >= o) r_excl += v;
+            }
+            const int total = __shfl_sync(FULL, r_excl, 31);
+            r_excl -= r_cnt;
 
-            bool more = next_piece();
-            while (more) {
-                /* fill the stage, then test it */
-                while (more && nst + 32 <= NL_CAP) {
-                    const int k = k_cur + lane;
-                    bool valid = k < k_end;
-                    float4 pb = make_float4(0.f, 0.f, 0.f, 0.f);
-                    int zrel = 0;
-                    if (valid) {
-                        pb = P0[k];
-                        zrel = zs_cur - zmin + (skey[k] - lin_s);
-                        if (shifted) valid = img_ok<ND>(tg[k] >> 8, sh);
-                    }
-                    const unsigned m = __ballot_sync(FULL, valid);
-                    if (valid) {
-                        const int pos = nst + __popc(m & lt_mask);
-                        float qv[3] = {pb.x + off[0], pb.y + off[1], pb.z + off[2]};
-                        qv[Z] = (Z == 0 ? pb.x : (Z == 1 ? pb.y : pb.z)) + (float)zrel * cz;
-                        cpos[pos] = make_float4(qv[0], qv[1], qv[2], pb.w * pb.w);
-                        cent[pos] = k | code_o;
-                        czr[pos] = (unsigned char)(zrel + 1);
-                    }
-                    nst += __popc(m);
-                    k_cur += 32;
-                    if (k_cur >= k_end) more = next_piece();
+            for (int t = 0;;) {
+              for (; t < total && nst + 32 <= NL_CAP; t += 32) {
+                const int j = t + lane;
+                /* the range holding flat index j: the last lane with excl <= j */
+                int src = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const int e = __shfl_sync(FULL, r_excl, src + step);
+                    if (e <= j) src += step;
                 }
-                evaluate();
+                const int b0 = __shfl_sync(FULL, r_b0, src), ex = __shfl_sync(FULL, r_excl, src);
+                const int lin = __shfl_sync(FULL, r_lin, src), zoff = __shfl_sync(FULL, r_zoff, src);
+                const int code = __shfl_sync(FULL, r_code, src), shp = __shfl_sync(FULL, r_sh, src);
+                const float ox = __shfl_sync(FULL, r_ox, src), oy = __shfl_sync(FULL, r_oy, src);
+                bool valid = j < total;
+                float4 pb = make_float4(0.f, 0.f, 0.f, 0.f);
+                int k = 0, zrel = 0;
+                if (valid) {
+                    k = b0 + (j - ex);
+                    pb = P0[k];
+                    zrel = zoff + (skey[k] - lin);
+                    if (shp != 0x15) {
+                        const int shv[3] = {(shp & 3) - 1, ((shp >> 2) & 3) - 1, ((shp >> 4) & 3) - 1};
+                        valid = img_ok<ND>(tg[k] >> 8, shv);
+                    }
+                }
+                const unsigned m = __ballot_sync(FULL, valid);
+                if (valid) {
+                    const int pos = nst + __popc(m & lt_mask);
+                    float qv[3] = {pb.x, pb.y, pb.z};
+                    if (Z > 0) qv[0] += ox;
+                    if (Z > 1) qv[1] += oy;
+                    qv[Z] += (float)zrel * cz;
+                    cpos[pos] = make_float4(qv[0], qv[1], qv[2], pb.w * pb.w);
+                    cent[pos] = k | code;
+                    czr[pos] = (unsigned char)(zrel + 1);
+                }
+                nst += __popc(m);
+              }
+              evaluate();
+              if (t >= total) break;
             }
         }
         if (act) {
@@ -955,181 +1000,357 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
 }
 
 /* ---------------------------------------------------------------------- */
-/* SPH -> DEM coupling, warp per SPH bucket.  MODE 0: porosity + Shepard
- * scatter; MODE 1: DEM->SPH drag + finalisePorosity (+ boundary porosity). */
+/* SPH <-> DEM coupling sums over the reference's coupling neighbours
+ * (calcNeighboursCoupling, dataLL.cpp:1104-1192: DEM within Rc, with the
+ * asymmetric bucket rule).  MODE 0: calcPorosity + the DEM Shepard sums
+ * (sph.h calcPorosity / calcShepSum); MODE 1: calcDEMtoSPHDrag +
+ * finalisePorosity.
+ *
+ * Work split as in k_nlist: a warp takes 32 consecutive particles of the
+ * bucket order, forms runs of buckets along the last axis, and stages the DEM
+ * particles of every DEM bucket within Rc of the run in shared memory
+ * (position in the run's frame, reference DEM bucket of the image, the
+ * partner's packed fields); every lane then tests all staged partners.  The
+ * Shepard contribution of one partner is reduced over the warp and added
+ * with one FP64 atomic. */
+constexpr int CP_WARPS = 8;
+constexpr int CP_CAP = 128;
+
+/* coupling_rule on packed bucket indices; lim_ceil = ceil(couple_lim), so
+ * that for the integer sums rP < couple_lim <=> rP < lim_ceil */
+template <int ND>
+__device__ __forceinline__ bool coupling_rule_packed(int cs, int cd, int num, int lim_ceil) {
+    int rP = 0, rM = 0;
+#pragma unroll
+    for (int d = 0; d < ND; d++) {
+        const int o = ((cd >> (10 * d)) & 1023) - ((cs >> (10 * d)) & 1023);
+        if (o < -num || o > num) return false;
+        rP += (o + 1) * (o + 1);
+        rM += (o - 1) * (o - 1);
+    }
+    if (ND == 1) return true;
+    return rP < lim_ceil || rM < lim_ceil;
+}
+
 template <int ND, int MODE>
-__global__ void __launch_bounds__(BLK) k_couple(DevCfg c, const DevCfg *__restrict__ cp, DevState s, const int *__restrict__ start,
-                                                const DevGlobals *__restrict__ g, const float4 *__restrict__ P0,
-                                                const float4 *__restrict__ P1, const float4 *__restrict__ P2,
-                                                const float4 *__restrict__ DP, const int *__restrict__ tg) {
+__global__ void __launch_bounds__(CP_WARPS * 32, 3) k_couple(DevCfg c, const DevCfg *__restrict__ cp, DevState s,
+                                                          const int *__restrict__ start, const int *__restrict__ skey,
+                                                          const DevGlobals *__restrict__ g,
+                                                          const float4 *__restrict__ P0, const float4 *__restrict__ P1,
+                                                          const float4 *__restrict__ P2, const float4 *__restrict__ DP,
+                                                          const int *__restrict__ tg, const int4 *__restrict__ RC4,
+                                                          const int4 *__restrict__ win, int win_cap,
+                                                          float *__restrict__ shep32) {
+    constexpr int Z = ND - 1;
+    constexpr unsigned FULL = 0xffffffffu;
+    __shared__ float4 s_pos[CP_WARPS][CP_CAP];
+    __shared__ float4 s_aux[CP_WARPS][CP_CAP];
+    __shared__ int2 s_id[CP_WARPS][CP_CAP];
     const int lane = threadIdx.x & 31;
-    const int warps = (blockDim.x >> 5) * gridDim.x;
+    const int w = threadIdx.x >> 5;
+    float4 *cpos = s_pos[w];
+    float4 *caux = s_aux[w];
+    int2 *cid = s_id[w];
+    const unsigned lt_mask = (1u << lane) - 1u;
     const int nsc = g->n_sph_cells;
+    const int n_t = start[nsc];
     const int sdims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
+    const int zdim = sdims[Z];
+    float cell[3];
+    load_cell32(c, g, cell);
+    const float cz = cell[Z];
     const float wcon = (float)c.wcon, two_over_rc = (float)c.two_over_rc;
     const float c_ihn = (float)c.c_ihn, c_ihn2 = (float)c.c_ihn2;
     const float por_incr = (float)c.por_incr, dem_vol = (float)c.dem_vol;
     const float rc2 = (float)c.rc2;
-    for (int ci = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; ci < nsc; ci += warps) {
-        const int s0 = start[ci], s1 = start[ci + 1];
-        if (s0 == s1) continue;
-        int cc[3] = {0, 0, 0};
-        decode<ND>(ci, sdims, cc);
-        int klo[3] = {0, 0, 0}, khi[3] = {0, 0, 0};
-        /* delta(k) = origin(SPH bucket) - origin(DEM bucket k) = base - (k - klo)*dcell:
-         * one FP64 difference per warp, the rest in FP32 (periodic wrap of
-         * k changes the origin by a multiple of L, i.e. nothing) */
-        float obase[3] = {0.f, 0.f, 0.f}, dcf[3] = {0.f, 0.f, 0.f};
+    const float rdens2d = (float)(1.0 / (2.0 * c.dem_radius));
+    const int lim_ceil = (int)ceil(c.couple_lim);
+    const float rc2x = (float)(2.0 * c.rc);
+    float dcf[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-        for (int d = 0; d < ND; d++) {
-            const double orig = sph_origin(c, g, d, cc[d]);
-            klo[d] = (int)floor((orig - c.rc - c.dorig[d]) * c.rdcell[d]);
-            khi[d] = (int)floor((orig + sph_width(c, g, d) + c.rc - c.dorig[d]) * c.rdcell[d]);
-            if (!c.periodic[d]) {
-                klo[d] = max(klo[d], 0);
-                khi[d] = min(khi[d], c.ddims[d] - 1);
-            } else if (khi[d] - klo[d] + 1 > c.ddims[d]) {
-                khi[d] = klo[d] + c.ddims[d] - 1;
-            }
-            obase[d] = (float)(orig - (c.dorig[d] + klo[d] * c.dcell[d]));
-            dcf[d] = (float)c.dcell[d];
+    for (int d = 0; d < ND; d++) dcf[d] = (float)c.dcell[d];
+
+    for (int t0 = (blockIdx.x * CP_WARPS + w) * 32; t0 < n_t; t0 += CP_WARPS * gridDim.x * 32) {
+        const int a = t0 + lane;
+        int ta = -1, key = 0;
+        if (a < n_t) {
+            key = skey[a];
+            ta = tg[a] & 0xff;
         }
-        /* offset terms reach one SPH bucket + 2 Rc + 2 DEM buckets */
-        float lmax = 0.f;
+        const bool act = is_sph_or_sphb(ta);
+        if (MODE == 1 && is_boundary(ta)) s.row(FD_POR)[a] = 1.0;
+        int cc[3] = {0, 0, 0};
+        decode<ND>(key, sdims, cc);
+        const int col = key / zdim;
+        /* this lane's particle: packed fields and reference DEM bucket */
+        float4 pa0 = make_float4(0.f, 0.f, 0.f, 0.f), va = make_float4(0.f, 0.f, 0.f, 0.f);
+        float dvol = 0.f, rdens = 0.f;
+        int cs = 0;
+        if (act) {
+            pa0 = P0[a];
+            va = P1[a];
+            cs = RC4[a].x;
+            const float densa = P2[a].x;
+            dvol = va.w / densa;
+            rdens = ND == 2 ? rdens2d / densa : 1.f / densa;
+        }
+        Kahan por, dpd, acc[ND];
+        por.init(0.f);
+        dpd.init(0.f);
 #pragma unroll
-        for (int d = 0; d < ND; d++)
-            lmax = fmaxf(lmax, (float)(sph_width(c, g, d) + 2.0 * c.rc + 2.0 * c.dcell[d]));
-        const float band_c = fp32_band(rc2, lmax * lmax);
-        for (int base = s0; base < s1; base += 32) {
-            const int a = base + lane;
-            const int ta = a < s1 ? (tg[a] & 0xff) : -1;
-            const bool act = is_sph_or_sphb(ta);
-            if (MODE == 1 && is_boundary(ta)) s.row(FD_POR)[a] = 1.0;
-            float4 pa = make_float4(0.f, 0.f, 0.f, 0.f), va = make_float4(0.f, 0.f, 0.f, 0.f);
-            int cs[3] = {0, 0, 0};
-            float dvol = 0.f, rdens = 0.f;
-            if (act) {
-                pa = P0[a];
-                va = P1[a];
+        for (int k = 0; k < ND; k++) acc[k].init(0.f);
+
+        unsigned pending = __ballot_sync(FULL, act);
+        while (pending) {
+            const int leader = __ffs(pending) - 1;
+            const int lcol = __shfl_sync(FULL, col, leader);
+            const int zmin = __shfl_sync(FULL, cc[Z], leader);
+            const unsigned gmask = __ballot_sync(FULL, act && col == lcol && cc[Z] <= zmin + 2) & pending;
+            pending &= ~gmask;
+            const int zmax = __shfl_sync(FULL, cc[Z], 31 - __clz(gmask));
+            int ccol[3] = {0, 0, 0};
 #pragma unroll
-                for (int d = 0; d < ND; d++) cs[d] = ref_dem_cell(s.row(FD_R + d)[a], c, d);
-                const float densa = P2[a].x;
-                dvol = va.w / densa;
-                rdens = ND == 2 ? (float)(1.0 / (2.0 * c.dem_radius)) / densa : 1.f / densa;
+            for (int d = 0; d < ND; d++) ccol[d] = __shfl_sync(FULL, cc[d], leader);
+            const bool mine = (gmask >> lane) & 1u;
+            float pv[3] = {1e30f, 1e30f, 1e30f};
+            if (mine) {
+                pv[0] = pa0.x;
+                pv[1] = pa0.y;
+                pv[2] = pa0.z;
+                pv[Z] += (float)(cc[Z] - zmin) * cz;
             }
-            Kahan por, dpd, acc[ND];
-            por.init(0.f);
-            dpd.init(0.f);
+            /* DEM buckets within Rc of the run; the origin of DEM bucket k in
+             * the run's frame (origin of bucket (ccol, zmin)) is
+             * obase - (k - klo) * dcell, one FP64 difference per axis */
+            int klo[3] = {0, 0, 0}, khi[3] = {0, 0, 0};
+            float obase[3] = {0.f, 0.f, 0.f};
+            float lmax = 0.f;
 #pragma unroll
-            for (int k = 0; k < ND; k++) acc[k].init(0.f);
-            int k3[3] = {0, 0, 0};
-            for (k3[0] = klo[0]; k3[0] <= khi[0]; k3[0]++)
-                for (k3[1] = (ND > 1 ? klo[1] : 0); k3[1] <= (ND > 1 ? khi[1] : 0); k3[1]++)
-                    for (k3[2] = (ND > 2 ? klo[2] : 0); k3[2] <= (ND > 2 ? khi[2] : 0); k3[2]++) {
-                        int t[3] = {0, 0, 0}, sh[3] = {0, 0, 0};
-                        int lin = 0;
-#pragma unroll
-                        for (int d = 0; d < ND; d++) {
-                            t[d] = k3[d];
-                            if (t[d] < 0) {
-                                t[d] += c.ddims[d];
-                                sh[d] = -1;
-                            } else if (t[d] >= c.ddims[d]) {
-                                t[d] -= c.ddims[d];
-                                sh[d] = 1;
-                            }
-                            lin = lin * c.ddims[d] + t[d];
+            for (int d = 0; d < ND; d++) {
+                const int4 wlo = win[d * win_cap + (d == Z ? zmin : ccol[d])];
+                klo[d] = wlo.x;
+                khi[d] = d == Z ? win[d * win_cap + zmax].y : wlo.y;
+                obase[d] = __int_as_float(wlo.z);
+                if (c.periodic[d] && khi[d] - klo[d] + 1 > c.ddims[d]) khi[d] = klo[d] + c.ddims[d] - 1;
+                lmax = fmaxf(lmax, (d == Z ? (float)(zmax - zmin + 1) : 1.f) * cell[d] + rc2x + 2.f * dcf[d]);
+            }
+            const float band_c = fp32_band(rc2, lmax * lmax);
+            int nst = 0;
+
+            auto evaluate = [&]() {
+                __syncwarp();
+                for (int j = 0; j < nst; j++) {
+                    const float4 q = cpos[j];
+                    const float dd0 = pv[0] - q.x;
+                    const float dd1 = ND > 1 ? pv[1] - q.y : 0.f;
+                    const float dd2 = ND > 2 ? pv[2] - q.z : 0.f;
+                    const float r2 = fmaf(dd2, dd2, fmaf(dd1, dd1, dd0 * dd0));
+                    float wgt = 0.f;
+                    if (r2 < rc2 + band_c) {
+                        const int2 id = cid[j];
+                        bool in = coupling_rule_packed<ND>(cs, id.y, c.couple_num, lim_ceil);
+                        if (in && r2 >= rc2 - band_c) {
+                            const int shp = (unsigned)id.x >> B_BITS;
+                            in = exact_pair<ND>(cp, s, a, id.x & B_MASK, (shp & 3) - 1, ((shp >> 2) & 3) - 1,
+                                                ((shp >> 4) & 3) - 1, c.rc2, 1);
                         }
-                        const int b0 = start[nsc + lin], b1 = start[nsc + lin + 1];
-                        if (b0 == b1) continue;
-                        const bool shifted = any_shift<ND>(sh);
-                        float delta[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-                        for (int d = 0; d < ND; d++) delta[d] = obase[d] - (float)(k3[d] - klo[d]) * dcf[d];
-                        for (int b = b0; b < b1; b++) {
-                            const int tgb = tg[b];
-                            if ((tgb & 0xff) != T_DEM) continue;
-                            if (shifted && !img_ok<ND>(tgb >> 8, sh)) continue;
-                            int cd[3] = {0, 0, 0};
-#pragma unroll
-                            for (int d = 0; d < ND; d++)
-                                cd[d] = shifted ? ref_dem_cell(image_pos(s.row(FD_R + d)[b], sh[d], c.rmin[d], c.rmax[d]), c, d)
-                                                : s.irow(FI_RDC0 + d)[b];
-                            const float4 pb = P0[b];
-                            float w = 0.f;
-                            if (act) {
-                                float dd[3] = {0.f, 0.f, 0.f};
-                                dd[0] = pa.x - pb.x + delta[0];
-                                if (ND > 1) dd[1] = pa.y - pb.y + delta[1];
-                                if (ND > 2) dd[2] = pa.z - pb.z + delta[2];
-                                const float r2 = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
-                                bool in = r2 < rc2 + band_c;
-                                if (in && r2 >= rc2 - band_c)
-                                    in = exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], c.rc2, 1);
-                                if (in) in = coupling_rule(cs, cd, c) != 0;
-                                if (in) {
-                                    const float r = sqrtf(r2);
-                                    const float q = r * two_over_rc;
-                                    w = c_ihn * wK32(q, wcon);
-                                    if (MODE == 0) {
-                                        por.add(por_incr * w);
-                                        if (r != 0.f) {
-                                            const float4 vb = P1[b];
-                                            const float Fq = c_ihn2 * wdK32(q, wcon) / q;
-                                            const float vd = (va.x - vb.x) * dd[0] + (va.y - vb.y) * dd[1] +
-                                                             (va.z - vb.z) * dd[2];
-                                            dpd.add(-dem_vol * vd * Fq);
-#pragma unroll
-                                            for (int k = 0; k < ND; k++) acc[k].add(dem_vol * dd[k] * Fq);
-                                        }
-                                    } else {
-                                        const float4 dp = DP[b];  /* (m/shep, fdrag) of the DEM particle */
-                                        const float sc = dp.x * rdens * w;
-                                        const float fdb[3] = {dp.y, dp.z, dp.w};
-#pragma unroll
-                                        for (int k = 0; k < ND; k++) acc[k].add(-sc * fdb[k]);
-                                    }
-                                }
-                            }
+                        if (in) {
+                            const float r = sqrtf(r2);
+                            const float qq = r * two_over_rc;
+                            wgt = c_ihn * wK32(qq, wcon);
+                            const float4 x = caux[j];
                             if (MODE == 0) {
-                                const float sum = warp_sum(dvol * w);
-                                if (lane == 0 && sum != 0.f) atomicAdd(&s.row(FD_SHEP)[b], (double)sum);
+                                por.add(por_incr * wgt);
+                                if (r != 0.f) {
+                                    const float Fq = c_ihn2 * wdK32(qq, wcon) / qq;
+                                    const float vd = (va.x - x.x) * dd0 + (va.y - x.y) * dd1 + (va.z - x.z) * dd2;
+                                    dpd.add(-dem_vol * vd * Fq);
+                                    const float ddv[3] = {dd0, dd1, dd2};
+#pragma unroll
+                                    for (int k = 0; k < ND; k++) acc[k].add(dem_vol * ddv[k] * Fq);
+                                }
+                            } else {
+                                /* x = (m/shep, fdrag) of the DEM particle */
+                                const float sc = x.x * rdens * wgt;
+                                const float fdb[3] = {x.y, x.z, x.w};
+#pragma unroll
+                                for (int k = 0; k < ND; k++) acc[k].add(-sc * fdb[k]);
                             }
                         }
                     }
-            if (!act) continue;
-            if (MODE == 0) {
-                s.row(FD_POR)[a] = por.s;
-                s.row(FD_DPORDT)[a] = dpd.s;
-#pragma unroll
-                for (int k = 0; k < ND; k++) s.row(FD_GPOR + k)[a] = acc[k].s;
-            } else {
-#pragma unroll
-                for (int k = 0; k < ND; k++) {
-                    const double v = acc[k].s;
-                    s.row(FD_FDRAG + k)[a] = v;
-                    s.row(FD_F + k)[a] += v;
+                    if (MODE == 0 && __any_sync(FULL, wgt != 0.f)) {
+                        const float sum = warp_sum(dvol * wgt);
+                        if (lane == 0 && sum != 0.f) atomicAdd(&shep32[cid[j].x & B_MASK], sum);
+                    }
                 }
-                double p = 1.0 - s.row(FD_POR)[a];
-                if (p < 0.37) {
-                    p = 0.37;
-                    s.row(FD_DPORDT)[a] = 0.0;
-                    for (int k = 0; k < 3; k++) s.row(FD_GPOR + k)[a] = 0.0;
+                __syncwarp();
+                nst = 0;
+            };
+
+            /* Range table in rounds of 32 lanes: one lane per (DEM column of the
+             * window, period piece along the last axis), each a run of
+             * consecutive DEM keys.  All lanes load their ranges at once; the
+             * candidates of a round are then gathered flat. */
+            int nwcol = 1;
+#pragma unroll
+            for (int d = 0; d < Z; d++) nwcol *= khi[d] - klo[d] + 1;
+            const int nranges = 3 * nwcol;
+            const int ddz = c.ddims[Z];
+            const int dstart = nsc;
+            int r0 = -32, t = 0, total = 0;
+            int r_b0 = 0, r_cnt = 0, r_lin = 0, r_zq = 0, r_sh = 0, r_excl = 0;
+            float r_dx = 0.f, r_dy = 0.f;
+            /* next round of ranges with at least one candidate */
+            auto load_round = [&]() -> bool {
+                for (r0 += 32; r0 < nranges; r0 += 32) {
+                    r_b0 = r_cnt = r_lin = r_zq = r_sh = 0;
+                    r_dx = r_dy = 0.f;
+                    const int ri = r0 + lane;
+                    if (ri < nranges) {
+                        const int colq = ri / 3, wz = ri % 3 - 1;
+                        int kq[2] = {0, 0};
+                        if (Z == 2) {
+                            const int nwy = khi[1] - klo[1] + 1;
+                            kq[0] = klo[0] + colq / nwy;
+                            kq[1] = klo[1] + colq % nwy;
+                        } else if (Z == 1) {
+                            kq[0] = klo[0] + colq;
+                        }
+                        int col_lin = 0, shp = 0;
+                        float dl[2] = {0.f, 0.f};
+#pragma unroll
+                        for (int d = ND; d < 3; d++) shp |= 1 << (2 * d);
+#pragma unroll
+                        for (int d = 0; d < Z; d++) {
+                            int tt = kq[d], shd = 0;
+                            if (tt < 0) {
+                                tt += c.ddims[d];
+                                shd = -1;
+                            } else if (tt >= c.ddims[d]) {
+                                tt -= c.ddims[d];
+                                shd = 1;
+                            }
+                            col_lin = col_lin * c.ddims[d] + tt;
+                            dl[d] = (float)(kq[d] - klo[d]) * dcf[d] - obase[d];
+                            shp |= (shd + 1) << (2 * d);
+                        }
+                        shp |= (wz + 1) << (2 * Z);
+                        const bool ok = wz == 0 || c.periodic[Z];
+                        const int zlo = max(klo[Z], wz * ddz), zhi = min(khi[Z], (wz + 1) * ddz - 1);
+                        if (ok && zlo <= zhi) {
+                            r_lin = dstart + col_lin * ddz + (zlo - wz * ddz);
+                            r_b0 = start[r_lin];
+                            r_cnt = start[r_lin + (zhi - zlo) + 1] - r_b0;
+                            r_zq = zlo - klo[Z];
+                            r_sh = shp;
+                            r_dx = dl[0];
+                            r_dy = dl[1];
+                        }
+                    }
+                    r_excl = r_cnt;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(FULL, r_excl, o);
+                        if (lane >= o) r_excl += v;
+                    }
+                    total = __shfl_sync(FULL, r_excl, 31);
+                    r_excl -= r_cnt;
+                    t = 0;
+                    if (total > 0) return true;
                 }
-                s.row(FD_POR)[a] = p;
+                return false;
+            };
+
+            bool more = load_round();
+            for (;;) {
+                while (more && nst + 32 <= CP_CAP) {
+                    const int j = t + lane;
+                    int src = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const int e = __shfl_sync(FULL, r_excl, src + step);
+                        if (e <= j) src += step;
+                    }
+                    const int b0 = __shfl_sync(FULL, r_b0, src), ex = __shfl_sync(FULL, r_excl, src);
+                    const int lin = __shfl_sync(FULL, r_lin, src), zq = __shfl_sync(FULL, r_zq, src);
+                    const int shp = __shfl_sync(FULL, r_sh, src);
+                    const float dx = __shfl_sync(FULL, r_dx, src), dy = __shfl_sync(FULL, r_dy, src);
+                    bool valid = false;
+                    float4 pb = make_float4(0.f, 0.f, 0.f, 0.f), xb = make_float4(0.f, 0.f, 0.f, 0.f);
+                    int b = 0, cdp = 0;
+                    float dzl = 0.f;
+                    if (j < total) {
+                        b = b0 + (j - ex);
+                        const int tgb = tg[b];
+                        const int shv[3] = {(shp & 3) - 1, ((shp >> 2) & 3) - 1, ((shp >> 4) & 3) - 1};
+                        valid = (tgb & 0xff) == T_DEM && (shp == 0x15 || img_ok<ND>(tgb >> 8, shv));
+                        if (valid) {
+                            pb = P0[b];
+                            xb = MODE == 0 ? P1[b] : DP[b];
+                            dzl = (float)(zq + (skey[b] - lin)) * dcf[Z] - obase[Z];
+                            const int4 rc = RC4[b];
+                            cdp = rc.x;
+#pragma unroll
+                            for (int d = 0; d < ND; d++) {
+                                const int m = 1023 << (10 * d);
+                                if (shv[d]) cdp = (cdp & ~m) | ((shv[d] < 0 ? rc.y : rc.z) & m);
+                            }
+                        }
+                    }
+                    const unsigned m = __ballot_sync(FULL, valid);
+                    if (valid) {
+                        const int pos = nst + __popc(m & lt_mask);
+                        float qv[3] = {pb.x, pb.y, pb.z};
+                        if (Z > 0) qv[0] += dx;
+                        if (Z > 1) qv[1] += dy;
+                        qv[Z] += dzl;
+                        cpos[pos] = make_float4(qv[0], qv[1], qv[2], 0.f);
+                        caux[pos] = xb;
+                        cid[pos] = make_int2(b | (shp << B_BITS), cdp);
+                    }
+                    nst += __popc(m);
+                    t += 32;
+                    if (t >= total) more = load_round();
+                }
+                evaluate();
+                if (!more) break;
             }
+        }
+        if (!act) continue;
+        if (MODE == 0) {
+            s.row(FD_POR)[a] = por.s;
+            s.row(FD_DPORDT)[a] = dpd.s;
+#pragma unroll
+            for (int k = 0; k < ND; k++) s.row(FD_GPOR + k)[a] = acc[k].s;
+        } else {
+#pragma unroll
+            for (int k = 0; k < ND; k++) {
+                const double v = acc[k].s;
+                s.row(FD_FDRAG + k)[a] = v;
+                s.row(FD_F + k)[a] += v;
+            }
+            double p = 1.0 - s.row(FD_POR)[a];
+            if (p < 0.37) {
+                p = 0.37;
+                s.row(FD_DPORDT)[a] = 0.0;
+                for (int k = 0; k < 3; k++) s.row(FD_GPOR + k)[a] = 0.0;
+            }
+            s.row(FD_POR)[a] = p;
         }
     }
 }
 
 /* (m/shep, fdrag) of every DEM particle for the DEM->SPH drag (sph.h:1359) */
-__global__ void k_pack_dem_drag(DevState s, float4 *__restrict__ DP, int64_t n) {
+__global__ void k_pack_dem_drag(DevState s, const float *__restrict__ shep32, const float4 *__restrict__ P1,
+                                float4 *__restrict__ DP, int64_t n) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (s.irow(FI_IAM)[i] != T_DEM) return;
-    const double sh = s.row(FD_SHEP)[i];
-    DP[i] = make_float4(sh != 0.0 ? (float)(s.row(FD_MASS)[i] / sh) : 0.f, (float)s.row(FD_FDRAG)[i],
-                        (float)s.row(FD_FDRAG + 1)[i], (float)s.row(FD_FDRAG + 2)[i]);
+    /* the Shepard sum was accumulated in FP32 by k_couple<.., 0> */
+    const float sh = shep32[i];
+    s.row(FD_SHEP)[i] = sh;
+    DP[i] = make_float4(sh != 0.f ? P1[i].w / sh : 0.f, (float)s.row(FD_FDRAG)[i], (float)s.row(FD_FDRAG + 1)[i],
+                        (float)s.row(FD_FDRAG + 2)[i]);
 }
 
 /* ---------------------------------------------------------------------- */
@@ -1373,6 +1594,21 @@ __global__ void k_list_export(DevState s, const int *tg, const int *nbr, const i
 }
 
 int warp_blocks(int items) { return std::max(1, std::min(1 << 16, (items + (BLK / 32) - 1) / (BLK / 32))); }
+/* coupling passes: grid-stride over 32-particle slices, one wave of resident blocks */
+template <int ND, int MODE>
+int resident_blocks(int64_t particles) {
+    static int resident = 0;
+    if (!resident) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_couple<ND, MODE>, CP_WARPS * 32, 0);
+        resident = std::max(1, sms * per_sm);
+    }
+    const int64_t need = (particles + 32 * CP_WARPS - 1) / (32 * CP_WARPS);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(resident, need));
+}
+
 /* list build: grid-stride over 32-particle slices, one wave of resident blocks */
 template <int ND, bool COUNT>
 int nlist_blocks(int64_t particles) {
@@ -1409,12 +1645,24 @@ void mixed_list_export(sphdem_ctx *c, int *cnt, const long long *offs, int *idx)
 
 namespace mixed {
 
-void pack(sphdem_ctx *c) {
+void pack(sphdem_ctx *c, bool coupling) {
+    coupling = coupling && c->cfg.liq_dem();
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "pack32", k_pack<ND>, grid_for(c->n, 256), 256, 0, c->cfg, c->A, c->buf.skey, c->g,         \
-                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_poslo, c->mx_tg, c->n)
+                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_poslo, c->mx_tg, c->mx_rc4, (int)coupling, c->n)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
+    if (coupling) {
+#define L_(ND)                                                                                                  \
+    SPHDEM_LAUNCH(c, "couple_win", k_win<ND>, grid_for(3 * (int64_t)c->mx_win_cap, 256), 256, 0, c->cfg, c->g,   \
+                  c->mx_win, c->mx_win_cap)
+        SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
+#undef L_
+    }
+}
+
+void zero_shep(sphdem_ctx *c) {
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(c->mx_shep32, 0, c->n * sizeof(float), c->stream));
 }
 
 void pack_fpi(sphdem_ctx *c) {
@@ -1482,20 +1730,19 @@ void dddt(sphdem_ctx *c) {
 }
 
 void porosity(sphdem_ctx *c) {
-    const int blocks = warp_blocks(c->cfg.sph_cells_cap);
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "porosity32", (k_couple<ND, 0>), blocks, BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->g,          \
-                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg)
+    SPHDEM_LAUNCH(c, "porosity32", (k_couple<ND, 0>), (resident_blocks<ND, 0>(c->n)), CP_WARPS * 32, 0, c->cfg,   \
+                  c->dcfg, c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg, c->mx_rc4, c->mx_win, c->mx_win_cap, c->mx_shep32)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
 
 void dem_drag(sphdem_ctx *c) {
-    const int blocks = warp_blocks(c->cfg.sph_cells_cap);
-    SPHDEM_LAUNCH(c, "pack_dem_drag32", k_pack_dem_drag, grid_for(c->n, 256), 256, 0, c->A, c->mx_dp, c->n);
+    SPHDEM_LAUNCH(c, "pack_dem_drag32", k_pack_dem_drag, grid_for(c->n, 256), 256, 0, c->A, c->mx_shep32, c->mx_vel,
+                  c->mx_dp, c->n);
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "dem_drag32", (k_couple<ND, 1>), blocks, BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->g,          \
-                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg)
+    SPHDEM_LAUNCH(c, "dem_drag32", (k_couple<ND, 1>), (resident_blocks<ND, 1>(c->n)), CP_WARPS * 32, 0, c->cfg,   \
+                  c->dcfg, c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg, c->mx_rc4, c->mx_win, c->mx_win_cap, c->mx_shep32)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
