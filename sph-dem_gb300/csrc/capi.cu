@@ -263,6 +263,7 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->mx_poslo);
     cudaFree(c->mx_rc4);
     cudaFree(c->mx_shep32);
+    cudaFree(c->mx_ds);
     cudaFree(c->mx_win);
     cudaFree(c->mx_bandq);
     cudaFree(c->mx_bandn);
@@ -499,6 +500,7 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_poslo, capacity * sizeof(float4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_rc4, capacity * sizeof(int4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_shep32, capacity * sizeof(float)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_ds, capacity * sizeof(float4)));
             c->mx_win_cap = win_cap;
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_win, 3 * (size_t)win_cap * sizeof(int4)));
             /* list entries that FP32 cannot decide (mostly FP64 ties: a staggered

@@ -71,6 +71,7 @@ struct sphdem_ctx {
     int4 *mx_win = nullptr;     /* coupling windows per SPH bucket index and axis */
     int mx_win_cap = 0;         /* entries per axis */
     float *mx_shep32 = nullptr; /* FP32 Shepard sums of DEM particles */
+    float4 *mx_ds = nullptr;    /* DEM particles: offset in their SPH bucket, bucket key */
     int2 *mx_bandq = nullptr;   /* per particle: list entries within the FP32 band */
     int *mx_bandn = nullptr;    /* per particle: how many are recorded */
     int mx_band_per_particle = 0;

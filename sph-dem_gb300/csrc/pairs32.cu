@@ -197,7 +197,7 @@ template <int ND>
 __global__ void k_pack(DevCfg c, DevState s, const int *__restrict__ skey, const DevGlobals *__restrict__ g,
                        float4 *__restrict__ P0, float4 *__restrict__ P1, float4 *__restrict__ P2,
                        float4 *__restrict__ P0lo, int *__restrict__ tg, int4 *__restrict__ RC4, int with_rc,
-                       int64_t n) {
+                       float4 *__restrict__ DS, int64_t n) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int t = s.irow(FI_IAM)[i];
@@ -228,8 +228,27 @@ __global__ void k_pack(DevCfg c, DevState s, const int *__restrict__ skey, const
     for (int d = 0; d < ND; d++) vh[d] = (float)s.row(FD_VHAT + d)[i];
     P0[i] = make_float4(off[0], off[1], off[2], (float)s.row(FD_H)[i]);
     P1[i] = make_float4(vh[0], vh[1], vh[2], (float)s.row(FD_MASS)[i]);
-    P2[i] = make_float4((float)s.row(FD_DENS)[i], (float)s.row(FD_PDR2)[i], (float)s.row(FD_POR)[i],
-                        (float)s.row(FD_IH)[i]);
+    /* a DEM particle's pdr2 slot holds its radius (the contact pre-test) */
+    const double rad = s.row(FD_RADIUS)[i] > 0 ? s.row(FD_RADIUS)[i] : c.dem_radius;
+    P2[i] = make_float4((float)s.row(FD_DENS)[i], (float)(t == T_DEM ? rad : s.row(FD_PDR2)[i]),
+                        (float)s.row(FD_POR)[i], (float)s.row(FD_IH)[i]);
+    if (dem) {
+        /* the SPH bucket of a DEM particle and its FP32 offset there (calcFPI) */
+        const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
+        int k[3] = {0, 0, 0}, key = 0;
+        float o[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int d = 0; d < ND; d++) {
+            const double r = s.row(FD_R + d)[i];
+            int kd = c.periodic[d] ? (int)floor((r - c.dmin[d]) * g->rscell[d])
+                                   : trunc_index(r, c.dmin[d], g->sr2, g->rsr2_f, 3.0);
+            kd = kd < 0 ? 0 : (kd >= dims[d] ? dims[d] - 1 : kd);
+            k[d] = kd;
+            key = key * dims[d] + kd;
+            o[d] = (float)(r - sph_origin(c, g, d, kd));
+        }
+        DS[i] = make_float4(o[0], o[1], o[2], __int_as_float(key));
+    }
     if (with_rc) {
         /* reference DEM buckets (dem_getCellI) of the particle and, for DEM
          * particles, of its periodic images one period below / above */
@@ -667,18 +686,33 @@ __global__ void k_band_fix(DevCfg c, DevState s, const DevGlobals *__restrict__ 
     }
 }
 
-template <int ND>
-__device__ __forceinline__ void nb_delta(int e, const float *cell, float4 pa, float4 pb, float *d) {
-    const int code = e >> B_BITS;
-    const int o0 = code / 9 - 1, o1 = (code / 3) % 3 - 1, o2 = code % 3 - 1;
-    d[0] = pa.x - pb.x - o0 * cell[0];
-    d[1] = ND > 1 ? pa.y - pb.y - o1 * cell[1] : 0.f;
-    d[2] = ND > 2 ? pa.z - pb.z - o2 * cell[2] : 0.f;
-}
-
 __device__ __forceinline__ void load_cell32(const DevCfg &c, const DevGlobals *g, float *cell) {
 #pragma unroll
     for (int d = 0; d < 3; d++) cell[d] = (float)(c.periodic[d] ? g->scell[d] : g->sr2);
+}
+
+/* The 27 stencil shifts o * bucket size, indexed by the list entry's code,
+ * in shared memory: one load per pair instead of a decode and three
+ * int-to-float conversions.  Every thread of the block must call this. */
+__device__ __forceinline__ const float4 *stencil_shifts(const DevCfg &c, const DevGlobals *g) {
+    __shared__ float4 tab[27];
+    if (threadIdx.x < 27) {
+        const int code = threadIdx.x;
+        const float o0 = (float)(code / 9 - 1), o1 = (float)((code / 3) % 3 - 1), o2 = (float)(code % 3 - 1);
+        float cell[3];
+        load_cell32(c, g, cell);
+        tab[code] = make_float4(o0 * cell[0], o1 * cell[1], o2 * cell[2], 0.f);
+    }
+    __syncthreads();
+    return tab;
+}
+
+template <int ND>
+__device__ __forceinline__ void nb_delta_t(int e, const float4 *tab, float4 pa, float4 pb, float *d) {
+    const float4 sft = tab[e >> B_BITS];
+    d[0] = pa.x - pb.x - sft.x;
+    d[1] = ND > 1 ? pa.y - pb.y - sft.y : 0.f;
+    d[2] = ND > 2 ? pa.z - pb.z - sft.z : 0.f;
 }
 
 /* ---------------------------------------------------------------------- */
@@ -689,12 +723,11 @@ __global__ void __launch_bounds__(BLK) k_omega_eos(DevCfg c, DevState s, const D
                                                    const int *__restrict__ nbr, const int *__restrict__ ncnt,
                                                    int64_t ld, int64_t n, int do_omega, int do_eos,
                                                    float *__restrict__ om32) {
+    const float4 *shift = stencil_shifts(c, g);
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (a >= n) return;
     if (!is_sph_or_sphb(tg[a] & 0xff)) return;
     if (do_omega) {
-        float cell[3];
-        load_cell32(c, g, cell);
         const float wcon = (float)c.wcon;
         const float4 pa = P0[a];
         const float iha = 1.f / pa.w;
@@ -712,7 +745,7 @@ __global__ void __launch_bounds__(BLK) k_omega_eos(DevCfg c, DevState s, const D
             const float mb = P1[b].w;
             const int tb = tg[b] & 0xff;
             float d[3];
-            nb_delta<ND>(e, cell, pa, pb, d);
+            nb_delta_t<ND>(e, shift, pa, pb, d);
             const float q = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * iha;
             const float pdkh = -q * wdK32(q, wcon) * iha;
             if (is_sph_or_sphb(tb)) om.add(mb * (ihna * pdkh - pd_coef * wK32(q, wcon)));
@@ -829,12 +862,11 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
                                                const float4 *__restrict__ P2, const float *__restrict__ om32,
                                                const int *__restrict__ tg, const int *__restrict__ nbr,
                                                const int *__restrict__ ncnt, int64_t ld, int64_t n) {
+    const float4 *shift = stencil_shifts(c, g);
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float ndt = FLT_MAX;
     const int ta = a < n ? (tg[a] & 0xff) : -1;
     if (is_sph_or_sphb(ta)) {
-        float cell[3];
-        load_cell32(c, g, cell);
         const float wcon = (float)c.wcon;
         const float4 pa = P0[a], va = P1[a], xa = P2[a];
         const float ha = pa.w, iha = xa.w;
@@ -865,7 +897,7 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
             const float4 pb = P0[b], vb = P1[b], xb = P2[b];
             const int tb = tg[b] & 0xff;
             float d[3];
-            nb_delta<ND>(e, cell, pa, pb, d);
+            nb_delta_t<ND>(e, shift, pa, pb, d);
             const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
             const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
             const float r = r2 * rinv;
@@ -957,11 +989,10 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
                                               const float4 *__restrict__ P2, const float *__restrict__ om32,
                                               const int *__restrict__ tg, const int *__restrict__ nbr,
                                               const int *__restrict__ ncnt, int64_t ld, int64_t n) {
+    const float4 *shift = stencil_shifts(c, g);
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (a >= n) return;
     if (!is_sph_or_sphb(tg[a] & 0xff)) return;
-    float cell[3];
-    load_cell32(c, g, cell);
     const float wcon = (float)c.wcon;
     const float4 pa = P0[a], va = P1[a];
     const float ha = pa.w, iha = P2[a].w;
@@ -979,7 +1010,7 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
         const float4 pb = P0[b], vb = P1[b];
         const float ihb = P2[b].w;
         float d[3];
-        nb_delta<ND>(e, cell, pa, pb, d);
+        nb_delta_t<ND>(e, shift, pa, pb, d);
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
         const float rinv = r2 > 0.f ? rsqrtf(r2) : 0.f;
         const float r = r2 * rinv;
@@ -1353,91 +1384,286 @@ __global__ void k_pack_dem_drag(DevState s, const float *__restrict__ shep32, co
                         (float)s.row(FD_FDRAG + 2)[i]);
 }
 
-/* ---------------------------------------------------------------------- */
-/* calcFPI + calcParticleDrag + calcDEMContacts, one warp per DEM particle */
+/* One lane's entry of a bucket range table around a run of buckets (ccol
+ * on the leading axes, zmin..zmax on the last axis Z): lane = 3 * column +
+ * period piece, for the 3^(d-1) neighbour columns; each entry is a run of
+ * consecutive keys key0 + lin .. (buckets zmin-1 .. zmax+1 of the column,
+ * cut at a periodic seam).  Entries of other lanes are empty. */
+struct RangeEntry {
+    int b0, cnt, lin, zoff, shp, code;
+    float ox, oy;
+};
+
 template <int ND>
-__global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restrict__ cp, DevState s, const int *__restrict__ start,
+__device__ __forceinline__ RangeEntry range_entry(int lane, const int *ccol, int zmin, int zmax, const int *dims,
+                                                  const int *periodic, const float *cell, int key0,
+                                                  const int *__restrict__ start) {
+    constexpr int Z = ND - 1;
+    constexpr int NCOL = Z == 2 ? 9 : (Z == 1 ? 3 : 1);
+    RangeEntry r = {0, 0, 0, 0, 0x15, 0, 0.f, 0.f};
+    if (lane >= 3 * NCOL) return r;
+    const int colidx = lane / 3, wz = lane % 3 - 1;
+    int o[2] = {0, 0};
+    if (Z == 2) {
+        o[0] = colidx / 3 - 1;
+        o[1] = colidx % 3 - 1;
+    } else if (Z == 1) {
+        o[0] = colidx - 1;
+    }
+    bool ok = wz == 0 || periodic[Z];
+    int col_lin = 0, code = 0, shp = 0;
+    float off[2] = {0.f, 0.f};
+#pragma unroll
+    for (int d = ND; d < 3; d++) {
+        shp |= 1 << (2 * d);
+        code += code_stride(d);
+    }
+#pragma unroll
+    for (int d = 0; d < Z; d++) {
+        int t = ccol[d] + o[d], shd = 0;
+        if (t < 0) {
+            ok = ok && periodic[d];
+            t += dims[d];
+            shd = -1;
+        } else if (t >= dims[d]) {
+            ok = ok && periodic[d];
+            t -= dims[d];
+            shd = 1;
+        }
+        col_lin = col_lin * dims[d] + t;
+        code += (o[d] + 1) * code_stride(d);
+        off[d] = (float)o[d] * cell[d];
+        shp |= (shd + 1) << (2 * d);
+    }
+    shp |= (wz + 1) << (2 * Z);
+    const int zdim = dims[Z];
+    const int zlo = max(zmin - 1, wz * zdim), zhi = min(zmax + 1, (wz + 1) * zdim - 1);
+    if (ok && zlo <= zhi) {
+        r.lin = key0 + col_lin * zdim + (zlo - wz * zdim);
+        r.b0 = start[r.lin];
+        r.cnt = start[r.lin + (zhi - zlo) + 1] - r.b0;
+        r.zoff = zlo - zmin;
+        r.shp = shp;
+        r.code = code << B_BITS;
+        r.ox = off[0];
+        r.oy = off[1];
+    }
+    return r;
+}
+
+/* exclusive prefix of v over the warp; *total = the sum */
+__device__ __forceinline__ int warp_excl_scan(int v, int lane, int *total) {
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    *total = __shfl_sync(0xffffffffu, x, 31);
+    return x - v;
+}
+
+/* the lane whose range holds flat index j: the last lane with excl <= j */
+__device__ __forceinline__ int warp_range_src(int excl, int j) {
+    int src = 0;
+#pragma unroll
+    for (int step = 16; step > 0; step >>= 1) {
+        const int e = __shfl_sync(0xffffffffu, excl, src + step);
+        if (e <= j) src += step;
+    }
+    return src;
+}
+
+/* One DEM-DEM contact in FP64 (calcDEMContacts, sph.h:1676-1706): the
+ * overlap (Ra + Rb) - r cancels, so r and the spring-dashpot force are FP64 */
+template <int ND>
+__device__ __noinline__ void dem_contact(const DevCfg *__restrict__ cp, const DevState s, int a, int b,
+                                         const int *sh, double *fc) {
+    const double Ra = s.row(FD_RADIUS)[a] > 0 ? s.row(FD_RADIUS)[a] : cp->dem_radius;
+    const double Rb = s.row(FD_RADIUS)[b] > 0 ? s.row(FD_RADIUS)[b] : cp->dem_radius;
+    double dx[3] = {0, 0, 0}, r = 0.0;
+#pragma unroll
+    for (int k = 0; k < ND; k++) {
+        dx[k] = s.row(FD_R + k)[a] - image_pos(s.row(FD_R + k)[b], sh[k], cp->rmin[k], cp->rmax[k]);
+        r += dx[k] * dx[k];
+    }
+    r = sqrt(r);
+    const double overlap = (Ra + Rb) - r;
+    if (!(overlap > 0.0)) return;
+    const double ma = s.row(FD_MASS)[a];
+    double odot = 0.0;
+#pragma unroll
+    for (int k = 0; k < ND; k++) odot -= (s.row(FD_VHAT + k)[a] - s.row(FD_VHAT + k)[b]) * (dx[k] / r);
+    const double sN = cp->dem_k * overlap + cp->dem_gamma * odot;
+#pragma unroll
+    for (int k = 0; k < ND; k++) fc[k] += (sN * (dx[k] / r)) / ma;
+}
+
+/* Update of DEM particle a from its warp-reduced FPI and contact sums
+ * (calcFPI normalisation, sph.h:1708-1792; Di Felice drag, sph.h:1575-1631,
+ * with the drag coefficient in FP32); state accumulation in FP64 */
+template <int ND>
+__device__ __noinline__ void dem_end_update(const DevCfg *__restrict__ cp, const DevState s, int a, float sum,
+                                            float por, const float *fpfb, const float *fv, const float *fvel,
+                                            const double *fc) {
+    double f[3] = {0, 0, 0}, fpv[3] = {0, 0, 0};
+    float vel[3] = {0.f, 0.f, 0.f}, fdrag_out[3] = {0.f, 0.f, 0.f};
+    float pr = por;
+#pragma unroll
+    for (int k = 0; k < ND; k++) {
+        f[k] = s.row(FD_F + k)[a];
+        fpv[k] = s.row(FD_FP + k)[a];
+        vel[k] = fvel[k];
+    }
+    if (sum > 0.5f) {
+        const float rsum = 1.f / sum;
+        float fpfbd[3] = {0.f, 0.f, 0.f}, fvd[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int k = 0; k < ND; k++) {
+            fpfbd[k] = fpfb[k] * rsum;
+            fvd[k] = fv[k] * rsum;
+            vel[k] *= rsum;
+            s.row(FD_FB + k)[a] = fpfbd[k];
+            s.row(FD_FV + k)[a] = fvd[k];
+        }
+        pr *= rsum;
+        float dv[3] = {0.f, 0.f, 0.f}, vd2 = 0.f;
+#pragma unroll
+        for (int k = 0; k < ND; k++) {
+            dv[k] = pr * (vel[k] - (float)s.row(FD_VHAT + k)[a]);
+            vd2 += dv[k] * dv[k];
+        }
+        const float vdiff = sqrtf(vd2);
+        float fdv[3] = {0.f, 0.f, 0.f};
+        if (vdiff != 0.f) {
+            const float A = (float)(cp->pi * (cp->dem_radius * cp->dem_radius));
+            const float Re = (float)(2.0 * cp->dem_radius / cp->viscosity) * vdiff;
+            const float lg = 1.5f - log10f(Re);
+            const float dragGamma = 3.7f - 0.65f * expf(-(lg * lg) / 2.f);
+            const float cc0 = 0.63f + 4.8f / sqrtf(Re);
+            const float sc = 0.5f * A * (cc0 * cc0) * vdiff;
+            const float pw = powf(pr, -dragGamma);
+#pragma unroll
+            for (int k = 0; k < ND; k++) fdv[k] = sc * dv[k] * pw;
+        }
+        const double ma = s.row(FD_MASS)[a];
+        const float vm = (float)(cp->dem_vol / ma), dm = (float)(cp->dens / ma);
+#pragma unroll
+        for (int k = 0; k < ND; k++) {
+            fdrag_out[k] = vm * (fvd[k] + fpfbd[k]) + dm * fdv[k];
+            f[k] += fdrag_out[k];
+        }
+    }
+    for (int k = 0; k < 3; k++) {
+        s.row(FD_FVEL + k)[a] = vel[k];
+        s.row(FD_FDRAG + k)[a] = fdrag_out[k];
+    }
+    s.row(FD_POR)[a] = pr;
+    s.row(FD_SHEP)[a] = sum;
+#pragma unroll
+    for (int k = 0; k < ND; k++) {
+        s.row(FD_F + k)[a] = f[k] + fc[k];
+        s.row(FD_FP + k)[a] = fpv[k] + fc[k];
+    }
+}
+
+/* ---------------------------------------------------------------------- */
+/* calcFPI + calcParticleDrag + calcDEMContacts, one warp per DEM particle.
+ * The candidates of the 3^d SPH buckets and of the 3^d DEM buckets come from
+ * range tables (one lane per bucket run, all loaded at once) and are spread
+ * flat over the lanes; sums are reduced over the warp.  Contacts (the overlap
+ * 2R - r cancels) and the state update are FP64; the Di Felice drag
+ * coefficient is FP32. */
+template <int ND>
+__global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restrict__ cp, DevState s,
+                                                 const int *__restrict__ start, const int *__restrict__ skey,
                                                  const DevGlobals *__restrict__ g, const float4 *__restrict__ P0,
                                                  const float4 *__restrict__ P1, const float4 *__restrict__ P2,
                                                  const float4 *__restrict__ Q0, const float4 *__restrict__ Q1,
-                                                 const float4 *__restrict__ Q2, const int *__restrict__ tg) {
+                                                 const float4 *__restrict__ Q2, const int *__restrict__ tg,
+                                                 const float4 *__restrict__ DS) {
+    constexpr int Z = ND - 1;
+    constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int warps = (blockDim.x >> 5) * gridDim.x;
     const int nsc = g->n_sph_cells;
     const int dem0 = start[nsc], dem1 = start[nsc + c.n_dem_cells];
     const int sdims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
-    float cell[3];
+    float cell[3], dcellf[3];
     load_cell32(c, g, cell);
     float cs2 = 0.f, cd2 = 0.f;
 #pragma unroll
-    for (int d = 0; d < ND; d++) {
-        cs2 = fmaxf(cs2, cell[d] * cell[d]);
-        cd2 = fmaxf(cd2, (float)(c.dcell[d] * c.dcell[d]));
+    for (int d = 0; d < 3; d++) {
+        dcellf[d] = (float)c.dcell[d];
+        if (d < ND) {
+            cs2 = fmaxf(cs2, 4.f * cell[d] * cell[d]);
+            cd2 = fmaxf(cd2, 4.f * dcellf[d] * dcellf[d]);
+        }
     }
     const float wcon = (float)c.wcon;
     for (int a = dem0 + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5); a < dem1; a += warps) {
         if ((tg[a] & 0xff) != T_DEM) continue;
-        double ra[3] = {0, 0, 0};
+        const float4 pa = P0[a];
+        const float ha = pa.w;
+        /* FPI over the SPH candidates: this particle in its SPH bucket's frame */
+        const float4 ds = DS[a];
         int cs[3] = {0, 0, 0};
-        float oa[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-        for (int d = 0; d < ND; d++) {
-            ra[d] = s.row(FD_R + d)[a];
-            int k = c.periodic[d] ? (int)floor((ra[d] - c.dmin[d]) * g->rscell[d])
-                                  : trunc_index(ra[d], c.dmin[d], g->sr2, g->rsr2_f, 3.0);
-            k = k < 0 ? 0 : (k >= sdims[d] ? sdims[d] - 1 : k);
-            cs[d] = k;
-            oa[d] = (float)(ra[d] - sph_origin(c, g, d, k));
-        }
-        const float ha = P0[a].w;
-        /* per-lane partial FPI sums over the SPH candidates */
+        decode<ND>(__float_as_int(ds.w), sdims, cs);
+        const float oa[3] = {ds.x, ds.y, ds.z};
         float sum = 0.f, por = 0.f;
         float fpfb[3] = {0, 0, 0}, fv[3] = {0, 0, 0}, fvel[3] = {0, 0, 0};
-        int o[3] = {0, 0, 0};
-        for (o[0] = -1; o[0] <= 1; o[0]++)
-            for (o[1] = (ND > 1 ? -1 : 0); o[1] <= (ND > 1 ? 1 : 0); o[1]++)
-                for (o[2] = (ND > 2 ? -1 : 0); o[2] <= (ND > 2 ? 1 : 0); o[2]++) {
-                    int sh[3] = {0, 0, 0};
-                    const int lin = nb_cell<ND>(cs, o, sdims, c.periodic, sh);
-                    if (lin < 0) continue;
-                    const bool shifted = any_shift<ND>(sh);
-                    const int b1 = start[lin + 1];
-                    for (int b = start[lin] + lane; b < b1; b += 32) {
-                        const float4 pb = P0[b];
-                        const int tgb = tg[b];
-                        float dd[3] = {0.f, 0.f, 0.f};
-                        dd[0] = oa[0] - pb.x - o[0] * cell[0];
-                        if (ND > 1) dd[1] = oa[1] - pb.y - o[1] * cell[1];
-                        if (ND > 2) dd[2] = oa[2] - pb.z - o[2] * cell[2];
-                        const float r2 = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
-                        const float tt = 2.f * fmaxf(ha, pb.w);
-                        const float T = tt * tt;
-                        const float band = fp32_band(T, cs2);
-                        if (r2 > T + band) continue;
-                        if (r2 >= T - band && !exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], 0.0, 0))
-                            continue;
-                        if (shifted && !img_ok<ND>(tgb >> 8, sh)) continue;
-                        if ((tgb & 0xff) == T_BOUNDARY) continue;
-                        const float4 vb = P1[b], xb = P2[b];
-                        const float mb = vb.w;
-                        const float q = sqrtf(r2) * xb.w;
-                        const float Wab = powi<ND>(xb.w) * wK32(q, wcon);
-                        const float dvW = (mb / xb.x) * Wab, mW = mb * Wab;
-                        const float4 q0 = Q0[b], q1 = Q1[b];
-                        const float fvb[3] = {q0.w, q1.x, q1.y};
-                        const float fb_[3] = {q0.x, q0.y, q0.z};
+        {
+            const RangeEntry re = range_entry<ND>(lane, cs, cs[Z], cs[Z], sdims, c.periodic, cell, 0, start);
+            int total = 0;
+            const int excl = warp_excl_scan(re.cnt, lane, &total);
+            for (int t = 0; t < total; t += 32) {
+                const int j = t + lane;
+                const int src = warp_range_src(excl, j);
+                const int b0 = __shfl_sync(FULL, re.b0, src), ex = __shfl_sync(FULL, excl, src);
+                const int lin = __shfl_sync(FULL, re.lin, src), zoff = __shfl_sync(FULL, re.zoff, src);
+                const int shp = __shfl_sync(FULL, re.shp, src);
+                const float ox = __shfl_sync(FULL, re.ox, src), oy = __shfl_sync(FULL, re.oy, src);
+                if (j >= total) continue;
+                const int b = b0 + (j - ex);
+                const float4 pb = P0[b];
+                const int zrel = zoff + (skey[b] - lin);
+                float qv[3] = {pb.x, pb.y, pb.z};
+                if (Z > 0) qv[0] += ox;
+                if (Z > 1) qv[1] += oy;
+                qv[Z] += (float)zrel * cell[Z];
+                const float d0 = oa[0] - qv[0];
+                const float d1 = ND > 1 ? oa[1] - qv[1] : 0.f;
+                const float d2 = ND > 2 ? oa[2] - qv[2] : 0.f;
+                const float r2 = fmaf(d2, d2, fmaf(d1, d1, d0 * d0));
+                const float tt = 2.f * fmaxf(ha, pb.w);
+                const float T = tt * tt;
+                const float band = fp32_band(T, cs2);
+                if (r2 > T + band) continue;
+                const int sh[3] = {(shp & 3) - 1, ((shp >> 2) & 3) - 1, ((shp >> 4) & 3) - 1};
+                if (r2 >= T - band && !exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], 0.0, 0)) continue;
+                const int tgb = tg[b];
+                if (shp != 0x15 && !img_ok<ND>(tgb >> 8, sh)) continue;
+                if ((tgb & 0xff) == T_BOUNDARY) continue;
+                const float4 vb = P1[b], xb = P2[b];
+                const float mb = vb.w;
+                const float q = sqrtf(r2) * xb.w;
+                const float Wab = powi<ND>(xb.w) * wK32(q, wcon);
+                const float dvW = (mb / xb.x) * Wab, mW = mb * Wab;
+                const float4 q0 = Q0[b], q1 = Q1[b];
+                const float fvb[3] = {q0.w, q1.x, q1.y};
+                const float fb_[3] = {q0.x, q0.y, q0.z};
 #pragma unroll
-                        for (int k = 0; k < ND; k++) {
-                            fpfb[k] += mW * fb_[k];
-                            fv[k] += mW * fvb[k] + dvW * fvb[k];
-                        }
-                        fvel[0] += dvW * vb.x;
-                        fvel[1] += dvW * vb.y;
-                        fvel[2] += dvW * vb.z;
-                        por += dvW * xb.z;
-                        sum += dvW;
-                    }
+                for (int k = 0; k < ND; k++) {
+                    fpfb[k] += mW * fb_[k];
+                    fv[k] += mW * fvb[k] + dvW * fvb[k];
                 }
+                fvel[0] += dvW * vb.x;
+                fvel[1] += dvW * vb.y;
+                fvel[2] += dvW * vb.z;
+                por += dvW * xb.z;
+                sum += dvW;
+            }
+        }
         sum = warp_sum(sum);
         por = warp_sum(por);
 #pragma unroll
@@ -1448,127 +1674,51 @@ __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restr
         }
         /* DEM contacts over the DEM grid (sph.h:1676-1706), FP64 per contact */
         int cdm[3] = {0, 0, 0};
-        float od[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-        for (int d = 0; d < ND; d++) {
-            int k = (int)floor((ra[d] - c.dorig[d]) * c.rdcell[d]);
-            if (k < 0) k = c.periodic[d] ? c.ddims[d] - 1 : 0;
-            if (k >= c.ddims[d]) k = c.periodic[d] ? 0 : c.ddims[d] - 1;
-            cdm[d] = k;
-            od[d] = (float)(ra[d] - dem_origin(c, d, k));
-        }
-        const double Ra = s.row(FD_RADIUS)[a] > 0 ? s.row(FD_RADIUS)[a] : c.dem_radius;
-        const double ma = s.row(FD_MASS)[a];
+        decode<ND>(skey[a] - nsc, c.ddims, cdm);
+        const float od[3] = {pa.x, pa.y, pa.z};
+        const float Ra_f = P2[a].y;
         double fc[3] = {0, 0, 0};
-        for (o[0] = -1; o[0] <= 1; o[0]++)
-            for (o[1] = (ND > 1 ? -1 : 0); o[1] <= (ND > 1 ? 1 : 0); o[1]++)
-                for (o[2] = (ND > 2 ? -1 : 0); o[2] <= (ND > 2 ? 1 : 0); o[2]++) {
-                    int sh[3] = {0, 0, 0};
-                    const int lin = nb_cell<ND>(cdm, o, c.ddims, c.periodic, sh);
-                    if (lin < 0) continue;
-                    const bool shifted = any_shift<ND>(sh);
-                    const int b1 = start[nsc + lin + 1];
-                    for (int b = start[nsc + lin] + lane; b < b1; b += 32) {
-                        if (b == a && !shifted) continue;
-                        const int tgb = tg[b];
-                        if ((tgb & 0xff) != T_DEM) continue;
-                        const float4 pb = P0[b];
-                        float dd[3] = {0.f, 0.f, 0.f};
-                        dd[0] = od[0] - pb.x - o[0] * (float)c.dcell[0];
-                        if (ND > 1) dd[1] = od[1] - pb.y - o[1] * (float)c.dcell[1];
-                        if (ND > 2) dd[2] = od[2] - pb.z - o[2] * (float)c.dcell[2];
-                        const float r2 = dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2];
-                        const float tt = 2.f * fmaxf(ha, pb.w);
-                        const float T = tt * tt;
-                        const float band = fp32_band(T, cd2);
-                        if (r2 > T + band) continue;
-                        if (r2 >= T - band && !exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], 0.0, 0))
-                            continue;
-                        if (shifted && !img_ok<ND>(tgb >> 8, sh)) continue;
-                        const double Rb = s.row(FD_RADIUS)[b] > 0 ? s.row(FD_RADIUS)[b] : c.dem_radius;
-                        if ((float)(Ra + Rb) * 1.0001f - sqrtf(r2) <= 0.f) continue;
-                        /* a contact: overlap = 2R - r cancels, so r and the force in FP64 */
-                        double dx[3] = {0, 0, 0}, r = 0.0;
-#pragma unroll
-                        for (int k = 0; k < ND; k++) {
-                            dx[k] = ra[k] - image_pos(s.row(FD_R + k)[b], sh[k], c.rmin[k], c.rmax[k]);
-                            r += dx[k] * dx[k];
-                        }
-                        r = sqrt(r);
-                        const double overlap = (Ra + Rb) - r;
-                        if (overlap > 0.0) {
-                            double odot = 0.0;
-#pragma unroll
-                            for (int k = 0; k < ND; k++)
-                                odot -= (s.row(FD_VHAT + k)[a] - s.row(FD_VHAT + k)[b]) * (dx[k] / r);
-                            const double sN = c.dem_k * overlap + c.dem_gamma * odot;
-#pragma unroll
-                            for (int k = 0; k < ND; k++) fc[k] += (sN * (dx[k] / r)) / ma;
-                        }
-                    }
-                }
+        {
+            const RangeEntry re = range_entry<ND>(lane, cdm, cdm[Z], cdm[Z], c.ddims, c.periodic, dcellf, nsc, start);
+            int total = 0;
+            const int excl = warp_excl_scan(re.cnt, lane, &total);
+            for (int t = 0; t < total; t += 32) {
+                const int j = t + lane;
+                const int src = warp_range_src(excl, j);
+                const int b0 = __shfl_sync(FULL, re.b0, src), ex = __shfl_sync(FULL, excl, src);
+                const int lin = __shfl_sync(FULL, re.lin, src), zoff = __shfl_sync(FULL, re.zoff, src);
+                const int shp = __shfl_sync(FULL, re.shp, src);
+                const float ox = __shfl_sync(FULL, re.ox, src), oy = __shfl_sync(FULL, re.oy, src);
+                if (j >= total) continue;
+                const int b = b0 + (j - ex);
+                if (b == a && shp == 0x15) continue;
+                const int tgb = tg[b];
+                if ((tgb & 0xff) != T_DEM) continue;
+                const float4 pb = P0[b];
+                const int zrel = zoff + (skey[b] - lin);
+                float qv[3] = {pb.x, pb.y, pb.z};
+                if (Z > 0) qv[0] += ox;
+                if (Z > 1) qv[1] += oy;
+                qv[Z] += (float)zrel * dcellf[Z];
+                const float d0 = od[0] - qv[0];
+                const float d1 = ND > 1 ? od[1] - qv[1] : 0.f;
+                const float d2 = ND > 2 ? od[2] - qv[2] : 0.f;
+                const float r2 = fmaf(d2, d2, fmaf(d1, d1, d0 * d0));
+                const float tt = 2.f * fmaxf(ha, pb.w);
+                const float T = tt * tt;
+                const float band = fp32_band(T, cd2);
+                if (r2 > T + band) continue;
+                const int sh[3] = {(shp & 3) - 1, ((shp >> 2) & 3) - 1, ((shp >> 4) & 3) - 1};
+                if (r2 >= T - band && !exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], 0.0, 0)) continue;
+                if (shp != 0x15 && !img_ok<ND>(tgb >> 8, sh)) continue;
+                if ((Ra_f + P2[b].y) * 1.0001f - sqrtf(r2) <= 0.f) continue;
+                dem_contact<ND>(cp, s, a, b, sh, fc);
+            }
+        }
 #pragma unroll
         for (int k = 0; k < ND; k++)
-            for (int oo = 16; oo > 0; oo >>= 1) fc[k] += __shfl_xor_sync(0xffffffffu, fc[k], oo);
-        if (lane != 0) continue;
-        double f[3] = {0, 0, 0}, fpv[3] = {0, 0, 0}, vel[3] = {0, 0, 0}, fdrag_out[3] = {0, 0, 0};
-        double pr = por;
-#pragma unroll
-        for (int k = 0; k < ND; k++) {
-            f[k] = s.row(FD_F + k)[a];
-            fpv[k] = s.row(FD_FP + k)[a];
-            vel[k] = fvel[k];
-        }
-        const double ssum = sum;
-        if (ssum > 0.5) {
-            const double rsum = 1.0 / ssum;
-            double fpfbd[3] = {0, 0, 0}, fvd[3] = {0, 0, 0};
-#pragma unroll
-            for (int k = 0; k < ND; k++) {
-                fpfbd[k] = fpfb[k] * rsum;
-                fvd[k] = fv[k] * rsum;
-                vel[k] *= rsum;
-                s.row(FD_FB + k)[a] = fpfbd[k];
-                s.row(FD_FV + k)[a] = fvd[k];
-            }
-            pr *= rsum;
-            /* Di Felice drag (sph.h:1575-1631), per particle in FP64 */
-            double dv[3] = {0, 0, 0}, vd2 = 0.0;
-#pragma unroll
-            for (int k = 0; k < ND; k++) {
-                dv[k] = pr * (vel[k] - s.row(FD_VHAT + k)[a]);
-                vd2 += dv[k] * dv[k];
-            }
-            const double vdiff = sqrt(vd2);
-            double fdv[3] = {0, 0, 0};
-            if (vdiff != 0) {
-                const double A = c.pi * (c.dem_radius * c.dem_radius);
-                const double Re = (2.0 * c.dem_radius / c.viscosity) * vdiff;
-                const double lg = 1.5 - log10(Re);
-                const double dragGamma = 3.7 - 0.65 * exp(-(lg * lg) / 2.0);
-                const double cc0 = 0.63 + 4.8 / sqrt(Re);
-                const double sc = 0.5 * A * (cc0 * cc0) * vdiff;
-                const double pw = pow(pr, -dragGamma);
-#pragma unroll
-                for (int k = 0; k < ND; k++) fdv[k] = sc * dv[k] * pw;
-            }
-#pragma unroll
-            for (int k = 0; k < ND; k++) {
-                fdrag_out[k] = (c.dem_vol / ma) * (fvd[k] + fpfbd[k]) + (c.dens / ma) * fdv[k];
-                f[k] += fdrag_out[k];
-            }
-        }
-        for (int k = 0; k < 3; k++) {
-            s.row(FD_FVEL + k)[a] = vel[k];
-            s.row(FD_FDRAG + k)[a] = fdrag_out[k];
-        }
-        s.row(FD_POR)[a] = pr;
-        s.row(FD_SHEP)[a] = ssum;
-#pragma unroll
-        for (int k = 0; k < ND; k++) {
-            s.row(FD_F + k)[a] = f[k] + fc[k];
-            s.row(FD_FP + k)[a] = fpv[k] + fc[k];
-        }
+            for (int oo = 16; oo > 0; oo >>= 1) fc[k] += __shfl_xor_sync(FULL, fc[k], oo);
+        if (lane == 0) dem_end_update<ND>(cp, s, a, sum, por, fpfb, fv, fvel, fc);
     }
 }
 
@@ -1649,7 +1799,7 @@ void pack(sphdem_ctx *c, bool coupling) {
     coupling = coupling && c->cfg.liq_dem();
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "pack32", k_pack<ND>, grid_for(c->n, 256), 256, 0, c->cfg, c->A, c->buf.skey, c->g,         \
-                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_poslo, c->mx_tg, c->mx_rc4, (int)coupling, c->n)
+                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_poslo, c->mx_tg, c->mx_rc4, (int)coupling, c->mx_ds, c->n)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
     if (coupling) {
@@ -1751,8 +1901,8 @@ void dem_end(sphdem_ctx *c) {
     pack_fpi(c);
     const int blocks = warp_blocks((int)std::min<int64_t>(c->n, 1 << 22));
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "dem_end32", k_dem_end<ND>, blocks, BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->g, c->mx_pos,    \
-                  c->mx_vel, c->mx_aux, c->mx_q0, c->mx_q1, c->mx_q2, c->mx_tg)
+    SPHDEM_LAUNCH(c, "dem_end32", k_dem_end<ND>, blocks, BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->buf.skey,  \
+                  c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_q0, c->mx_q1, c->mx_q2, c->mx_tg, c->mx_ds)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
