@@ -201,6 +201,10 @@ void build_devcfg(const SphDemConfig &h, DevCfg &c) {
         const double t = 2.0 - q;
         c.k_anti = q <= 2.0 ? c.wcon * std::pow(t, 4) * (1.0 + 2.0 * q) : 0.0;
     }
+    c.f_pi = (float)h.pi;
+    c.f_c0 = (float)h.spsound;
+    c.f_rpsep = h.psep > 0 ? (float)(1.0 / h.psep) : 0.f;
+    c.f_rdelp = h.bfac * h.psep > 0 ? (float)(1.0 / (h.bfac * h.psep)) : 0.f;
 }
 
 std::string validate(const SphDemConfig *cfg, const SphDemParticles *p, int64_t cap) {
@@ -264,6 +268,7 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->mx_rc4);
     cudaFree(c->mx_shep32);
     cudaFree(c->mx_ds);
+    cudaFree(c->mx_nb);
     cudaFree(c->mx_win);
     cudaFree(c->mx_bandq);
     cudaFree(c->mx_bandn);
@@ -501,6 +506,7 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_rc4, capacity * sizeof(int4)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_shep32, capacity * sizeof(float)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_ds, capacity * sizeof(float4)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_nb, 3 * capacity * sizeof(float4)));
             c->mx_win_cap = win_cap;
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_win, 3 * (size_t)win_cap * sizeof(int4)));
             /* list entries that FP32 cannot decide (mostly FP64 ties: a staggered

@@ -87,6 +87,8 @@ struct DevCfg {
     double two_over_rc, rc2, c_ihn, c_ihn2, c_hinv;
     double por_incr;      /* (4/3) PI DEM_RADIUS^3 [/(2 DEM_RADIUS) in 2D] */
     double k_anti;        /* K(1/HFAC) for anticlumping */
+    /* FP32 copies for the mixed-precision boundary force */
+    float f_pi, f_c0, f_rpsep, f_rdelp; /* PI, SPSOUND, 1/PSEP, 1/(BFAC*PSEP) */
     __host__ __device__ bool liq_dem() const { return flags & SPHDEM_F_LIQ_DEM; }
     __host__ __device__ bool var_h() const { return flags & SPHDEM_F_VAR_H_CORRECTION; }
 };

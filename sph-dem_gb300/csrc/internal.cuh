@@ -72,6 +72,7 @@ struct sphdem_ctx {
     int mx_win_cap = 0;         /* entries per axis */
     float *mx_shep32 = nullptr; /* FP32 Shepard sums of DEM particles */
     float4 *mx_ds = nullptr;    /* DEM particles: offset in their SPH bucket, bucket key */
+    float4 *mx_nb = nullptr;    /* boundary particles: FP32 normals n1 (+concave), n2, n3 */
     int2 *mx_bandq = nullptr;   /* per particle: list entries within the FP32 band */
     int *mx_bandn = nullptr;    /* per particle: how many are recorded */
     int mx_band_per_particle = 0;

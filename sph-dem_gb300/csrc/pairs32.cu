@@ -197,7 +197,7 @@ template <int ND>
 __global__ void k_pack(DevCfg c, DevState s, const int *__restrict__ skey, const DevGlobals *__restrict__ g,
                        float4 *__restrict__ P0, float4 *__restrict__ P1, float4 *__restrict__ P2,
                        float4 *__restrict__ P0lo, int *__restrict__ tg, int4 *__restrict__ RC4, int with_rc,
-                       float4 *__restrict__ DS, int64_t n) {
+                       float4 *__restrict__ DS, float4 *__restrict__ NB, int64_t n) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int t = s.irow(FI_IAM)[i];
@@ -232,6 +232,18 @@ __global__ void k_pack(DevCfg c, DevState s, const int *__restrict__ skey, const
     const double rad = s.row(FD_RADIUS)[i] > 0 ? s.row(FD_RADIUS)[i] : c.dem_radius;
     P2[i] = make_float4((float)s.row(FD_DENS)[i], (float)(t == T_DEM ? rad : s.row(FD_PDR2)[i]),
                         (float)s.row(FD_POR)[i], (float)s.row(FD_IH)[i]);
+    if (is_boundary(t)) {
+        float nv[3][3] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+#pragma unroll
+        for (int k = 0; k < ND; k++) {
+            nv[0][k] = (float)s.row(FD_N1 + k)[i];
+            nv[1][k] = (float)s.row(FD_N2 + k)[i];
+            nv[2][k] = ND == 3 ? (float)s.row(FD_N3 + k)[i] : 0.f;
+        }
+        NB[3 * i] = make_float4(nv[0][0], nv[0][1], nv[0][2], s.irow(FI_CONCAVE)[i] ? 1.f : -1.f);
+        NB[3 * i + 1] = make_float4(nv[1][0], nv[1][1], nv[1][2], 0.f);
+        NB[3 * i + 2] = make_float4(nv[2][0], nv[2][1], nv[2][2], 0.f);
+    }
     if (dem) {
         /* the SPH bucket of a DEM particle and its FP32 offset there (calcFPI) */
         const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
@@ -801,18 +813,14 @@ __device__ __forceinline__ void block_min_atomic(float v, unsigned long long *ta
 
 /* boundary force of sph.h:736-918 in FP32 (b is a repulsive boundary particle) */
 template <int ND>
-__device__ __noinline__ void boundary32(const DevCfg *__restrict__ cp, const DevState s, int b, float d0, float d1,
-                                        float d2, float r, float dv0, float dv1, float dv2, float ma, float mb,
+__device__ __noinline__ void boundary32(const DevCfg *__restrict__ cp, const float4 *__restrict__ NB, int b, float d0,
+                                        float d1, float d2, float r, float dv0, float dv1, float dv2, float ma, float mb,
                                         float *fbx) {
     const DevCfg &c = *cp;
     const float d[3] = {d0, d1, d2}, dv[3] = {dv0, dv1, dv2};
-    float n1[3] = {0, 0, 0}, n2[3] = {0, 0, 0}, nt[3] = {0, 0, 0}, np[3];
-#pragma unroll
-    for (int k = 0; k < ND; k++) {
-        n1[k] = (float)s.row(FD_N1 + k)[b];
-        n2[k] = (float)s.row(FD_N2 + k)[b];
-        nt[k] = ND == 3 ? (float)s.row(FD_N3 + k)[b] : 0.f;
-    }
+    const float4 N1 = NB[3 * b], N2 = NB[3 * b + 1], N3 = NB[3 * b + 2];
+    const float n1[3] = {N1.x, N1.y, N1.z}, n2[3] = {N2.x, N2.y, N2.z}, nt[3] = {N3.x, N3.y, N3.z};
+    float np[3];
     if (n2[0] == 0.f && n2[1] == 0.f && n2[2] == 0.f) {
         for (int k = 0; k < 3; k++) np[k] = n1[k];
     } else {
@@ -822,13 +830,13 @@ __device__ __noinline__ void boundary32(const DevCfg *__restrict__ cp, const Dev
         if (rnt <= 0.f) {
             for (int k = 0; k < 3; k++) np[k] = d[k] / r;
         } else {
-            const int con = s.irow(FI_CONCAVE)[b] ? 1 : -1;
+            const float con = N1.w;
             for (int k = 0; k < 3; k++) np[k] = con * (rd1 - rd2) > 0.f ? n1[k] : n2[k];
         }
     }
     const float rperp = np[0] * d[0] + np[1] * d[1] + np[2] * d[2];
     const float rt0 = d[0] - rperp * np[0], rt1 = d[1] - rperp * np[1], rt2 = d[2] - rperp * np[2];
-    const float rdelp = (float)(1.0 / (c.bfac * c.psep));
+    const float rdelp = c.f_rdelp;
     float pt0, pt1;
     if (ND == 3) {
         pt0 = fabsf(rt0 * nt[0] + rt1 * nt[1] + rt2 * nt[2]);
@@ -840,9 +848,9 @@ __device__ __noinline__ void boundary32(const DevCfg *__restrict__ cp, const Dev
     }
     const float pd0 = pt0 * rdelp, pd1 = pt1 * rdelp;
     if (!(pd0 <= 1.f && pd1 <= 1.f)) return;
-    const float pif = (float)c.pi, c0 = (float)c.spsound;
+    const float pif = c.f_pi, c0 = c.f_c0;
     const float pesky = 0.25f * (1.f + cosf(pif * pd0)) * (1.f + cosf(pif * pd1));
-    const float q = fabsf(rperp) * (float)(1.0 / c.psep);
+    const float q = fabsf(rperp) * c.f_rpsep;
     if (!(q < 2.f)) return;
     const int beta = (d[0] * dv[0] + d[1] * dv[1] + d[2] * dv[2]) < 0.f ? 1 : 0;
     const float bigA = 0.01f * c0 * c0 - beta * c0 * (dv[0] * np[0] + dv[1] * np[1] + dv[2] * np[2]);
@@ -861,7 +869,8 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
                                                const float4 *__restrict__ P0, const float4 *__restrict__ P1,
                                                const float4 *__restrict__ P2, const float *__restrict__ om32,
                                                const int *__restrict__ tg, const int *__restrict__ nbr,
-                                               const int *__restrict__ ncnt, int64_t ld, int64_t n) {
+                                               const int *__restrict__ ncnt, int64_t ld, int64_t n,
+                                               const float4 *__restrict__ NB) {
     const float4 *shift = stencil_shifts(c, g);
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float ndt = FLT_MAX;
@@ -950,7 +959,7 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
             }
             if (is_boundary(tb)) {
                 float fbx[3] = {0.f, 0.f, 0.f};
-                boundary32<ND>(cp, s, b, d[0], d[1], d[2], r, dv0, dv1, dv2, ma, mb, fbx);
+                boundary32<ND>(cp, NB, b, d[0], d[1], d[2], r, dv0, dv1, dv2, ma, mb, fbx);
 #pragma unroll
                 for (int k = 0; k < ND; k++) fb[k].add(fbx[k]);
             } else if (tb == T_SPH || tb == T_SPHB) {
@@ -1799,7 +1808,8 @@ void pack(sphdem_ctx *c, bool coupling) {
     coupling = coupling && c->cfg.liq_dem();
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "pack32", k_pack<ND>, grid_for(c->n, 256), 256, 0, c->cfg, c->A, c->buf.skey, c->g,         \
-                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_poslo, c->mx_tg, c->mx_rc4, (int)coupling, c->mx_ds, c->n)
+                  c->mx_pos, c->mx_vel, c->mx_aux, c->mx_poslo, c->mx_tg, c->mx_rc4, (int)coupling, c->mx_ds,      \
+                  c->mx_nb, c->n)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
     if (coupling) {
@@ -1866,7 +1876,7 @@ void omega_eos(sphdem_ctx *c, bool omega, bool eos) {
 void force(sphdem_ctx *c) {
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "force32", k_force<ND>, grid_for(c->n, BLK), BLK, 0, c->cfg, c->dcfg, c->A, c->g, c->mx_pos,         \
-                  c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap, c->n)
+                  c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap, c->n, c->mx_nb)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
