@@ -229,6 +229,31 @@ int sphdem_pairs(sphdem_handle h, int kind, int64_t *offsets, int32_t *idx,
  * for DEM, as int32 triples (unused z = 0). */
 int sphdem_cell_ids(sphdem_handle h, int32_t *cell_xyz);
 
+/* ---------------------------------------------------------------------- */
+/* Batched ensembles: no counterpart in the reference, which runs one
+ * simulation per process.  A batch steps many independent handles (any
+ * particle counts, configurations and time steps) with one CUDA graph per
+ * step whose branches are the members' own step sequences.  Members stay
+ * usable on their own (get/set fields, stats); a batch call orders itself
+ * after their pending work and their later calls after it.  Destroy the
+ * batch before its members. */
+typedef struct sphdem_batch_ctx *sphdem_batch;
+
+int sphdem_batch_create(const sphdem_handle *members, int n, sphdem_batch *out);
+int sphdem_batch_destroy(sphdem_batch b);
+/* nsteps full steps of every member (hooks on the device, as sphdem_step) */
+int sphdem_batch_step(sphdem_batch b, int nsteps);
+/* one untimed step, then device time of nsteps graph replays in *ms */
+int sphdem_batch_time_steps(sphdem_batch b, int nsteps, double *ms);
+/* Autotuner: for every member, times steps_per_trial graph-replayed steps
+ * alone for each candidate launch configuration (block size of the
+ * list-consumer passes 64 / 128, grid of the slice passes full or 1/4) and
+ * keeps the fastest.  This advances every member by 4 x (steps_per_trial + 1)
+ * steps.  `chosen` (optional, 2 ints per member) receives block size and
+ * grid divisor. */
+int sphdem_batch_tune(sphdem_batch b, int steps_per_trial, int *chosen);
+int sphdem_batch_last_error(sphdem_batch b, char *buf, size_t len);
+
 /* Largest particle count sphdem_cell_ids_noalloc accepts. */
 #define SPHDEM_CELL_IDS_NOALLOC_MAX 262144
 

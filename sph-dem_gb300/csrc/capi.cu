@@ -368,6 +368,11 @@ void run_full_step(sphdem_ctx *c) {
 
 }  // namespace
 
+namespace sphdem {
+void step_sequence(sphdem_ctx *c) { run_full_step(c); }
+int device_status(sphdem_ctx *c) { return check_device(c); }
+}  // namespace sphdem
+
 extern "C" {
 
 const char *sphdem_version(void) { return "sphdem-gb300 0.1 (sm_103a)"; }

@@ -73,6 +73,9 @@ struct sphdem_ctx {
     float *mx_shep32 = nullptr; /* FP32 Shepard sums of DEM particles */
     float4 *mx_ds = nullptr;    /* DEM particles: offset in their SPH bucket, bucket key */
     float4 *mx_nb = nullptr;    /* boundary particles: FP32 normals n1 (+concave), n2, n3 */
+    /* launch knobs chosen by the batch autotuner */
+    int blk_pair = 128;         /* block size of the list-consumer passes (<= 128) */
+    int grid_div = 1;           /* divides the resident-block grid of the slice passes */
     int2 *mx_bandq = nullptr;   /* per particle: list entries within the FP32 band */
     int *mx_bandn = nullptr;    /* per particle: how many are recorded */
     int mx_band_per_particle = 0;
@@ -132,6 +135,11 @@ void porosity(sphdem_ctx *c);
 void dem_drag(sphdem_ctx *c);
 void dem_end(sphdem_ctx *c);
 }  // namespace mixed
+
+/* capi.cu: one full step (all phases and hooks) on the handle's stream, and
+ * the device error flags (synchronises) */
+void step_sequence(sphdem_ctx *c);
+int device_status(sphdem_ctx *c);
 
 /* fields.cu */
 void field_get(sphdem_ctx *c, int row, int ncomp, double *host);

@@ -1833,7 +1833,7 @@ int band_records_per_particle() { return NL_QB; }
 
 void nlist(sphdem_ctx *c) {
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "nlist32", (k_nlist<ND, false>), (nlist_blocks<ND, false>(c->n)), NL_WARPS * 32, 0, c->cfg,  \
+    SPHDEM_LAUNCH(c, "nlist32", (k_nlist<ND, false>), (std::max(1, nlist_blocks<ND, false>(c->n) / c->grid_div)), NL_WARPS * 32, 0, c->cfg,  \
                   c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->mx_maxn,  \
                   c->cap, c->mx_bandq, c->mx_bandn)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
@@ -1866,7 +1866,8 @@ int nlist_max_count(sphdem_ctx *c) {
 
 void omega_eos(sphdem_ctx *c, bool omega, bool eos) {
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, omega ? "omega_eos32" : "eos32", k_omega_eos<ND>, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, \
+    SPHDEM_LAUNCH(c, omega ? "omega_eos32" : "eos32", k_omega_eos<ND>, grid_for(c->n, c->blk_pair), c->blk_pair, 0, \
+                  c->cfg, c->A, \
                   c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap, c->n,         \
                   (int)omega, (int)eos, c->mx_om)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
@@ -1875,7 +1876,8 @@ void omega_eos(sphdem_ctx *c, bool omega, bool eos) {
 
 void force(sphdem_ctx *c) {
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "force32", k_force<ND>, grid_for(c->n, BLK), BLK, 0, c->cfg, c->dcfg, c->A, c->g, c->mx_pos,         \
+    SPHDEM_LAUNCH(c, "force32", k_force<ND>, grid_for(c->n, c->blk_pair), c->blk_pair, 0, c->cfg, c->dcfg, c->A,   \
+                  c->g, c->mx_pos, \
                   c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap, c->n, c->mx_nb)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
@@ -1883,7 +1885,8 @@ void force(sphdem_ctx *c) {
 
 void dddt(sphdem_ctx *c) {
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "dddt32", k_dddt<ND>, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, c->g, c->mx_pos, c->mx_vel, \
+    SPHDEM_LAUNCH(c, "dddt32", k_dddt<ND>, grid_for(c->n, c->blk_pair), c->blk_pair, 0, c->cfg, c->A, c->g,      \
+                  c->mx_pos, c->mx_vel, \
                   c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap, c->n)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
@@ -1891,7 +1894,7 @@ void dddt(sphdem_ctx *c) {
 
 void porosity(sphdem_ctx *c) {
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "porosity32", (k_couple<ND, 0>), (resident_blocks<ND, 0>(c->n)), CP_WARPS * 32, 0, c->cfg,   \
+    SPHDEM_LAUNCH(c, "porosity32", (k_couple<ND, 0>), (std::max(1, resident_blocks<ND, 0>(c->n) / c->grid_div)), CP_WARPS * 32, 0, c->cfg,   \
                   c->dcfg, c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg, c->mx_rc4, c->mx_win, c->mx_win_cap, c->mx_shep32)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
@@ -1901,7 +1904,7 @@ void dem_drag(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "pack_dem_drag32", k_pack_dem_drag, grid_for(c->n, 256), 256, 0, c->A, c->mx_shep32, c->mx_vel,
                   c->mx_dp, c->n);
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "dem_drag32", (k_couple<ND, 1>), (resident_blocks<ND, 1>(c->n)), CP_WARPS * 32, 0, c->cfg,   \
+    SPHDEM_LAUNCH(c, "dem_drag32", (k_couple<ND, 1>), (std::max(1, resident_blocks<ND, 1>(c->n) / c->grid_div)), CP_WARPS * 32, 0, c->cfg,   \
                   c->dcfg, c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg, c->mx_rc4, c->mx_win, c->mx_win_cap, c->mx_shep32)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_

@@ -209,6 +209,12 @@ class Library:
                                    C.c_int64, C.POINTER(C.c_int64)]
         L.sphdem_cell_ids.argtypes = [H, C.POINTER(C.c_int32)]
         L.sphdem_cell_ids_noalloc.argtypes = [H, C.POINTER(C.c_int32)]
+        L.sphdem_batch_create.argtypes = [C.POINTER(H), C.c_int, C.POINTER(H)]
+        L.sphdem_batch_destroy.argtypes = [H]
+        L.sphdem_batch_step.argtypes = [H, C.c_int]
+        L.sphdem_batch_time_steps.argtypes = [H, C.c_int, C.POINTER(C.c_double)]
+        L.sphdem_batch_tune.argtypes = [H, C.c_int, C.POINTER(C.c_int)]
+        L.sphdem_batch_last_error.argtypes = [H, C.c_char_p, C.c_size_t]
         L.sphdem_kernel_times.argtypes = [H, C.c_char_p, C.c_size_t, C.POINTER(C.c_double),
                                           C.POINTER(C.c_int64), C.c_int, C.POINTER(C.c_int)]
         L.sphdem_kernel_times_reset.argtypes = [H, C.c_int]
@@ -320,3 +326,50 @@ class Simulation:
                      self.h, "kernel_times")
         keys = names.value.decode().split("\n")
         return {keys[i]: (ms[i], cnt[i]) for i in range(nk.value)}
+
+
+class Batch:
+    """Many Simulations stepped by one CUDA graph per step
+    (sphdem_batch_*).  Keep the member Simulations alive while the batch
+    exists; close the batch first."""
+
+    def __init__(self, lib: "Library", sims):
+        self.L = lib
+        self.sims = list(sims)
+        arr = (C.c_void_p * len(self.sims))(*[s.h.value for s in self.sims])
+        h = C.c_void_p()
+        rc = lib.lib.sphdem_batch_create(arr, len(self.sims), C.byref(h))
+        if rc:
+            raise SphDemError(f"sphdem_batch_create: {ERR_NAMES.get(rc, rc)}")
+        self.h = h
+
+    def _check(self, rc, what):
+        if rc:
+            buf = C.create_string_buffer(1024)
+            self.L.lib.sphdem_batch_last_error(self.h, buf, len(buf))
+            raise SphDemError(f"{what}: {ERR_NAMES.get(rc, rc)}: {buf.value.decode(errors='replace')}")
+
+    def step(self, n: int = 1):
+        self._check(self.L.lib.sphdem_batch_step(self.h, n), "sphdem_batch_step")
+
+    def time_steps(self, n: int) -> float:
+        ms = C.c_double(0)
+        self._check(self.L.lib.sphdem_batch_time_steps(self.h, n, C.byref(ms)), "sphdem_batch_time_steps")
+        return ms.value
+
+    def tune(self, steps_per_trial: int = 3):
+        chosen = (C.c_int * (2 * len(self.sims)))()
+        self._check(self.L.lib.sphdem_batch_tune(self.h, steps_per_trial, chosen), "sphdem_batch_tune")
+        return [(chosen[2 * i], chosen[2 * i + 1]) for i in range(len(self.sims))]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.lib.sphdem_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+

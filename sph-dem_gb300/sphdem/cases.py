@@ -384,6 +384,21 @@ def sediment3d(nx: int = 80, L: float = 0.2, height: float = 0.4,
 # --------------------------------------------------------------------------
 # named workloads
 # --------------------------------------------------------------------------
+def dambreak_ensemble(n_instances: int = 256, seed: int = 5, n_min: int = 2000, n_max: int = 40000,
+                      h_min: float = 1.0, h_max: float = 2.5, width: float = 1.0) -> list:
+    """Batched-ensemble workload: independent 2D dam breaks whose fluid
+    particle counts are log-uniform in [n_min, n_max] (set through dx) and
+    whose column heights are uniform in [h_min, h_max]; one seeded draw."""
+    rng = np.random.default_rng(seed)
+    n_target = np.exp(rng.uniform(math.log(n_min), math.log(n_max), n_instances))
+    heights = rng.uniform(h_min, h_max, n_instances)
+    out = []
+    for k in range(n_instances):
+        dx = math.sqrt(width * heights[k] / n_target[k])
+        out.append(dambreak2d(dx=dx, width=width, height=float(heights[k]), seed=seed + 1 + k))
+    return out
+
+
 def workload(name: str, **kw) -> Case:
     """The five configurations at full size, plus the small variants used as
     golden-fixture and parity cases."""
