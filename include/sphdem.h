@@ -230,6 +230,35 @@ int sphdem_pairs(sphdem_handle h, int kind, int64_t *offsets, int32_t *idx,
 int sphdem_cell_ids(sphdem_handle h, int32_t *cell_xyz);
 
 /* ---------------------------------------------------------------------- */
+/* Adjoint (reverse-mode gradients) of the DEM step: no counterpart in the
+ * reference, which has no derivatives.  Covers handles whose particles are
+ * all DEM (LIQ_DEM without fluid), fixed dt, no damping or freezing;
+ * other handles get SPHDEM_ERR_UNSUPPORTED.
+ *
+ * sphdem_adjoint_forward runs nsteps ordinary steps from the current state,
+ * keeping a device checkpoint every ckpt_every steps.
+ * sphdem_adjoint_backward takes the adjoint of the final r, v and vhat (tag
+ * order, 3 per particle; NULL = zero), replays each checkpoint segment once
+ * and applies the step's vector-Jacobian product in reverse order.  It
+ * returns dL/d(dem_k), dL/d(dem_gamma) and the adjoints of the initial r, v
+ * and vhat (NULL to skip), and leaves the handle at the final state. */
+#define SPHDEM_GRAD_DEM_K      (1u << 0)
+#define SPHDEM_GRAD_DEM_GAMMA  (1u << 1)
+#define SPHDEM_GRAD_POSITIONS  (1u << 2)
+#define SPHDEM_GRAD_VISCOSITY  (1u << 3)
+#define SPHDEM_GRAD_DRAG_SCALE (1u << 4)
+
+typedef struct SphDemGrads {
+    double dem_k, dem_gamma, viscosity, drag_scale;
+    uint32_t valid;             /* SPHDEM_GRAD_* bits of the entries computed */
+} SphDemGrads;
+
+int sphdem_adjoint_forward(sphdem_handle h, int nsteps, int ckpt_every);
+int sphdem_adjoint_backward(sphdem_handle h, const double *dL_dr, const double *dL_dv,
+                            const double *dL_dvhat, SphDemGrads *grads,
+                            double *dL_dr0, double *dL_dv0, double *dL_dvhat0);
+
+/* ---------------------------------------------------------------------- */
 /* Batched ensembles: no counterpart in the reference, which runs one
  * simulation per process.  A batch steps many independent handles (any
  * particle counts, configurations and time steps) with one CUDA graph per

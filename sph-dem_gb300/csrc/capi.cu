@@ -244,6 +244,7 @@ std::string validate(const SphDemConfig *cfg, const SphDemParticles *p, int64_t 
 
 void free_ctx(sphdem_ctx *c) {
     if (!c) return;
+    adjoint_free(c);
     cudaFree(c->A.d);
     cudaFree(c->A.i);
     cudaFree(c->B.d);
@@ -795,6 +796,34 @@ int sphdem_cell_ids(sphdem_handle h, int32_t *cells) {
     } catch (const std::string &e) {
         return fail(h, SPHDEM_ERR_CUDA, e);
     }
+}
+
+int sphdem_adjoint_forward(sphdem_handle h, int nsteps, int ckpt_every) {
+    if (!h || nsteps <= 0 || ckpt_every <= 0) return SPHDEM_ERR_INVALID;
+    try {
+        const std::string why = adjoint_supported(h);
+        if (!why.empty()) return fail(h, SPHDEM_ERR_UNSUPPORTED, why);
+        return adjoint_forward(h, nsteps, ckpt_every);
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+}
+
+int sphdem_adjoint_backward(sphdem_handle h, const double *dL_dr, const double *dL_dv, const double *dL_dvhat,
+                            SphDemGrads *grads, double *dL_dr0, double *dL_dv0, double *dL_dvhat0) {
+    if (!h || !grads) return SPHDEM_ERR_INVALID;
+    std::memset(grads, 0, sizeof(*grads));
+    try {
+        double dk = 0.0, dg = 0.0;
+        const int rc = adjoint_backward(h, dL_dr, dL_dv, dL_dvhat, &dk, &dg, dL_dr0, dL_dv0, dL_dvhat0);
+        if (rc) return fail(h, rc, "more DEM contacts per particle than the adjoint records");
+        grads->dem_k = dk;
+        grads->dem_gamma = dg;
+        grads->valid = SPHDEM_GRAD_DEM_K | SPHDEM_GRAD_DEM_GAMMA | SPHDEM_GRAD_POSITIONS;
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+    return check_device(h);
 }
 
 int sphdem_cell_ids_noalloc(sphdem_handle h, int32_t *cells) {

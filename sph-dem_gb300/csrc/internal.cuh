@@ -10,6 +10,9 @@
 #include "common.cuh"
 
 struct sphdem_ctx;
+namespace sphdem {
+struct AdjointData;
+}
 
 namespace sphdem {
 
@@ -73,6 +76,7 @@ struct sphdem_ctx {
     float *mx_shep32 = nullptr; /* FP32 Shepard sums of DEM particles */
     float4 *mx_ds = nullptr;    /* DEM particles: offset in their SPH bucket, bucket key */
     float4 *mx_nb = nullptr;    /* boundary particles: FP32 normals n1 (+concave), n2, n3 */
+    sphdem::AdjointData *adj = nullptr; /* checkpoints and buffers of the DEM adjoint */
     /* launch knobs chosen by the batch autotuner */
     int blk_pair = 128;         /* block size of the list-consumer passes (<= 128) */
     int grid_div = 1;           /* divides the resident-block grid of the slice passes */
@@ -135,6 +139,13 @@ void porosity(sphdem_ctx *c);
 void dem_drag(sphdem_ctx *c);
 void dem_end(sphdem_ctx *c);
 }  // namespace mixed
+
+/* adjoint.cu */
+void adjoint_free(sphdem_ctx *c);
+std::string adjoint_supported(sphdem_ctx *c);
+int adjoint_forward(sphdem_ctx *c, int nsteps, int ckpt_every);
+int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, const double *seed_vh,
+                     double *dk, double *dgamma, double *dr0, double *dv0, double *dvh0);
 
 /* capi.cu: one full step (all phases and hooks) on the handle's stream, and
  * the device error flags (synchronises) */

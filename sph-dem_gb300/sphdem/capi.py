@@ -86,6 +86,14 @@ class SphDemGlobals(C.Structure):
                 ("sph_step", C.c_int64), ("n_deleted", C.c_int64)]
 
 
+GRAD_DEM_K, GRAD_DEM_GAMMA, GRAD_POSITIONS, GRAD_VISCOSITY, GRAD_DRAG_SCALE = 1, 2, 4, 8, 16
+
+
+class SphDemGrads(C.Structure):
+    _fields_ = [("dem_k", C.c_double), ("dem_gamma", C.c_double), ("viscosity", C.c_double),
+                ("drag_scale", C.c_double), ("valid", C.c_uint32)]
+
+
 class SphDemStats(C.Structure):
     _fields_ = [("n_particles", C.c_int64), ("n_alive", C.c_int64), ("n_list_pairs", C.c_int64),
                 ("list_depth", C.c_int64), ("n_sph_cells", C.c_int64), ("n_dem_cells", C.c_int64),
@@ -209,6 +217,9 @@ class Library:
                                    C.c_int64, C.POINTER(C.c_int64)]
         L.sphdem_cell_ids.argtypes = [H, C.POINTER(C.c_int32)]
         L.sphdem_cell_ids_noalloc.argtypes = [H, C.POINTER(C.c_int32)]
+        D = C.POINTER(C.c_double)
+        L.sphdem_adjoint_forward.argtypes = [H, C.c_int, C.c_int]
+        L.sphdem_adjoint_backward.argtypes = [H, D, D, D, C.POINTER(SphDemGrads), D, D, D]
         L.sphdem_batch_create.argtypes = [C.POINTER(H), C.c_int, C.POINTER(H)]
         L.sphdem_batch_destroy.argtypes = [H]
         L.sphdem_batch_step.argtypes = [H, C.c_int]
@@ -313,6 +324,26 @@ class Simulation:
         ms = C.c_double(0)
         self.L.check(self.L.lib.sphdem_time_steps(self.h, n, C.byref(ms)), self.h, "time_steps")
         return ms.value
+
+    def adjoint_forward(self, nsteps: int, ckpt_every: int):
+        self.L.check(self.L.lib.sphdem_adjoint_forward(self.h, nsteps, ckpt_every), self.h, "adjoint_forward")
+
+    def adjoint_backward(self, dL_dr=None, dL_dv=None, dL_dvhat=None):
+        """Adjoint of the final state (tag order, (n, 3) arrays or None) ->
+        (SphDemGrads, dL/dr0, dL/dv0, dL/dvhat0)."""
+        def arg(x):
+            if x is None:
+                return None
+            x = np.ascontiguousarray(x, dtype=np.float64).reshape(self.n, 3)
+            return x.ctypes.data_as(C.POINTER(C.c_double))
+        keep = [np.ascontiguousarray(x, dtype=np.float64).reshape(self.n, 3) if x is not None else None
+                for x in (dL_dr, dL_dv, dL_dvhat)]
+        outs = [np.zeros((self.n, 3)) for _ in range(3)]
+        g = SphDemGrads()
+        self.L.check(self.L.lib.sphdem_adjoint_backward(
+            self.h, *[arg(x) for x in keep], C.byref(g),
+            *[o.ctypes.data_as(C.POINTER(C.c_double)) for o in outs]), self.h, "adjoint_backward")
+        return g, outs[0], outs[1], outs[2]
 
     def kernel_times_reset(self, enable: bool = True):
         self.L.check(self.L.lib.sphdem_kernel_times_reset(self.h, int(enable)), self.h, "kt_reset")
