@@ -196,6 +196,39 @@ def cpu_baseline(steps=2, warm=1, procs=1):
 
 
 # --------------------------------------------------------------------------
+def measure_adjoint(lib, capi, cases, nsteps=100, ckpt=10):
+    """Wall time of sphdem_adjoint_forward + sphdem_adjoint_backward over the
+    wall time of the same steps stepped plainly, on a DEM-only settling
+    workload (4,913 spheres, FP64 and mixed) -- the configuration the
+    adjoint covers."""
+    case = cases.dem_settling3d(lattice=(17, 17, 17), box=(0.067, 0.067, 0.067), spread=0.0,
+                                nsteps=nsteps, vel_amp=0.3)
+    out = {"workload": f"DEM-only settling, {case.n} spheres, {nsteps} steps, checkpoint every {ckpt}"}
+    for name, prec in (("fp64", cases.PREC_FP64), ("mixed", cases.PREC_MIXED)):
+        sim = capi.Simulation(lib, case.cfg, case.particles, precision=prec)
+        sim.step(2)
+        t0 = time.perf_counter()
+        sim.step(nsteps)
+        t_fwd = time.perf_counter() - t0
+        sim.close()
+        sim = capi.Simulation(lib, case.cfg, case.particles, precision=prec)
+        sim.step(2)
+        a = sim.get(capi.FIELD_IAM)
+        seed = np.zeros((sim.n, 3))
+        dem = a["iam"] == cases.DEM
+        seed[dem, 2] = 1.0 / max(1, dem.sum())
+        t0 = time.perf_counter()
+        sim.adjoint_forward(nsteps, ckpt)
+        t_af = time.perf_counter() - t0
+        sim.adjoint_backward(dL_dr=seed)
+        t_ab = time.perf_counter() - t0 - t_af
+        sim.close()
+        out[name] = {"forward_s": t_fwd, "adjoint_forward_s": t_af, "adjoint_backward_s": t_ab,
+                     "ratio": (t_af + t_ab) / t_fwd}
+    out["ratio"] = out["mixed"]["ratio"]
+    return out
+
+
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return
@@ -276,6 +309,9 @@ def run_ours(args, rank, world):
     ref.close()
     cmp.close()
 
+    # ---- adjoint / forward on the DEM-only workload -----------------------
+    adjoint = measure_adjoint(lib, capi, cases) if not args.no_adjoint else None
+
     # ---- end to end through the C ABI with host buffers -------------------
     e2e_steps = args.steps
     init = capi.ParticleBuffers(n, case.particles, pinned=lib)
@@ -316,7 +352,8 @@ def run_ours(args, rank, world):
                  "mixed_over_fp64": value / fp64_value},
         "error_vs_fp64": {"steps": ref_steps, "max_abs_drho_over_rho0": err_dens,
                           "max_abs_df_over_max_f": err_f},
-        "adjoint_over_forward": None,
+        "adjoint_over_forward": adjoint["ratio"] if adjoint else None,
+        "adjoint": adjoint,
         "roofline": {
             "kernel": "force32", "bound": "hbm", "achieved": achieved_gbs, "peak": peaks.get("hbm_gbs"),
             "unit": "GB/s", "frac": achieved_gbs / peaks.get("hbm_gbs", 6800.0), "traffic": traffic,
@@ -398,6 +435,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=2)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--profile", action="store_true", help="mixed path only (for profiler captures)")
     ap.add_argument("--quarter", action="store_true", help="with --profile: 1/4 sub-box of the workload")
     ap.add_argument("--ensemble", action="store_true", help="batched dam-break ensemble instead")
