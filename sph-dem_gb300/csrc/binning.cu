@@ -15,9 +15,11 @@
  *               non-periodic axes, an L/floor(L/2h) grid on periodic axes;
  *               DEM particles go to the DEM search grid
  *   k_scan_*    bucket starts
- *   k_scatter + k_rank   deterministic counting sort by (bucket, tag): the
- *               within-bucket order is the particle-container order the
- *               reference inserts in (dataLL.cpp:226-231)
+ *   k_scatter + k_rank   deterministic counting sort by bucket, and within
+ *               a bucket by the coordinate on the last axis (ties by tag), so
+ *               that a run of consecutive buckets along that axis is sorted
+ *               by it and the slice passes can cut their candidate ranges
+ *               by binary search
  *   k_gather    one launch moves every live field row into sorted order
  *
  * All sizes and widths live in DevGlobals, so the sequence replays in a CUDA
@@ -353,16 +355,27 @@ __global__ void k_scan_down(const int *cnt, const DevGlobals *g, const int *bsum
     if (base + (int64_t)(threadIdx.x + 1) * SCAN_ITEMS == m) start[m] = run;
 }
 
-__global__ void k_scatter(const int *key, const int *start, int *fill, int *slot, int64_t n) {
+/* order-preserving integer image of a double (integer compares are full rate) */
+__device__ __forceinline__ unsigned long long order_key(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+__global__ void k_scatter(const int *key, const int *start, int *fill, int *slot, const int *tag, const double *rz,
+                          int *slot_tag, unsigned long long *slot_z, int64_t n) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int k = key[i];
-    slot[start[k] + atomicAdd(&fill[k], 1)] = (int)i;
+    const int pos = start[k] + atomicAdd(&fill[k], 1);
+    slot[pos] = (int)i;
+    slot_tag[pos] = tag[i];
+    slot_z[pos] = order_key(rz[i]);
 }
 
-/* rank within the bucket by tag: perm[start + rank] = previous slot */
-__global__ void k_rank(const int *key, const int *start, const int *slot, const int *tag,
-                       int *perm, int *skey, const DevGlobals *g, int64_t n) {
+/* rank within the bucket by (last-axis coordinate, tag) from the scatter's
+ * contiguous copies: perm[start + rank] = previous slot */
+__global__ void k_rank(const int *key, const int *start, const int *slot, const int *slot_tag,
+                       const unsigned long long *slot_z, int *perm, int *skey, const DevGlobals *g, int64_t n) {
     const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (j >= n) return;
     const int dead_key = g->n_total_cells - 1;
@@ -371,9 +384,13 @@ __global__ void k_rank(const int *key, const int *start, const int *slot, const 
     const int s0 = start[k], s1 = start[k + 1];
     int rank = (int)j - s0;  /* deleted particles: any order */
     if (k != dead_key) {
-        const int my = tag[i];
+        const int my = slot_tag[j];
+        const unsigned long long mz = slot_z[j];
         rank = 0;
-        for (int u = s0; u < s1; u++) rank += tag[slot[u]] < my;
+        for (int u = s0; u < s1; u++) {
+            const unsigned long long z = slot_z[u];
+            rank += z < mz || (z == mz && slot_tag[u] < my);
+        }
     }
     perm[s0 + rank] = i;
     skey[s0 + rank] = k;
@@ -439,9 +456,10 @@ void rebuild(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "rebuild_scan_blocks", k_scan_blocks, 1, SCAN_BLK, 0, b.bsum, nscan);
     SPHDEM_LAUNCH(c, "rebuild_scan_down", k_scan_down, nscan, SCAN_BLK, 0, b.cnt, c->g, b.bsum, b.start, b.fill);
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(b.perm, 0, (size_t)n * sizeof(int), c->stream));
-    SPHDEM_LAUNCH(c, "rebuild_scatter", k_scatter, gb, BLK, 0, b.key, b.start, b.fill, b.slot, n);
-    SPHDEM_LAUNCH(c, "rebuild_rank", k_rank, gb, BLK, 0, b.key, b.start, b.slot, c->A.irow(FI_TAG),
-                  b.perm, b.skey, c->g, n);
+    SPHDEM_LAUNCH(c, "rebuild_scatter", k_scatter, gb, BLK, 0, b.key, b.start, b.fill, b.slot, c->A.irow(FI_TAG),
+                  c->A.row(FD_R + c->cfg.nd - 1), b.slot_tag, b.slot_z, n);
+    SPHDEM_LAUNCH(c, "rebuild_rank", k_rank, gb, BLK, 0, b.key, b.start, b.slot, b.slot_tag, b.slot_z, b.perm,
+                  b.skey, c->g, n);
     dim3 gg(gb, b.n_fields_d + b.n_fields_i);
     SPHDEM_LAUNCH(c, "rebuild_gather", k_gather, gg, BLK, 0, c->A, c->B, b.perm, b.fields_d,
                   b.n_fields_d, b.fields_i, b.n_fields_i, n);

@@ -251,7 +251,9 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->B.i);
     cudaFree(c->g);
     Buffers &b = c->buf;
-    for (int *p : {b.skey, b.perm, b.slot, b.key, b.cnt, b.start, b.fill, b.bsum, b.fields_d, b.fields_i, b.pair_cnt})
+    cudaFree(b.slot_z);
+    for (int *p : {b.skey, b.perm, b.slot, b.slot_tag, b.key, b.cnt, b.start, b.fill, b.bsum, b.fields_d, b.fields_i,
+                   b.pair_cnt})
         cudaFree(p);
     cudaFree(c->mx_pos);
     cudaFree(c->mx_vel);
@@ -462,7 +464,8 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
         c->cfg.sph_cells_cap = (int)sc;
         Buffers &b = c->buf;
         b.cells_cap = (int)sc + c->cfg.n_dem_cells + 2;
-        for (int **p : {&b.skey, &b.perm, &b.slot, &b.key})
+        SPHDEM_CUDA_CHECK(cudaMalloc(&b.slot_z, capacity * sizeof(unsigned long long)));
+        for (int **p : {&b.skey, &b.perm, &b.slot, &b.slot_tag, &b.key})
             SPHDEM_CUDA_CHECK(cudaMalloc(p, capacity * sizeof(int)));
         SPHDEM_CUDA_CHECK(cudaMalloc(&b.cnt, (size_t)b.cells_cap * sizeof(int)));
         SPHDEM_CUDA_CHECK(cudaMalloc(&b.start, ((size_t)b.cells_cap + 1) * sizeof(int)));

@@ -26,6 +26,8 @@ struct Buffers {
     int *skey = nullptr;     /* bucket key of each sorted particle        */
     int *perm = nullptr;     /* sorted slot -> previous slot              */
     int *slot = nullptr;     /* scatter scratch                           */
+    int *slot_tag = nullptr;             /* tag and order key of the last-axis */
+    unsigned long long *slot_z = nullptr; /* coordinate per scatter slot       */
     int *key = nullptr;      /* bucket key of each particle, previous order */
     int *cnt = nullptr;      /* bucket counts                             */
     int *start = nullptr;    /* bucket starts (exclusive scan)            */

@@ -456,6 +456,7 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
     for (int d = ND; d < 3; d++) code_fixed += code_stride(d);
     const int zstride = code_stride(Z) << B_BITS;
     const int self_e = CENTER_CODE;
+    const float supp = (float)(2.0 * g->sr) * (1.f + 1e-5f) + 1e-5f * cz;
     const float K_HI = 4.f * (1.f + 5e-7f), K_LO = 4.f * (1.f - 5e-7f);
 
     for (int t0 = (blockIdx.x * NL_WARPS + w) * 32; t0 < n_t; t0 += NL_WARPS * gridDim.x * 32) {
@@ -499,6 +500,16 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
             const int lane_zr = cc[Z] - zmin + 1;
             const float L = fmaxf(l_other, (float)(zmax - zmin + 2) * cz);
             const float EPS = 1.5e-6f * L * L;
+            /* the run's extent on the last axis, widened by the largest support
+             * 2 sr >= 2 max(h) and a rounding margin: nothing outside is a neighbour */
+            float zt_lo = mine ? pv[Z] : 1e30f, zt_hi = mine ? pv[Z] : -1e30f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                zt_lo = fminf(zt_lo, __shfl_xor_sync(FULL, zt_lo, o));
+                zt_hi = fmaxf(zt_hi, __shfl_xor_sync(FULL, zt_hi, o));
+            }
+            zt_lo -= supp;
+            zt_hi += supp;
             int nst = 0;
 
             auto evaluate = [&]() {
@@ -592,6 +603,27 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
                     r_sh = shp;
                     r_ox = off[0];
                     r_oy = off[1];
+                    /* buckets hold their particles sorted on the last axis, so the
+                     * run is sorted there: keep only [zt_lo, zt_hi] (binary search) */
+                    int lo = 0, hi = r_cnt;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1, k = r_b0 + mid;
+                        const float4 q = P0[k];
+                        const float z = (Z == 0 ? q.x : (Z == 1 ? q.y : q.z)) + (float)(r_zoff + skey[k] - r_lin) * cz;
+                        if (z < zt_lo) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    const int first = lo;
+                    hi = r_cnt;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1, k = r_b0 + mid;
+                        const float4 q = P0[k];
+                        const float z = (Z == 0 ? q.x : (Z == 1 ? q.y : q.z)) + (float)(r_zoff + skey[k] - r_lin) * cz;
+                        if (z <= zt_hi) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    r_b0 += first;
+                    r_cnt = lo - first;
                 }
             }
             /* exclusive prefix of the range sizes over the lanes */
@@ -1106,6 +1138,7 @@ __global__ void __launch_bounds__(CP_WARPS * 32, 3) k_couple(DevCfg c, const Dev
     const float rdens2d = (float)(1.0 / (2.0 * c.dem_radius));
     const int lim_ceil = (int)ceil(c.couple_lim);
     const float rc2x = (float)(2.0 * c.rc);
+    const float rc_w = (float)c.rc * (1.f + 1e-5f);
     float dcf[3] = {0.f, 0.f, 0.f};
 #pragma unroll
     for (int d = 0; d < ND; d++) dcf[d] = (float)c.dcell[d];
@@ -1175,6 +1208,16 @@ __global__ void __launch_bounds__(CP_WARPS * 32, 3) k_couple(DevCfg c, const Dev
                 lmax = fmaxf(lmax, (d == Z ? (float)(zmax - zmin + 1) : 1.f) * cell[d] + rc2x + 2.f * dcf[d]);
             }
             const float band_c = fp32_band(rc2, lmax * lmax);
+            /* the run's extent on the last axis, widened by Rc and a rounding
+             * margin: no DEM partner lies outside */
+            float zw_lo = mine ? pv[Z] : 1e30f, zw_hi = mine ? pv[Z] : -1e30f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                zw_lo = fminf(zw_lo, __shfl_xor_sync(FULL, zw_lo, o));
+                zw_hi = fmaxf(zw_hi, __shfl_xor_sync(FULL, zw_hi, o));
+            }
+            zw_lo -= rc_w + 1e-5f * lmax;
+            zw_hi += rc_w + 1e-5f * lmax;
             int nst = 0;
 
             auto evaluate = [&]() {
@@ -1285,6 +1328,29 @@ __global__ void __launch_bounds__(CP_WARPS * 32, 3) k_couple(DevCfg c, const Dev
                             r_sh = shp;
                             r_dx = dl[0];
                             r_dy = dl[1];
+                            /* DEM buckets hold their particles sorted on the last axis:
+                             * keep those within Rc of the run there (binary search) */
+                            int lo = 0, hi = r_cnt;
+                            while (lo < hi) {
+                                const int mid = (lo + hi) >> 1, b = r_b0 + mid;
+                                const float4 q = P0[b];
+                                const float z = (Z == 0 ? q.x : (Z == 1 ? q.y : q.z)) +
+                                                ((float)(r_zq + skey[b] - r_lin) * dcf[Z] - obase[Z]);
+                                if (z < zw_lo) lo = mid + 1;
+                                else hi = mid;
+                            }
+                            const int first = lo;
+                            hi = r_cnt;
+                            while (lo < hi) {
+                                const int mid = (lo + hi) >> 1, b = r_b0 + mid;
+                                const float4 q = P0[b];
+                                const float z = (Z == 0 ? q.x : (Z == 1 ? q.y : q.z)) +
+                                                ((float)(r_zq + skey[b] - r_lin) * dcf[Z] - obase[Z]);
+                                if (z <= zw_hi) lo = mid + 1;
+                                else hi = mid;
+                            }
+                            r_b0 += first;
+                            r_cnt = lo - first;
                         }
                     }
                     r_excl = r_cnt;
