@@ -1,0 +1,98 @@
+/*
+ * The case's compile-time configuration (customConstants.h constants and
+ * feature macros) as the run-time SphDemConfig of the C ABI.  Constants are
+ * read under the same feature macros the reference's own headers read them
+ * under, so any case that compiles with the reference compiles here.
+ * Gravity, walls and freezing stay with the case's hooks.
+ */
+#ifndef SPHDEM_CASE_CONFIG_H
+#define SPHDEM_CASE_CONFIG_H
+
+#include <cstring>
+
+#include "../../../include/sphdem.h"
+#include "customConstants.h"
+#include "demConstants.h"
+
+#if !defined(WENDLAND)
+#error "the device path implements the Wendland C2 kernel only (#define WENDLAND)"
+#endif
+#if defined(LUBRICATION) || defined(HERTZ) || defined(HERTZ_KUWABARA) || defined(CORRECTED_GRADIENT)
+#error "option not implemented by the device path"
+#endif
+
+inline SphDemConfig sphdem_case_config(int precision, bool fixed_dt) {
+    SphDemConfig c;
+    std::memset(&c, 0, sizeof c);
+    c.ndim = NDIM;
+    c.precision = precision;
+#if defined(VISC_MORRIS)
+    c.visc_model = SPHDEM_VISC_MORRIS;
+#elif defined(VISC_MONAGHAN)
+    c.visc_model = SPHDEM_VISC_MONAGHAN;
+#elif defined(VISC_ARTIFICIAL)
+    c.visc_model = SPHDEM_VISC_ARTIFICIAL;
+    c.alpha_artificial = ALPHA_ARTIFICIAL;
+#else
+    c.visc_model = SPHDEM_VISC_NONE;
+#endif
+    c.flags = 0;
+#ifdef CONST_H
+    c.flags |= SPHDEM_F_CONST_H;
+#endif
+#ifdef NO_ANTICLUMPING
+    c.flags |= SPHDEM_F_NO_ANTICLUMPING;
+#endif
+#ifdef VAR_H_CORRECTION
+    c.flags |= SPHDEM_F_VAR_H_CORRECTION;
+#endif
+#ifdef LIQ_DEM
+    c.flags |= SPHDEM_F_LIQ_DEM;
+#endif
+    if (fixed_dt) c.flags |= SPHDEM_F_FIXED_DT;
+    c.pi = PI;
+    for (int d = 0; d < NDIM; d++) {
+        c.periodic[d] = PERIODIC[d];
+        c.rmin[d] = RMIN[d];
+        c.rmax[d] = RMAX[d];
+        /* the processor domain of a single-rank setup: exact on periodic
+         * axes, 25% margin on the others */
+        const double ext = RMAX[d] - RMIN[d];
+        c.domain_min[d] = PERIODIC[d] ? RMIN[d] : RMIN[d] - 0.25 * ext;
+        c.domain_max[d] = PERIODIC[d] ? RMAX[d] : RMAX[d] + 0.25 * ext;
+    }
+    c.hfac = HFAC;
+    c.psep = PSEP;
+    c.h = H;
+    c.dens = DENS;
+    c.refd = REFD;
+    c.gamma = GAMMA;
+    c.prb = PRB;
+    c.spsound = SPSOUND;
+    c.viscosity = VISCOSITY;
+    c.bfac = BFAC;
+    c.maxdt = MAXTIME / OUTSTEP; /* run.cpp:87 */
+    c.damptime = DAMPTIME;
+#ifdef LIQ_DEM
+    c.dem_radius = DEM_RADIUS;
+    c.dem_dens = DEM_DENS;
+    c.dem_k = DEM_K;
+    c.dem_gamma = DEM_GAMMA;
+    c.dem_search_radius = DEM_SEARCH_RADIUS;
+    c.dem_vol = DEM_VOL;
+    c.coupling_radius = LIQ_DEM_COUPLING_RADIUS;
+#ifdef LINEAR
+    c.dem_timestep = DEM_TIMESTEP;
+#endif
+    c.liq_dem_timestep = LIQ_DEM_TIMESTEP;
+#endif
+#if defined(LIQ_DEM) && !defined(FIXED_DEM) && !defined(NO_DEM_CONTACTS)
+    c.time_drop_particle = TIME_DROP_PARTICLE; /* the DEM dt bound starts then (sphIncompress.cpp:133) */
+#else
+    c.time_drop_particle = 1e30;
+#endif
+    c.freeze_dem_until = -1.0; /* freezing is the case hooks' business */
+    return c;
+}
+
+#endif

@@ -1,0 +1,148 @@
+/*
+ * Driver of a case directory on the device (the step loop of run.cpp:80-170):
+ * compiled together with the case's customConstants.h, customSim.cpp and
+ * customOutput.cpp against the façade headers (include/), linked with
+ * libsphdem.so.
+ *
+ *   run_case <initial state SPDMST01> <nsteps> <final state out> [--mixed] [--fixed-dt]
+ *
+ * Every step calls the case's beforeStart / beforeMiddle / beforeEnd /
+ * afterEnd hooks on the host mirror between the device phases
+ * (SPHDEM_PHASE_START / MIDDLE / END), and calcOutput every OUTSTEP steps.
+ * The final state is written as r, v, vhat, f, dens, h per particle (tag
+ * order) after a 16-byte header ("SPDMFAC1", n).
+ */
+#include <cstdint>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <string>
+#include <vector>
+
+#include "customConstants.h"
+#include "customOutput.h"
+#include "customSim.h"
+#include "sphdem_case_config.h"
+
+namespace {
+
+bool read_state(const char *path, SphDemParticles &p, std::vector<std::vector<char> > &keep) {
+    std::ifstream in(path, std::ios::binary);
+    char magic[8];
+    if (!in.read(magic, 8) || std::memcmp(magic, "SPDMST01", 8) != 0) return false;
+    int64_t n = 0;
+    in.read(reinterpret_cast<char *>(&n), 8);
+    auto take = [&](size_t bytes) -> char * {
+        keep.emplace_back(bytes);
+        in.read(keep.back().data(), (std::streamsize)bytes);
+        return keep.back().data();
+    };
+    std::memset(&p, 0, sizeof p);
+    p.n = n;
+    p.iam = reinterpret_cast<int32_t *>(take(4 * n));
+    p.tag = reinterpret_cast<int32_t *>(take(4 * n));
+    int32_t *conc = reinterpret_cast<int32_t *>(take(4 * n));
+    keep.emplace_back(n);
+    p.concave = reinterpret_cast<uint8_t *>(keep.back().data());
+    for (int64_t i = 0; i < n; i++) p.concave[i] = conc[i] != 0;
+    p.r = reinterpret_cast<double *>(take(24 * n));
+    p.v = reinterpret_cast<double *>(take(24 * n));
+    p.vhat = p.v;
+    p.mass = reinterpret_cast<double *>(take(8 * n));
+    p.dens = reinterpret_cast<double *>(take(8 * n));
+    p.h = reinterpret_cast<double *>(take(8 * n));
+    p.radius = reinterpret_cast<double *>(take(8 * n));
+    p.norm1 = reinterpret_cast<double *>(take(24 * n));
+    p.norm2 = reinterpret_cast<double *>(take(24 * n));
+    p.norm3 = reinterpret_cast<double *>(take(24 * n));
+    return (bool)in;
+}
+
+void write_final(const char *path, const particleContainer &ps) {
+    std::ofstream out(path, std::ios::binary);
+    out.write("SPDMFAC1", 8);
+    const int64_t n = (int64_t)ps.size();
+    out.write(reinterpret_cast<const char *>(&n), 8);
+    for (const Cparticle &q : ps) {
+        double rec[14] = {0};
+        for (int d = 0; d < NDIM; d++) {
+            rec[d] = q.r[d];
+            rec[3 + d] = q.v[d];
+            rec[6 + d] = q.vhat[d];
+            rec[9 + d] = q.f[d];
+        }
+        rec[12] = q.dens;
+        rec[13] = q.h;
+        out.write(reinterpret_cast<const char *>(rec), sizeof rec);
+    }
+}
+
+}  // namespace
+
+int main(int argc, char *argv[]) {
+    if (argc < 4) {
+        std::cout << "Usage: run_case <initial state> <nsteps> <final state> [--mixed] [--fixed-dt]" << std::endl;
+        return -1;
+    }
+    bool mixed = false, fixed_dt = false;
+    for (int i = 4; i < argc; i++) {
+        if (!std::strcmp(argv[i], "--mixed")) mixed = true;
+        if (!std::strcmp(argv[i], "--fixed-dt")) fixed_dt = true;
+    }
+    SphDemParticles init;
+    std::vector<std::vector<char> > keep;
+    if (!read_state(argv[1], init, keep)) {
+        std::cerr << "cannot read " << argv[1] << std::endl;
+        return -1;
+    }
+    const int nsteps = std::atoi(argv[2]);
+    SphDemConfig cfg = sphdem_case_config(mixed ? SPHDEM_PREC_MIXED : SPHDEM_PREC_FP64, fixed_dt);
+    sphdem_handle h = nullptr;
+    if (sphdem_create(&cfg, &init, init.n, &h) != SPHDEM_OK) {
+        std::cerr << "sphdem_create failed" << std::endl;
+        return -1;
+    }
+    CglobalVars globals;
+    particleContainer ps((size_t)init.n);
+    CdataLL data(ps, globals, h);
+    data.pull();
+    CcustomSim customSim(&data, globals.time);
+    CcustomOutput customOutput(&data);
+    Cio_data_vtk io(std::string(argv[3]), &globals);
+    auto phase = [&](int p, const char *what) {
+        if (sphdem_phase(h, p) != SPHDEM_OK) {
+            char msg[512];
+            sphdem_last_error(h, msg, sizeof msg);
+            std::cerr << what << ": " << msg << std::endl;
+            std::exit(-1);
+        }
+    };
+    int outstep = 0;
+    for (int s = 0; s < nsteps; s++) {
+        data.pull();
+        customSim.beforeStart(globals.time);
+        data.push();
+        phase(SPHDEM_PHASE_START, "start");
+        data.pull();
+        customSim.beforeMiddle(globals.time);
+        data.push();
+        phase(SPHDEM_PHASE_MIDDLE, "middle");
+        data.pull();
+        customSim.beforeEnd(globals.time);
+        data.push();
+        phase(SPHDEM_PHASE_END, "end");
+        data.pull();
+        customSim.afterEnd(globals.time);
+        data.push();
+        if ((s + 1) % OUTSTEP == 0) {
+            data.pull();
+            customOutput.calcOutput(++outstep, &customSim, &io);
+        }
+    }
+    data.pull();
+    write_final(argv[3], ps);
+    sphdem_destroy(h);
+    return 0;
+}

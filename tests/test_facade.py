@@ -1,0 +1,90 @@
+"""The C++ façade of the plug-in surface: case directories compile against
+it (-m "not gpu") and a case's host hooks driving the device phases give the
+same state as the device's built-in hooks (-m gpu)."""
+import os
+import struct
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from sphdem import capi, cases, state
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+FACADE = os.path.join(REPO, "sph-dem_gb300", "facade")
+sys.path.insert(0, FACADE)
+from build_case import build_case  # noqa: E402
+
+LIB = os.path.join(REPO, "sph-dem_gb300", "libsphdem.so")
+
+
+def _need_lib():
+    if not os.path.exists(LIB):
+        import __graft_entry__
+        __graft_entry__.build()
+
+
+def test_example_case_builds(tmp_path):
+    _need_lib()
+    out = build_case(os.path.join(FACADE, "example_sediment"), str(tmp_path / "run_example"))
+    assert os.path.exists(out)
+
+
+def test_example_constants_in_step(tmp_path):
+    sys.path.insert(0, os.path.join(FACADE, "example_sediment"))
+    import make_constants
+    with open(os.path.join(FACADE, "example_sediment", "customConstants.h")) as fh:
+        assert fh.read() == make_constants.constants()
+
+
+REF_CASE = "/root/reference/sediment3D"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_CASE), reason="reference sources not present")
+def test_reference_case_sources_build_unchanged(tmp_path):
+    """The reference's own sediment3D hooks and output code, unmodified."""
+    _need_lib()
+    out = build_case(REF_CASE, str(tmp_path / "run_sediment3D"))
+    assert os.path.exists(out)
+
+
+def read_final(path):
+    with open(path, "rb") as fh:
+        buf = fh.read()
+    assert buf[:8] == b"SPDMFAC1"
+    (n,) = struct.unpack_from("<q", buf, 8)
+    rec = np.frombuffer(buf, "<f8", 14 * n, 16).reshape(n, 14)
+    return {"r": rec[:, 0:3], "v": rec[:, 3:6], "vhat": rec[:, 6:9], "f": rec[:, 9:12],
+            "dens": rec[:, 12], "h": rec[:, 13]}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_case_hooks_match_device_hooks(tmp_path, precision):
+    import __graft_entry__
+    __graft_entry__.build()
+    exe = build_case(os.path.join(FACADE, "example_sediment"), str(tmp_path / "run_example"))
+    case = cases.workload("sediment3d_small")
+    init = tmp_path / "init.spdm"
+    state.write_state(str(init), case.particles)
+    final = tmp_path / "final.bin"
+    nsteps = 5
+    args = [exe, str(init), str(nsteps), str(final), "--fixed-dt"] + (["--mixed"] if precision == "mixed" else [])
+    res = subprocess.run(args, capture_output=True, text=True, timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    a = read_final(str(final))
+    lib = capi.Library()
+    prec = cases.PREC_MIXED if precision == "mixed" else cases.PREC_FP64
+    sim = capi.Simulation(lib, case.cfg, case.particles, precision=prec)
+    sim.step(nsteps)
+    b = sim.get()
+    sim.close()
+    # same arithmetic on the host as in the device hooks; only the order of
+    # the force sums (FP32 atomics in the mixed coupling) may differ
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    for k in ("r", "vhat", "dens"):
+        scale = np.abs(b[k]).max()
+        err = np.abs(a[k] - b[k]).max() / scale
+        print(precision, k, err)
+        assert err <= tol, f"{k}: {err}"
