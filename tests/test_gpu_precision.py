@@ -1,0 +1,59 @@
+"""Mixed precision against the FP64 path at full size over a long run
+(-m gpu): the 2D dam break (20,000 fluid + the 3-layer walls, dx = 0.01),
+1000 steps.  Bar: max |rho_mixed - rho_fp64| / rho0 <= 1e-4 after 1000 steps;
+positions are reported relative to the column height."""
+import numpy as np
+import pytest
+
+from sphdem import capi, cases
+
+pytestmark = pytest.mark.gpu
+
+NSTEPS = 1000
+RHO_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import __graft_entry__
+    __graft_entry__.build()
+    return capi.Library()
+
+
+def test_dambreak_mixed_vs_fp64_1000_steps(lib):
+    case = cases.dambreak2d(dx=0.01, nsteps=NSTEPS)
+    mixed = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    fp64 = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_FP64)
+    errs = []
+    for k in range(NSTEPS // 100):
+        mixed.step(100)
+        fp64.step(100)
+        a, b = mixed.get(capi.FIELD_DENS | capi.FIELD_R), fp64.get(capi.FIELD_DENS | capi.FIELD_R)
+        e_rho = float(np.abs(a["dens"] - b["dens"]).max() / case.cfg["dens"])
+        e_r = float(np.abs(a["r"] - b["r"]).max() / 2.0)
+        errs.append((100 * (k + 1), e_rho, e_r))
+    mixed.close()
+    fp64.close()
+    for s, e_rho, e_r in errs:
+        print(f"step {s}: max drho/rho0 {e_rho:.2e}  max dr/H {e_r:.2e}")
+    assert errs[-1][1] <= RHO_TOL
+
+
+def test_coupled_mixed_vs_fp64(lib):
+    """The coupled sedimentation workload on its 1/4 periodic sub-box
+    (270,100 particles, same dx and physics), 200 steps."""
+    case = cases.sediment3d(nx=40, L=0.1, height=0.4, n_dem=12500, seed=3, nsteps=200)
+    mixed = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    fp64 = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_FP64)
+    mixed.step(200)
+    fp64.step(200)
+    a, b = mixed.get(), fp64.get()
+    mixed.close()
+    fp64.close()
+    e_rho = float(np.abs(a["dens"] - b["dens"]).max() / case.cfg["dens"])
+    dem = b["iam"] == cases.DEM
+    e_dem = float(np.abs(a["r"][dem] - b["r"][dem]).max() / case.cfg["dem_radius"])
+    e_por = float(np.abs(a["porosity"] - b["porosity"]).max())
+    print(f"coupled 200 steps: max drho/rho0 {e_rho:.2e}  max dr_DEM/R {e_dem:.2e}  max dporosity {e_por:.2e}")
+    assert e_rho <= RHO_TOL
+    assert e_por <= RHO_TOL
