@@ -196,14 +196,11 @@ def cpu_baseline(steps=2, warm=1, procs=1):
 
 
 # --------------------------------------------------------------------------
-def measure_adjoint(lib, capi, cases, nsteps=100, ckpt=10):
-    """Wall time of sphdem_adjoint_forward + sphdem_adjoint_backward over the
-    wall time of the same steps stepped plainly, on a DEM-only settling
-    workload (4,913 spheres, FP64 and mixed) -- the configuration the
-    adjoint covers."""
-    case = cases.dem_settling3d(lattice=(17, 17, 17), box=(0.067, 0.067, 0.067), spread=0.0,
-                                nsteps=nsteps, vel_amp=0.3)
-    out = {"workload": f"DEM-only settling, {case.n} spheres, {nsteps} steps, checkpoint every {ckpt}"}
+def _time_adjoint(lib, capi, cases, case, nsteps, ckpt, seed_fn):
+    """(plain forward, adjoint forward, adjoint backward) wall times of the
+    same nsteps from the same state, FP64 and mixed (each call returns after
+    the device finished)."""
+    out = {}
     for name, prec in (("fp64", cases.PREC_FP64), ("mixed", cases.PREC_MIXED)):
         sim = capi.Simulation(lib, case.cfg, case.particles, precision=prec)
         sim.step(2)
@@ -213,19 +210,50 @@ def measure_adjoint(lib, capi, cases, nsteps=100, ckpt=10):
         sim.close()
         sim = capi.Simulation(lib, case.cfg, case.particles, precision=prec)
         sim.step(2)
-        a = sim.get(capi.FIELD_IAM)
-        seed = np.zeros((sim.n, 3))
-        dem = a["iam"] == cases.DEM
-        seed[dem, 2] = 1.0 / max(1, dem.sum())
+        seeds = seed_fn(sim)
         t0 = time.perf_counter()
         sim.adjoint_forward(nsteps, ckpt)
         t_af = time.perf_counter() - t0
-        sim.adjoint_backward(dL_dr=seed)
+        sim.adjoint_backward(**seeds)
         t_ab = time.perf_counter() - t0 - t_af
         sim.close()
         out[name] = {"forward_s": t_fwd, "adjoint_forward_s": t_af, "adjoint_backward_s": t_ab,
                      "ratio": (t_af + t_ab) / t_fwd}
-    out["ratio"] = out["mixed"]["ratio"]
+    return out
+
+
+def measure_adjoint(lib, capi, cases, nsteps=100, ckpt=10):
+    """Wall time of sphdem_adjoint_forward + sphdem_adjoint_backward over the
+    wall time of the same steps stepped plainly, FP64 and mixed, for the two
+    step families the adjoint covers: DEM-only settling (4,913 spheres) and
+    the 2D dam break at its full size (dx = 0.01, artificial viscosity)."""
+    out = {}
+    dem = cases.dem_settling3d(lattice=(17, 17, 17), box=(0.067, 0.067, 0.067), spread=0.0,
+                               nsteps=nsteps, vel_amp=0.3)
+
+    def dem_seed(sim):
+        a = sim.get(capi.FIELD_IAM)
+        seed = np.zeros((sim.n, 3))
+        m = a["iam"] == cases.DEM
+        seed[m, 2] = 1.0 / max(1, m.sum())
+        return {"dL_dr": seed}
+
+    out["dem"] = _time_adjoint(lib, capi, cases, dem, nsteps, ckpt, dem_seed)
+    out["dem"]["workload"] = (f"DEM-only settling, {dem.n} spheres, {nsteps} steps, "
+                              f"checkpoint every {ckpt}")
+    fluid = cases.workload("dambreak2d")
+
+    def fluid_seed(sim):
+        a = sim.get(capi.FIELD_IAM)
+        seed = np.zeros((sim.n, 3))
+        m = a["iam"] == cases.SPH
+        seed[m, 1] = 1.0 / max(1, m.sum())
+        return {"dL_dr": seed}
+
+    out["fluid"] = _time_adjoint(lib, capi, cases, fluid, nsteps, ckpt, fluid_seed)
+    out["fluid"]["workload"] = (f"2D dam break, {fluid.n} particles (artificial viscosity), "
+                                f"{nsteps} steps, checkpoint every {ckpt}")
+    out["ratio"] = max(out["dem"]["mixed"]["ratio"], out["fluid"]["mixed"]["ratio"])
     return out
 
 
@@ -309,7 +337,7 @@ def run_ours(args, rank, world):
     ref.close()
     cmp.close()
 
-    # ---- adjoint / forward on the DEM-only workload -----------------------
+    # ---- adjoint / forward on the DEM-only and dam-break workloads --------
     adjoint = measure_adjoint(lib, capi, cases) if not args.no_adjoint else None
 
     # ---- end to end through the C ABI with host buffers -------------------

@@ -230,18 +230,26 @@ int sphdem_pairs(sphdem_handle h, int kind, int64_t *offsets, int32_t *idx,
 int sphdem_cell_ids(sphdem_handle h, int32_t *cell_xyz);
 
 /* ---------------------------------------------------------------------- */
-/* Adjoint (reverse-mode gradients) of the DEM step: no counterpart in the
- * reference, which has no derivatives.  Covers handles whose particles are
- * all DEM (LIQ_DEM without fluid), fixed dt, no damping or freezing;
- * other handles get SPHDEM_ERR_UNSUPPORTED.
+/* Adjoint (reverse-mode gradients) of the step: no counterpart in the
+ * reference, which has no derivatives.  Covers, with fixed dt and no
+ * damping:
+ *  - handles whose particles are all DEM (LIQ_DEM without fluid, no
+ *    freezing): gradients dem_k, dem_gamma and the initial state;
+ *  - fluid handles of SPH and SPH-boundary particles (no LIQ_DEM) with
+ *    artificial viscosity, CONST_H, NO_ANTICLUMPING, no VAR_H_CORRECTION and
+ *    no periodic axes (the dam break): gradients `viscosity` =
+ *    dL/d(alpha_artificial) and the initial state.
+ * Other handles get SPHDEM_ERR_UNSUPPORTED.
  *
  * sphdem_adjoint_forward runs nsteps ordinary steps from the current state,
  * keeping a device checkpoint every ckpt_every steps.
  * sphdem_adjoint_backward takes the adjoint of the final r, v and vhat (tag
  * order, 3 per particle; NULL = zero), replays each checkpoint segment once
  * and applies the step's vector-Jacobian product in reverse order.  It
- * returns dL/d(dem_k), dL/d(dem_gamma) and the adjoints of the initial r, v
- * and vhat (NULL to skip), and leaves the handle at the final state. */
+ * returns the gradients flagged in grads->valid and the adjoints of the
+ * initial r, v and vhat (NULL to skip), and leaves the handle at the final
+ * state.  SPHDEM_ERR_CAPACITY: a step used more pairs than the lists sized
+ * at the forward pass hold. */
 #define SPHDEM_GRAD_DEM_K      (1u << 0)
 #define SPHDEM_GRAD_DEM_GAMMA  (1u << 1)
 #define SPHDEM_GRAD_POSITIONS  (1u << 2)

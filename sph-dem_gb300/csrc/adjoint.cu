@@ -1,9 +1,19 @@
 /*
- * Adjoint of the DEM step (reverse mode, FP64), with step checkpointing.
+ * Adjoint of the step (reverse mode, FP64), with step checkpointing.
  *
- * Scope: handles whose particles are all DEM (LIQ_DEM without fluid: the
- * granular settling configuration), fixed dt, no damping or freezing.  The
- * step the forward path takes for a DEM particle (k_start, k_middle_tail,
+ * sphdem_adjoint_forward runs the steps through the ordinary path and keeps
+ * the state (r, v, vh, f, dens, dddt in tag order) and the step globals every
+ * `ckpt_every` steps.  sphdem_adjoint_backward walks the segments from the
+ * last: it restores the segment's checkpoint into the handle, replays its
+ * steps while keeping every step's state and the pairs the step used (the
+ * same exact FP64 predicate, particle.h:236-238), then applies the step's
+ * vector-Jacobian product in reverse order.  Replays are bit-identical to the
+ * first forward pass (the bucket order is a deterministic function of the
+ * positions), so the gradients are those of the computed trajectory.  Two
+ * step families are differentiated.
+ *
+ * DEM (handles whose particles are all DEM: LIQ_DEM without fluid, the
+ * granular settling configuration).  The step (k_start, k_middle_tail,
  * k_hook_before_end, the contact pass of the end phase, k_end_tail;
  * sphIncompress.cpp:3-251 with the sediment3D hooks) reduces to
  *
@@ -16,18 +26,33 @@
  * f_a += (k d + gamma d') n / m_a, d = Ra + Rb - |u|, n = u/|u|,
  * d' = -(vh_a - vh_b).n, u = r_a - image(r_b), and planar walls
  * (sediment3D customSim.cpp:67-81): f += (k (R - (r-p).n_w) - gamma vh.n_w) n_w / m.
+ * Gradients: dem_k, dem_gamma, initial r / v / vh.  Contact pairs are
+ * scattered with FP64 atomics.
  *
- * sphdem_adjoint_forward runs the steps through the ordinary path (graph
- * replay) and keeps the state (r, v, vh, f in tag order) and the step
- * globals every `ckpt_every` steps.  sphdem_adjoint_backward walks the
- * segments from the last: it restores the segment's checkpoint into the
- * handle, replays its steps while keeping every step's state and the
- * contact pairs the end phase used (the same exact FP64 predicate and
- * overlap test), then applies the step's vector-Jacobian product in reverse
- * order.  Replays are bit-identical to the first forward pass (the bucket
- * order is a deterministic function of the positions), so the gradients are
- * those of the computed trajectory.  Contacts are scattered with FP64
- * atomics; gamma and k gradients are warp-reduced first.
+ * SPH (weakly compressible fluid with fixed sphBoundary particles: types SPH
+ * and SPHB only, artificial viscosity, constant h, no anticlumping, no
+ * VAR_H_CORRECTION, no periodic axes; the dam break).  With hd = dt/2 and
+ * tag-order state, for an SPH particle (an SPHB particle is never kicked:
+ * vh_s = vh1 = vh0, v1 = v0, and its force is read by nothing):
+ *
+ *   r_s = r0 + hd vh0,  vh_s = vh0 + hd f0,  rho_s = rho0 + hd dddt0      (start, sphIncompress.h:643-704)
+ *   pdr2_s = PRB((rho_s/refd)^7 - 1) / rho_s^2                           (sphIncompress.h:863-896)
+ *   f1  = g + sum_b [m_b Pi_ab - m_b (pdr2_a + pdr2_b)] G_ab d_ab         (calcForce, sph.h:579-734)
+ *   vh1 = vh0 + dt f1,  v1 = v0 + dt f1                                  (kick, sphIncompress.h:706-742)
+ *   r1  = r_s + hd vh1                                                   (driftR)
+ *   dddt1 = sum_b m_b (vh1_a - vh1_b) . G_ab d_ab                        (calcDddtDudt, sphIncompress.h:783-851)
+ *   rho1 = rho_s + hd dddt1                                              (driftRest)
+ *
+ * where d_ab = r_a - r_b, G_ab = (F(r, h_a) + F(r, h_b)) / 2 with the
+ * Wendland C2 gradient factor F(r, h) = -10 C (2 - r/h)^3 / h^(d+2), and the
+ * artificial viscosity Pi_ab = alpha s (2 c0 - 4 s) / (rho_a + rho_b) for
+ * s = d.(vh_a - vh_b) / r < 0 (sph.h:633-646).  The middle sums run over the
+ * pairs of the middle rebuild (at r_s), the continuity sum over those of the
+ * end rebuild (at r1).  Gradients: alpha (reported as the viscosity
+ * gradient), initial r / v / vh.  Every ordered pair (a, b) is listed with
+ * its reverse (b, a), so the reverse passes gather, per particle, the terms
+ * of its own pairs and those of its partners' pairs: no atomics, and the
+ * result does not depend on the launch order.
  */
 #include <algorithm>
 #include <cstring>
@@ -38,29 +63,44 @@
 
 namespace sphdem {
 
-constexpr int ADJ_NC = 12;         /* r, v, vh, f per particle */
+constexpr int ADJ_NC = 14;         /* r, v, vh, f, dens, dddt per particle */
 constexpr int ADJ_MAX_CONTACTS = 32;
+constexpr int ADJ_AUX = 8;         /* SPH: r_s, vh_s, rho_s, pdr2_s */
 
 struct AdjointData {
+    int mode = 0;
     int nsteps = 0, K = 0;
     int64_t n = 0;
     std::vector<double *> ckpt;     /* state at steps 0, K, 2K, ... and the final state */
     std::vector<DevGlobals> ckpt_g;
     double *seg = nullptr;          /* (K + 1) states of one segment */
-    int4 *pairs = nullptr;          /* contacts of each step of a segment */
-    int *pair_cnt = nullptr;        /* K counters */
+    int4 *pairs = nullptr;          /* DEM: contacts of each step of a segment */
+    int *pair_cnt = nullptr;        /* K counters (DEM contacts; SPH middle pairs) */
     double *adj = nullptr;          /* adjoint of the state (ADJ_NC per particle) */
     double *racc = nullptr;         /* accumulated adjoint of r1 through the forces */
-    double *vmacc = nullptr;        /* adjoint of vhm */
+    double *vmacc = nullptr;        /* DEM: adjoint of vhm; SPH: adjoint of vh1 */
     double *fbar = nullptr;         /* adjoint of f1 */
     double *mass = nullptr, *rad = nullptr;   /* tag order */
-    double *grads = nullptr;        /* d/dk, d/dgamma */
+    int *typ = nullptr;             /* particle type, tag order */
+    double *hh = nullptr;           /* smoothing length, tag order */
+    /* SPH pair lists of each step of a segment: partner tag | shift code << 26,
+     * grouped by particle; (offset, count) per tag */
+    int64_t pair_cap = 0;           /* entries per step and list */
+    int *nb_mid = nullptr, *nb_end = nullptr;
+    int2 *oc_mid = nullptr, *oc_end = nullptr;
+    int *cnt_end = nullptr;
+    int *slot = nullptr;            /* step index inside the segment, read by the replay graph */
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    double *aux = nullptr;          /* SPH: r_s, vh_s, rho_s, pdr2_s per particle */
+    double *grads = nullptr;        /* d/dk, d/dgamma, d/dalpha */
 };
 
 void adjoint_free(sphdem_ctx *c) {
     AdjointData *a = c->adj;
     if (!a) return;
     for (double *p : a->ckpt) cudaFree(p);
+    for (cudaGraphExec_t g : a->graph)
+        if (g) cudaGraphExecDestroy(g);
     cudaFree(a->seg);
     cudaFree(a->pairs);
     cudaFree(a->pair_cnt);
@@ -70,6 +110,15 @@ void adjoint_free(sphdem_ctx *c) {
     cudaFree(a->fbar);
     cudaFree(a->mass);
     cudaFree(a->rad);
+    cudaFree(a->typ);
+    cudaFree(a->hh);
+    cudaFree(a->nb_mid);
+    cudaFree(a->nb_end);
+    cudaFree(a->oc_mid);
+    cudaFree(a->oc_end);
+    cudaFree(a->cnt_end);
+    cudaFree(a->slot);
+    cudaFree(a->aux);
     cudaFree(a->grads);
     delete a;
     c->adj = nullptr;
@@ -78,10 +127,12 @@ void adjoint_free(sphdem_ctx *c) {
 namespace {
 
 constexpr int ABLK = 256;
+constexpr int SH_SHIFT = 26;       /* partner tag bits below, shift code above */
 
-__global__ void k_save(DevState s, int64_t n, double *dst) {
+__global__ void k_save(DevState s, int64_t n, double *dst, const int *slot) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= n) return;
+    if (slot) dst += (int64_t)(*slot + 1) * n * ADJ_NC;
     double *o = dst + (int64_t)s.irow(FI_TAG)[k] * ADJ_NC;
     for (int d = 0; d < 3; d++) {
         o[d] = s.row(FD_R + d)[k];
@@ -89,6 +140,8 @@ __global__ void k_save(DevState s, int64_t n, double *dst) {
         o[6 + d] = s.row(FD_VHAT + d)[k];
         o[9 + d] = s.row(FD_F + d)[k];
     }
+    o[12] = s.row(FD_DENS)[k];
+    o[13] = s.row(FD_DDDT)[k];
 }
 
 __global__ void k_restore(DevState s, int64_t n, const double *src) {
@@ -101,15 +154,23 @@ __global__ void k_restore(DevState s, int64_t n, const double *src) {
         s.row(FD_VHAT + d)[k] = o[6 + d];
         s.row(FD_F + d)[k] = o[9 + d];
     }
+    s.row(FD_DENS)[k] = o[12];
+    s.row(FD_DDDT)[k] = o[13];
 }
 
-__global__ void k_save_const(DevCfg c, DevState s, int64_t n, double *mass, double *rad) {
+__global__ void k_slot_inc(int *slot) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *slot += 1;
+}
+
+__global__ void k_save_const(DevCfg c, DevState s, int64_t n, double *mass, double *rad, int *typ, double *hh) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int t = s.irow(FI_TAG)[k];
     mass[t] = s.row(FD_MASS)[k];
     /* radius, or -1 for a particle that is not (or no longer) DEM */
     rad[t] = s.irow(FI_IAM)[k] != T_DEM ? -1.0 : (s.row(FD_RADIUS)[k] > 0 ? s.row(FD_RADIUS)[k] : c.dem_radius);
+    typ[t] = s.irow(FI_IAM)[k];
+    hh[t] = s.row(FD_H)[k];
 }
 
 /* the contact pairs the end phase just used: DEM neighbours (exact FP64
@@ -171,10 +232,82 @@ __global__ void k_contacts(DevCfg c, DevState s, const int *start, const int *sk
             }
 }
 
+/* SPH pairs of particle a in the current buckets: every SPH/SPHB b with
+ * |r_a - image(r_b)|^2 <= (2 max(h_a, h_b))^2 (particle.h:236-238, FP64
+ * without contraction); with WRITE, the first `room` of them are written as
+ * tag_b | shift code << 26.  Returns the count. */
+template <bool WRITE>
+__device__ __forceinline__ int sph_pairs_of(const DevCfg &c, const DevState &s, const int *start, const int *skey,
+                                            const int *dims, int64_t a, int *out, int64_t room) {
+    const CellCoord cc = decode_cell(skey[a], dims, c.nd);
+    double ra[3] = {0, 0, 0};
+    for (int d = 0; d < c.nd; d++) ra[d] = s.row(FD_R + d)[a];
+    const double ha = s.row(FD_H)[a];
+    int k = 0;
+    for (int ox = -1; ox <= 1; ox++)
+        for (int oy = (c.nd > 1 ? -1 : 0); oy <= (c.nd > 1 ? 1 : 0); oy++)
+            for (int oz = (c.nd > 2 ? -1 : 0); oz <= (c.nd > 2 ? 1 : 0); oz++) {
+                int sh[3];
+                const int lin = neighbour_cell(cc, ox, oy, oz, dims, c.periodic, c.nd, sh);
+                if (lin < 0) continue;
+                const bool shifted = sh[0] || sh[1] || sh[2];
+                for (int b = start[lin]; b < start[lin + 1]; b++) {
+                    if (b == a && !shifted) continue;
+                    if (!is_sph_or_sphb(s.irow(FI_IAM)[b])) continue;
+                    if (shifted && !image_exists(s.irow(FI_GCODE)[b], sh, c.nd)) continue;
+                    double dx[3] = {0, 0, 0};
+                    for (int d = 0; d < c.nd; d++)
+                        dx[d] = dsub(ra[d], image_pos(s.row(FD_R + d)[b], sh[d], c.rmin[d], c.rmax[d]));
+                    const double r2 = exact_len2(dx, c.nd);
+                    const double hb = s.row(FD_H)[b];
+                    const double t2 = 2.0 * (ha > hb ? ha : hb);
+                    if (!(r2 <= dmul(t2, t2))) continue;
+                    if (WRITE && k < room)
+                        out[k] = s.irow(FI_TAG)[b] |
+                                 (((sh[0] + 1) | ((sh[1] + 1) << 2) | ((sh[2] + 1) << 4)) << SH_SHIFT);
+                    k++;
+                }
+            }
+    return k;
+}
+
+/* The SPH pair list of the current buckets, grouped by particle:
+ * nb[slot * cap + ...] = partner entries, oc[slot * n + tag_a] = (offset,
+ * count), cnt[slot] = entries used.  One atomic per warp reserves the warp's
+ * entries.  With nb == nullptr only cnt[0] is counted.  An overflowing
+ * particle records count 0 and the caller sees cnt > cap. */
+__global__ void k_sph_pairs(DevCfg c, DevState s, const int *start, const int *skey, const DevGlobals *g, int64_t n,
+                            int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
+    const bool live = a < n && is_sph_or_sphb(s.irow(FI_IAM)[a]);
+    const int j = slot ? *slot : 0;
+    const int k = live ? sph_pairs_of<false>(c, s, start, skey, dims, a, nullptr, 0) : 0;
+    const int lane = threadIdx.x & 31;
+    int incl = k;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(cnt + j, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    if (!nb || !live) return;
+    const int64_t off = (int64_t)base + incl - k;
+    const int64_t room = cap - off;
+    int *out = nb + (int64_t)j * cap + off;
+    sph_pairs_of<true>(c, s, start, skey, dims, a, out, room > 0 ? room : 0);
+    oc[(int64_t)j * n + s.irow(FI_TAG)[a]] = make_int2((int)off, room >= k ? k : 0);
+}
+
 __device__ __forceinline__ double warp_sum_d(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
+
+/* ------------------------------------------------------------------------ */
+/* DEM step VJP */
 
 /* per particle: adjoint of f1 and the wall terms */
 __global__ void k_vjp_particles(DevCfg c, int64_t n, double dt, const double *s0, const double *s1,
@@ -291,8 +424,190 @@ __global__ void k_vjp_assemble(int64_t n, double dt, double *adj, const double *
     }
 }
 
-void save_state(sphdem_ctx *c, double *dst) {
-    k_save<<<grid_for(c->n, ABLK), ABLK, 0, c->stream>>>(c->A, c->n, dst);
+/* ------------------------------------------------------------------------ */
+/* SPH step VJP */
+
+/* G = (F(r, h_a) + F(r, h_b)) / 2 and dG/dr, F(r, h) = -10 C (2-q)^3 / h^(d+2)
+ * (the Wendland C2 gradient factor of sph.h:322-342; 0 for q > 2) */
+__device__ __forceinline__ void grad_factor(const DevCfg &c, double r, double ha, double hb, double &G, double &Gp) {
+    G = 0.0;
+    Gp = 0.0;
+    const double hs[2] = {ha, hb};
+    for (int k = 0; k < 2; k++) {
+        const double h = hs[k], q = r / h;
+        if (q > 2.0) continue;
+        double ihn2 = 1.0 / (h * h);
+        for (int d = 0; d < c.nd; d++) ihn2 /= h;
+        const double t = 2.0 - q;
+        G += -10.0 * c.wcon * (t * t * t) * ihn2;
+        Gp += 30.0 * c.wcon * (t * t) * ihn2 / h;
+    }
+    G *= 0.5;
+    Gp *= 0.5;
+}
+
+/* VJP of the force of the ordered pair (x, y) on x,
+ *   T = [m_y Pi - m_y (pdr2_x + pdr2_y)] G(r) d,  d = r_x - r_y, w = vh_x - vh_y,
+ * against the adjoint Fb of f_x.  Adds sign * dT/dd^T Fb to Db and
+ * sign * dT/dw^T Fb to Wb (sign -1 when the caller is y), and the adjoints of
+ * rho_x (= that of rho_y) to Rb, of pdr2_x (= pdr2_y) to Qb, of alpha to Ab. */
+__device__ __forceinline__ void force_pair_vjp(const DevCfg &c, const double *d, const double *w, double r,
+                                               double G, double Gp, const double *Fb, double my, double rhox,
+                                               double rhoy, double pdr2x, double pdr2y, double sign, double *Db,
+                                               double *Wb, double &Rb, double &Qb, double &Ab) {
+    double P = 0.0, vdr = 0.0;
+    for (int k = 0; k < c.nd; k++) {
+        P += Fb[k] * d[k];
+        vdr += d[k] * w[k];
+    }
+    const double ir = 1.0 / r;
+    double s = -my * (pdr2x + pdr2y);
+    Qb += -my * G * P;
+    double coefw = 0.0, coefd = 0.0;
+    if (vdr < 0.0) {
+        const double viss = vdr * ir, rs = 1.0 / (rhox + rhoy);
+        const double Pi = c.alpha_art * viss * (2.0 * c.spsound - 4.0 * viss) * rs;
+        const double dPi = c.alpha_art * (2.0 * c.spsound - 8.0 * viss) * rs;
+        const double K = G * P;
+        s += my * Pi;
+        coefw = my * K * dPi * ir;                 /* d viss / d w = d / r */
+        coefd = -my * K * dPi * viss * ir * ir;    /* d viss / d d = w / r - viss d / r^2 */
+        Rb += -my * K * Pi * rs;
+        Ab += my * K * viss * (2.0 * c.spsound - 4.0 * viss) * rs;
+        for (int k = 0; k < c.nd; k++) Wb[k] += sign * coefw * d[k];
+    }
+    const double gpd = Gp * P * ir;
+    for (int k = 0; k < c.nd; k++) Db[k] += sign * (s * (G * Fb[k] + gpd * d[k]) + coefw * w[k] + coefd * d[k]);
+}
+
+/* tag-order intermediates of the step from its start state s0 */
+__global__ void k_sadj_pre(DevCfg c, int64_t n, double dt, const double *s0, const int *typ, double *aux) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *x = s0 + i * ADJ_NC;
+    double *o = aux + i * ADJ_AUX;
+    const double hd = 0.5 * dt;
+    const bool sph = typ[i] == T_SPH;
+    for (int d = 0; d < 3; d++) {
+        o[d] = x[d] + hd * x[6 + d];
+        o[3 + d] = sph ? x[6 + d] + hd * x[9 + d] : x[6 + d];
+    }
+    const double rho = x[12] + hd * x[13];
+    const double q = rho / c.refd, q2 = q * q;
+    o[6] = rho;
+    o[7] = c.prb * (q2 * q2 * q2 * q - 1.0) / (rho * rho);
+}
+
+/* continuity (end phase, pairs at r1): adjoints of r1 and vh1, then of f1 */
+__global__ void k_sadj_end(DevCfg c, int64_t n, double dt, const double *s1, const double *mass, const double *hh,
+                           const int *typ, const int *nb, const int2 *oc, const double *adj, double *racc,
+                           double *vh1b, double *fbar) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const double hd = 0.5 * dt;
+    const double *xa = s1 + a * ADJ_NC, *aa = adj + a * ADJ_NC;
+    const double Da = aa[13] + hd * aa[12], ma = mass[a], ha = hh[a];
+    double rb[3] = {0, 0, 0}, wb[3] = {0, 0, 0};
+    const int2 o = oc[a];
+    for (int k = 0; k < o.y; k++) {
+        const int e = nb[o.x + k];
+        const int b = e & ((1 << SH_SHIFT) - 1);
+        const int code = (int)((unsigned)e >> SH_SHIFT);
+        const int sh[3] = {(code & 3) - 1, ((code >> 2) & 3) - 1, ((code >> 4) & 3) - 1};
+        const double *xb = s1 + (int64_t)b * ADJ_NC, *ab = adj + (int64_t)b * ADJ_NC;
+        double d[3] = {0, 0, 0}, w[3] = {0, 0, 0}, r2 = 0.0, wd = 0.0;
+        for (int q = 0; q < c.nd; q++) {
+            d[q] = xa[q] - image_pos(xb[q], sh[q], c.rmin[q], c.rmax[q]);
+            w[q] = xa[6 + q] - xb[6 + q];
+            r2 += d[q] * d[q];
+            wd += w[q] * d[q];
+        }
+        const double r = sqrt(r2);
+        if (!(r > 0.0)) continue;
+        double G, Gp;
+        grad_factor(c, r, ha, hh[b], G, Gp);
+        /* own term m_b D_a and the partner's m_a D_b: d and w flip sign together */
+        const double coef = mass[b] * Da + ma * (ab[13] + hd * ab[12]);
+        for (int q = 0; q < c.nd; q++) {
+            rb[q] += coef * (G * w[q] + Gp * wd * d[q] / r);
+            wb[q] += coef * G * d[q];
+        }
+    }
+    const bool sph = typ[a] == T_SPH;
+    for (int q = 0; q < 3; q++) {
+        const double rt = aa[q] + rb[q];                 /* r1 = r_s + hd vh1 */
+        const double vt = aa[6 + q] + wb[q] + hd * rt;   /* total adjoint of vh1 */
+        racc[a * 3 + q] = rt;
+        vh1b[a * 3 + q] = vt;
+        fbar[a * 3 + q] = sph ? aa[9 + q] + dt * (vt + aa[3 + q]) : 0.0;  /* f1 feeds f, vh1, v1 */
+    }
+}
+
+/* force (middle phase, pairs at r_s), EOS, and the adjoint of the state
+ * before the step */
+__global__ void k_sadj_mid(DevCfg c, int64_t n, double dt, const double *aux, const double *mass, const double *hh,
+                           const int *typ, const int *nb, const int2 *oc, const double *fbar, const double *racc,
+                           const double *vh1b, double *adj, double *grads) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    double Ab = 0.0;
+    if (a < n) {
+        const double hd = 0.5 * dt;
+        const double *xa = aux + a * ADJ_AUX;
+        const double ma = mass[a], ha = hh[a];
+        const bool sph_a = typ[a] == T_SPH;
+        double Fa[3] = {0, 0, 0};
+        for (int q = 0; q < c.nd; q++) Fa[q] = fbar[a * 3 + q];
+        double Db[3] = {0, 0, 0}, Wb[3] = {0, 0, 0}, Rb = 0.0, Qb = 0.0, Adum = 0.0;
+        const int2 o = oc[a];
+        for (int k = 0; k < o.y; k++) {
+            const int e = nb[o.x + k];
+            const int b = e & ((1 << SH_SHIFT) - 1);
+            const int code = (int)((unsigned)e >> SH_SHIFT);
+            const int sh[3] = {(code & 3) - 1, ((code >> 2) & 3) - 1, ((code >> 4) & 3) - 1};
+            const double *xb = aux + (int64_t)b * ADJ_AUX;
+            double d[3] = {0, 0, 0}, w[3] = {0, 0, 0}, md[3] = {0, 0, 0}, mw[3] = {0, 0, 0}, r2 = 0.0;
+            for (int q = 0; q < c.nd; q++) {
+                d[q] = xa[q] - image_pos(xb[q], sh[q], c.rmin[q], c.rmax[q]);
+                w[q] = xa[3 + q] - xb[3 + q];
+                md[q] = -d[q];
+                mw[q] = -w[q];
+                r2 += d[q] * d[q];
+            }
+            const double r = sqrt(r2);
+            if (!(r > 0.0)) continue;
+            double G, Gp;
+            grad_factor(c, r, ha, hh[b], G, Gp);
+            /* a's own pair (a, b); an SPHB particle's force is read by nothing */
+            if (sph_a)
+                force_pair_vjp(c, d, w, r, G, Gp, Fa, mass[b], xa[6], xb[6], xa[7], xb[7], 1.0, Db, Wb, Rb, Qb, Ab);
+            /* the partner's pair (b, a): r_a and vh_a enter it with a minus sign */
+            if (typ[b] == T_SPH) {
+                double Fbv[3] = {0, 0, 0};
+                for (int q = 0; q < c.nd; q++) Fbv[q] = fbar[(int64_t)b * 3 + q];
+                force_pair_vjp(c, md, mw, r, G, Gp, Fbv, ma, xb[6], xa[6], xb[7], xa[7], -1.0, Db, Wb, Rb, Qb, Adum);
+            }
+        }
+        /* EOS: d pdr2 / d rho = PRB (5 x^7 + 2) / rho^3, x = rho / refd */
+        const double rho = xa[6], x = rho / c.refd, x2 = x * x;
+        const double dpdr2 = c.prb * (5.0 * (x2 * x2 * x2 * x) + 2.0) / (rho * rho * rho);
+        double *aa = adj + a * ADJ_NC;
+        const double rhos_b = aa[12] + Rb + Qb * dpdr2;    /* rho1 = rho_s + ..., force, EOS */
+        for (int q = 0; q < 3; q++) {
+            const double rs_b = racc[a * 3 + q] + Db[q];    /* total adjoint of r_s */
+            aa[q] = rs_b;                                    /* r_s = r0 + hd vh0 */
+            aa[6 + q] = vh1b[a * 3 + q] + Wb[q] + hd * rs_b; /* vh1 = vh0 + dt f1, vh_s, r_s */
+            aa[9 + q] = sph_a ? hd * Wb[q] : 0.0;            /* vh_s = vh0 + hd f0 */
+            /* v0: v1 = v0 + dt f1 only */
+        }
+        aa[12] = rhos_b;            /* rho_s = rho0 + hd dddt0 */
+        aa[13] = hd * rhos_b;
+    }
+    Ab = warp_sum_d(Ab);
+    if ((threadIdx.x & 31) == 0 && Ab != 0.0) atomicAdd(&grads[2], Ab);
+}
+
+void save_state(sphdem_ctx *c, double *dst, const int *slot = nullptr) {
+    k_save<<<grid_for(c->n, ABLK), ABLK, 0, c->stream>>>(c->A, c->n, dst, slot);
 }
 
 void restore_state(sphdem_ctx *c, const double *src, const DevGlobals &g) {
@@ -313,25 +628,128 @@ int one_step(sphdem_ctx *c) {
     return rc;
 }
 
+void sph_pairs(sphdem_ctx *c, int *nb, int2 *oc, int *cnt, const int *slot) {
+    AdjointData *a = c->adj;
+    k_sph_pairs<<<grid_for(c->n, 128), 128, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->buf.skey, c->g, c->n, nb,
+                                                            oc, cnt, a->pair_cap, slot);
+}
+
+/* One replayed SPH step with its taps, as a CUDA graph (one per buffer
+ * parity): the phases of the step, the middle pairs after the middle
+ * rebuild, the end pairs after the end rebuild, the state after the step
+ * (all at the segment slot a->slot), then slot += 1. */
+void replay_sph_step(sphdem_ctx *c) {
+    AdjointData *a = c->adj;
+    cudaGraphExec_t &ge = a->graph[c->flipped ? 1 : 0];
+    if (!ge) {
+        cudaGraph_t graph = nullptr;
+        const bool p0 = c->flipped;
+        c->in_capture = true;
+        SPHDEM_CUDA_CHECK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            for (int p = SPHDEM_HOOK_BEFORE_START; p <= SPHDEM_HOOK_AFTER_END; p++) {
+                phase_sequence(c, p);
+                if (p == SPHDEM_PHASE_MIDDLE) sph_pairs(c, a->nb_mid, a->oc_mid, a->pair_cnt, a->slot);
+                if (p == SPHDEM_PHASE_END) sph_pairs(c, a->nb_end, a->oc_end, a->cnt_end, a->slot);
+            }
+            save_state(c, a->seg, a->slot);
+            k_slot_inc<<<1, 32, 0, c->stream>>>(a->slot);
+        } catch (...) {
+            c->in_capture = false;
+            cudaStreamEndCapture(c->stream, &graph);
+            if (graph) cudaGraphDestroy(graph);
+            throw;
+        }
+        c->in_capture = false;
+        SPHDEM_CUDA_CHECK(cudaStreamEndCapture(c->stream, &graph));
+        if (c->flipped != p0) {
+            cudaGraphDestroy(graph);
+            throw std::string("a step must rebuild an even number of times");
+        }
+        const cudaError_t e = cudaGraphInstantiate(&ge, graph, 0);
+        cudaGraphDestroy(graph);
+        SPHDEM_CUDA_CHECK(e);
+    }
+    SPHDEM_CUDA_CHECK(cudaGraphLaunch(ge, c->stream));
+}
+
+void backward_dem(sphdem_ctx *c, AdjointData *a, int steps, double dt, int cap) {
+    const int64_t n = c->n;
+    for (int j = 1; j <= steps; j++) {
+        one_step(c);
+        save_state(c, a->seg + (size_t)j * n * ADJ_NC);
+        k_contacts<<<grid_for(n, 128), 128, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->buf.skey, c->g, n,
+                                                            a->pairs + (size_t)(j - 1) * cap, a->pair_cnt + j - 1,
+                                                            cap);
+    }
+    for (int j = steps; j >= 1; j--) {
+        const double *s0 = a->seg + (size_t)(j - 1) * n * ADJ_NC, *s1 = a->seg + (size_t)j * n * ADJ_NC;
+        k_vjp_particles<<<grid_for(n, ABLK), ABLK, 0, c->stream>>>(c->cfg, n, dt, s0, s1, a->mass, a->rad, a->adj,
+                                                                  a->fbar, a->racc, a->vmacc, a->grads);
+        k_vjp_contacts<<<grid_for(cap, ABLK), ABLK, 0, c->stream>>>(
+            c->cfg, a->pairs + (size_t)(j - 1) * cap, a->pair_cnt + j - 1, cap, dt, s0, s1, a->mass, a->rad,
+            a->fbar, a->racc, a->vmacc, a->grads);
+        k_vjp_assemble<<<grid_for(n, ABLK), ABLK, 0, c->stream>>>(n, dt, a->adj, a->racc, a->vmacc);
+    }
+}
+
+void backward_sph(sphdem_ctx *c, AdjointData *a, int steps, double dt) {
+    const int64_t n = c->n, cap = a->pair_cap;
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->slot, 0, sizeof(int), c->stream));
+    /* a particle that stops being SPH/SPHB (deleted) keeps an empty list */
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_mid, 0, (size_t)a->K * n * sizeof(int2), c->stream));
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_end, 0, (size_t)a->K * n * sizeof(int2), c->stream));
+    for (int j = 1; j <= steps; j++) replay_sph_step(c);
+    for (int j = steps; j >= 1; j--) {
+        const double *s0 = a->seg + (size_t)(j - 1) * n * ADJ_NC, *s1 = a->seg + (size_t)j * n * ADJ_NC;
+        const int *nbm = a->nb_mid + (size_t)(j - 1) * cap, *nbe = a->nb_end + (size_t)(j - 1) * cap;
+        const int2 *ocm = a->oc_mid + (size_t)(j - 1) * n, *oce = a->oc_end + (size_t)(j - 1) * n;
+        k_sadj_pre<<<grid_for(n, ABLK), ABLK, 0, c->stream>>>(c->cfg, n, dt, s0, a->typ, a->aux);
+        k_sadj_end<<<grid_for(n, 128), 128, 0, c->stream>>>(c->cfg, n, dt, s1, a->mass, a->hh, a->typ, nbe, oce,
+                                                            a->adj, a->racc, a->vmacc, a->fbar);
+        k_sadj_mid<<<grid_for(n, 128), 128, 0, c->stream>>>(c->cfg, n, dt, a->aux, a->mass, a->hh, a->typ, nbm, ocm,
+                                                            a->fbar, a->racc, a->vmacc, a->adj, a->grads);
+    }
+}
+
 }  // namespace
 
-std::string adjoint_supported(sphdem_ctx *c) {
+std::string adjoint_supported(sphdem_ctx *c, int *mode) {
     const DevCfg &cfg = c->cfg;
-    if (!cfg.liq_dem()) return "the adjoint covers LIQ_DEM handles of DEM particles";
+    *mode = 0;
     if (!(cfg.flags & SPHDEM_F_FIXED_DT)) return "the adjoint needs a fixed time step";
     if (cfg.damptime > 0) return "the adjoint does not cover velocity damping";
-    if (cfg.freeze_until >= 0) return "the adjoint does not cover freezing";
     std::vector<int> iam(c->n);
     field_get_int(c, FI_IAM, iam.data());
-    for (int t : iam)
-        if (t != T_DEM && t != T_DEAD) return "the adjoint covers handles whose particles are all DEM";
+    bool all_dem = true, all_fluid = true;
+    for (int t : iam) {
+        all_dem = all_dem && (t == T_DEM || t == T_DEAD);
+        all_fluid = all_fluid && is_sph_or_sphb(t);
+    }
+    if (cfg.liq_dem()) {
+        if (!all_dem) return "the adjoint covers LIQ_DEM handles whose particles are all DEM";
+        if (cfg.freeze_until >= 0) return "the adjoint does not cover freezing";
+        *mode = ADJ_MODE_DEM;
+        return "";
+    }
+    if (!all_fluid) return "the fluid adjoint covers handles of SPH and SPH-boundary particles only";
+    if (cfg.visc != SPHDEM_VISC_ARTIFICIAL) return "the fluid adjoint covers artificial viscosity only";
+    if (!(cfg.flags & SPHDEM_F_CONST_H)) return "the fluid adjoint needs a constant smoothing length";
+    if (!(cfg.flags & SPHDEM_F_NO_ANTICLUMPING)) return "the fluid adjoint does not cover anticlumping";
+    if (cfg.var_h()) return "the fluid adjoint does not cover VAR_H_CORRECTION";
+    for (int d = 0; d < cfg.nd; d++)
+        if (cfg.periodic[d]) return "the fluid adjoint does not cover periodic axes";
+    /* tags fit below the shift code, and int pair counters do not wrap */
+    if (c->n > (4 << 20)) return "the fluid adjoint covers at most 4M particles";
+    *mode = ADJ_MODE_SPH;
     return "";
 }
 
-int adjoint_forward(sphdem_ctx *c, int nsteps, int K) {
+int adjoint_forward(sphdem_ctx *c, int nsteps, int K, int mode) {
     adjoint_free(c);
     AdjointData *a = new AdjointData;
     c->adj = a;
+    a->mode = mode;
     a->nsteps = nsteps;
     a->K = K;
     a->n = c->n;
@@ -345,7 +763,19 @@ int adjoint_forward(sphdem_ctx *c, int nsteps, int K) {
     a->ckpt_g.resize(nseg + 1);
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->mass, c->n * sizeof(double)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->rad, c->n * sizeof(double)));
-    k_save_const<<<grid_for(c->n, ABLK), ABLK, 0, c->stream>>>(c->cfg, c->A, c->n, a->mass, a->rad);
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->typ, c->n * sizeof(int)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->hh, c->n * sizeof(double)));
+    k_save_const<<<grid_for(c->n, ABLK), ABLK, 0, c->stream>>>(c->cfg, c->A, c->n, a->mass, a->rad, a->typ, a->hh);
+    if (mode == ADJ_MODE_SPH) {
+        /* size the per-step pair lists from the pairs of the current buckets */
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->slot, sizeof(int)));
+        SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->slot, 0, sizeof(int), c->stream));
+        sph_pairs(c, nullptr, nullptr, a->slot, nullptr);
+        int n0 = 0;
+        SPHDEM_CUDA_CHECK(cudaMemcpyAsync(&n0, a->slot, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+        a->pair_cap = (int64_t)n0 + n0 / 2 + 4096;
+    }
     for (int s = 0; s < nseg; s++) {
         save_state(c, a->ckpt[s]);
         a->ckpt_g[s] = read_globals(c);
@@ -360,24 +790,34 @@ int adjoint_forward(sphdem_ctx *c, int nsteps, int K) {
 }
 
 int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, const double *seed_vh,
-                     double *dk, double *dgamma, double *dr0, double *dv0, double *dvh0) {
+                     double *grads3, double *dr0, double *dv0, double *dvh0) {
     AdjointData *a = c->adj;
     if (!a || a->n != c->n) throw std::string("no adjoint forward pass recorded for this handle");
     const int64_t n = c->n;
     const int K = a->K;
     const size_t sbytes = (size_t)n * ADJ_NC * sizeof(double);
     const int cap = ADJ_MAX_CONTACTS * (int)n;
+    const bool sph = a->mode == ADJ_MODE_SPH;
     if (!a->seg) {
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->seg, (size_t)(K + 1) * sbytes));
-        SPHDEM_CUDA_CHECK(cudaMalloc(&a->pairs, (size_t)K * cap * sizeof(int4)));
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->pair_cnt, (size_t)K * sizeof(int)));
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->adj, sbytes));
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->racc, n * 3 * sizeof(double)));
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->vmacc, n * 3 * sizeof(double)));
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->fbar, n * 3 * sizeof(double)));
-        SPHDEM_CUDA_CHECK(cudaMalloc(&a->grads, 2 * sizeof(double)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->grads, 3 * sizeof(double)));
+        if (sph) {
+            SPHDEM_CUDA_CHECK(cudaMalloc(&a->nb_mid, (size_t)K * a->pair_cap * sizeof(int)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&a->nb_end, (size_t)K * a->pair_cap * sizeof(int)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&a->oc_mid, (size_t)K * n * sizeof(int2)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&a->oc_end, (size_t)K * n * sizeof(int2)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&a->cnt_end, (size_t)K * sizeof(int)));
+            SPHDEM_CUDA_CHECK(cudaMalloc(&a->aux, (size_t)n * ADJ_AUX * sizeof(double)));
+        } else {
+            SPHDEM_CUDA_CHECK(cudaMalloc(&a->pairs, (size_t)K * cap * sizeof(int4)));
+        }
     }
-    /* seeds: adjoint of the final (r, v, vh, f) in tag order */
+    /* seeds: adjoint of the final (r, v, vh) in tag order; f, dens, dddt 0 */
     {
         std::vector<double> h((size_t)n * ADJ_NC, 0.0);
         for (int64_t i = 0; i < n; i++)
@@ -387,48 +827,46 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
                 h[i * ADJ_NC + 6 + d] = seed_vh ? seed_vh[3 * i + d] : 0.0;
             }
         SPHDEM_CUDA_CHECK(cudaMemcpyAsync(a->adj, h.data(), sbytes, cudaMemcpyHostToDevice, c->stream));
-        SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->grads, 0, 2 * sizeof(double), c->stream));
+        SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->grads, 0, 3 * sizeof(double), c->stream));
         SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
     }
     const int nseg = (a->nsteps + K - 1) / K;
     const double dt = a->ckpt_g[0].dt;
-    for (int sg = nseg - 1; sg >= 0; sg--) {
+    bool overflow = false;
+    for (int sg = nseg - 1; sg >= 0 && !overflow; sg--) {
         const int steps = std::min(K, a->nsteps - sg * K);
         restore_state(c, a->ckpt[sg], a->ckpt_g[sg]);
         SPHDEM_CUDA_CHECK(cudaMemcpyAsync(a->seg, a->ckpt[sg], sbytes, cudaMemcpyDeviceToDevice, c->stream));
         SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->pair_cnt, 0, K * sizeof(int), c->stream));
-        for (int j = 1; j <= steps; j++) {
-            one_step(c);
-            save_state(c, a->seg + (size_t)j * n * ADJ_NC);
-            k_contacts<<<grid_for(n, 128), 128, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->buf.skey, c->g, n,
-                                                                a->pairs + (size_t)(j - 1) * cap, a->pair_cnt + j - 1,
-                                                                cap);
-        }
-        for (int j = steps; j >= 1; j--) {
-            const double *s0 = a->seg + (size_t)(j - 1) * n * ADJ_NC, *s1 = a->seg + (size_t)j * n * ADJ_NC;
-            k_vjp_particles<<<grid_for(n, ABLK), ABLK, 0, c->stream>>>(c->cfg, n, dt, s0, s1, a->mass, a->rad, a->adj,
-                                                                      a->fbar, a->racc, a->vmacc, a->grads);
-            k_vjp_contacts<<<grid_for(cap, ABLK), ABLK, 0, c->stream>>>(
-                c->cfg, a->pairs + (size_t)(j - 1) * cap, a->pair_cnt + j - 1, cap, dt, s0, s1, a->mass, a->rad,
-                a->fbar, a->racc, a->vmacc, a->grads);
-            k_vjp_assemble<<<grid_for(n, ABLK), ABLK, 0, c->stream>>>(n, dt, a->adj, a->racc, a->vmacc);
+        if (sph) {
+            SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cnt_end, 0, K * sizeof(int), c->stream));
+            backward_sph(c, a, steps, dt);
+        } else {
+            backward_dem(c, a, steps, dt, cap);
         }
         SPHDEM_CUDA_CHECK(cudaGetLastError());
-    }
-    /* contact overflow check */
-    {
-        std::vector<int> cnt(K);
+        /* list overflow check of this segment */
+        std::vector<int> cnt(2 * K, 0);
         SPHDEM_CUDA_CHECK(cudaMemcpyAsync(cnt.data(), a->pair_cnt, K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        if (sph)
+            SPHDEM_CUDA_CHECK(
+                cudaMemcpyAsync(cnt.data() + K, a->cnt_end, K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
-        for (int v : cnt)
-            if (v > cap) return SPHDEM_ERR_CAPACITY;
+        const int64_t lim = sph ? a->pair_cap : cap;
+        for (int v : cnt) overflow = overflow || v > lim;
+        const int rc = device_status(c);
+        if (rc != SPHDEM_OK) return rc;
+    }
+    if (overflow) {
+        restore_state(c, a->ckpt[nseg], a->ckpt_g[nseg]);
+        SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+        return SPHDEM_ERR_CAPACITY;
     }
     /* outputs, then put the handle back at the final state */
     {
         std::vector<double> h((size_t)n * ADJ_NC);
-        double g[2];
         SPHDEM_CUDA_CHECK(cudaMemcpyAsync(h.data(), a->adj, sbytes, cudaMemcpyDeviceToHost, c->stream));
-        SPHDEM_CUDA_CHECK(cudaMemcpyAsync(g, a->grads, sizeof(g), cudaMemcpyDeviceToHost, c->stream));
+        SPHDEM_CUDA_CHECK(cudaMemcpyAsync(grads3, a->grads, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
         for (int64_t i = 0; i < n; i++)
             for (int d = 0; d < 3; d++) {
@@ -436,8 +874,6 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
                 if (dv0) dv0[3 * i + d] = h[i * ADJ_NC + 3 + d];
                 if (dvh0) dvh0[3 * i + d] = h[i * ADJ_NC + 6 + d];
             }
-        *dk = g[0];
-        *dgamma = g[1];
     }
     restore_state(c, a->ckpt[nseg], a->ckpt_g[nseg]);
     SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));

@@ -373,6 +373,7 @@ void run_full_step(sphdem_ctx *c) {
 
 namespace sphdem {
 void step_sequence(sphdem_ctx *c) { run_full_step(c); }
+void phase_sequence(sphdem_ctx *c, int phase) { run_phase(c, phase); }
 int device_status(sphdem_ctx *c) { return check_device(c); }
 }  // namespace sphdem
 
@@ -804,9 +805,10 @@ int sphdem_cell_ids(sphdem_handle h, int32_t *cells) {
 int sphdem_adjoint_forward(sphdem_handle h, int nsteps, int ckpt_every) {
     if (!h || nsteps <= 0 || ckpt_every <= 0) return SPHDEM_ERR_INVALID;
     try {
-        const std::string why = adjoint_supported(h);
+        int mode = 0;
+        const std::string why = adjoint_supported(h, &mode);
         if (!why.empty()) return fail(h, SPHDEM_ERR_UNSUPPORTED, why);
-        return adjoint_forward(h, nsteps, ckpt_every);
+        return adjoint_forward(h, nsteps, ckpt_every, mode);
     } catch (const std::string &e) {
         return fail(h, SPHDEM_ERR_CUDA, e);
     }
@@ -817,12 +819,18 @@ int sphdem_adjoint_backward(sphdem_handle h, const double *dL_dr, const double *
     if (!h || !grads) return SPHDEM_ERR_INVALID;
     std::memset(grads, 0, sizeof(*grads));
     try {
-        double dk = 0.0, dg = 0.0;
-        const int rc = adjoint_backward(h, dL_dr, dL_dv, dL_dvhat, &dk, &dg, dL_dr0, dL_dv0, dL_dvhat0);
-        if (rc) return fail(h, rc, "more DEM contacts per particle than the adjoint records");
-        grads->dem_k = dk;
-        grads->dem_gamma = dg;
-        grads->valid = SPHDEM_GRAD_DEM_K | SPHDEM_GRAD_DEM_GAMMA | SPHDEM_GRAD_POSITIONS;
+        double g3[3] = {0.0, 0.0, 0.0};
+        const int rc = adjoint_backward(h, dL_dr, dL_dv, dL_dvhat, g3, dL_dr0, dL_dv0, dL_dvhat0);
+        if (rc == SPHDEM_ERR_CAPACITY) return fail(h, rc, "more pairs per step than the adjoint records");
+        if (rc) return rc;
+        if (h->cfg.liq_dem()) {
+            grads->dem_k = g3[0];
+            grads->dem_gamma = g3[1];
+            grads->valid = SPHDEM_GRAD_DEM_K | SPHDEM_GRAD_DEM_GAMMA | SPHDEM_GRAD_POSITIONS;
+        } else {
+            grads->viscosity = g3[2];
+            grads->valid = SPHDEM_GRAD_VISCOSITY | SPHDEM_GRAD_POSITIONS;
+        }
     } catch (const std::string &e) {
         return fail(h, SPHDEM_ERR_CUDA, e);
     }

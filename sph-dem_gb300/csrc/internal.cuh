@@ -78,7 +78,7 @@ struct sphdem_ctx {
     float *mx_shep32 = nullptr; /* FP32 Shepard sums of DEM particles */
     float4 *mx_ds = nullptr;    /* DEM particles: offset in their SPH bucket, bucket key */
     float4 *mx_nb = nullptr;    /* boundary particles: FP32 normals n1 (+concave), n2, n3 */
-    sphdem::AdjointData *adj = nullptr; /* checkpoints and buffers of the DEM adjoint */
+    sphdem::AdjointData *adj = nullptr; /* checkpoints and buffers of the adjoint */
     /* launch knobs chosen by the batch autotuner */
     int blk_pair = 128;         /* block size of the list-consumer passes (<= 128) */
     int grid_div = 1;           /* divides the resident-block grid of the slice passes */
@@ -144,14 +144,19 @@ void dem_end(sphdem_ctx *c);
 
 /* adjoint.cu */
 void adjoint_free(sphdem_ctx *c);
-std::string adjoint_supported(sphdem_ctx *c);
-int adjoint_forward(sphdem_ctx *c, int nsteps, int ckpt_every);
+constexpr int ADJ_MODE_DEM = 1;   /* all-DEM handle: contacts, walls, leapfrog */
+constexpr int ADJ_MODE_SPH = 2;   /* fluid + fixed boundary particles, artificial viscosity */
+/* "" and the step family in *mode when the handle's step is covered, else why not */
+std::string adjoint_supported(sphdem_ctx *c, int *mode);
+int adjoint_forward(sphdem_ctx *c, int nsteps, int ckpt_every, int mode);
+/* grads3 = d/d(dem_k), d/d(dem_gamma), d/d(alpha_artificial) */
 int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, const double *seed_vh,
-                     double *dk, double *dgamma, double *dr0, double *dv0, double *dvh0);
+                     double *grads3, double *dr0, double *dv0, double *dvh0);
 
-/* capi.cu: one full step (all phases and hooks) on the handle's stream, and
- * the device error flags (synchronises) */
+/* capi.cu: one full step (all phases and hooks) on the handle's stream, one
+ * phase of it, and the device error flags (synchronises) */
 void step_sequence(sphdem_ctx *c);
+void phase_sequence(sphdem_ctx *c, int phase);
 int device_status(sphdem_ctx *c);
 
 /* fields.cu */

@@ -1,11 +1,12 @@
-"""Adjoint of the DEM step (sphdem_adjoint_forward / _backward) against FP64
+"""Adjoint of the step (sphdem_adjoint_forward / _backward) against FP64
 central finite differences through the C ABI (-m gpu).
 
-Loss: mean final DEM height plus the summed squared final vhat.  Gradients
-w.r.t. the spring constant k, the dashpot coefficient gamma (hence the
-restitution), and the initial positions along seeded random directions,
-each compared with a central difference of relative step 1e-6; tolerance
-1e-3 relative.
+DEM step: loss = mean final DEM height plus the summed squared final vhat;
+gradients w.r.t. the spring constant k, the dashpot coefficient gamma
+(hence the restitution), and the initial positions along seeded random
+directions.  Fluid step: see the dam-break section below.  Each gradient is
+compared with a central difference of relative step 1e-6; tolerance 1e-3
+relative.
 """
 import copy
 
@@ -87,8 +88,112 @@ def test_dem_adjoint_vs_central_differences(lib, precision):
         assert abs(ad - fd) <= RTOL * max(abs(fd), 1e-9), f"direction {k}: adjoint {ad} fd {fd}"
 
 
-def test_adjoint_rejects_fluid(lib):
+# ---------------------------------------------------------------------------
+# Fluid step (dam break: SPH + fixed SPH-boundary particles, artificial
+# viscosity).  Loss: mean final fluid height + kinetic energy of the fluid
+# (through v) + summed squared fluid vhat.  Gradients w.r.t. alpha (the
+# artificial viscosity coefficient) and the initial positions / vhat along
+# seeded random directions, against FP64 central differences.
+
+SPH_STEPS, SPH_K = 40, 7      # 7 does not divide 40: a short last segment
+
+
+def moving_dambreak():
+    """The small dam break with a seeded velocity field on the fluid.  At rest
+    every pair sits exactly on the artificial-viscosity switch (vdr = 0,
+    sph.h:633-646), where the loss has a kink in vhat and a central
+    difference averages the two one-sided slopes."""
     case = cases.workload("dambreak2d_small")
+    fl = np.asarray(case.particles["iam"]) == cases.SPH
+    v = np.zeros((case.n, 3))
+    v[fl, :2] = np.random.default_rng(7).normal(0.0, 0.05, size=(fl.sum(), 2))
+    case.particles["v"] = v
+    case.particles["vhat"] = v.copy()
+    return case
+
+
+def sph_loss_and_seed(sim):
+    a = sim.get()
+    fl = a["iam"] == cases.SPH
+    m = a["mass"][:, None]
+    L = (a["r"][fl, 1].mean() + 0.5 * (m[fl] * a["v"][fl] ** 2).sum()
+         + (a["vhat"][fl] ** 2).sum())
+    dr = np.zeros((sim.n, 3))
+    dr[fl, 1] = 1.0 / fl.sum()
+    dv = np.zeros((sim.n, 3))
+    dv[fl] = m[fl] * a["v"][fl]
+    dvh = np.zeros((sim.n, 3))
+    dvh[fl] = 2.0 * a["vhat"][fl]
+    return L, dr, dv, dvh
+
+
+def sph_run_loss(lib, case, cfg=None, r=None, vhat=None):
+    parts = copy.deepcopy(case.particles)
+    if r is not None:
+        parts["r"] = r
+    if vhat is not None:
+        parts["vhat"] = vhat
+    sim = capi.Simulation(lib, cfg or case.cfg, parts, precision=cases.PREC_FP64)
+    sim.step(SPH_STEPS)
+    L = sph_loss_and_seed(sim)[0]
+    sim.close()
+    return L
+
+
+@pytest.mark.parametrize("precision", [cases.PREC_FP64, cases.PREC_MIXED])
+def test_sph_adjoint_vs_central_differences(lib, precision):
+    case = moving_dambreak()
+    sim = capi.Simulation(lib, case.cfg, case.particles, precision=precision)
+    sim.adjoint_forward(SPH_STEPS, SPH_K)
+    L0, dr, dv, dvh = sph_loss_and_seed(sim)
+    grads, dr0, dv0, dvh0 = sim.adjoint_backward(dL_dr=dr, dL_dv=dv, dL_dvhat=dvh)
+    assert sph_loss_and_seed(sim)[0] == L0      # back at the final state
+    sim.close()
+    assert grads.valid & capi.GRAD_VISCOSITY and grads.valid & capi.GRAD_POSITIONS
+    assert not grads.valid & capi.GRAD_DEM_K
+
+    # FP64 finite differences for both precisions: the mixed path's FP32
+    # pair sums are too noisy for a difference quotient of step 1e-6
+    base = case.cfg["alpha_artificial"]
+    eps = 1e-6 * base
+    cp, cm = dict(case.cfg), dict(case.cfg)
+    cp["alpha_artificial"] = base + eps
+    cm["alpha_artificial"] = base - eps
+    fd = (sph_run_loss(lib, case, cfg=cp) - sph_run_loss(lib, case, cfg=cm)) / (2 * eps)
+    print("alpha adjoint", grads.viscosity, "fd", fd)
+    assert abs(grads.viscosity - fd) <= RTOL * abs(fd), f"alpha: adjoint {grads.viscosity} fd {fd}"
+
+    rng = np.random.default_rng(4)
+    r0 = np.asarray(case.particles["r"], dtype=np.float64).copy()
+    scale = np.abs(r0).max()
+    for k in range(3):
+        u = rng.normal(size=r0.shape)
+        u[:, 2] = 0.0
+        u /= np.linalg.norm(u)
+        eps = 1e-6 * scale
+        fd = (sph_run_loss(lib, case, r=r0 + eps * u) - sph_run_loss(lib, case, r=r0 - eps * u)) / (2 * eps)
+        ad = float((dr0 * u).sum())
+        print("r direction", k, "adjoint", ad, "fd", fd)
+        assert abs(ad - fd) <= RTOL * abs(fd), f"r direction {k}: adjoint {ad} fd {fd}"
+
+    vh0 = np.asarray(case.particles["vhat"], dtype=np.float64).copy()
+    u = rng.normal(size=vh0.shape)
+    u[:, 2] = 0.0
+    u /= np.linalg.norm(u)
+    eps = 1e-4
+    fd = (sph_run_loss(lib, case, vhat=vh0 + eps * u) - sph_run_loss(lib, case, vhat=vh0 - eps * u)) / (2 * eps)
+    ad = float((dvh0 * u).sum())
+    print("vhat direction adjoint", ad, "fd", fd)
+    assert abs(ad - fd) <= RTOL * abs(fd), f"vhat direction: adjoint {ad} fd {fd}"
+    # v0 enters the loss only through v1 = v0 + dt sum f
+    fl = np.asarray(case.particles["iam"]) == cases.SPH
+    assert np.allclose(dv0[fl], dv[fl], rtol=0, atol=0)
+
+
+def test_adjoint_rejects_unsupported_fluid(lib):
+    # damBreak's own options (Monaghan viscosity, anticlumping, h following
+    # density) are outside the fluid adjoint
+    case = cases.workload("dambreak2d_monaghan_small")
     sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_FP64)
     with pytest.raises(capi.SphDemError, match="UNSUPPORTED"):
         sim.adjoint_forward(4, 2)
