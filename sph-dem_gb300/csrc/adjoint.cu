@@ -1,5 +1,5 @@
 /*
- * Adjoint of the step (reverse mode, FP64), with step checkpointing.
+ * Adjoint of the step (reverse mode), with step checkpointing.
  *
  * sphdem_adjoint_forward runs the steps through the ordinary path and keeps
  * the state (r, v, vh, f, dens, dddt in tag order) and the step globals every
@@ -66,6 +66,7 @@ namespace sphdem {
 constexpr int ADJ_NC = 14;         /* r, v, vh, f, dens, dddt per particle */
 constexpr int ADJ_MAX_CONTACTS = 32;
 constexpr int ADJ_AUX = 8;         /* SPH: r_s, vh_s, rho_s, pdr2_s */
+constexpr int ADJ_NREC = 7;        /* SPH, mixed: float4 records per particle */
 
 struct AdjointData {
     int mode = 0;
@@ -92,6 +93,7 @@ struct AdjointData {
     int *slot = nullptr;            /* step index inside the segment, read by the replay graph */
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     double *aux = nullptr;          /* SPH: r_s, vh_s, rho_s, pdr2_s per particle */
+    float4 *rec = nullptr;          /* SPH, mixed: FP32 records, ADJ_NREC x n */
     double *grads = nullptr;        /* d/dk, d/dgamma, d/dalpha */
 };
 
@@ -119,6 +121,7 @@ void adjoint_free(sphdem_ctx *c) {
     cudaFree(a->cnt_end);
     cudaFree(a->slot);
     cudaFree(a->aux);
+    cudaFree(a->rec);
     cudaFree(a->grads);
     delete a;
     c->adj = nullptr;
@@ -606,6 +609,254 @@ __global__ void k_sadj_mid(DevCfg c, int64_t n, double dt, const double *aux, co
     if ((threadIdx.x & 31) == 0 && Ab != 0.0) atomicAdd(&grads[2], Ab);
 }
 
+/* ------------------------------------------------------------------------ */
+/* SPH step VJP, mixed precision: the same formulas with FP32 pair math.
+ * Positions enter as double-float pairs (hi = (float)r, lo = (float)(r - hi)),
+ * so a pair's displacement (hi_a - hi_b) + (lo_a - lo_b) keeps ~1e-7 of
+ * itself without FP64 work per pair; velocities, densities, pdr2 and the
+ * adjoints are FP32; per-particle sums are Kahan-compensated and land in the
+ * FP64 adjoint state once.
+ *
+ * Records (tag order), middle state:  M0 = (r_s hi, 1/h), M1 = (r_s lo, m),
+ * M2 = (vh_s, rho_s), M3 = (adjoint of f1, pdr2_s); end state: E0 = (r1 hi,
+ * 1/h), E1 = (r1 lo, m), E2 = (vh1, adjoint of dddt1 + hd adjoint of rho1). */
+enum { R_M0 = 0, R_M1, R_M2, R_M3, R_E0, R_E1, R_E2 };
+
+struct Kf {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ void split2(double x, float &hi, float &lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
+template <int ND>
+__device__ __forceinline__ float ipow_nd2(float ih) {   /* ih^(ND+2) */
+    float v = ih * ih;
+#pragma unroll
+    for (int d = 0; d < ND; d++) v *= ih;
+    return v;
+}
+
+/* G and dG/dr in FP32 (grad_factor) from 1/h of both particles */
+template <int ND>
+__device__ __forceinline__ void grad_factor32(float wcon, float r, float iha, float ihb, float &G, float &Gp) {
+    G = 0.f;
+    Gp = 0.f;
+    const float ih[2] = {iha, ihb};
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const float q = r * ih[k];
+        if (q > 2.f) continue;
+        const float t = 2.f - q, f = wcon * ipow_nd2<ND>(ih[k]);
+        G += -10.f * f * (t * t * t);
+        Gp += 30.f * f * (t * t) * ih[k];
+    }
+    G *= 0.5f;
+    Gp *= 0.5f;
+}
+
+template <int ND>
+__device__ __forceinline__ void force_pair_vjp32(float alpha, float c0, const float *d, const float *w, float r,
+                                                 float G, float Gp, const float *Fb, float my, float rhox, float rhoy,
+                                                 float pdr2x, float pdr2y, float sign, Kf *Db, Kf *Wb, Kf &Rb,
+                                                 Kf &Qb, float &Ab) {
+    float P = 0.f, vdr = 0.f;
+#pragma unroll
+    for (int k = 0; k < ND; k++) {
+        P = fmaf(Fb[k], d[k], P);
+        vdr = fmaf(d[k], w[k], vdr);
+    }
+    const float ir = 1.f / r;
+    float s = -my * (pdr2x + pdr2y);
+    Qb.add(-my * G * P);
+    float coefw = 0.f, coefd = 0.f;
+    if (vdr < 0.f) {
+        const float viss = vdr * ir, rs = 1.f / (rhox + rhoy);
+        const float Pi = alpha * viss * (2.f * c0 - 4.f * viss) * rs;
+        const float dPi = alpha * (2.f * c0 - 8.f * viss) * rs;
+        const float K = G * P;
+        s += my * Pi;
+        coefw = my * K * dPi * ir;
+        coefd = -my * K * dPi * viss * ir * ir;
+        Rb.add(-my * K * Pi * rs);
+        Ab += my * K * viss * (2.f * c0 - 4.f * viss) * rs;
+#pragma unroll
+        for (int k = 0; k < ND; k++) Wb[k].add(sign * coefw * d[k]);
+    }
+    const float gpd = Gp * P * ir;
+#pragma unroll
+    for (int k = 0; k < ND; k++) Db[k].add(sign * (s * (G * Fb[k] + gpd * d[k]) + coefw * w[k] + coefd * d[k]));
+}
+
+/* decode a table entry: partner tag and the image displacement to add */
+template <int ND>
+__device__ __forceinline__ int entry_of(const DevCfg &c, int e, float *img) {
+    const int code = (int)((unsigned)e >> SH_SHIFT);
+#pragma unroll
+    for (int q = 0; q < ND; q++) {
+        const int sh = ((code >> (2 * q)) & 3) - 1;
+        img[q] = sh == 0 ? 0.f : (float)(sh * (c.rmax[q] - c.rmin[q]));
+    }
+    return e & ((1 << SH_SHIFT) - 1);
+}
+
+/* the FP32 records of one step from its FP64 start / end states */
+__global__ void k_sadj_pre32(DevCfg c, int64_t n, double dt, const double *s0, const double *s1, const double *adj,
+                             const double *mass, const double *hh, const int *typ, float4 *rec) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double *x0 = s0 + i * ADJ_NC, *x1 = s1 + i * ADJ_NC, *aa = adj + i * ADJ_NC;
+    const double hd = 0.5 * dt;
+    const bool sph = typ[i] == T_SPH;
+    const float ih = (float)(1.0 / hh[i]), m = (float)mass[i];
+    float hi[3], lo[3], vh[3];
+    for (int d = 0; d < 3; d++) {
+        split2(x0[d] + hd * x0[6 + d], hi[d], lo[d]);
+        vh[d] = (float)(sph ? x0[6 + d] + hd * x0[9 + d] : x0[6 + d]);
+    }
+    const double rho = x0[12] + hd * x0[13];
+    const double q = rho / c.refd, q2 = q * q;
+    const double pdr2 = c.prb * (q2 * q2 * q2 * q - 1.0) / (rho * rho);
+    rec[R_M0 * n + i] = make_float4(hi[0], hi[1], hi[2], ih);
+    rec[R_M1 * n + i] = make_float4(lo[0], lo[1], lo[2], m);
+    rec[R_M2 * n + i] = make_float4(vh[0], vh[1], vh[2], (float)rho);
+    rec[R_M3 * n + i] = make_float4(0.f, 0.f, 0.f, (float)pdr2);
+    for (int d = 0; d < 3; d++) split2(x1[d], hi[d], lo[d]);
+    rec[R_E0 * n + i] = make_float4(hi[0], hi[1], hi[2], ih);
+    rec[R_E1 * n + i] = make_float4(lo[0], lo[1], lo[2], m);
+    rec[R_E2 * n + i] = make_float4((float)x1[6], (float)x1[7], (float)x1[8], (float)(aa[13] + hd * aa[12]));
+}
+
+template <int ND>
+__global__ void __launch_bounds__(128) k_sadj_end32(DevCfg c, int64_t n, double dt, const int *typ,
+                                                    const int *__restrict__ nb, const int2 *__restrict__ oc,
+                                                    const double *adj, double *racc, double *vh1b, float4 *rec) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const float4 *E0 = rec + R_E0 * n, *E1 = rec + R_E1 * n, *E2 = rec + R_E2 * n;
+    const float wcon = (float)c.wcon;
+    const float4 p0 = E0[a], p1 = E1[a], p2 = E2[a];
+    const float pa[3] = {p0.x, p0.y, p0.z}, la[3] = {p1.x, p1.y, p1.z}, va[3] = {p2.x, p2.y, p2.z};
+    Kf rb[ND], wb[ND];
+    const int2 o = oc[a];
+    for (int k = 0; k < o.y; k++) {
+        float img[3];
+        const int b = entry_of<ND>(c, __ldg(nb + o.x + k), img);
+        const float4 q0 = E0[b], q1 = E1[b], q2 = E2[b];
+        const float pb[3] = {q0.x, q0.y, q0.z}, lb[3] = {q1.x, q1.y, q1.z}, vb[3] = {q2.x, q2.y, q2.z};
+        float d[3], w[3], r2 = 0.f, wd = 0.f;
+#pragma unroll
+        for (int q = 0; q < ND; q++) {
+            d[q] = ((pa[q] - pb[q]) + (la[q] - lb[q])) - img[q];
+            w[q] = va[q] - vb[q];
+            r2 = fmaf(d[q], d[q], r2);
+            wd = fmaf(w[q], d[q], wd);
+        }
+        if (!(r2 > 0.f)) continue;
+        const float r = sqrtf(r2);
+        float G, Gp;
+        grad_factor32<ND>(wcon, r, p0.w, q0.w, G, Gp);
+        const float coef = q1.w * p2.w + p1.w * q2.w;  /* m_b D_a + m_a D_b */
+        const float gw = Gp * wd / r;
+#pragma unroll
+        for (int q = 0; q < ND; q++) {
+            rb[q].add(coef * (G * w[q] + gw * d[q]));
+            wb[q].add(coef * G * d[q]);
+        }
+    }
+    const double hd = 0.5 * dt;
+    const double *aa = adj + a * ADJ_NC;
+    const bool sph = typ[a] == T_SPH;
+    float F[3] = {0.f, 0.f, 0.f};
+    for (int q = 0; q < 3; q++) {
+        const double rt = aa[q] + (q < ND ? rb[q].value() : 0.0);
+        const double vt = aa[6 + q] + (q < ND ? wb[q].value() : 0.0) + hd * rt;
+        racc[a * 3 + q] = rt;
+        vh1b[a * 3 + q] = vt;
+        F[q] = sph ? (float)(aa[9 + q] + dt * (vt + aa[3 + q])) : 0.f;
+    }
+    float4 *M3 = rec + R_M3 * n;
+    M3[a] = make_float4(F[0], F[1], F[2], M3[a].w);
+}
+
+template <int ND>
+__global__ void __launch_bounds__(128) k_sadj_mid32(DevCfg c, int64_t n, double dt, const double *s0,
+                                                    const int *typ, const int *__restrict__ nb,
+                                                    const int2 *__restrict__ oc, const double *racc,
+                                                    const double *vh1b, const float4 *__restrict__ rec, double *adj,
+                                                    double *grads) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float Ab = 0.f;
+    if (a < n) {
+        const float4 *M0 = rec + R_M0 * n, *M1 = rec + R_M1 * n, *M2 = rec + R_M2 * n, *M3 = rec + R_M3 * n;
+        const float wcon = (float)c.wcon, alpha = (float)c.alpha_art, c0 = (float)c.spsound;
+        const float4 p0 = M0[a], p1 = M1[a], p2 = M2[a], p3 = M3[a];
+        const float pa[3] = {p0.x, p0.y, p0.z}, la[3] = {p1.x, p1.y, p1.z}, va[3] = {p2.x, p2.y, p2.z};
+        const float Fa[3] = {p3.x, p3.y, p3.z};
+        const bool own = Fa[0] != 0.f || Fa[1] != 0.f || Fa[2] != 0.f;
+        Kf Db[ND], Wb[ND], Rb, Qb;
+        float Adum = 0.f;
+        const int2 o = oc[a];
+        for (int k = 0; k < o.y; k++) {
+            float img[3];
+            const int b = entry_of<ND>(c, __ldg(nb + o.x + k), img);
+            const float4 q0 = M0[b], q1 = M1[b], q2 = M2[b], q3 = M3[b];
+            const float pb[3] = {q0.x, q0.y, q0.z}, lb[3] = {q1.x, q1.y, q1.z}, vb[3] = {q2.x, q2.y, q2.z};
+            const float Fb[3] = {q3.x, q3.y, q3.z};
+            float d[3], w[3], md[3], mw[3], r2 = 0.f;
+#pragma unroll
+            for (int q = 0; q < ND; q++) {
+                d[q] = ((pa[q] - pb[q]) + (la[q] - lb[q])) - img[q];
+                w[q] = va[q] - vb[q];
+                md[q] = -d[q];
+                mw[q] = -w[q];
+                r2 = fmaf(d[q], d[q], r2);
+            }
+            if (!(r2 > 0.f)) continue;
+            const float r = sqrtf(r2);
+            float G, Gp;
+            grad_factor32<ND>(wcon, r, p0.w, q0.w, G, Gp);
+            if (own)
+                force_pair_vjp32<ND>(alpha, c0, d, w, r, G, Gp, Fa, q1.w, p2.w, q2.w, p3.w, q3.w, 1.f, Db, Wb, Rb, Qb,
+                                     Ab);
+            if (Fb[0] != 0.f || Fb[1] != 0.f || Fb[2] != 0.f)
+                force_pair_vjp32<ND>(alpha, c0, md, mw, r, G, Gp, Fb, p1.w, q2.w, p2.w, q3.w, p3.w, -1.f, Db, Wb, Rb,
+                                     Qb, Adum);
+        }
+        const double hd = 0.5 * dt;
+        const double *x0 = s0 + a * ADJ_NC;
+        const double rho = x0[12] + hd * x0[13], x = rho / c.refd, x2 = x * x;
+        const double dpdr2 = c.prb * (5.0 * (x2 * x2 * x2 * x) + 2.0) / (rho * rho * rho);
+        double *aa = adj + a * ADJ_NC;
+        const double rhos_b = aa[12] + Rb.value() + Qb.value() * dpdr2;
+        const bool sph_a = typ[a] == T_SPH;
+        for (int q = 0; q < 3; q++) {
+            const double D = q < ND ? Db[q].value() : 0.0, W = q < ND ? Wb[q].value() : 0.0;
+            const double rs_b = racc[a * 3 + q] + D;
+            aa[q] = rs_b;
+            aa[6 + q] = vh1b[a * 3 + q] + W + hd * rs_b;
+            aa[9 + q] = sph_a ? hd * W : 0.0;
+        }
+        aa[12] = rhos_b;
+        aa[13] = hd * rhos_b;
+    }
+    Ab += __shfl_xor_sync(0xffffffffu, Ab, 16);
+    Ab += __shfl_xor_sync(0xffffffffu, Ab, 8);
+    Ab += __shfl_xor_sync(0xffffffffu, Ab, 4);
+    Ab += __shfl_xor_sync(0xffffffffu, Ab, 2);
+    Ab += __shfl_xor_sync(0xffffffffu, Ab, 1);
+    if ((threadIdx.x & 31) == 0 && Ab != 0.f) atomicAdd(&grads[2], (double)Ab);
+}
+
 void save_state(sphdem_ctx *c, double *dst, const int *slot = nullptr) {
     k_save<<<grid_for(c->n, ABLK), ABLK, 0, c->stream>>>(c->A, c->n, dst, slot);
 }
@@ -649,8 +900,15 @@ void replay_sph_step(sphdem_ctx *c) {
         try {
             for (int p = SPHDEM_HOOK_BEFORE_START; p <= SPHDEM_HOOK_AFTER_END; p++) {
                 phase_sequence(c, p);
-                if (p == SPHDEM_PHASE_MIDDLE) sph_pairs(c, a->nb_mid, a->oc_mid, a->pair_cnt, a->slot);
-                if (p == SPHDEM_PHASE_END) sph_pairs(c, a->nb_end, a->oc_end, a->cnt_end, a->slot);
+                const bool mixed = c->cfg.precision == SPHDEM_PREC_MIXED && c->mx_maxn > 0;
+                if (p == SPHDEM_PHASE_MIDDLE) {
+                    if (mixed) mixed_adj_pairs(c, a->nb_mid, a->oc_mid, a->pair_cnt, a->pair_cap, a->slot);
+                    else sph_pairs(c, a->nb_mid, a->oc_mid, a->pair_cnt, a->slot);
+                }
+                if (p == SPHDEM_PHASE_END) {
+                    if (mixed) mixed_adj_pairs(c, a->nb_end, a->oc_end, a->cnt_end, a->pair_cap, a->slot);
+                    else sph_pairs(c, a->nb_end, a->oc_end, a->cnt_end, a->slot);
+                }
             }
             save_state(c, a->seg, a->slot);
             k_slot_inc<<<1, 32, 0, c->stream>>>(a->slot);
@@ -704,6 +962,22 @@ void backward_sph(sphdem_ctx *c, AdjointData *a, int steps, double dt) {
         const double *s0 = a->seg + (size_t)(j - 1) * n * ADJ_NC, *s1 = a->seg + (size_t)j * n * ADJ_NC;
         const int *nbm = a->nb_mid + (size_t)(j - 1) * cap, *nbe = a->nb_end + (size_t)(j - 1) * cap;
         const int2 *ocm = a->oc_mid + (size_t)(j - 1) * n, *oce = a->oc_end + (size_t)(j - 1) * n;
+        if (a->rec) {
+            k_sadj_pre32<<<grid_for(n, ABLK), ABLK, 0, c->stream>>>(c->cfg, n, dt, s0, s1, a->adj, a->mass, a->hh,
+                                                                    a->typ, a->rec);
+#define L_(ND)                                                                                                  \
+    do {                                                                                                        \
+        k_sadj_end32<ND><<<grid_for(n, 128), 128, 0, c->stream>>>(c->cfg, n, dt, a->typ, nbe, oce, a->adj, a->racc, \
+                                                                  a->vmacc, a->rec);                             \
+        k_sadj_mid32<ND><<<grid_for(n, 128), 128, 0, c->stream>>>(c->cfg, n, dt, s0, a->typ, nbm, ocm, a->racc,     \
+                                                                  a->vmacc, a->rec, a->adj, a->grads);           \
+    } while (0)
+            if (c->cfg.nd == 3) L_(3);
+            else if (c->cfg.nd == 2) L_(2);
+            else L_(1);
+#undef L_
+            continue;
+        }
         k_sadj_pre<<<grid_for(n, ABLK), ABLK, 0, c->stream>>>(c->cfg, n, dt, s0, a->typ, a->aux);
         k_sadj_end<<<grid_for(n, 128), 128, 0, c->stream>>>(c->cfg, n, dt, s1, a->mass, a->hh, a->typ, nbe, oce,
                                                             a->adj, a->racc, a->vmacc, a->fbar);
@@ -812,7 +1086,10 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
             SPHDEM_CUDA_CHECK(cudaMalloc(&a->oc_mid, (size_t)K * n * sizeof(int2)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&a->oc_end, (size_t)K * n * sizeof(int2)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&a->cnt_end, (size_t)K * sizeof(int)));
-            SPHDEM_CUDA_CHECK(cudaMalloc(&a->aux, (size_t)n * ADJ_AUX * sizeof(double)));
+            if (c->cfg.precision == SPHDEM_PREC_MIXED)
+                SPHDEM_CUDA_CHECK(cudaMalloc(&a->rec, (size_t)n * ADJ_NREC * sizeof(float4)));
+            else
+                SPHDEM_CUDA_CHECK(cudaMalloc(&a->aux, (size_t)n * ADJ_AUX * sizeof(double)));
         } else {
             SPHDEM_CUDA_CHECK(cudaMalloc(&a->pairs, (size_t)K * cap * sizeof(int4)));
         }

@@ -142,6 +142,10 @@ void dem_drag(sphdem_ctx *c);
 void dem_end(sphdem_ctx *c);
 }  // namespace mixed
 
+/* pairs32.cu: the mixed lists of the last rebuild as the adjoint's pair
+ * tables (tag space, slot *slot of nb / oc / cnt) */
+void mixed_adj_pairs(sphdem_ctx *c, int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot);
+
 /* adjoint.cu */
 void adjoint_free(sphdem_ctx *c);
 constexpr int ADJ_MODE_DEM = 1;   /* all-DEM handle: contacts, walls, leapfrog */

@@ -1818,6 +1818,61 @@ __global__ void k_list_export(DevState s, const int *tg, const int *nbr, const i
     }
 }
 
+/* The list rows of the SPH/SPHB particles as the adjoint's per-step pair
+ * tables, in tag space: nb[slot * cap + off + k] = tag_b | shift << 26 (shift
+ * = (sh_x + 1) | (sh_y + 1) << 2 | (sh_z + 1) << 4, the periodic image of b),
+ * oc[slot * n + tag_a] = (off, count).  One atomic per warp reserves the
+ * warp's entries; an overflowing particle records count 0 and the caller sees
+ * cnt[slot] > cap. */
+template <int ND>
+__global__ void k_adj_pairs(DevState s, const DevGlobals *__restrict__ g, const int *__restrict__ skey,
+                            const int *__restrict__ tg, const int *__restrict__ nbr, const int *__restrict__ ncnt,
+                            int64_t ld, int64_t n, int *nb, int2 *oc, int *cnt, int64_t cap,
+                            const int *__restrict__ slot) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool live = a < n && is_sph_or_sphb(tg[a] & 0xff);
+    const int m = live ? ncnt[a] : 0;
+    int k = 0;
+    for (int j = 0; j < m; j++) k += nbr[(int64_t)j * ld + a] >= 0;
+    const int lane = threadIdx.x & 31;
+    int incl = k;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int js = *slot;
+    int base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(cnt + js, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    if (!live) return;
+    const int64_t off = (int64_t)base + incl - k;
+    const int64_t room = cap - off;
+    int *out = nb + (int64_t)js * cap + off;
+    const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
+    int cc[3] = {0, 0, 0};
+    decode<ND>(skey[a], dims, cc);
+    int q = 0;
+    for (int j = 0; j < m && q < room; j++) {
+        const int e = nbr[(int64_t)j * ld + a];
+        if (e < 0) continue;
+        int o[3];
+        nl_decode_code(e >> B_BITS, o);
+        int code = 0;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            int sh = 0;
+            if (d < ND) {
+                const int t = cc[d] + o[d];
+                sh = t < 0 ? -1 : (t >= dims[d] ? 1 : 0);
+            }
+            code |= (sh + 1) << (2 * d);
+        }
+        out[q++] = s.irow(FI_TAG)[e & B_MASK] | (code << B_BITS);
+    }
+    oc[(int64_t)js * n + s.irow(FI_TAG)[a]] = make_int2((int)off, room >= k ? k : 0);
+}
+
 int warp_blocks(int items) { return std::max(1, std::min(1 << 16, (items + (BLK / 32) - 1) / (BLK / 32))); }
 /* coupling passes: grid-stride over 32-particle slices, one wave of resident blocks */
 template <int ND, int MODE>
@@ -1854,6 +1909,19 @@ int nlist_blocks(int64_t particles) {
 void mixed_list_export(sphdem_ctx *c, int *cnt, const long long *offs, int *idx) {
     k_list_export<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->A, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap, c->n,
                                                               cnt, offs, idx);
+}
+
+void mixed_adj_pairs(sphdem_ctx *c, int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot) {
+    const int g = grid_for(c->n, 128);
+    if (c->cfg.nd == 3)
+        k_adj_pairs<3><<<g, 128, 0, c->stream>>>(c->A, c->g, c->buf.skey, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap,
+                                                 c->n, nb, oc, cnt, cap, slot);
+    else if (c->cfg.nd == 2)
+        k_adj_pairs<2><<<g, 128, 0, c->stream>>>(c->A, c->g, c->buf.skey, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap,
+                                                 c->n, nb, oc, cnt, cap, slot);
+    else
+        k_adj_pairs<1><<<g, 128, 0, c->stream>>>(c->A, c->g, c->buf.skey, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap,
+                                                 c->n, nb, oc, cnt, cap, slot);
 }
 
 /* ---------------------------------------------------------------------- */
