@@ -113,6 +113,8 @@ typedef struct SphDemConfig {
     double   gravity_sph[3];       /* built-in beforeMiddle hook, type sph only    */
     double   gravity_dem[3];       /* built-in beforeEnd hook, type dem only       */
     SphDemWall walls[SPHDEM_MAX_WALLS];
+    double   drag_scale;           /* factor on the Di Felice drag force of calcParticleDrag
+                                      (sph.h:1593-1598); 0 is read as 1, the reference's law */
 } SphDemConfig;
 
 /* Host-side particle arrays (structure of arrays).  Vector fields hold three

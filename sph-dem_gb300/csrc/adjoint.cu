@@ -59,43 +59,9 @@
 #include <string>
 #include <vector>
 
-#include "internal.cuh"
+#include "adjoint.cuh"
 
 namespace sphdem {
-
-constexpr int ADJ_NC = 14;         /* r, v, vh, f, dens, dddt per particle */
-constexpr int ADJ_MAX_CONTACTS = 32;
-constexpr int ADJ_AUX = 8;         /* SPH: r_s, vh_s, rho_s, pdr2_s */
-constexpr int ADJ_NREC = 7;        /* SPH, mixed: float4 records per particle */
-
-struct AdjointData {
-    int mode = 0;
-    int nsteps = 0, K = 0;
-    int64_t n = 0;
-    std::vector<double *> ckpt;     /* state at steps 0, K, 2K, ... and the final state */
-    std::vector<DevGlobals> ckpt_g;
-    double *seg = nullptr;          /* (K + 1) states of one segment */
-    int4 *pairs = nullptr;          /* DEM: contacts of each step of a segment */
-    int *pair_cnt = nullptr;        /* K counters (DEM contacts; SPH middle pairs) */
-    double *adj = nullptr;          /* adjoint of the state (ADJ_NC per particle) */
-    double *racc = nullptr;         /* accumulated adjoint of r1 through the forces */
-    double *vmacc = nullptr;        /* DEM: adjoint of vhm; SPH: adjoint of vh1 */
-    double *fbar = nullptr;         /* adjoint of f1 */
-    double *mass = nullptr, *rad = nullptr;   /* tag order */
-    int *typ = nullptr;             /* particle type, tag order */
-    double *hh = nullptr;           /* smoothing length, tag order */
-    /* SPH pair lists of each step of a segment: partner tag | shift code << 26,
-     * grouped by particle; (offset, count) per tag */
-    int64_t pair_cap = 0;           /* entries per step and list */
-    int *nb_mid = nullptr, *nb_end = nullptr;
-    int2 *oc_mid = nullptr, *oc_end = nullptr;
-    int *cnt_end = nullptr;
-    int *slot = nullptr;            /* step index inside the segment, read by the replay graph */
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
-    double *aux = nullptr;          /* SPH: r_s, vh_s, rho_s, pdr2_s per particle */
-    float4 *rec = nullptr;          /* SPH, mixed: FP32 records, ADJ_NREC x n */
-    double *grads = nullptr;        /* d/dk, d/dgamma, d/dalpha */
-};
 
 void adjoint_free(sphdem_ctx *c) {
     AdjointData *a = c->adj;
@@ -123,6 +89,7 @@ void adjoint_free(sphdem_ctx *c) {
     cudaFree(a->aux);
     cudaFree(a->rec);
     cudaFree(a->grads);
+    cpl_free(a);
     delete a;
     c->adj = nullptr;
 }
@@ -130,7 +97,6 @@ void adjoint_free(sphdem_ctx *c) {
 namespace {
 
 constexpr int ABLK = 256;
-constexpr int SH_SHIFT = 26;       /* partner tag bits below, shift code above */
 
 __global__ void k_save(DevState s, int64_t n, double *dst, const int *slot) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -143,8 +109,13 @@ __global__ void k_save(DevState s, int64_t n, double *dst, const int *slot) {
         o[6 + d] = s.row(FD_VHAT + d)[k];
         o[9 + d] = s.row(FD_F + d)[k];
     }
-    o[12] = s.row(FD_DENS)[k];
-    o[13] = s.row(FD_DDDT)[k];
+    o[AS_DENS] = s.row(FD_DENS)[k];
+    o[AS_DDDT] = s.row(FD_DDDT)[k];
+    for (int d = 0; d < 3; d++) {
+        o[AS_FDRAG + d] = s.row(FD_FDRAG + d)[k];
+        o[AS_FP + d] = s.row(FD_FP + d)[k];
+        o[AS_FV + d] = s.row(FD_FV + d)[k];
+    }
 }
 
 __global__ void k_restore(DevState s, int64_t n, const double *src) {
@@ -157,8 +128,13 @@ __global__ void k_restore(DevState s, int64_t n, const double *src) {
         s.row(FD_VHAT + d)[k] = o[6 + d];
         s.row(FD_F + d)[k] = o[9 + d];
     }
-    s.row(FD_DENS)[k] = o[12];
-    s.row(FD_DDDT)[k] = o[13];
+    s.row(FD_DENS)[k] = o[AS_DENS];
+    s.row(FD_DDDT)[k] = o[AS_DDDT];
+    for (int d = 0; d < 3; d++) {
+        s.row(FD_FDRAG + d)[k] = o[AS_FDRAG + d];
+        s.row(FD_FP + d)[k] = o[AS_FP + d];
+        s.row(FD_FV + d)[k] = o[AS_FV + d];
+    }
 }
 
 __global__ void k_slot_inc(int *slot) {
@@ -304,10 +280,6 @@ __global__ void k_sph_pairs(DevCfg c, DevState s, const int *start, const int *s
     oc[(int64_t)j * n + s.irow(FI_TAG)[a]] = make_int2((int)off, room >= k ? k : 0);
 }
 
-__device__ __forceinline__ double warp_sum_d(double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
 
 /* ------------------------------------------------------------------------ */
 /* DEM step VJP */
@@ -429,25 +401,6 @@ __global__ void k_vjp_assemble(int64_t n, double dt, double *adj, const double *
 
 /* ------------------------------------------------------------------------ */
 /* SPH step VJP */
-
-/* G = (F(r, h_a) + F(r, h_b)) / 2 and dG/dr, F(r, h) = -10 C (2-q)^3 / h^(d+2)
- * (the Wendland C2 gradient factor of sph.h:322-342; 0 for q > 2) */
-__device__ __forceinline__ void grad_factor(const DevCfg &c, double r, double ha, double hb, double &G, double &Gp) {
-    G = 0.0;
-    Gp = 0.0;
-    const double hs[2] = {ha, hb};
-    for (int k = 0; k < 2; k++) {
-        const double h = hs[k], q = r / h;
-        if (q > 2.0) continue;
-        double ihn2 = 1.0 / (h * h);
-        for (int d = 0; d < c.nd; d++) ihn2 /= h;
-        const double t = 2.0 - q;
-        G += -10.0 * c.wcon * (t * t * t) * ihn2;
-        Gp += 30.0 * c.wcon * (t * t) * ihn2 / h;
-    }
-    G *= 0.5;
-    Gp *= 0.5;
-}
 
 /* VJP of the force of the ordered pair (x, y) on x,
  *   T = [m_y Pi - m_y (pdr2_x + pdr2_y)] G(r) d,  d = r_x - r_y, w = vh_x - vh_y,
@@ -885,10 +838,11 @@ void sph_pairs(sphdem_ctx *c, int *nb, int2 *oc, int *cnt, const int *slot) {
                                                             oc, cnt, a->pair_cap, slot);
 }
 
-/* One replayed SPH step with its taps, as a CUDA graph (one per buffer
- * parity): the phases of the step, the middle pairs after the middle
- * rebuild, the end pairs after the end rebuild, the state after the step
- * (all at the segment slot a->slot), then slot += 1. */
+/* One replayed fluid or coupled step with its taps, as a CUDA graph (one per
+ * buffer parity): the phases of the step, the middle pairs after the middle
+ * rebuild (coupled: also the fluid -> DEM pairs and the positions), the end
+ * pairs after the end rebuild (coupled: also the FPI and contact pairs), the
+ * state after the step (all at the segment slot a->slot), then slot += 1. */
 void replay_sph_step(sphdem_ctx *c) {
     AdjointData *a = c->adj;
     cudaGraphExec_t &ge = a->graph[c->flipped ? 1 : 0];
@@ -904,10 +858,12 @@ void replay_sph_step(sphdem_ctx *c) {
                 if (p == SPHDEM_PHASE_MIDDLE) {
                     if (mixed) mixed_adj_pairs(c, a->nb_mid, a->oc_mid, a->pair_cnt, a->pair_cap, a->slot);
                     else sph_pairs(c, a->nb_mid, a->oc_mid, a->pair_cnt, a->slot);
+                    if (a->mode == ADJ_MODE_COUPLED) cpl_taps_middle(c, a);
                 }
                 if (p == SPHDEM_PHASE_END) {
                     if (mixed) mixed_adj_pairs(c, a->nb_end, a->oc_end, a->cnt_end, a->pair_cap, a->slot);
                     else sph_pairs(c, a->nb_end, a->oc_end, a->cnt_end, a->slot);
+                    if (a->mode == ADJ_MODE_COUPLED) cpl_taps_end(c, a);
                 }
             }
             save_state(c, a->seg, a->slot);
@@ -986,6 +942,16 @@ void backward_sph(sphdem_ctx *c, AdjointData *a, int steps, double dt) {
     }
 }
 
+void backward_cpl(sphdem_ctx *c, AdjointData *a, int steps, double dt) {
+    const int64_t n = c->n;
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->slot, 0, sizeof(int), c->stream));
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_mid, 0, (size_t)a->K * n * sizeof(int2), c->stream));
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_end, 0, (size_t)a->K * n * sizeof(int2), c->stream));
+    cpl_reset_segment(c, a);
+    for (int j = 1; j <= steps; j++) replay_sph_step(c);
+    for (int j = steps; j >= 1; j--) cpl_backward_step(c, a, j, dt);
+}
+
 }  // namespace
 
 std::string adjoint_supported(sphdem_ctx *c, int *mode) {
@@ -995,15 +961,27 @@ std::string adjoint_supported(sphdem_ctx *c, int *mode) {
     if (cfg.damptime > 0) return "the adjoint does not cover velocity damping";
     std::vector<int> iam(c->n);
     field_get_int(c, FI_IAM, iam.data());
-    bool all_dem = true, all_fluid = true;
+    bool all_dem = true, all_fluid = true, all_coupled = true;
     for (int t : iam) {
         all_dem = all_dem && (t == T_DEM || t == T_DEAD);
         all_fluid = all_fluid && is_sph_or_sphb(t);
+        all_coupled = all_coupled && (is_sph_or_sphb(t) || t == T_DEM);
     }
     if (cfg.liq_dem()) {
-        if (!all_dem) return "the adjoint covers LIQ_DEM handles whose particles are all DEM";
         if (cfg.freeze_until >= 0) return "the adjoint does not cover freezing";
-        *mode = ADJ_MODE_DEM;
+        if (all_dem) {
+            *mode = ADJ_MODE_DEM;
+            return "";
+        }
+        if (!all_coupled)
+            return "the coupled adjoint covers SPH, SPH-boundary and DEM particles (no repulsive boundary particles)";
+        if (cfg.visc != SPHDEM_VISC_MORRIS) return "the coupled adjoint covers Morris viscosity only";
+        if (!(cfg.flags & SPHDEM_F_CONST_H)) return "the coupled adjoint needs a constant smoothing length";
+        if (!(cfg.flags & SPHDEM_F_NO_ANTICLUMPING)) return "the coupled adjoint does not cover anticlumping";
+        if (cfg.var_h()) return "the coupled adjoint does not cover VAR_H_CORRECTION";
+        if (cfg.gamma != 7.0) return "the coupled adjoint covers the gamma = 7 equation of state";
+        if (c->n > (4 << 20)) return "the coupled adjoint covers at most 4M particles";
+        *mode = ADJ_MODE_COUPLED;
         return "";
     }
     if (!all_fluid) return "the fluid adjoint covers handles of SPH and SPH-boundary particles only";
@@ -1040,7 +1018,7 @@ int adjoint_forward(sphdem_ctx *c, int nsteps, int K, int mode) {
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->typ, c->n * sizeof(int)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->hh, c->n * sizeof(double)));
     k_save_const<<<grid_for(c->n, ABLK), ABLK, 0, c->stream>>>(c->cfg, c->A, c->n, a->mass, a->rad, a->typ, a->hh);
-    if (mode == ADJ_MODE_SPH) {
+    if (mode == ADJ_MODE_SPH || mode == ADJ_MODE_COUPLED) {
         /* size the per-step pair lists from the pairs of the current buckets */
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->slot, sizeof(int)));
         SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->slot, 0, sizeof(int), c->stream));
@@ -1049,6 +1027,7 @@ int adjoint_forward(sphdem_ctx *c, int nsteps, int K, int mode) {
         SPHDEM_CUDA_CHECK(cudaMemcpyAsync(&n0, a->slot, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
         a->pair_cap = (int64_t)n0 + n0 / 2 + 4096;
+        if (mode == ADJ_MODE_COUPLED) cpl_count_tables(c, a);
     }
     for (int s = 0; s < nseg; s++) {
         save_state(c, a->ckpt[s]);
@@ -1064,14 +1043,14 @@ int adjoint_forward(sphdem_ctx *c, int nsteps, int K, int mode) {
 }
 
 int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, const double *seed_vh,
-                     double *grads3, double *dr0, double *dv0, double *dvh0) {
+                     double *grads5, uint32_t *valid, double *dr0, double *dv0, double *dvh0) {
     AdjointData *a = c->adj;
     if (!a || a->n != c->n) throw std::string("no adjoint forward pass recorded for this handle");
     const int64_t n = c->n;
     const int K = a->K;
     const size_t sbytes = (size_t)n * ADJ_NC * sizeof(double);
     const int cap = ADJ_MAX_CONTACTS * (int)n;
-    const bool sph = a->mode == ADJ_MODE_SPH;
+    const bool sph = a->mode == ADJ_MODE_SPH, cpl = a->mode == ADJ_MODE_COUPLED;
     if (!a->seg) {
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->seg, (size_t)(K + 1) * sbytes));
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->pair_cnt, (size_t)K * sizeof(int)));
@@ -1079,14 +1058,16 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->racc, n * 3 * sizeof(double)));
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->vmacc, n * 3 * sizeof(double)));
         SPHDEM_CUDA_CHECK(cudaMalloc(&a->fbar, n * 3 * sizeof(double)));
-        SPHDEM_CUDA_CHECK(cudaMalloc(&a->grads, 3 * sizeof(double)));
-        if (sph) {
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->grads, ADJ_NGRAD * sizeof(double)));
+        if (sph || cpl) {
             SPHDEM_CUDA_CHECK(cudaMalloc(&a->nb_mid, (size_t)K * a->pair_cap * sizeof(int)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&a->nb_end, (size_t)K * a->pair_cap * sizeof(int)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&a->oc_mid, (size_t)K * n * sizeof(int2)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&a->oc_end, (size_t)K * n * sizeof(int2)));
             SPHDEM_CUDA_CHECK(cudaMalloc(&a->cnt_end, (size_t)K * sizeof(int)));
-            if (c->cfg.precision == SPHDEM_PREC_MIXED)
+            if (cpl)
+                cpl_alloc(c, a);
+            else if (c->cfg.precision == SPHDEM_PREC_MIXED)
                 SPHDEM_CUDA_CHECK(cudaMalloc(&a->rec, (size_t)n * ADJ_NREC * sizeof(float4)));
             else
                 SPHDEM_CUDA_CHECK(cudaMalloc(&a->aux, (size_t)n * ADJ_AUX * sizeof(double)));
@@ -1104,7 +1085,7 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
                 h[i * ADJ_NC + 6 + d] = seed_vh ? seed_vh[3 * i + d] : 0.0;
             }
         SPHDEM_CUDA_CHECK(cudaMemcpyAsync(a->adj, h.data(), sbytes, cudaMemcpyHostToDevice, c->stream));
-        SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->grads, 0, 3 * sizeof(double), c->stream));
+        SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->grads, 0, ADJ_NGRAD * sizeof(double), c->stream));
         SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
     }
     const int nseg = (a->nsteps + K - 1) / K;
@@ -1115,9 +1096,10 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
         restore_state(c, a->ckpt[sg], a->ckpt_g[sg]);
         SPHDEM_CUDA_CHECK(cudaMemcpyAsync(a->seg, a->ckpt[sg], sbytes, cudaMemcpyDeviceToDevice, c->stream));
         SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->pair_cnt, 0, K * sizeof(int), c->stream));
-        if (sph) {
+        if (sph || cpl) {
             SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cnt_end, 0, K * sizeof(int), c->stream));
-            backward_sph(c, a, steps, dt);
+            if (cpl) backward_cpl(c, a, steps, dt);
+            else backward_sph(c, a, steps, dt);
         } else {
             backward_dem(c, a, steps, dt, cap);
         }
@@ -1125,12 +1107,13 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
         /* list overflow check of this segment */
         std::vector<int> cnt(2 * K, 0);
         SPHDEM_CUDA_CHECK(cudaMemcpyAsync(cnt.data(), a->pair_cnt, K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-        if (sph)
+        if (sph || cpl)
             SPHDEM_CUDA_CHECK(
                 cudaMemcpyAsync(cnt.data() + K, a->cnt_end, K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
-        const int64_t lim = sph ? a->pair_cap : cap;
+        const int64_t lim = (sph || cpl) ? a->pair_cap : cap;
         for (int v : cnt) overflow = overflow || v > lim;
+        if (cpl) overflow = overflow || cpl_overflow(c, a);
         const int rc = device_status(c);
         if (rc != SPHDEM_OK) return rc;
     }
@@ -1143,7 +1126,8 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
     {
         std::vector<double> h((size_t)n * ADJ_NC);
         SPHDEM_CUDA_CHECK(cudaMemcpyAsync(h.data(), a->adj, sbytes, cudaMemcpyDeviceToHost, c->stream));
-        SPHDEM_CUDA_CHECK(cudaMemcpyAsync(grads3, a->grads, 3 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        SPHDEM_CUDA_CHECK(
+            cudaMemcpyAsync(grads5, a->grads, ADJ_NGRAD * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
         SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
         for (int64_t i = 0; i < n; i++)
             for (int d = 0; d < 3; d++) {
@@ -1152,6 +1136,10 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
                 if (dvh0) dvh0[3 * i + d] = h[i * ADJ_NC + 6 + d];
             }
     }
+    *valid = SPHDEM_GRAD_POSITIONS;
+    if (a->mode == ADJ_MODE_DEM) *valid |= SPHDEM_GRAD_DEM_K | SPHDEM_GRAD_DEM_GAMMA;
+    if (sph) *valid |= SPHDEM_GRAD_VISCOSITY;
+    if (cpl) *valid |= SPHDEM_GRAD_DEM_K | SPHDEM_GRAD_DEM_GAMMA | SPHDEM_GRAD_VISCOSITY | SPHDEM_GRAD_DRAG_SCALE;
     restore_state(c, a->ckpt[nseg], a->ckpt_g[nseg]);
     SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
     return SPHDEM_OK;

@@ -117,6 +117,7 @@ void build_devcfg(const SphDemConfig &h, DevCfg &c) {
     c.prb = h.prb;
     c.spsound = h.spsound;
     c.viscosity = h.viscosity;
+    c.drag_scale = h.drag_scale != 0.0 ? h.drag_scale : 1.0;
     c.alpha_art = h.alpha_artificial;
     c.alpha_mon = h.viscosity * (112.0 / 15.0) / (h.spsound * h.h);  /* viscToAlpha, misc.h:41-43 */
     c.bfac = h.bfac;
@@ -819,18 +820,18 @@ int sphdem_adjoint_backward(sphdem_handle h, const double *dL_dr, const double *
     if (!h || !grads) return SPHDEM_ERR_INVALID;
     std::memset(grads, 0, sizeof(*grads));
     try {
-        double g3[3] = {0.0, 0.0, 0.0};
-        const int rc = adjoint_backward(h, dL_dr, dL_dv, dL_dvhat, g3, dL_dr0, dL_dv0, dL_dvhat0);
+        double g5[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        uint32_t valid = 0;
+        const int rc = adjoint_backward(h, dL_dr, dL_dv, dL_dvhat, g5, &valid, dL_dr0, dL_dv0, dL_dvhat0);
         if (rc == SPHDEM_ERR_CAPACITY) return fail(h, rc, "more pairs per step than the adjoint records");
         if (rc) return rc;
-        if (h->cfg.liq_dem()) {
-            grads->dem_k = g3[0];
-            grads->dem_gamma = g3[1];
-            grads->valid = SPHDEM_GRAD_DEM_K | SPHDEM_GRAD_DEM_GAMMA | SPHDEM_GRAD_POSITIONS;
-        } else {
-            grads->viscosity = g3[2];
-            grads->valid = SPHDEM_GRAD_VISCOSITY | SPHDEM_GRAD_POSITIONS;
-        }
+        grads->dem_k = g5[0];
+        grads->dem_gamma = g5[1];
+        /* the viscosity parameter of the handle's model: alpha_artificial
+         * for artificial viscosity, the kinematic viscosity for Morris */
+        grads->viscosity = h->cfg.visc == SPHDEM_VISC_ARTIFICIAL ? g5[2] : g5[3];
+        grads->drag_scale = g5[4];
+        grads->valid = valid;
     } catch (const std::string &e) {
         return fail(h, SPHDEM_ERR_CUDA, e);
     }

@@ -66,6 +66,7 @@ struct DevCfg {
     double g_sph[3], g_dem[3];
     double wall_p[SPHDEM_MAX_WALLS][3], wall_n[SPHDEM_MAX_WALLS][3];
     double wcon;          /* WCON_WENDLAND for nd */
+    double drag_scale;    /* factor on the Di Felice drag force */
     /* DEM search grid (static): cell size >= max(Rc, 2 DEM_SEARCH_RADIUS) */
     int ddims[3];
     double dcell[3], dorig[3], rdcell[3];
@@ -249,6 +250,73 @@ __device__ __forceinline__ int coupling_rule(const int *cs, const int *cd, const
     if (rP < c.couple_lim) return 1;
     if (rM < c.couple_lim) return 2;
     return 0;
+}
+
+/* bucket grid of the last rebuild as the pair passes read it, the bucket of
+ * a position (SPH grid: getCellI, dataLL.h:303-305; DEM search grid), and
+ * the 3^d stencil visit (x outer, z inner, as dataLL.cpp:1052-1071) */
+struct GridInfo {
+    int sdims[3];
+    int n_sph_cells;
+    double sr2, rscell[3];
+    float rsr2_f;
+};
+
+__device__ __forceinline__ GridInfo load_grid(const DevGlobals *g) {
+    GridInfo gi;
+    for (int d = 0; d < 3; d++) {
+        gi.sdims[d] = g->sdims[d];
+        gi.rscell[d] = g->rscell[d];
+    }
+    gi.n_sph_cells = g->n_sph_cells;
+    gi.sr2 = g->sr2;
+    gi.rsr2_f = g->rsr2_f;
+    return gi;
+}
+
+__device__ __forceinline__ CellCoord sph_cell_of(const DevCfg &c, const GridInfo &gi, const double *r) {
+    CellCoord cc;
+    cc.c[0] = cc.c[1] = cc.c[2] = 0;
+    for (int d = 0; d < c.nd; d++) {
+        int k;
+        if (c.periodic[d]) {
+            k = (int)floor((r[d] - c.dmin[d]) * gi.rscell[d]);
+        } else {
+            k = trunc_index(r[d], c.dmin[d], gi.sr2, gi.rsr2_f, 3.0);
+        }
+        if (k < 0) k = 0;
+        if (k >= gi.sdims[d]) k = gi.sdims[d] - 1;
+        cc.c[d] = k;
+    }
+    return cc;
+}
+
+__device__ __forceinline__ CellCoord dem_cell_of(const DevCfg &c, const double *r) {
+    CellCoord cc;
+    cc.c[0] = cc.c[1] = cc.c[2] = 0;
+    for (int d = 0; d < c.nd; d++) {
+        int k = (int)floor((r[d] - c.dorig[d]) * c.rdcell[d]);
+        if (k < 0) k = c.periodic[d] ? c.ddims[d] - 1 : 0;
+        if (k >= c.ddims[d]) k = c.periodic[d] ? 0 : c.ddims[d] - 1;
+        cc.c[d] = k;
+    }
+    return cc;
+}
+
+/* visit every particle of the 3^d buckets around cc (x outer, z inner, as
+ * dataLL.cpp:1052-1071) */
+template <class Body>
+__device__ __forceinline__ void scan_cells(const CellCoord &cc, const int *dims, const int *periodic, int nd,
+                                           const int *start, int base, Body &&body) {
+    for (int ox = -1; ox <= 1; ox++)
+        for (int oy = (nd > 1 ? -1 : 0); oy <= (nd > 1 ? 1 : 0); oy++)
+            for (int oz = (nd > 2 ? -1 : 0); oz <= (nd > 2 ? 1 : 0); oz++) {
+                int sh[3];
+                const int lin = neighbour_cell(cc, ox, oy, oz, dims, periodic, nd, sh);
+                if (lin < 0) continue;
+                const int b0 = start[base + lin], b1 = start[base + lin + 1];
+                for (int b = b0; b < b1; b++) body(b, sh);
+            }
 }
 
 }  // namespace sphdem

@@ -150,12 +150,15 @@ void mixed_adj_pairs(sphdem_ctx *c, int *nb, int2 *oc, int *cnt, int64_t cap, co
 void adjoint_free(sphdem_ctx *c);
 constexpr int ADJ_MODE_DEM = 1;   /* all-DEM handle: contacts, walls, leapfrog */
 constexpr int ADJ_MODE_SPH = 2;   /* fluid + fixed boundary particles, artificial viscosity */
+constexpr int ADJ_MODE_COUPLED = 3;  /* fluid + fixed boundary + DEM, Morris viscosity, drag */
 /* "" and the step family in *mode when the handle's step is covered, else why not */
 std::string adjoint_supported(sphdem_ctx *c, int *mode);
 int adjoint_forward(sphdem_ctx *c, int nsteps, int ckpt_every, int mode);
-/* grads3 = d/d(dem_k), d/d(dem_gamma), d/d(alpha_artificial) */
+/* grads5 = d/d(dem_k), d/d(dem_gamma), d/d(alpha_artificial), d/d(viscosity),
+ * d/d(drag_scale); *valid = the SPHDEM_GRAD_* bits the handle's step family
+ * gives */
 int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, const double *seed_vh,
-                     double *grads3, double *dr0, double *dv0, double *dvh0);
+                     double *grads5, uint32_t *valid, double *dr0, double *dv0, double *dvh0);
 
 /* capi.cu: one full step (all phases and hooks) on the handle's stream, one
  * phase of it, and the device error flags (synchronises) */

@@ -1617,7 +1617,7 @@ __device__ __noinline__ void dem_end_update(const DevCfg *__restrict__ cp, const
             const float dragGamma = 3.7f - 0.65f * expf(-(lg * lg) / 2.f);
             const float cc0 = 0.63f + 4.8f / sqrtf(Re);
             const float sc = 0.5f * A * (cc0 * cc0) * vdiff;
-            const float pw = powf(pr, -dragGamma);
+            const float pw = powf(pr, -dragGamma) * (float)cp->drag_scale;
 #pragma unroll
             for (int k = 0; k < ND; k++) fdv[k] = sc * dv[k] * pw;
         }

@@ -58,6 +58,7 @@ class SphDemConfig(C.Structure):
         ("freeze_dem_until", C.c_double),
         ("gravity_sph", D3), ("gravity_dem", D3),
         ("walls", SphDemWall * 6),
+        ("drag_scale", C.c_double),
     ]
 
 
@@ -115,7 +116,7 @@ def config_struct(cfg: dict, precision: int | None = None) -> SphDemConfig:
                 s.walls[i].point = D3(*w["point"])
                 s.walls[i].normal = D3(*w["normal"])
             continue
-        val = cfg[name]
+        val = cfg.get(name, 1.0) if name == "drag_scale" else cfg[name]
         if ctype in (D3, I3):
             setattr(s, name, ctype(*val))
         else:

@@ -68,7 +68,7 @@ def _base_cfg(ndim: int) -> dict:
         dem_radius=0.0, dem_dens=2500.0, dem_k=0.0, dem_gamma=0.0,
         dem_search_radius=0.0, dem_vol=0.0, coupling_radius=0.0,
         dem_timestep=1e30, liq_dem_timestep=1e30,
-        time_drop_particle=1e30, freeze_dem_until=-1.0,
+        time_drop_particle=1e30, freeze_dem_until=-1.0, drag_scale=1.0,
         gravity_sph=[0.0, 0.0, 0.0], gravity_dem=[0.0, 0.0, 0.0],
         walls=[],
     )
@@ -271,13 +271,17 @@ def sediment3d(nx: int = 80, L: float = 0.2, height: float = 0.4,
                n_dem: int = 50000, dem_radius_factor: float = 0.5,
                rho_s: float = 2500.0, k: float = 1e4, restitution: float = 0.5,
                viscosity: float = 1e-6, seed: int = 3, nsteps: int = 1000,
-               dt: float | None = None) -> Case:
+               dt: float | None = None, floor: str = "boundary", var_h: bool = True) -> Case:
     """Coupled SPH-DEM sedimentation in a periodic-x/y box L x L x height with
     a bottom wall.  Fluid lattice as sediment3D/setup.cpp:65-108 (staggered
     odd layers, one `boundary` layer at k=0), h = 1.5 dx, Morris viscosity
     (kinematic `viscosity`), VAR_H_CORRECTION, porosity-weighted Tait EOS,
     Di Felice drag.  DEM spheres of radius dem_radius_factor*dx seeded
-    uniformly in the top half with overlap rejection (periodic in x, y)."""
+    uniformly in the top half with overlap rejection (periodic in x, y).
+
+    floor="sphb3" makes the floor three fixed sphBoundary layers (k = 0..2)
+    instead of the repulsive boundary layer, and var_h=False gives constant
+    h without VAR_H_CORRECTION: the coupled form the adjoint covers."""
     ndim = 3
     psep = L / nx
     nz = int(round(height / psep))
@@ -300,10 +304,14 @@ def sediment3d(nx: int = 80, L: float = 0.2, height: float = 0.4,
     ps["r"][:, 0] = np.where(odd, ii * psep, (ii + 0.5) * psep)
     ps["r"][:, 1] = np.where(odd, jj * psep, (jj + 0.5) * psep)
     ps["r"][:, 2] = kk * psep
-    bnd = kk <= 0
-    ps["iam"][:] = np.where(bnd, BOUNDARY, SPH).astype(np.int32)
-    ps["norm1"][bnd] = (0.0, 0.0, 1.0)
-    ps["norm3"][bnd] = (0.0, 1.0, 0.0)
+    if floor == "sphb3":
+        bnd = kk <= 2
+        ps["iam"][:] = np.where(bnd, SPH_BOUNDARY, SPH).astype(np.int32)
+    else:
+        bnd = kk <= 0
+        ps["iam"][:] = np.where(bnd, BOUNDARY, SPH).astype(np.int32)
+        ps["norm1"][bnd] = (0.0, 0.0, 1.0)
+        ps["norm3"][bnd] = (0.0, 1.0, 0.0)
     ps["mass"][:] = psep ** 3 * rho0
     ps["dens"][:] = rho0
     ps["h"][:] = 1.5 * (psep ** 3) ** (1.0 / 3.0)
@@ -359,7 +367,8 @@ def sediment3d(nx: int = 80, L: float = 0.2, height: float = 0.4,
     cfg = _base_cfg(ndim)
     cfg.update(
         visc_model=VISC_MORRIS,
-        flags=F_LIQ_DEM | F_VAR_H_CORRECTION | F_NO_ANTICLUMPING | F_FIXED_DT,
+        flags=(F_LIQ_DEM | F_VAR_H_CORRECTION | F_NO_ANTICLUMPING | F_FIXED_DT) if var_h
+        else (F_LIQ_DEM | F_CONST_H | F_NO_ANTICLUMPING | F_FIXED_DT),
         periodic=[1, 1, 0],
         rmin=[0.0, 0.0, 0.0], rmax=[L, L, height],
         hfac=1.5, psep=psep, h=h, dens=rho0, refd=rho0, gamma=7.0,
@@ -407,7 +416,10 @@ def workload(name: str, **kw) -> Case:
         "dambreak2d": lambda: dambreak2d(),
         "dem_settling3d": lambda: dem_settling3d(),
         "sediment3d": lambda: sediment3d(),
-        "sediment3d_adjoint": lambda: sediment3d(nx=37, n_dem=5000, nsteps=500, seed=4),
+        # differentiated coupled workload: 100k fluid, 5k DEM, in the form the
+        # adjoint covers (three fixed sphBoundary floor layers, constant h)
+        "sediment3d_adjoint": lambda: sediment3d(nx=37, n_dem=5000, nsteps=500, seed=4, floor="sphb3",
+                                                 var_h=False),
         # small parity cases (seconds on one CPU core)
         "dambreak2d_small": lambda: dambreak2d(dx=0.05, nsteps=40),
         # damBreak's own options: Monaghan viscosity (nu = 1e-2), anticlumping,
@@ -422,6 +434,8 @@ def workload(name: str, **kw) -> Case:
                                                  nsteps=600, vel_amp=0.3),
         "sediment3d_small": lambda: sediment3d(nx=10, L=0.04, height=0.08, n_dem=100,
                                                nsteps=20),
+        "sediment3d_adjoint_small": lambda: sediment3d(nx=10, L=0.04, height=0.08, n_dem=60, nsteps=30,
+                                                       floor="sphb3", var_h=False, viscosity=1e-4),
     }
     if name not in table:
         raise KeyError(f"unknown workload {name!r}; known: {sorted(table)}")

@@ -190,6 +190,112 @@ def test_sph_adjoint_vs_central_differences(lib, precision):
     assert np.allclose(dv0[fl], dv[fl], rtol=0, atol=0)
 
 
+# ---------------------------------------------------------------------------
+# Coupled SPH-DEM step (periodic x/y box, fluid over three fixed boundary
+# layers, DEM spheres in the top half; Morris viscosity, porosity, Shepard
+# sums, two-way Di Felice drag, contacts, a DEM floor wall).  Loss: mean final
+# DEM height + the squared kinetic energy of the fluid.  Gradients w.r.t. the
+# viscosity, the drag scale, k, gamma (restitution) and the initial DEM
+# positions along seeded random directions, against FP64 central
+# differences.
+
+CPL_STEPS, CPL_K = 30, 7
+
+
+def moving_coupled():
+    """The small coupled case with seeded velocities on fluid and DEM, so that
+    the drag law works away from zero slip (where its Jacobian is that of the
+    Stokes limit, which the adjoint does not take)."""
+    case = cases.workload("sediment3d_adjoint_small")
+    iam = np.asarray(case.particles["iam"])
+    rng = np.random.default_rng(9)
+    # pair the DEM spheres up with a 2% overlap, so that contacts (k, gamma)
+    # act from the first step
+    idx = np.flatnonzero(iam == cases.DEM)
+    R = case.cfg["dem_radius"]
+    r = np.asarray(case.particles["r"], dtype=np.float64).copy()
+    for a, b in zip(idx[0::2], idx[1::2]):
+        u = rng.normal(size=3)
+        u /= np.linalg.norm(u)
+        r[b] = r[a] + 1.98 * R * u
+    case.particles["r"] = r
+    v = np.zeros((case.n, 3))
+    fl, dem = iam == cases.SPH, iam == cases.DEM
+    v[fl] = rng.normal(0.0, 0.02, size=(fl.sum(), 3))
+    v[dem] = rng.normal(0.0, 0.05, size=(dem.sum(), 3))
+    case.particles["v"] = v
+    case.particles["vhat"] = v.copy()
+    return case
+
+
+def cpl_loss_and_seed(sim):
+    a = sim.get()
+    fl, dem = a["iam"] == cases.SPH, a["iam"] == cases.DEM
+    m = a["mass"][:, None]
+    ke = 0.5 * (m[fl] * a["v"][fl] ** 2).sum()
+    L = a["r"][dem, 2].mean() + ke * ke
+    dr = np.zeros((sim.n, 3))
+    dr[dem, 2] = 1.0 / dem.sum()
+    dv = np.zeros((sim.n, 3))
+    dv[fl] = 2.0 * ke * m[fl] * a["v"][fl]
+    return L, dr, dv
+
+
+def cpl_run_loss(lib, case, cfg=None, r=None):
+    parts = copy.deepcopy(case.particles)
+    if r is not None:
+        parts["r"] = r
+    sim = capi.Simulation(lib, cfg or case.cfg, parts, precision=cases.PREC_FP64)
+    sim.step(CPL_STEPS)
+    L = cpl_loss_and_seed(sim)[0]
+    sim.close()
+    return L
+
+
+@pytest.mark.parametrize("precision", [cases.PREC_FP64, cases.PREC_MIXED])
+def test_coupled_adjoint_vs_central_differences(lib, precision):
+    case = moving_coupled()
+    sim = capi.Simulation(lib, case.cfg, case.particles, precision=precision)
+    sim.adjoint_forward(CPL_STEPS, CPL_K)
+    L0, dr, dv = cpl_loss_and_seed(sim)
+    grads, dr0, dv0, dvh0 = sim.adjoint_backward(dL_dr=dr, dL_dv=dv)
+    assert cpl_loss_and_seed(sim)[0] == L0
+    sim.close()
+    want = (capi.GRAD_DEM_K | capi.GRAD_DEM_GAMMA | capi.GRAD_VISCOSITY | capi.GRAD_DRAG_SCALE
+            | capi.GRAD_POSITIONS)
+    assert grads.valid & want == want
+
+    # FP64 differences for both precisions.  Steps: 1e-6 relative on k and
+    # gamma; 1e-4 on the viscosity and the drag scale, whose effect on this
+    # short run is small enough that a 1e-6 step would sit in the roundoff of
+    # the loss (the central difference is O(step^2) accurate in both).
+    for name, attr, rel in (("dem_k", "dem_k", 1e-6), ("dem_gamma", "dem_gamma", 1e-6),
+                            ("viscosity", "viscosity", 1e-4), ("drag_scale", "drag_scale", 1e-4)):
+        base = case.cfg.get(name, 1.0)
+        eps = rel * base
+        cp, cm = dict(case.cfg), dict(case.cfg)
+        cp[name] = base + eps
+        cm[name] = base - eps
+        fd = (cpl_run_loss(lib, case, cfg=cp) - cpl_run_loss(lib, case, cfg=cm)) / (2 * eps)
+        ad = getattr(grads, attr)
+        print(name, "adjoint", ad, "fd", fd)
+        assert abs(ad - fd) <= RTOL * abs(fd), f"{name}: adjoint {ad} fd {fd}"
+
+    rng = np.random.default_rng(4)
+    r0 = np.asarray(case.particles["r"], dtype=np.float64).copy()
+    dem = np.asarray(case.particles["iam"]) == cases.DEM
+    scale = np.abs(r0).max()
+    for k in range(4):
+        u = np.zeros_like(r0)
+        u[dem] = rng.normal(size=(dem.sum(), 3))
+        u /= np.linalg.norm(u)
+        eps = 1e-6 * scale
+        fd = (cpl_run_loss(lib, case, r=r0 + eps * u) - cpl_run_loss(lib, case, r=r0 - eps * u)) / (2 * eps)
+        ad = float((dr0 * u).sum())
+        print("DEM direction", k, "adjoint", ad, "fd", fd)
+        assert abs(ad - fd) <= RTOL * abs(fd), f"DEM direction {k}: adjoint {ad} fd {fd}"
+
+
 def test_adjoint_rejects_unsupported_fluid(lib):
     # damBreak's own options (Monaghan viscosity, anticlumping, h following
     # density) are outside the fluid adjoint
