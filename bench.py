@@ -196,12 +196,13 @@ def cpu_baseline(steps=2, warm=1, procs=1):
 
 
 # --------------------------------------------------------------------------
-def _time_adjoint(lib, capi, cases, case, nsteps, ckpt, seed_fn):
+def _time_adjoint(lib, capi, cases, case, nsteps, ckpt, seed_fn, precisions=("fp64", "mixed")):
     """(plain forward, adjoint forward, adjoint backward) wall times of the
-    same nsteps from the same state, FP64 and mixed (each call returns after
-    the device finished)."""
+    same nsteps from the same state, FP64 and / or mixed (each call returns
+    after the device finished)."""
     out = {}
-    for name, prec in (("fp64", cases.PREC_FP64), ("mixed", cases.PREC_MIXED)):
+    for name in precisions:
+        prec = cases.PREC_FP64 if name == "fp64" else cases.PREC_MIXED
         sim = capi.Simulation(lib, case.cfg, case.particles, precision=prec)
         sim.step(2)
         t0 = time.perf_counter()
@@ -224,9 +225,11 @@ def _time_adjoint(lib, capi, cases, case, nsteps, ckpt, seed_fn):
 
 def measure_adjoint(lib, capi, cases, nsteps=100, ckpt=10):
     """Wall time of sphdem_adjoint_forward + sphdem_adjoint_backward over the
-    wall time of the same steps stepped plainly, FP64 and mixed, for the two
-    step families the adjoint covers: DEM-only settling (4,913 spheres) and
-    the 2D dam break at its full size (dx = 0.01, artificial viscosity)."""
+    wall time of the same steps stepped plainly, for the three step families
+    the adjoint covers: DEM-only settling (4,913 spheres), the 2D dam break
+    at its full size (dx = 0.01, artificial viscosity), both FP64 and mixed,
+    and the coupled SPH-DEM workload of 100k fluid + 5k DEM particles
+    (mixed)."""
     out = {}
     dem = cases.dem_settling3d(lattice=(17, 17, 17), box=(0.067, 0.067, 0.067), spread=0.0,
                                nsteps=nsteps, vel_amp=0.3)
@@ -253,7 +256,23 @@ def measure_adjoint(lib, capi, cases, nsteps=100, ckpt=10):
     out["fluid"] = _time_adjoint(lib, capi, cases, fluid, nsteps, ckpt, fluid_seed)
     out["fluid"]["workload"] = (f"2D dam break, {fluid.n} particles (artificial viscosity), "
                                 f"{nsteps} steps, checkpoint every {ckpt}")
-    out["ratio"] = max(out["dem"]["mixed"]["ratio"], out["fluid"]["mixed"]["ratio"])
+    # the differentiated coupled workload: 100k fluid + 5k DEM (periodic x/y,
+    # fixed boundary floor, porosity, two-way drag, contacts), mixed precision
+    cpl = cases.workload("sediment3d_adjoint")
+    cpl_steps, cpl_ckpt = 100, 50
+
+    def cpl_seed(sim):
+        a = sim.get(capi.FIELD_IAM)
+        seed = np.zeros((sim.n, 3))
+        m = a["iam"] == cases.DEM
+        seed[m, 2] = 1.0 / max(1, m.sum())
+        return {"dL_dr": seed}
+
+    out["coupled"] = _time_adjoint(lib, capi, cases, cpl, cpl_steps, cpl_ckpt, cpl_seed, precisions=("mixed",))
+    out["coupled"]["workload"] = (f"coupled SPH-DEM, {cpl.n} particles ({cpl.notes['n_fluid']} fluid, "
+                                  f"{cpl.notes['n_dem']} DEM), {cpl_steps} steps, checkpoint every {cpl_ckpt}")
+    out["ratio"] = max(out["dem"]["mixed"]["ratio"], out["fluid"]["mixed"]["ratio"],
+                       out["coupled"]["mixed"]["ratio"])
     return out
 
 

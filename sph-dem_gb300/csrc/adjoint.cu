@@ -575,48 +575,6 @@ __global__ void k_sadj_mid(DevCfg c, int64_t n, double dt, const double *aux, co
  * 1/h), E1 = (r1 lo, m), E2 = (vh1, adjoint of dddt1 + hd adjoint of rho1). */
 enum { R_M0 = 0, R_M1, R_M2, R_M3, R_E0, R_E1, R_E2 };
 
-struct Kf {
-    float s = 0.f, c = 0.f;
-    __device__ __forceinline__ void add(float x) {
-        const float y = x - c;
-        const float t = s + y;
-        c = (t - s) - y;
-        s = t;
-    }
-    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
-};
-
-__device__ __forceinline__ void split2(double x, float &hi, float &lo) {
-    hi = (float)x;
-    lo = (float)(x - (double)hi);
-}
-
-template <int ND>
-__device__ __forceinline__ float ipow_nd2(float ih) {   /* ih^(ND+2) */
-    float v = ih * ih;
-#pragma unroll
-    for (int d = 0; d < ND; d++) v *= ih;
-    return v;
-}
-
-/* G and dG/dr in FP32 (grad_factor) from 1/h of both particles */
-template <int ND>
-__device__ __forceinline__ void grad_factor32(float wcon, float r, float iha, float ihb, float &G, float &Gp) {
-    G = 0.f;
-    Gp = 0.f;
-    const float ih[2] = {iha, ihb};
-#pragma unroll
-    for (int k = 0; k < 2; k++) {
-        const float q = r * ih[k];
-        if (q > 2.f) continue;
-        const float t = 2.f - q, f = wcon * ipow_nd2<ND>(ih[k]);
-        G += -10.f * f * (t * t * t);
-        Gp += 30.f * f * (t * t) * ih[k];
-    }
-    G *= 0.5f;
-    Gp *= 0.5f;
-}
-
 template <int ND>
 __device__ __forceinline__ void force_pair_vjp32(float alpha, float c0, const float *d, const float *w, float r,
                                                  float G, float Gp, const float *Fb, float my, float rhox, float rhoy,

@@ -26,6 +26,8 @@ constexpr int ADJ_NGRAD = 5;       /* d/dk, d/dgamma, d/dalpha, d/dnu, d/d(drag 
 constexpr int CP_NACC = 24;        /* coupled step: accumulators per particle */
 constexpr int CP_NEND = 15;        /* coupled step: end-phase results per particle */
 constexpr int CP_NMID = 8;         /* coupled step: middle intermediates per particle */
+constexpr int CP_NREC32 = 8;       /* coupled step, mixed: float4 records per particle */
+constexpr int CP_FPI_PER = 384;    /* FPI partners per DEM particle per step (3D fluid at rest: ~122) */
 
 /* a grouped pair table of every step of a segment: entries partner tag |
  * shift << 26 grouped by particle, (offset, count) per tag and step, entries
@@ -75,6 +77,10 @@ struct AdjointData {
     double *cacc = nullptr;         /* CP_NACC accumulators per particle */
     double *cend = nullptr;         /* CP_NEND end-phase results per particle */
     double *cmid = nullptr;         /* CP_NMID middle intermediates per particle */
+    float4 *crec = nullptr;         /* mixed: CP_NREC32 FP32 records per particle */
+    float4 *dpos = nullptr;         /* middle-phase DEM positions by state index (FP32) */
+    int n_dem = 0;                  /* DEM particles at the forward pass */
+    int *dem_tags = nullptr;        /* their tags */
 };
 
 /* G = (F(r, h_a) + F(r, h_b)) / 2 and dG/dr, F(r, h) = -10 C (2-q)^3 / h^(d+2)
@@ -112,6 +118,50 @@ __device__ __forceinline__ int table_entry(int e, int *sh) {
 
 __device__ __forceinline__ int shift_code(const int *sh) {
     return ((sh[0] + 1) | ((sh[1] + 1) << 2) | ((sh[2] + 1) << 4)) << SH_SHIFT;
+}
+
+/* FP32 pair math of the mixed-precision reverse passes: Kahan sums, double-float
+ * positions, and the gradient factor G, dG/dr */
+struct Kf {
+    float s = 0.f, c = 0.f;
+    __device__ __forceinline__ void add(float x) {
+        const float y = x - c;
+        const float t = s + y;
+        c = (t - s) - y;
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+__device__ __forceinline__ void split2(double x, float &hi, float &lo) {
+    hi = (float)x;
+    lo = (float)(x - (double)hi);
+}
+
+template <int ND>
+__device__ __forceinline__ float ipow_nd2(float ih) {   /* ih^(ND+2) */
+    float v = ih * ih;
+#pragma unroll
+    for (int d = 0; d < ND; d++) v *= ih;
+    return v;
+}
+
+/* G and dG/dr in FP32 (grad_factor) from 1/h of both particles */
+template <int ND>
+__device__ __forceinline__ void grad_factor32(float wcon, float r, float iha, float ihb, float &G, float &Gp) {
+    G = 0.f;
+    Gp = 0.f;
+    const float ih[2] = {iha, ihb};
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+        const float q = r * ih[k];
+        if (q > 2.f) continue;
+        const float t = 2.f - q, f = wcon * ipow_nd2<ND>(ih[k]);
+        G += -10.f * f * (t * t * t);
+        Gp += 30.f * f * (t * t) * ih[k];
+    }
+    G *= 0.5f;
+    Gp *= 0.5f;
 }
 
 /* adjoint_cpl.cu: the coupled step */

@@ -35,6 +35,11 @@
  * particle kind into the other (fluid <-> DEM) are FP64 atomics; sums within
  * the fluid gather over the symmetric pair table.
  *
+ * Mixed-precision handles run the two fluid pair passes (continuity and
+ * forces, ~100 pairs per particle in 3D) in FP32 on double-float position
+ * records with Kahan sums; the coupling passes (a few DEM partners per
+ * fluid particle) stay FP64.
+ *
  * Positions of the middle phase are snapshotted after it in the replay (a
  * periodic wrap in the middle rebuild would otherwise separate the
  * recomputed r_s from the frame the pair tables were built in).
@@ -106,67 +111,6 @@ __device__ __forceinline__ int64_t reserve(int k, int *cnt) {
 
 /* ---- taps: pair tables of the current buckets ------------------------ */
 
-/* fluid particle a -> DEM within Rc under the coupling search of
- * calcNeighboursCoupling (dataLL.cpp:1104-1192), as the middle phase uses it.
- * The tap runs after the whole middle phase, whose tail has drifted the DEM
- * particles by hd vhat0 since the coupling passes saw them: DEM positions
- * are taken back by that drift (same rebuild, same periodic frame). */
-template <bool WRITE>
-__device__ int cpl_scan(const DevCfg &c, const DevState &s, const int *start, int dem_base, double hd, int64_t a,
-                        int *out, int64_t room) {
-    double ra[3] = {0, 0, 0};
-    for (int d = 0; d < c.nd; d++) ra[d] = s.row(FD_R + d)[a];
-    int cs[3] = {0, 0, 0};
-    for (int d = 0; d < c.nd; d++) cs[d] = ref_dem_cell(ra[d], c, d);
-    const CellCoord cc = dem_cell_of(c, ra);
-    int k = 0;
-    scan_cells(cc, c.ddims, c.periodic, c.nd, start, dem_base, [&](int b, const int *sh) {
-        if (s.irow(FI_IAM)[b] != T_DEM) return;
-        const bool shifted = (sh[0] | sh[1] | sh[2]) != 0;
-        int cd[3] = {0, 0, 0};
-        double rb[3] = {0, 0, 0};
-        for (int d = 0; d < c.nd; d++) {
-            rb[d] = image_pos(s.row(FD_R + d)[b] - hd * s.row(FD_VHAT0 + d)[b], sh[d], c.rmin[d], c.rmax[d]);
-            cd[d] = shifted ? ref_dem_cell(rb[d], c, d) : s.irow(FI_RDC0 + d)[b];
-        }
-        if (!coupling_rule(cs, cd, c)) return;
-        double dx[3] = {0, 0, 0};
-        for (int d = 0; d < c.nd; d++) dx[d] = dsub(ra[d], rb[d]);
-        if (!(exact_len2(dx, c.nd) < c.rc2)) return;
-        if (shifted && !image_exists(s.irow(FI_GCODE)[b], sh, c.nd)) return;
-        if (WRITE && k < room) out[k] = s.irow(FI_TAG)[b] | shift_code(sh);
-        k++;
-    });
-    return k;
-}
-
-/* DEM particle i -> fluid within 2 max(h_i, h_b) over the SPH buckets, as
- * calcFPI visits them (no repulsive boundary particles) */
-template <bool WRITE>
-__device__ int fpi_scan(const DevCfg &c, const DevState &s, const int *start, const DevGlobals *g, int64_t a,
-                        int *out, int64_t room) {
-    double ra[3] = {0, 0, 0};
-    for (int d = 0; d < c.nd; d++) ra[d] = s.row(FD_R + d)[a];
-    const double ha = s.row(FD_H)[a];
-    const GridInfo gi = load_grid(g);
-    const CellCoord cs = sph_cell_of(c, gi, ra);
-    int k = 0;
-    scan_cells(cs, gi.sdims, c.periodic, c.nd, start, 0, [&](int b, const int *sh) {
-        double dx[3] = {0, 0, 0};
-        for (int d = 0; d < c.nd; d++)
-            dx[d] = dsub(ra[d], image_pos(s.row(FD_R + d)[b], sh[d], c.rmin[d], c.rmax[d]));
-        const double r2 = exact_len2(dx, c.nd);
-        const double hb = s.row(FD_H)[b];
-        const double t = 2.0 * (ha > hb ? ha : hb);
-        if (r2 > dmul(t, t)) return;
-        if ((sh[0] | sh[1] | sh[2]) && !image_exists(s.irow(FI_GCODE)[b], sh, c.nd)) return;
-        if (s.irow(FI_IAM)[b] == T_BOUNDARY) return;
-        if (WRITE && k < room) out[k] = s.irow(FI_TAG)[b] | shift_code(sh);
-        k++;
-    });
-    return k;
-}
-
 /* DEM particle i -> DEM in contact (neighbour predicate and positive
  * overlap), as calcDEMContacts visits them (sph.h:1676-1706) */
 template <bool WRITE>
@@ -198,30 +142,153 @@ __device__ int contact_scan(const DevCfg &c, const DevState &s, const int *start
     return k;
 }
 
-/* which = 0: coupling (fluid rows), 1: FPI (DEM rows), 2: contacts (DEM rows).
- * Writes slot *slot of the table (offset / count per tag); nb == nullptr
- * counts only. */
-__global__ void k_cp_table(DevCfg c, DevState s, const int *start, const DevGlobals *g, int64_t n, int which,
-                           int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot) {
-    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    const int t = a < n ? s.irow(FI_IAM)[a] : -1;
-    const bool live = a < n && (which == 0 ? is_fluid(t) : t == T_DEM);
-    const int j = slot ? *slot : 0;
-    int k = 0;
-    if (live) {
-        if (which == 0) k = cpl_scan<false>(c, s, start, g->n_sph_cells, 0.5 * g->dt, a, nullptr, 0);
-        else if (which == 1) k = fpi_scan<false>(c, s, start, g, a, nullptr, 0);
-        else k = contact_scan<false>(c, s, start, g, a, nullptr, 0);
+/* FP32 middle-phase positions of the DEM particles by state index (the tap
+ * runs after the middle phase's tail drifted them by hd vhat0) */
+__global__ void k_cp_dpos(DevState s, const DevGlobals *g, int64_t n, float4 *dpos) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n || s.irow(FI_IAM)[k] != T_DEM) return;
+    const double hd = 0.5 * g->dt;
+    float p[3];
+    for (int d = 0; d < 3; d++) p[d] = (float)(s.row(FD_R + d)[k] - hd * s.row(FD_VHAT0 + d)[k]);
+    dpos[k] = make_float4(p[0], p[1], p[2], 0.f);
+}
+
+/* fluid -> DEM coupling table: the bucket rule of calcNeighboursCoupling
+ * (dataLL.cpp:1104-1192, asymmetric: it leaves out some pairs within Rc) as
+ * the middle phase applies it, with the distance cut r < Rc as an FP32 test
+ * with a relative margin of 1e-4 on Rc^2 -- a superset of the coupled pairs,
+ * and pairs at or beyond Rc carry W_c = dW_c/dr = 0.  DEM positions are those
+ * of the middle phase (dpos; the rule's own DEM buckets were set at its
+ * rebuild). */
+/* reference DEM bucket of the periodic image of DEM particle b (out of line:
+ * only pairs across a periodic face take it) */
+__device__ __noinline__ void image_dem_cells(const DevCfg &c, const DevState &s, int b, const int *sh, double hd,
+                                             int *cd) {
+    for (int d = 0; d < c.nd; d++)
+        cd[d] = ref_dem_cell(image_pos(s.row(FD_R + d)[b] - hd * s.row(FD_VHAT0 + d)[b], sh[d], c.rmin[d], c.rmax[d]),
+                             c, d);
+}
+
+/* one out-of-line copy for the count pass (out == nullptr) and the write
+ * pass, so that the loop stays in the instruction cache */
+__device__ __noinline__ int cpl_scan32(const DevCfg &c, const DevState &s, const int *start, int dem_base,
+                                       const float4 *dpos, double hd, int64_t a, int *out, int64_t room) {
+    double rad[3] = {0, 0, 0};
+    float ra[3] = {0.f, 0.f, 0.f};
+    for (int d = 0; d < c.nd; d++) {
+        rad[d] = s.row(FD_R + d)[a];
+        ra[d] = (float)rad[d];
     }
+    int cs[3] = {0, 0, 0};
+    for (int d = 0; d < c.nd; d++) cs[d] = ref_dem_cell(rad[d], c, d);
+    const float lim = (float)(c.rc2 * (1.0 + 1e-4));
+    float L[3] = {0.f, 0.f, 0.f};
+    for (int d = 0; d < c.nd; d++) L[d] = (float)(c.rmax[d] - c.rmin[d]);
+    const CellCoord cc = dem_cell_of(c, rad);
+    int k = 0;
+    scan_cells(cc, c.ddims, c.periodic, c.nd, start, dem_base, [&](int b, const int *sh) {
+        if (s.irow(FI_IAM)[b] != T_DEM) return;
+        const bool shifted = (sh[0] | sh[1] | sh[2]) != 0;
+        int cd[3] = {0, 0, 0};
+        if (shifted)
+            image_dem_cells(c, s, b, sh, hd, cd);
+        else
+            for (int d = 0; d < c.nd; d++) cd[d] = s.irow(FI_RDC0 + d)[b];
+        if (!coupling_rule(cs, cd, c)) return;
+        const float4 p = dpos[b];
+        const float pb[3] = {p.x, p.y, p.z};
+        float r2 = 0.f;
+        for (int d = 0; d < c.nd; d++) {
+            const float dx = ra[d] - (pb[d] + (float)sh[d] * L[d]);
+            r2 = fmaf(dx, dx, r2);
+        }
+        if (!(r2 < lim)) return;
+        if ((sh[0] | sh[1] | sh[2]) && !image_exists(s.irow(FI_GCODE)[b], sh, c.nd)) return;
+        if (out && k < room) out[k] = s.irow(FI_TAG)[b] | shift_code(sh);
+        k++;
+    });
+    return k;
+}
+
+__global__ void k_cp_cpl_table(DevCfg c, DevState s, const int *start, const DevGlobals *g, int64_t n,
+                               const float4 *dpos, int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const bool live = a < n && is_fluid(s.irow(FI_IAM)[a]);
+    const int j = slot ? *slot : 0;
+    const int k = live ? cpl_scan32(c, s, start, g->n_sph_cells, dpos, 0.5 * g->dt, a, nullptr, 0) : 0;
     const int64_t off = reserve(k, cnt + j);
     if (!nb || !live) return;
     const int64_t room = cap - off;
-    int *out = nb + (int64_t)j * cap + off;
-    const int64_t rm = room > 0 ? room : 0;
-    if (which == 0) cpl_scan<true>(c, s, start, g->n_sph_cells, 0.5 * g->dt, a, out, rm);
-    else if (which == 1) fpi_scan<true>(c, s, start, g, a, out, rm);
-    else contact_scan<true>(c, s, start, g, a, out, rm);
+    cpl_scan32(c, s, start, g->n_sph_cells, dpos, 0.5 * g->dt, a, nb + (int64_t)j * cap + off,
+                      room > 0 ? room : 0);
     oc[(int64_t)j * n + s.irow(FI_TAG)[a]] = make_int2((int)off, room >= k ? k : 0);
+}
+
+/* FPI table, one warp per DEM particle (DEM particles follow the SPH buckets
+ * in the sorted order): the lanes split the 3^d SPH-bucket stencil, the
+ * exact FP64 predicate of calcFPI decides, a ballot compacts.  Each DEM
+ * particle owns `per` slots of the step's table (offset w * per); more
+ * partners than that mark the step overflowed (cnt > cap). */
+__global__ void k_cp_fpi_table(DevCfg c, DevState s, const int *start, const DevGlobals *g, int64_t n, int n_dem,
+                               int per, int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot) {
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n_dem) return;
+    const int64_t i = start[g->n_sph_cells] + w;
+    if (i >= n || s.irow(FI_IAM)[i] != T_DEM) return;
+    const int j = *slot;
+    double ra[3] = {0, 0, 0};
+    for (int d = 0; d < c.nd; d++) ra[d] = s.row(FD_R + d)[i];
+    const double ha = s.row(FD_H)[i];
+    const GridInfo gi = load_grid(g);
+    const CellCoord cs = sph_cell_of(c, gi, ra);
+    int *out = nb + (int64_t)j * cap + (int64_t)w * per;
+    int k = 0;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int ox = -1; ox <= 1; ox++)
+        for (int oy = (c.nd > 1 ? -1 : 0); oy <= (c.nd > 1 ? 1 : 0); oy++)
+            for (int oz = (c.nd > 2 ? -1 : 0); oz <= (c.nd > 2 ? 1 : 0); oz++) {
+                int sh[3];
+                const int lin = neighbour_cell(cs, ox, oy, oz, gi.sdims, c.periodic, c.nd, sh);
+                if (lin < 0) continue;
+                const int b1 = start[lin + 1];
+                for (int b0 = start[lin]; b0 < b1; b0 += 32) {
+                    const int b = b0 + lane;
+                    bool ok = b < b1;
+                    if (ok) {
+                        double dx[3] = {0, 0, 0};
+                        for (int d = 0; d < c.nd; d++)
+                            dx[d] = dsub(ra[d], image_pos(s.row(FD_R + d)[b], sh[d], c.rmin[d], c.rmax[d]));
+                        const double r2 = exact_len2(dx, c.nd);
+                        const double hb = s.row(FD_H)[b];
+                        const double t = 2.0 * (ha > hb ? ha : hb);
+                        ok = r2 <= dmul(t, t) && s.irow(FI_IAM)[b] != T_BOUNDARY &&
+                             (!(sh[0] | sh[1] | sh[2]) || image_exists(s.irow(FI_GCODE)[b], sh, c.nd));
+                    }
+                    const unsigned m = __ballot_sync(0xffffffffu, ok);
+                    const int pos = k + __popc(m & lt);
+                    if (ok && pos < per) out[pos] = s.irow(FI_TAG)[b] | shift_code(sh);
+                    k += __popc(m);
+                }
+            }
+    if (lane == 0) {
+        oc[(int64_t)j * n + s.irow(FI_TAG)[i]] = make_int2(w * per, k <= per ? k : 0);
+        if (k > per) atomicMax(cnt + j, (int)cap + 1);   /* marks the step overflowed */
+    }
+}
+
+/* contact table, one thread per DEM particle, `per` slots each */
+__global__ void k_cp_ct_table(DevCfg c, DevState s, const int *start, const DevGlobals *g, int64_t n, int n_dem,
+                              int per, int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot) {
+    const int w = (int)(blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+    if (w >= n_dem) return;
+    const int64_t i = start[g->n_sph_cells] + w;
+    if (i >= n || s.irow(FI_IAM)[i] != T_DEM) return;
+    const int j = *slot;
+    int *out = nb + (int64_t)j * cap + (int64_t)w * per;
+    const int k = contact_scan<true>(c, s, start, g, i, out, per);
+    oc[(int64_t)j * n + s.irow(FI_TAG)[i]] = make_int2(w * per, k <= per ? k : 0);
+    if (k > per) atomicMax(cnt + j, (int)cap + 1);
 }
 
 /* positions after the middle phase, tag order, at slot *slot */
@@ -302,7 +369,7 @@ __global__ void k_cp_por(DevCfg c, int64_t n, const double *aux, const double *m
 
 /* Di Felice drag Phi(dv, por) = 1/2 A C_d |dv| por^-chi dv (sph.h:1593-1598)
  * and its VJP against Pb: adds to dvb, porb, and returns the adjoint of nu */
-__device__ __forceinline__ void difelice(const DevCfg &c, const double *dv, double por, double *phi) {
+__device__ __noinline__ void difelice(const DevCfg &c, const double *dv, double por, double *phi) {
     double vd2 = 0.0;
     for (int q = 0; q < c.nd; q++) vd2 += dv[q] * dv[q];
     const double vd = sqrt(vd2);
@@ -317,7 +384,7 @@ __device__ __forceinline__ void difelice(const DevCfg &c, const double *dv, doub
     for (int q = 0; q < c.nd; q++) phi[q] = g * dv[q];
 }
 
-__device__ __forceinline__ double difelice_vjp(const DevCfg &c, const double *dv, double por, const double *Pb,
+__device__ __noinline__ double difelice_vjp(const DevCfg &c, const double *dv, double por, const double *Pb,
                                                double *dvb, double &porb) {
     double vd2 = 0.0, Pd = 0.0;
     for (int q = 0; q < c.nd; q++) {
@@ -344,130 +411,138 @@ __device__ __forceinline__ double difelice_vjp(const DevCfg &c, const double *dv
     return Pd * dgPsi_dRe * (-Re / c.viscosity);
 }
 
-/* FPI + Di Felice drag of each DEM particle (end phase): forward sums over
- * its fluid neighbours, then the VJP of Delta_i against the adjoint of f1 +
- * fdrag1; scatters into the fluid neighbours' accumulators */
-__global__ void k_cp_fpi(DevCfg c, int64_t n, double dt, const double *s1, const double *aux, const double *cmid,
-                         const double *mass, const double *hh, const int *typ, const int *nb, const int2 *oc,
+/* FPI + Di Felice drag of each DEM particle (end phase), one warp per DEM
+ * particle: the lanes split its fluid partners for the forward sums (warp
+ * reductions), every lane then runs the drag VJP on the reduced values, and
+ * the lanes split the partners again to scatter the adjoints into the fluid
+ * accumulators (FP64 atomics).  Delta_i's adjoint is that of f1 + fdrag1. */
+__global__ void k_cp_fpi(DevCfg c, int n_dem, const int *dem_tags, double dt, const double *s1, const double *aux,
+                         const double *cmid, const double *mass, const double *hh, const int *nb, const int2 *oc,
                          const double *adj, double *cacc, double *grads) {
-    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    double gnu = 0.0, gkap = 0.0;
-    if (i < n && typ[i] == T_DEM) {
-        const double *xi = s1 + i * ADJ_NC, *ai = adj + i * ADJ_NC;
-        const double *vhm = aux + i * ADJ_AUX + 3;
-        const int2 o = oc[i];
-        double sum = 0.0, Npor = 0.0, Nfp[3] = {0, 0, 0}, Nfv[3] = {0, 0, 0}, Nvel[3] = {0, 0, 0};
-        for (int k = 0; k < o.y; k++) {
-            int sh[3];
-            const int b = table_entry(nb[o.x + k], sh);
-            const double *xb = s1 + (int64_t)b * ADJ_NC;
-            double d[3], r;
-            image_d(c, xi, xb, sh, d, r);
-            const double hb = hh[b], q = r / hb;
-            if (q > 2.0) continue;
-            double ihn = 1.0;
-            for (int dd = 0; dd < c.nd; dd++) ihn /= hb;
-            const double t = 2.0 - q, t2 = t * t;
-            const double W = ihn * c.wcon * (t2 * t2) * (1.0 + 2.0 * q);
-            const double mb = mass[b], dvol = mb / aux[(int64_t)b * ADJ_AUX + 6];
-            sum += dvol * W;
-            Npor += dvol * W * cmid[(int64_t)b * CP_NMID + CM_EPS];
-            for (int q3 = 0; q3 < c.nd; q3++) {
-                Nfp[q3] += mb * W * xb[AS_FP + q3];
-                Nfv[q3] += (mb * W + dvol * W) * xb[AS_FV + q3];
-                Nvel[q3] += dvol * W * xb[AS_VH + q3];
-            }
-        }
-        if (sum > 0.5) {
-            const double mi = mass[i], rs = 1.0 / sum;
-            const double por = Npor * rs;
-            double fvel[3] = {0, 0, 0}, fpfb[3] = {0, 0, 0}, fvv[3] = {0, 0, 0}, dv[3] = {0, 0, 0};
-            for (int q = 0; q < c.nd; q++) {
-                fvel[q] = Nvel[q] * rs;
-                fpfb[q] = Nfp[q] * rs;
-                fvv[q] = Nfv[q] * rs;
-                dv[q] = por * (fvel[q] - vhm[q]);
-            }
-            double Db[3] = {0, 0, 0};
-            for (int q = 0; q < c.nd; q++) Db[q] = ai[AS_F + q] + dt * (ai[AS_V + q] + ai[AS_VH + q]) + ai[AS_FDRAG + q];
-            /* Delta = (V/m)(fv + fpfb) + (rho0/m) kappa Phi */
-            double phi[3];
-            difelice(c, dv, por, phi);
-            double Pb[3] = {0, 0, 0}, dvb[3] = {0, 0, 0}, porb = 0.0;
-            for (int q = 0; q < c.nd; q++) {
-                Pb[q] = (c.dens / mi) * c.drag_scale * Db[q];
-                gkap += (c.dens / mi) * Db[q] * phi[q];
-            }
-            gnu += difelice_vjp(c, dv, por, Pb, dvb, porb);
-            double fvelb[3] = {0, 0, 0}, ownvh[3] = {0, 0, 0};
-            for (int q = 0; q < c.nd; q++) {
-                fvelb[q] = por * dvb[q];
-                ownvh[q] = -por * dvb[q];
-                porb += (fvel[q] - vhm[q]) * dvb[q];
-            }
-            const double vm = c.dem_vol / mi;
-            double sumb = -porb * por;
-            double NfpB[3] = {0, 0, 0}, NfvB[3] = {0, 0, 0}, NvelB[3] = {0, 0, 0};
-            for (int q = 0; q < c.nd; q++) {
-                sumb -= vm * Db[q] * fpfb[q] + vm * Db[q] * fvv[q] + fvelb[q] * fvel[q];
-                NfpB[q] = vm * Db[q] * rs;
-                NfvB[q] = vm * Db[q] * rs;
-                NvelB[q] = fvelb[q] * rs;
-            }
-            sumb *= rs;
-            const double NporB = porb * rs;
-            double own_r[3] = {0, 0, 0};
-            for (int k = 0; k < o.y; k++) {
-                int sh[3];
-                const int b = table_entry(nb[o.x + k], sh);
-                const double *xb = s1 + (int64_t)b * ADJ_NC;
-                double d[3], r;
-                image_d(c, xi, xb, sh, d, r);
-                const double hb = hh[b], q = r / hb;
-                if (q > 2.0) continue;
-                double ihn = 1.0;
-                for (int dd = 0; dd < c.nd; dd++) ihn /= hb;
-                const double t = 2.0 - q, t2 = t * t;
-                const double W = ihn * c.wcon * (t2 * t2) * (1.0 + 2.0 * q);
-                const double Wp = ihn * c.wcon * (-10.0 * q * t2 * t) / hb;
-                const double mb = mass[b], rhob = aux[(int64_t)b * ADJ_AUX + 6], dvol = mb / rhob;
-                const double epsb = cmid[(int64_t)b * CP_NMID + CM_EPS];
-                double vfp = 0.0, vfv = 0.0, vvel = 0.0;
-                for (int q3 = 0; q3 < c.nd; q3++) {
-                    vfp += NfpB[q3] * xb[AS_FP + q3];
-                    vfv += NfvB[q3] * xb[AS_FV + q3];
-                    vvel += NvelB[q3] * xb[AS_VH + q3];
-                }
-                const double Wb = dvol * (sumb + NporB * epsb + vvel) + mb * vfp + (mb + dvol) * vfv;
-                const double dvolb = W * (sumb + NporB * epsb + vvel + vfv);
-                double *acc = cacc + (int64_t)b * CP_NACC;
-                atomicAdd(&acc[CA_RHO], -dvolb * dvol / rhob);
-                atomicAdd(&acc[CA_EPS], dvol * W * NporB);
-                if (r > 0.0) {
-                    for (int q3 = 0; q3 < c.nd; q3++) {
-                        const double gq = Wb * Wp * d[q3] / r;
-                        own_r[q3] += gq;
-                        atomicAdd(&acc[CA_R1 + q3], -gq);
-                    }
-                }
-                for (int q3 = 0; q3 < c.nd; q3++) {
-                    atomicAdd(&acc[CA_FP + q3], mb * W * NfpB[q3]);
-                    atomicAdd(&acc[CA_FV + q3], (mb + dvol) * W * NfvB[q3]);
-                    atomicAdd(&acc[CA_VH1 + q3], dvol * W * NvelB[q3]);
-                }
-            }
-            double *acc = cacc + i * CP_NACC;
-            for (int q = 0; q < c.nd; q++) {
-                acc[CA_R1 + q] += own_r[q];
-                acc[CA_VH1 + q] += ownvh[q];
-            }
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n_dem) return;
+    const int64_t i = dem_tags[w];
+    const double *xi = s1 + i * ADJ_NC, *ai = adj + i * ADJ_NC;
+    const double *vhm = aux + i * ADJ_AUX + 3;
+    const int2 o = oc[i];
+    double sum = 0.0, Npor = 0.0, Nfp[3] = {0, 0, 0}, Nfv[3] = {0, 0, 0}, Nvel[3] = {0, 0, 0};
+    for (int k = lane; k < o.y; k += 32) {
+        int sh[3];
+        const int b = table_entry(nb[o.x + k], sh);
+        const double *xb = s1 + (int64_t)b * ADJ_NC;
+        double d[3], r;
+        image_d(c, xi, xb, sh, d, r);
+        const double hb = hh[b], q = r / hb;
+        if (q > 2.0) continue;
+        double ihn = 1.0;
+        for (int dd = 0; dd < c.nd; dd++) ihn /= hb;
+        const double t = 2.0 - q, t2 = t * t;
+        const double W = ihn * c.wcon * (t2 * t2) * (1.0 + 2.0 * q);
+        const double mb = mass[b], dvol = mb / aux[(int64_t)b * ADJ_AUX + 6];
+        sum += dvol * W;
+        Npor += dvol * W * cmid[(int64_t)b * CP_NMID + CM_EPS];
+        for (int q3 = 0; q3 < c.nd; q3++) {
+            Nfp[q3] += mb * W * xb[AS_FP + q3];
+            Nfv[q3] += (mb * W + dvol * W) * xb[AS_FV + q3];
+            Nvel[q3] += dvol * W * xb[AS_VH + q3];
         }
     }
-    gnu = warp_sum_d(gnu);
-    gkap = warp_sum_d(gkap);
-    if ((threadIdx.x & 31) == 0 && (gnu != 0.0 || gkap != 0.0)) {
-        atomicAdd(&grads[3], gnu);
-        atomicAdd(&grads[4], gkap);
+    sum = warp_sum_d(sum);
+    Npor = warp_sum_d(Npor);
+    for (int q = 0; q < 3; q++) {
+        Nfp[q] = warp_sum_d(Nfp[q]);
+        Nfv[q] = warp_sum_d(Nfv[q]);
+        Nvel[q] = warp_sum_d(Nvel[q]);
+    }
+    if (!(sum > 0.5)) return;       /* no drag, Delta = 0 (uniform over the warp) */
+    const double mi = mass[i], rs = 1.0 / sum;
+    const double por = Npor * rs;
+    double fvel[3] = {0, 0, 0}, fpfb[3] = {0, 0, 0}, fvv[3] = {0, 0, 0}, dv[3] = {0, 0, 0}, Db[3] = {0, 0, 0};
+    for (int q = 0; q < c.nd; q++) {
+        fvel[q] = Nvel[q] * rs;
+        fpfb[q] = Nfp[q] * rs;
+        fvv[q] = Nfv[q] * rs;
+        dv[q] = por * (fvel[q] - vhm[q]);
+        Db[q] = ai[AS_F + q] + dt * (ai[AS_V + q] + ai[AS_VH + q]) + ai[AS_FDRAG + q];
+    }
+    /* Delta = (V/m)(fv + fpfb) + (rho0/m) kappa Phi */
+    double phi[3];
+    difelice(c, dv, por, phi);
+    double Pb[3] = {0, 0, 0}, dvb[3] = {0, 0, 0}, porb = 0.0, gkap = 0.0;
+    for (int q = 0; q < c.nd; q++) {
+        Pb[q] = (c.dens / mi) * c.drag_scale * Db[q];
+        gkap += (c.dens / mi) * Db[q] * phi[q];
+    }
+    const double gnu = difelice_vjp(c, dv, por, Pb, dvb, porb);
+    double fvelb[3] = {0, 0, 0}, ownvh[3] = {0, 0, 0};
+    for (int q = 0; q < c.nd; q++) {
+        fvelb[q] = por * dvb[q];
+        ownvh[q] = -por * dvb[q];
+        porb += (fvel[q] - vhm[q]) * dvb[q];
+    }
+    const double vm = c.dem_vol / mi;
+    double sumb = -porb * por;
+    double NfpB[3] = {0, 0, 0}, NfvB[3] = {0, 0, 0}, NvelB[3] = {0, 0, 0};
+    for (int q = 0; q < c.nd; q++) {
+        sumb -= vm * Db[q] * fpfb[q] + vm * Db[q] * fvv[q] + fvelb[q] * fvel[q];
+        NfpB[q] = vm * Db[q] * rs;
+        NfvB[q] = vm * Db[q] * rs;
+        NvelB[q] = fvelb[q] * rs;
+    }
+    sumb *= rs;
+    const double NporB = porb * rs;
+    double own_r[3] = {0, 0, 0};
+    for (int k = lane; k < o.y; k += 32) {
+        int sh[3];
+        const int b = table_entry(nb[o.x + k], sh);
+        const double *xb = s1 + (int64_t)b * ADJ_NC;
+        double d[3], r;
+        image_d(c, xi, xb, sh, d, r);
+        const double hb = hh[b], q = r / hb;
+        if (q > 2.0) continue;
+        double ihn = 1.0;
+        for (int dd = 0; dd < c.nd; dd++) ihn /= hb;
+        const double t = 2.0 - q, t2 = t * t;
+        const double W = ihn * c.wcon * (t2 * t2) * (1.0 + 2.0 * q);
+        const double Wp = ihn * c.wcon * (-10.0 * q * t2 * t) / hb;
+        const double mb = mass[b], rhob = aux[(int64_t)b * ADJ_AUX + 6], dvol = mb / rhob;
+        const double epsb = cmid[(int64_t)b * CP_NMID + CM_EPS];
+        double vfp = 0.0, vfv = 0.0, vvel = 0.0;
+        for (int q3 = 0; q3 < c.nd; q3++) {
+            vfp += NfpB[q3] * xb[AS_FP + q3];
+            vfv += NfvB[q3] * xb[AS_FV + q3];
+            vvel += NvelB[q3] * xb[AS_VH + q3];
+        }
+        const double Wb = dvol * (sumb + NporB * epsb + vvel) + mb * vfp + (mb + dvol) * vfv;
+        const double dvolb = W * (sumb + NporB * epsb + vvel + vfv);
+        double *acc = cacc + (int64_t)b * CP_NACC;
+        atomicAdd(&acc[CA_RHO], -dvolb * dvol / rhob);
+        atomicAdd(&acc[CA_EPS], dvol * W * NporB);
+        if (r > 0.0) {
+            for (int q3 = 0; q3 < c.nd; q3++) {
+                const double gq = Wb * Wp * d[q3] / r;
+                own_r[q3] += gq;
+                atomicAdd(&acc[CA_R1 + q3], -gq);
+            }
+        }
+        for (int q3 = 0; q3 < c.nd; q3++) {
+            atomicAdd(&acc[CA_FP + q3], mb * W * NfpB[q3]);
+            atomicAdd(&acc[CA_FV + q3], (mb + dvol) * W * NfvB[q3]);
+            atomicAdd(&acc[CA_VH1 + q3], dvol * W * NvelB[q3]);
+        }
+    }
+    for (int q = 0; q < 3; q++) own_r[q] = warp_sum_d(own_r[q]);
+    if (lane == 0) {
+        double *acc = cacc + i * CP_NACC;
+        for (int q = 0; q < c.nd; q++) {
+            acc[CA_R1 + q] += own_r[q];
+            acc[CA_VH1 + q] += ownvh[q];
+        }
+        if (gnu != 0.0 || gkap != 0.0) {
+            atomicAdd(&grads[3], gnu);
+            atomicAdd(&grads[4], gkap);
+        }
     }
 }
 
@@ -816,35 +891,235 @@ __global__ void k_cp_assemble(int64_t n, double dt, const int *typ, const double
     }
 }
 
-void table_launch(sphdem_ctx *c, int which, PairTable &t, const int *slot) {
-    k_cp_table<<<grid_for(c->n, CB), CB, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->g, c->n, which, t.nb, t.oc,
-                                                         t.cnt, t.cap, slot);
+/* ---- mixed precision: FP32 pair math of the fluid pair passes ------------
+ * Records per particle (float4, tag order): middle state R_M0 = (r_s hi,
+ * 1/h), R_M1 = (r_s lo, m), R_M2 = (vh_s, rho_s), R_M3 = (adjoint of fp,
+ * pdr2), R_M4 = (adjoint of fv, h); end state R_E0 = (r1 hi, 1/h), R_E1 =
+ * (r1 lo, m), R_E2 = (vh1, adjoint of dddt1 + hd adjoint of rho1).  Pair
+ * displacements come from the double-float positions; per-particle sums are
+ * Kahan-compensated and land in the FP64 accumulators once. */
+enum { R_M0 = 0, R_M1, R_M2, R_M3, R_M4, R_E0, R_E1, R_E2 };
+
+__global__ void k_cp_pack32(int64_t n, double dt, const double *aux, const double *cmid, const double *s1,
+                            const double *adj, const double *mass, const double *hh, const int *typ, float4 *rec) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n || !is_fluid(typ[i])) return;
+    const double *x = aux + i * ADJ_AUX, *x1 = s1 + i * ADJ_NC, *aa = adj + i * ADJ_NC;
+    const double hd = 0.5 * dt;
+    const float ih = (float)(1.0 / hh[i]), m = (float)mass[i];
+    float hi[3], lo[3];
+    for (int d = 0; d < 3; d++) split2(x[d], hi[d], lo[d]);
+    rec[R_M0 * n + i] = make_float4(hi[0], hi[1], hi[2], ih);
+    rec[R_M1 * n + i] = make_float4(lo[0], lo[1], lo[2], m);
+    rec[R_M2 * n + i] = make_float4((float)x[3], (float)x[4], (float)x[5], (float)x[6]);
+    rec[R_M3 * n + i] = make_float4(0.f, 0.f, 0.f, (float)cmid[i * CP_NMID + CM_PDR2]);
+    rec[R_M4 * n + i] = make_float4(0.f, 0.f, 0.f, (float)hh[i]);
+    for (int d = 0; d < 3; d++) split2(x1[AS_R + d], hi[d], lo[d]);
+    rec[R_E0 * n + i] = make_float4(hi[0], hi[1], hi[2], ih);
+    rec[R_E1 * n + i] = make_float4(lo[0], lo[1], lo[2], m);
+    rec[R_E2 * n + i] = make_float4((float)x1[AS_VH], (float)x1[AS_VH + 1], (float)x1[AS_VH + 2],
+                                    (float)(aa[AS_DDDT] + hd * aa[AS_DENS]));
 }
 
-int64_t count_table(sphdem_ctx *c, int which, int *tmp) {
-    SPHDEM_CUDA_CHECK(cudaMemsetAsync(tmp, 0, sizeof(int), c->stream));
-    k_cp_table<<<grid_for(c->n, CB), CB, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->g, c->n, which, nullptr,
-                                                         nullptr, tmp, 0, nullptr);
-    int v = 0;
-    SPHDEM_CUDA_CHECK(cudaMemcpyAsync(&v, tmp, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
-    return v;
+template <int ND>
+__device__ __forceinline__ void image32(const DevCfg &c, const int *sh, float *img) {
+#pragma unroll
+    for (int q = 0; q < ND; q++) img[q] = sh[q] == 0 ? 0.f : (float)(sh[q] * (c.rmax[q] - c.rmin[q]));
+}
+
+/* continuity (end pairs) in FP32, then the FP64 totals of r1, vh1 and the
+ * adjoints of f1, fp, fv (k_cp_end) */
+template <int ND>
+__global__ void __launch_bounds__(128) k_cp_end32(DevCfg c, int64_t n, double dt, const int *typ,
+                                                  const int *__restrict__ nb, const int2 *__restrict__ oc,
+                                                  const double *adj, const double *cacc, double *cend, float4 *rec) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a >= n || !is_fluid(typ[a])) return;
+    const float4 *E0 = rec + R_E0 * n, *E1 = rec + R_E1 * n, *E2 = rec + R_E2 * n;
+    const float wcon = (float)c.wcon;
+    const float4 p0 = E0[a], p1 = E1[a], p2 = E2[a];
+    const float pa[3] = {p0.x, p0.y, p0.z}, la[3] = {p1.x, p1.y, p1.z}, va[3] = {p2.x, p2.y, p2.z};
+    Kf rb[ND], wb[ND];
+    const int2 o = oc[a];
+    for (int k = 0; k < o.y; k++) {
+        int sh[3];
+        const int b = table_entry(__ldg(nb + o.x + k), sh);
+        float img[3];
+        image32<ND>(c, sh, img);
+        const float4 q0 = E0[b], q1 = E1[b], q2 = E2[b];
+        const float pb[3] = {q0.x, q0.y, q0.z}, lb[3] = {q1.x, q1.y, q1.z}, vb[3] = {q2.x, q2.y, q2.z};
+        float d[3], w[3], r2 = 0.f, wd = 0.f;
+#pragma unroll
+        for (int q = 0; q < ND; q++) {
+            d[q] = ((pa[q] - pb[q]) + (la[q] - lb[q])) - img[q];
+            w[q] = va[q] - vb[q];
+            r2 = fmaf(d[q], d[q], r2);
+            wd = fmaf(w[q], d[q], wd);
+        }
+        if (!(r2 > 0.f)) continue;
+        const float r = sqrtf(r2);
+        float G, Gp;
+        grad_factor32<ND>(wcon, r, p0.w, q0.w, G, Gp);
+        const float coef = q1.w * p2.w + p1.w * q2.w;
+        const float gw = Gp * wd / r;
+#pragma unroll
+        for (int q = 0; q < ND; q++) {
+            rb[q].add(coef * (G * w[q] + gw * d[q]));
+            wb[q].add(coef * G * d[q]);
+        }
+    }
+    const double hd = 0.5 * dt;
+    const double *aa = adj + a * ADJ_NC, *ac = cacc + a * CP_NACC;
+    const bool sph = typ[a] == T_SPH;
+    double *ce = cend + a * CP_NEND;
+    float P[3] = {0.f, 0.f, 0.f}, V[3] = {0.f, 0.f, 0.f};
+    for (int q = 0; q < 3; q++) {
+        const double rt = aa[AS_R + q] + ac[CA_R1 + q] + (q < ND ? rb[q].value() : 0.0);
+        const double vt = aa[AS_VH + q] + ac[CA_VH1 + q] + (q < ND ? wb[q].value() : 0.0) + hd * rt;
+        const double F = sph ? aa[AS_F + q] + dt * (vt + aa[AS_V + q]) : 0.0;
+        ce[CE_R1 + q] = rt;
+        ce[CE_VH1 + q] = vt;
+        ce[CE_F + q] = F;
+        ce[CE_P + q] = F + ac[CA_FP + q];
+        ce[CE_V + q] = sph ? F + ac[CA_FV + q] : 0.0;
+        P[q] = (float)ce[CE_P + q];
+        V[q] = (float)ce[CE_V + q];
+    }
+    float4 *M3 = rec + R_M3 * n, *M4 = rec + R_M4 * n;
+    M3[a] = make_float4(P[0], P[1], P[2], M3[a].w);
+    M4[a] = make_float4(V[0], V[1], V[2], M4[a].w);
+}
+
+/* cp_force_pair in FP32 with Kahan sums */
+template <int ND>
+__device__ __forceinline__ void cp_force_pair32(float nu, float rho0, const float *d, const float *w, float r,
+                                                float G, float Gp, float hbar, const float *Pb, const float *Vb,
+                                                float my, float rhox, float rhoy, float pdr2x, float pdr2y,
+                                                float sign, Kf *Db, Kf *Wb, Kf &Rb, Kf &Qb, float &nub) {
+    float P = 0.f, Vw = 0.f;
+#pragma unroll
+    for (int q = 0; q < ND; q++) {
+        P = fmaf(Pb[q], d[q], P);
+        Vw = fmaf(Vb[q], w[q], Vw);
+    }
+    const float ir = 1.f / r;
+    const float s = -my * (pdr2x + pdr2y);
+    Qb.add(-my * G * P);
+    const float gpd = Gp * P * ir;
+    const float eta2 = 0.01f * hbar * hbar, r2 = r * r, den = 1.f / (r2 + eta2);
+    const float phi = G * r2 * den;
+    const float dphi = Gp * r2 * den + G * 2.f * r * eta2 * den * den;
+    const float cxy = 2.f * nu * rho0 * my / (rhox * rhoy);
+    const float VT = cxy * phi * Vw;
+    Rb.add(-VT / (sign > 0.f ? rhox : rhoy));
+    nub += VT / nu;
+    const float cv = cxy * Vw * dphi * ir;
+#pragma unroll
+    for (int q = 0; q < ND; q++) {
+        Db[q].add(sign * (s * (G * Pb[q] + gpd * d[q]) + cv * d[q]));
+        Wb[q].add(sign * cxy * phi * Vb[q]);
+    }
+}
+
+/* forces (middle pairs) in FP32 and the EOS in FP64 (k_cp_force) */
+template <int ND>
+__global__ void __launch_bounds__(128) k_cp_force32(DevCfg c, int64_t n, const int *typ, const int *__restrict__ nb,
+                                                    const int2 *__restrict__ oc, const double *adj,
+                                                    const double *aux, const double *cend,
+                                                    const float4 *__restrict__ rec, double *cmid, double *cacc,
+                                                    double *grads) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float gnu = 0.f;
+    if (a < n && is_fluid(typ[a])) {
+        const float4 *M0 = rec + R_M0 * n, *M1 = rec + R_M1 * n, *M2 = rec + R_M2 * n, *M3 = rec + R_M3 * n,
+                     *M4 = rec + R_M4 * n;
+        const float wcon = (float)c.wcon, nu = (float)c.viscosity, rho0 = (float)c.dens;
+        const float4 p0 = M0[a], p1 = M1[a], p2 = M2[a], p3 = M3[a], p4 = M4[a];
+        const float pa[3] = {p0.x, p0.y, p0.z}, la[3] = {p1.x, p1.y, p1.z}, va[3] = {p2.x, p2.y, p2.z};
+        const float Pa[3] = {p3.x, p3.y, p3.z}, Va[3] = {p4.x, p4.y, p4.z};
+        const bool own = Pa[0] != 0.f || Pa[1] != 0.f || Pa[2] != 0.f || Va[0] != 0.f || Va[1] != 0.f ||
+                         Va[2] != 0.f;
+        Kf Db[ND], Wb[ND], Rb, Qb;
+        float dum = 0.f;
+        const int2 o = oc[a];
+        for (int k = 0; k < o.y; k++) {
+            int sh[3];
+            const int b = table_entry(__ldg(nb + o.x + k), sh);
+            float img[3];
+            image32<ND>(c, sh, img);
+            const float4 q0 = M0[b], q1 = M1[b], q2 = M2[b], q3 = M3[b], q4 = M4[b];
+            const float pb[3] = {q0.x, q0.y, q0.z}, lb[3] = {q1.x, q1.y, q1.z}, vb[3] = {q2.x, q2.y, q2.z};
+            const float Pbv[3] = {q3.x, q3.y, q3.z}, Vbv[3] = {q4.x, q4.y, q4.z};
+            float d[3], w[3], md[3], mw[3], r2 = 0.f;
+#pragma unroll
+            for (int q = 0; q < ND; q++) {
+                d[q] = ((pa[q] - pb[q]) + (la[q] - lb[q])) - img[q];
+                w[q] = va[q] - vb[q];
+                md[q] = -d[q];
+                mw[q] = -w[q];
+                r2 = fmaf(d[q], d[q], r2);
+            }
+            if (!(r2 > 0.f)) continue;
+            const float r = sqrtf(r2);
+            float G, Gp;
+            grad_factor32<ND>(wcon, r, p0.w, q0.w, G, Gp);
+            const float hbar = 0.5f * (p4.w + q4.w);
+            if (own)
+                cp_force_pair32<ND>(nu, rho0, d, w, r, G, Gp, hbar, Pa, Va, q1.w, p2.w, q2.w, p3.w, q3.w, 1.f, Db, Wb,
+                                    Rb, Qb, gnu);
+            if (Pbv[0] != 0.f || Pbv[1] != 0.f || Pbv[2] != 0.f || Vbv[0] != 0.f || Vbv[1] != 0.f || Vbv[2] != 0.f)
+                cp_force_pair32<ND>(nu, rho0, md, mw, r, G, Gp, hbar, Pbv, Vbv, p1.w, q2.w, p2.w, q3.w, p3.w, -1.f, Db,
+                                    Wb, Rb, Qb, dum);
+        }
+        const double rhoa = aux[a * ADJ_AUX + 6];
+        const double eps = cmid[a * CP_NMID + CM_EPS];
+        const double x = rhoa / (c.refd * eps), x2 = x * x, x7 = x2 * x2 * x2 * x;
+        const double dp_drho = c.prb * (5.0 * x7 + 2.0) / (rhoa * rhoa * rhoa);
+        const double dp_deps = -7.0 * c.prb * x7 / (eps * rhoa * rhoa);
+        double *ac = cacc + a * CP_NACC;
+        const double *aa = adj + a * ADJ_NC, *ea = cend + a * CP_NEND;
+        const double Qv = Qb.value();
+        ac[CA_RHOS] = aa[AS_DENS] + ac[CA_RHO] + Rb.value() + Qv * dp_drho;
+        const double epsb = ac[CA_EPS] + Qv * dp_deps;
+        ac[CA_EBAR] = cmid[a * CP_NMID + CM_CLAMP] != 0.0 ? 0.0 : -epsb;
+        for (int q = 0; q < 3; q++) {
+            ac[CA_RS + q] = ea[CE_R1 + q] + (q < ND ? Db[q].value() : 0.0);
+            cmid[a * CP_NMID + CM_VHS + q] = q < ND ? Wb[q].value() : 0.0;
+        }
+    }
+    gnu += __shfl_xor_sync(0xffffffffu, gnu, 16);
+    gnu += __shfl_xor_sync(0xffffffffu, gnu, 8);
+    gnu += __shfl_xor_sync(0xffffffffu, gnu, 4);
+    gnu += __shfl_xor_sync(0xffffffffu, gnu, 2);
+    gnu += __shfl_xor_sync(0xffffffffu, gnu, 1);
+    if ((threadIdx.x & 31) == 0 && gnu != 0.f) atomicAdd(&grads[3], (double)gnu);
 }
 
 }  // namespace
 
 void cpl_count_tables(sphdem_ctx *c, AdjointData *a) {
-    int *tmp = a->slot;  /* a device int, reset by the replay before use */
-    const int64_t nc = count_table(c, 0, tmp), nf = count_table(c, 1, tmp), nt = count_table(c, 2, tmp);
-    a->cpl.cap = nc + nc / 2 + 4096;
-    a->fpi.cap = nf + nf / 2 + 4096;
-    int64_t n_dem = 0;
-    {
-        std::vector<int> iam(c->n);
-        field_get_int(c, FI_IAM, iam.data());
-        for (int t : iam) n_dem += t == T_DEM;
+    /* the coupling pairs of the current buckets, counted with the tap's own
+     * scan (a->slot is a device int the replay resets before use) */
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->dpos, (size_t)c->n * sizeof(float4)));
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->slot, 0, sizeof(int), c->stream));
+    k_cp_dpos<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->A, c->g, c->n, a->dpos);
+    k_cp_cpl_table<<<grid_for(c->n, CB), CB, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->g, c->n, a->dpos,
+                                                             nullptr, nullptr, a->slot, 0, nullptr);
+    int nc = 0;
+    SPHDEM_CUDA_CHECK(cudaMemcpyAsync(&nc, a->slot, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    a->cpl.cap = (int64_t)nc + nc / 2 + 4096;
+    std::vector<int> iam(c->n), tags;
+    field_get_int(c, FI_IAM, iam.data());   /* tag order */
+    for (int64_t i = 0; i < c->n; i++)
+        if (iam[i] == T_DEM) tags.push_back((int)i);
+    a->n_dem = (int)tags.size();
+    a->fpi.cap = (int64_t)std::max(1, a->n_dem) * CP_FPI_PER;
+    a->ct_cap = (int64_t)std::max(1, a->n_dem) * ADJ_MAX_CONTACTS;
+    if (!tags.empty()) {
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->dem_tags, tags.size() * sizeof(int)));
+        SPHDEM_CUDA_CHECK(cudaMemcpy(a->dem_tags, tags.data(), tags.size() * sizeof(int), cudaMemcpyHostToDevice));
     }
-    a->ct_cap = (int)std::min<int64_t>(std::max<int64_t>(nt + nt / 2, 16 * n_dem) + 4096, 1 << 30);
 }
 
 void cpl_alloc(sphdem_ctx *c, AdjointData *a) {
@@ -861,6 +1136,8 @@ void cpl_alloc(sphdem_ctx *c, AdjointData *a) {
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->cend, (size_t)n * CP_NEND * sizeof(double)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->cmid, (size_t)n * CP_NMID * sizeof(double)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->aux, (size_t)n * ADJ_AUX * sizeof(double)));
+    if (c->cfg.precision == SPHDEM_PREC_MIXED)
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->crec, (size_t)n * CP_NREC32 * sizeof(float4)));
 }
 
 void cpl_free(AdjointData *a) {
@@ -871,7 +1148,13 @@ void cpl_free(AdjointData *a) {
     cudaFree(a->cacc);
     cudaFree(a->cend);
     cudaFree(a->cmid);
+    cudaFree(a->crec);
+    cudaFree(a->dpos);
+    cudaFree(a->dem_tags);
     a->rmid = a->cacc = a->cend = a->cmid = nullptr;
+    a->crec = nullptr;
+    a->dpos = nullptr;
+    a->dem_tags = nullptr;
 }
 
 void cpl_reset_segment(sphdem_ctx *c, AdjointData *a) {
@@ -883,13 +1166,20 @@ void cpl_reset_segment(sphdem_ctx *c, AdjointData *a) {
 }
 
 void cpl_taps_middle(sphdem_ctx *c, AdjointData *a) {
-    table_launch(c, 0, a->cpl, a->slot);
+    k_cp_dpos<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->A, c->g, c->n, a->dpos);
+    k_cp_cpl_table<<<grid_for(c->n, CB), CB, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->g, c->n, a->dpos,
+                                                             a->cpl.nb, a->cpl.oc, a->cpl.cnt, a->cpl.cap, a->slot);
     k_cp_tap_r<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->A, c->n, a->rmid, a->slot);
 }
 
 void cpl_taps_end(sphdem_ctx *c, AdjointData *a) {
-    table_launch(c, 1, a->fpi, a->slot);
-    table_launch(c, 2, a->ct, a->slot);
+    if (a->n_dem == 0) return;
+    k_cp_fpi_table<<<grid_for((int64_t)a->n_dem * 32, CB), CB, 0, c->stream>>>(
+        c->cfg, c->A, c->buf.start, c->g, c->n, a->n_dem, CP_FPI_PER, a->fpi.nb, a->fpi.oc, a->fpi.cnt, a->fpi.cap,
+        a->slot);
+    k_cp_ct_table<<<grid_for(a->n_dem, CB), CB, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->g, c->n, a->n_dem,
+                                                                ADJ_MAX_CONTACTS, a->ct.nb, a->ct.oc, a->ct.cnt,
+                                                                a->ct.cap, a->slot);
 }
 
 bool cpl_overflow(sphdem_ctx *c, AdjointData *a) {
@@ -920,13 +1210,30 @@ void cpl_backward_step(sphdem_ctx *c, AdjointData *a, int j, double dt) {
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cmid, 0, (size_t)n * CP_NMID * sizeof(double), st));
     k_cp_pre<<<grid_for(n, 256), 256, 0, st>>>(n, dt, s0, rm, a->typ, a->aux);
     k_cp_por<<<g, CB, 0, st>>>(c->cfg, n, a->aux, a->mass, a->typ, nbp(a->cpl), ocp(a->cpl), a->cmid);
-    k_cp_fpi<<<g, CB, 0, st>>>(c->cfg, n, dt, s1, a->aux, a->cmid, a->mass, a->hh, a->typ, nbp(a->fpi), ocp(a->fpi),
-                               a->adj, a->cacc, a->grads);
+    if (a->n_dem > 0)
+        k_cp_fpi<<<grid_for((int64_t)a->n_dem * 32, CB), CB, 0, st>>>(c->cfg, a->n_dem, a->dem_tags, dt, s1, a->aux,
+                                                                      a->cmid, a->mass, a->hh, nbp(a->fpi),
+                                                                      ocp(a->fpi), a->adj, a->cacc, a->grads);
     k_cp_dem<<<g, CB, 0, st>>>(c->cfg, n, dt, s1, a->aux, a->mass, a->rad, a->typ, nbp(a->ct), ocp(a->ct), a->adj,
                                a->cacc, a->grads);
-    k_cp_end<<<g, CB, 0, st>>>(c->cfg, n, dt, s1, a->mass, a->hh, a->typ, nbe, oce, a->adj, a->cacc, a->cend);
-    k_cp_force<<<g, CB, 0, st>>>(c->cfg, n, a->aux, a->mass, a->hh, a->typ, nbm, ocm, a->adj, a->cend, a->cmid,
-                                 a->cacc, a->grads);
+    if (a->crec) {
+        k_cp_pack32<<<grid_for(n, 256), 256, 0, st>>>(n, dt, a->aux, a->cmid, s1, a->adj, a->mass, a->hh, a->typ,
+                                                       a->crec);
+#define L_(ND)                                                                                                   \
+    do {                                                                                                         \
+        k_cp_end32<ND><<<g, CB, 0, st>>>(c->cfg, n, dt, a->typ, nbe, oce, a->adj, a->cacc, a->cend, a->crec);     \
+        k_cp_force32<ND><<<g, CB, 0, st>>>(c->cfg, n, a->typ, nbm, ocm, a->adj, a->aux, a->cend, a->crec, a->cmid, \
+                                           a->cacc, a->grads);                                                    \
+    } while (0)
+        if (c->cfg.nd == 3) L_(3);
+        else if (c->cfg.nd == 2) L_(2);
+        else L_(1);
+#undef L_
+    } else {
+        k_cp_end<<<g, CB, 0, st>>>(c->cfg, n, dt, s1, a->mass, a->hh, a->typ, nbe, oce, a->adj, a->cacc, a->cend);
+        k_cp_force<<<g, CB, 0, st>>>(c->cfg, n, a->aux, a->mass, a->hh, a->typ, nbm, ocm, a->adj, a->cend, a->cmid,
+                                     a->cacc, a->grads);
+    }
     k_cp_cpl_a<<<g, CB, 0, st>>>(c->cfg, n, s0, a->aux, a->cmid, a->cend, a->mass, a->typ, nbp(a->cpl), ocp(a->cpl),
                                  a->cacc);
     k_cp_cpl_b<<<g, CB, 0, st>>>(c->cfg, n, a->aux, a->mass, a->typ, nbp(a->cpl), ocp(a->cpl), a->cacc);
