@@ -276,6 +276,34 @@ def measure_adjoint(lib, capi, cases, nsteps=100, ckpt=10):
     return out
 
 
+def run_adjoint_profile(args):
+    """The differentiated coupled workload (100k fluid + 5k DEM, mixed) for
+    profiler captures: 2 plain steps, then sphdem_adjoint_forward over
+    args.steps steps with one checkpoint segment and sphdem_adjoint_backward
+    of the mean DEM height; prints the wall times."""
+    import __graft_entry__
+    __graft_entry__.build()
+    from sphdem import capi, cases
+    lib = capi.Library()
+    case = cases.workload("sediment3d_adjoint")
+    sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    sim.step(2)
+    a = sim.get(capi.FIELD_IAM)
+    seed = np.zeros((sim.n, 3))
+    m = a["iam"] == cases.DEM
+    seed[m, 2] = 1.0 / m.sum()
+    t0 = time.perf_counter()
+    sim.adjoint_forward(args.steps, args.steps)
+    t1 = time.perf_counter()
+    g = sim.adjoint_backward(dL_dr=seed)[0]
+    t2 = time.perf_counter()
+    sim.close()
+    print(json.dumps({"workload": "sediment3d_adjoint (coupled, %d particles)" % case.n, "steps": args.steps,
+                      "adjoint_forward_ms_per_step": 1e3 * (t1 - t0) / args.steps,
+                      "adjoint_backward_ms_per_step": 1e3 * (t2 - t1) / args.steps,
+                      "grad_viscosity": g.viscosity, "grad_drag_scale": g.drag_scale}), flush=True)
+
+
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return
@@ -486,13 +514,17 @@ def main():
     ap.add_argument("--profile", action="store_true", help="mixed path only (for profiler captures)")
     ap.add_argument("--quarter", action="store_true", help="with --profile: 1/4 sub-box of the workload")
     ap.add_argument("--ensemble", action="store_true", help="batched dam-break ensemble instead")
+    ap.add_argument("--adjoint-profile", action="store_true",
+                    help="coupled adjoint over --steps steps only (for profiler captures)")
     ap.add_argument("--instances", type=int, default=256)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
-    if args.profile:
+    if args.adjoint_profile:
+        run_adjoint_profile(args)
+    elif args.profile:
         run_profile(args)
     elif args.ensemble:
         run_ensemble(args)
