@@ -298,7 +298,8 @@ void run_phase_mixed(sphdem_ctx *c, int phase) {
                 mixed::dem_drag(c);
             }
             if (lists) {
-                mixed::omega_eos(c, c->cfg.var_h(), true);
+                /* elementwise EOS; Omega (VAR_H_CORRECTION) is summed inside the force pass */
+                mixed::omega_eos(c, false, true);
                 mixed::force(c);
             }
             if (liq) run_dem_accel(c);
@@ -311,8 +312,7 @@ void run_phase_mixed(sphdem_ctx *c, int phase) {
             mixed::pack(c, false);
             if (lists) {
                 mixed::nlist(c);
-                if (c->cfg.var_h()) mixed::omega_eos(c, true, false);
-                mixed::dddt(c);
+                mixed::dddt(c);  /* Omega (VAR_H_CORRECTION) is summed inside the continuity pass */
             }
             if (liq) mixed::dem_end(c);
             run_end_tail(c);

@@ -899,7 +899,7 @@ __device__ __noinline__ void boundary32(const DevCfg *__restrict__ cp, const flo
 template <int ND>
 __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restrict__ cp, DevState s, DevGlobals *__restrict__ g,
                                                const float4 *__restrict__ P0, const float4 *__restrict__ P1,
-                                               const float4 *__restrict__ P2, const float *__restrict__ om32,
+                                               const float4 *__restrict__ P2, float *__restrict__ om32,
                                                const int *__restrict__ tg, const int *__restrict__ nbr,
                                                const int *__restrict__ ncnt, int64_t ld, int64_t n,
                                                const float4 *__restrict__ NB) {
@@ -913,7 +913,13 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
         const float ha = pa.w, iha = xa.w;
         const float ihn2a = powi<ND>(iha) * iha * iha;
         const float densa = xa.x, pdr2a = xa.y, ma = va.w;
-        const float roma = c.var_h() ? 1.f / om32[a] : 1.f;
+        /* VAR_H_CORRECTION: every gradient of a's sums carries 1/Omega_a
+         * (gA = ga/Omega_a, gB = gb/Omega_a), so Omega_a (calcOmega,
+         * sph.h:438-451) is summed in this same loop and the gradient sums
+         * are scaled once at the end */
+        const float ihna = powi<ND>(iha), pd_coef = ND * ihna * iha;
+        Kahan om;
+        om.init(-ma * pd_coef * wK32(0.f, wcon));
         const bool sph = ta == T_SPH;
         const bool anti = !(c.flags & SPHDEM_F_NO_ANTICLUMPING);
         const float visc_nu = (float)c.viscosity, c0 = (float)c.spsound;
@@ -922,6 +928,8 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
         const float vdc = c.visc == SPHDEM_VISC_MONAGHAN ? 0.06f : 0.125f;
         const float k_anti_inv = c.k_anti != 0 ? (float)(1.0 / c.k_anti) : 0.f;
         Kahan fp[ND], fv[ND], fb[ND], fa[ND];
+        Kahan fq;  /* anticlumping: the same term on every component, not scaled by 1/Omega */
+        fq.init(0.f);
 #pragma unroll
         for (int k = 0; k < ND; k++) {
             fp[k].init(0.f);
@@ -948,11 +956,12 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
             /* gradW: dr*F(q,h), F = ihn2*dK/dq/q, 1/q = h/r */
             const float Fa = qa != 0.f ? ihn2a * wdK32(qa, wcon) * (ha * rinv) : 0.f;
             const float Fb = qb != 0.f ? ihn2b * wdK32(qb, wcon) * (hb * rinv) : 0.f;
-            float cA, cB, cM;  /* gA = d*cA, gB = d*cB, 0.5(gA+gB) = d*cM */
+            float cA, cB, cM;  /* gA = d*cA, gB = d*cB, 0.5(gA+gB) = d*cM (times Omega_a with VAR_H) */
             if (c.var_h()) {
-                cA = Fa * roma;
-                cB = Fb * roma;
+                cA = Fa;
+                cB = Fb;
                 cM = 0.5f * (cA + cB);
+                if (is_sph_or_sphb(tb)) om.add(vb.w * (ihna * (-qa * wdK32(qa, wcon) * iha) - pd_coef * wK32(qa, wcon)));
             } else {
                 cA = cB = cM = 0.5f * (Fa + Fb);
             }
@@ -1003,17 +1012,27 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
                 }
                 const float pc = pdr2a * cA + pdr2b * cB;
 #pragma unroll
-                for (int k = 0; k < ND; k++) fp[k].add(-mb * (pc * d[k] + antic));
+                for (int k = 0; k < ND; k++) fp[k].add(-mb * (pc * d[k]));
+                if (anti) fq.add(-mb * antic);
             }
+        }
+        float roma = 1.f;
+        if (c.var_h()) {
+            /* Omega = 1 + h*sum/(rho*NDIM): an O(1) number, FP32 is ample */
+            const float omega = 1.f + ha * om.s / (densa * ND);
+            s.row(FD_OMEGA)[a] = omega;
+            om32[a] = omega;
+            roma = 1.f / omega;
         }
         float fsum2 = 0.f;
 #pragma unroll
         for (int k = 0; k < ND; k++) {
-            s.row(FD_FP + k)[a] += fp[k].s;
-            s.row(FD_FV + k)[a] += fv[k].s;
+            const float fpk = fp[k].s * roma + fq.s, fvk = fv[k].s * roma, fak = fa[k].s * roma;
+            s.row(FD_FP + k)[a] += fpk;
+            s.row(FD_FV + k)[a] += fvk;
             s.row(FD_FB + k)[a] += fb[k].s;
             double *f = s.row(FD_F + k);
-            const double fk = f[a] + (double)((fa[k].s + fv[k].s) + (fb[k].s + fp[k].s));
+            const double fk = f[a] + (double)((fak + fvk) + (fb[k].s + fpk));
             f[a] = fk;
             const float fkf = (float)fk;
             fsum2 += fkf * fkf;
@@ -1027,7 +1046,7 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
 template <int ND>
 __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlobals *__restrict__ g,
                                               const float4 *__restrict__ P0, const float4 *__restrict__ P1,
-                                              const float4 *__restrict__ P2, const float *__restrict__ om32,
+                                              const float4 *__restrict__ P2, float *__restrict__ om32,
                                               const int *__restrict__ tg, const int *__restrict__ nbr,
                                               const int *__restrict__ ncnt, int64_t ld, int64_t n) {
     const float4 *shift = stencil_shifts(c, g);
@@ -1038,7 +1057,11 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
     const float4 pa = P0[a], va = P1[a];
     const float ha = pa.w, iha = P2[a].w;
     const float ihn2a = powi<ND>(iha) * iha * iha;
-    const float roma = c.var_h() ? 1.f / om32[a] : 1.f;
+    /* VAR_H_CORRECTION: the continuity sum carries 1/Omega_a only, so
+     * Omega_a is summed in this loop and applied once at the end */
+    const float ihna = powi<ND>(iha), pd_coef = ND * ihna * iha;
+    Kahan om;
+    om.init(-va.w * pd_coef * wK32(0.f, wcon));
     Kahan acc;
     acc.init(0.f);
     const int cnt = ncnt[a];
@@ -1059,7 +1082,8 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
         const float Fa = qa != 0.f ? ihn2a * wdK32(qa, wcon) * (ha * rinv) : 0.f;
         float F;
         if (c.var_h()) {
-            F = Fa * roma;
+            F = Fa;
+            if (is_sph_or_sphb(tb)) om.add(vb.w * (ihna * (-qa * wdK32(qa, wcon) * iha) - pd_coef * wK32(qa, wcon)));
         } else {
             const float qb = r * ihb;
             const float Fb = qb != 0.f ? powi<ND>(ihb) * ihb * ihb * wdK32(qb, wcon) * (pb.w * rinv) : 0.f;
@@ -1068,7 +1092,14 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
         const float vdr = (va.x - vb.x) * d[0] + (va.y - vb.y) * d[1] + (va.z - vb.z) * d[2];
         if (!(is_boundary(tb) || tb == T_DEM)) acc.add(vb.w * vdr * F);
     }
-    s.row(FD_DDDT)[a] += (double)acc.s;
+    float roma = 1.f;
+    if (c.var_h()) {
+        const float omega = 1.f + ha * om.s / (P2[a].x * ND);
+        s.row(FD_OMEGA)[a] = omega;
+        om32[a] = omega;
+        roma = 1.f / omega;
+    }
+    s.row(FD_DDDT)[a] += (double)(acc.s * roma);
 }
 
 /* ---------------------------------------------------------------------- */

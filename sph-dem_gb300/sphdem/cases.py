@@ -271,7 +271,8 @@ def sediment3d(nx: int = 80, L: float = 0.2, height: float = 0.4,
                n_dem: int = 50000, dem_radius_factor: float = 0.5,
                rho_s: float = 2500.0, k: float = 1e4, restitution: float = 0.5,
                viscosity: float = 1e-6, seed: int = 3, nsteps: int = 1000,
-               dt: float | None = None, floor: str = "boundary", var_h: bool = True) -> Case:
+               dt: float | None = None, floor: str = "boundary", var_h: bool = True,
+               dem_top_margin: float | None = None) -> Case:
     """Coupled SPH-DEM sedimentation in a periodic-x/y box L x L x height with
     a bottom wall.  Fluid lattice as sediment3D/setup.cpp:65-108 (staggered
     odd layers, one `boundary` layer at k=0), h = 1.5 dx, Morris viscosity
@@ -281,7 +282,10 @@ def sediment3d(nx: int = 80, L: float = 0.2, height: float = 0.4,
 
     floor="sphb3" makes the floor three fixed sphBoundary layers (k = 0..2)
     instead of the repulsive boundary layer, and var_h=False gives constant
-    h without VAR_H_CORRECTION: the coupled form the adjoint covers."""
+    h without VAR_H_CORRECTION: the coupled form the adjoint covers.
+    dem_top_margin keeps the DEM centres that far below the free surface
+    (default R): spheres at the surface see about half a kernel of fluid, the
+    0.5 threshold of calcFPI's Shepard normalisation (sph.h:1759-1760)."""
     ndim = 3
     psep = L / nx
     nz = int(round(height / psep))
@@ -319,7 +323,7 @@ def sediment3d(nx: int = 80, L: float = 0.2, height: float = 0.4,
 
     # DEM: uniform in the top half, periodic overlap rejection on a hash grid
     rng = np.random.default_rng(seed)
-    zlo, zhi = 0.5 * height + R, height - R
+    zlo, zhi = 0.5 * height + R, height - (R if dem_top_margin is None else max(R, dem_top_margin))
     cell = 2.0 * R
     ncx = max(1, int(L / cell))
     grid: dict = {}
