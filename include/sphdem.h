@@ -137,6 +137,9 @@ typedef struct SphDemParticles {
     double  *porosity, *dporositydt, *shep_sum, *omega;
     double  *fdrag, *fvel, *grad_porosity;  /* [3n]                              */
     double  *v0, *vhat0;             /* [3n] start-of-step velocities            */
+    /* calcEnergies integrals (sphIncompress.h:769-781), per unit mass: elastic
+     * energy u and its rate, viscous energy eViscF and its rate (sph only) */
+    double  *u, *dudt, *e_visc, *de_visc_dt;
 } SphDemParticles;
 
 /* Field-mask bits for get/set. */
@@ -153,6 +156,7 @@ typedef struct SphDemParticles {
 #define SPHDEM_FIELD_OMEGA    (1u << 10)
 #define SPHDEM_FIELD_V0       (1u << 11)  /* v0, vhat0 */
 #define SPHDEM_FIELD_IAM      (1u << 12)
+#define SPHDEM_FIELD_ENERGY   (1u << 13)  /* u, dudt, e_visc, de_visc_dt */
 #define SPHDEM_FIELD_ALL      0xffffffffu
 
 /* Step globals: the CglobalVars members of the hot path, globalVars.h:196-220. */
@@ -225,6 +229,24 @@ int sphdem_rebuild(sphdem_handle h);
  * idx == NULL to query the pair count in *n_pairs. */
 int sphdem_pairs(sphdem_handle h, int kind, int64_t *offsets, int32_t *idx,
                  int64_t idx_capacity, int64_t *n_pairs);
+
+/* Output-step diagnostics: the globals CsphIncompress::calcOutputVars
+ * (sphIncompress.h:274-319) computes at each output step of run.cpp:131 --
+ * momenta and energies of the sph particles, maxima, mean and variance of the
+ * density over sph and sphBoundary particles, the rms difference between the
+ * density and its SPH summation (calcAveDensFromMass, 266-272).  n counts all
+ * live particles, as the reference's particle container does; ff, eViscB and
+ * eBForce are zero on the reference's path as well (never accumulated). */
+typedef struct SphDemOutputVars {
+    double  lin_mom[3], ang_mom;
+    double  e_ke, e_elast, e_elast_exact, ed_elast_dt;
+    double  e_visc_f, ed_visc_f_dt, e_ff, ed_ff_dt, e_visc_b, e_b_force, e_total;
+    double  max_v, max_f, max_ff, rms_ff;
+    double  ave_dens, var_dens, ave_dens_from_mass;
+    int64_t n, n_sph;
+} SphDemOutputVars;
+
+int sphdem_output_vars(sphdem_handle h, SphDemOutputVars *out);
 
 /* Bucket index of every particle (tag order) in the reference's own maps:
  * getCellI (dataLL.h:303-305) for non-DEM, dem_getCellI (dataLL.h:308-311)

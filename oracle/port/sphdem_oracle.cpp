@@ -47,6 +47,7 @@ struct Part {
     double fdrag[3], fvel[3], gradPor[3];
     double norm1[3], norm2[3], norm3[3];
     double mass, dens, dddt, h, press, pdr2, omega, porosity, dpordt, shep, radius;
+    double u, dudt, eViscF, deViscFdt;   /* calcEnergies integrals (sphIncompress.h:769-781) */
 };
 
 /* A bucket entry: particle index plus the periodic image it stands for. */
@@ -971,9 +972,67 @@ struct Sim {
         }
         for (auto &p : ps)
             if (p.alive && sph_or_sphb(p.iam)) drift_rest(p, dt / 2);
-        /* calcEnergies (sphIncompress.h:769-781) refreshes press/pdr2 */
+        /* calcEnergies (sphIncompress.h:769-781): press/pdr2 refresh, elastic
+         * energy, and the viscous energy of sph particles */
         for (auto &p : ps)
-            if (p.alive && sph_or_sphb(p.iam)) calc_press(p);
+            if (p.alive && sph_or_sphb(p.iam)) {
+                if (p.iam == T_SPH) {
+                    p.deViscFdt = -dot(p.vhat, p.fv, nd);
+                    p.eViscF += dt * p.deViscFdt;
+                }
+                calc_press(p);
+                p.dudt = p.pdr2 * p.dddt;
+                p.u += dt * p.dudt;
+            }
+    }
+
+    /* calcOutputVars (sphIncompress.h:274-319): calcOutput over sph /
+     * sphBoundary (233-262), calcAveDensFromMass over the cached neighbour
+     * lists (266-272 with calcDensity, sph.h:1149-1191), calcVarDens (264) */
+    void output_vars(SphDemOutputVars &o) const {
+        o = SphDemOutputVars{};
+        double aveDens = 0, dfm = 0;
+        long long nlive = 0, nsph = 0;
+        for (size_t k = 0; k < ps.size(); k++) {
+            const Part &p = ps[k];
+            if (!p.alive) continue;
+            nlive++;
+            if (!sph_or_sphb(p.iam)) continue;
+            if (p.iam == T_SPH) {
+                for (int i = 0; i < nd; i++) o.lin_mom[i] += p.v[i] * p.mass;
+                o.ang_mom += (p.r[0] * p.v[1] - p.r[1] * p.v[0]) * p.mass;
+                o.e_ke += 0.5 * p.mass * len2(p.vhat);
+                o.e_visc_f += p.mass * p.eViscF;
+                o.ed_visc_f_dt += p.mass * p.deViscFdt;
+                nsph++;
+            }
+            o.max_v = std::max(o.max_v, len(p.v));
+            o.max_f = std::max(o.max_f, len(p.f));
+            aveDens += p.dens;
+            o.e_elast += p.mass * p.u;
+            o.ed_elast_dt += p.mass * p.dudt;
+            const double x = p.dens / c.refd;
+            o.e_elast_exact += p.mass * (c.prb * ((std::pow(x, 6) - 1) / 6 + 1 / x - 1)) / c.refd;
+            double rho = p.mass * Wk(0.0, p.h);
+            for (const Entry &e : nbrs[k]) {
+                const Part &pb = ps[e.idx];
+                if (!sph_or_sphb(pb.iam)) continue;
+                double rb[3], dr[3] = {0, 0, 0};
+                epos(e, rb);
+                for (int i = 0; i < nd; i++) dr[i] = p.r[i] - rb[i];
+                rho += pb.mass * Wk(len(dr) / p.h, p.h);
+            }
+            dfm += (rho - p.dens) * (rho - p.dens);
+        }
+        o.n = nlive;
+        o.n_sph = nsph;
+        o.ave_dens = aveDens / nlive;
+        o.ave_dens_from_mass = std::sqrt(dfm / nlive);
+        double var = 0;
+        for (const Part &p : ps)
+            if (p.alive && sph_or_sphb(p.iam)) var += (p.dens - o.ave_dens) * (p.dens - o.ave_dens);
+        o.var_dens = var / nlive;
+        o.e_total = o.e_ke + o.e_elast + o.e_visc_f + o.e_visc_b + o.e_b_force + o.e_ff;
     }
 
     void full_step() {
@@ -1105,7 +1164,13 @@ int oracle_get(void *h, SphDemParticles *o) {
         put1(o->porosity, p.porosity); put1(o->dporositydt, p.dpordt);
         put1(o->shep_sum, p.shep); put1(o->omega, p.omega);
         put1(o->radius, p.radius);
+        put1(o->u, p.u); put1(o->dudt, p.dudt); put1(o->e_visc, p.eViscF); put1(o->de_visc_dt, p.deViscFdt);
     }
+    return 0;
+}
+
+int oracle_output_vars(void *h, SphDemOutputVars *o) {
+    static_cast<Sim *>(h)->output_vars(*o);
     return 0;
 }
 

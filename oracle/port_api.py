@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(os.path.dirname(HERE), "sph-dem_gb300"))
 
 from sphdem.capi import (ParticleBuffers, SphDemConfig, SphDemGlobals,  # noqa: E402
-                         SphDemParticles, config_struct)
+                         SphDemOutputVars, SphDemParticles, config_struct)
 
 from . import build_oracle  # noqa: E402
 
@@ -37,6 +37,7 @@ def lib():
                                    C.c_int64, C.POINTER(C.c_int64)]
         L.oracle_cells.argtypes = [H, C.POINTER(C.c_int32)]
         L.oracle_globals.argtypes = [H, C.POINTER(SphDemGlobals)]
+        L.oracle_output_vars.argtypes = [H, C.POINTER(SphDemOutputVars)]
         L.oracle_last_error.restype = C.c_char_p
         _LIB = L
     return _LIB
@@ -97,3 +98,8 @@ class OracleSim:
         g = SphDemGlobals()
         self.L.oracle_globals(self.h, C.byref(g))
         return g
+
+    def output_vars(self) -> dict:
+        o = SphDemOutputVars()
+        self.L.oracle_output_vars(self.h, C.byref(o))
+        return o.as_dict()

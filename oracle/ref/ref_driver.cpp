@@ -178,6 +178,10 @@ int main(int argc, char **argv) {
     sca_field("press", &Cparticle::press);
     sca_field("pdr2", &Cparticle::pdr2);
     sca_field("mass", &Cparticle::mass);
+    sca_field("u", &Cparticle::u);
+    sca_field("dudt", &Cparticle::dudt);
+    sca_field("eViscF", &Cparticle::eViscF);
+    sca_field("deViscFdt", &Cparticle::deViscFdt);
 #ifdef LIQ_DEM
     sca_field("porosity", &Cparticle::porosity);
     sca_field("dporositydt", &Cparticle::dporositydt);
@@ -189,6 +193,16 @@ int main(int argc, char **argv) {
 #ifdef VAR_H_CORRECTION
     sca_field("omega", &Cparticle::omega);
 #endif
+
+    /* the output-step globals, as run.cpp:131 computes them (on the cached
+     * lists of the last reset) */
+    solver.calcOutputVars();
+    std::vector<double> ov;
+    for (int d = 0; d < 3; d++) ov.push_back(d < NDIM ? g.linMom[d] : 0.0);
+    const double ovs[] = {g.angMom, g.eKE, g.eElast, g.eElastExact, g.edElastdt, g.eViscF, g.edViscFdt,
+                          g.eFF, g.edFFdt, g.eViscB, g.eBForce, g.eTotal, g.maxV, g.maxF, g.maxFF, g.rmsFF,
+                          g.aveDens, g.varDens, g.aveDensFromMass, (double)g.n, (double)g.nSph};
+    for (double x : ovs) ov.push_back(x);
 
     /* neighbour relations at the final positions, after one more reset so
      * that the ghost copies carry the smoothing lengths driftRest just
@@ -273,6 +287,10 @@ int main(int argc, char **argv) {
     fwrite(cells.data(), 4, 3 * n, out);
     double tt[2] = {g.time, g.dt};
     fwrite(tt, 8, 2, out);
+    /* trailer: the calcOutputVars globals (order of SphDemOutputVars) */
+    long long nov = ov.size();
+    fwrite(&nov, 8, 1, out);
+    fwrite(ov.data(), 8, ov.size(), out);
     fclose(out);
     return dt_changed ? 3 : 0;
 }

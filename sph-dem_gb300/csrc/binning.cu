@@ -428,7 +428,7 @@ void setup_rebuild_buffers(sphdem_ctx *c) {
     if (liq) { vec(FD_FDRAG); vec(FD_FVEL); vec(FD_GPOR); }
     vec(FD_N1); vec(FD_N2); if (nd == 3) vec(FD_N3);
     for (int f : {FD_MASS, FD_DENS, FD_DDDT, FD_H, FD_PRESS, FD_PDR2, FD_OMEGA, FD_RADIUS,
-                  FD_IH, FD_IHN, FD_IHN2})
+                  FD_IH, FD_IHN, FD_IHN2, FD_U, FD_DUDT, FD_EVISCF, FD_DEVISCF})
         fd.push_back(f);
     fd.push_back(FD_POR);
     if (liq) for (int f : {FD_DPORDT, FD_SHEP}) fd.push_back(f);

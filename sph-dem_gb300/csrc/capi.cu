@@ -737,6 +737,10 @@ const FieldMap kFields[] = {
     {SPHDEM_FIELD_OMEGA, FD_OMEGA, 1, &SphDemParticles::omega},
     {SPHDEM_FIELD_V0, FD_V0, 3, &SphDemParticles::v0},
     {SPHDEM_FIELD_V0, FD_VHAT0, 3, &SphDemParticles::vhat0},
+    {SPHDEM_FIELD_ENERGY, FD_U, 1, &SphDemParticles::u},
+    {SPHDEM_FIELD_ENERGY, FD_DUDT, 1, &SphDemParticles::dudt},
+    {SPHDEM_FIELD_ENERGY, FD_EVISCF, 1, &SphDemParticles::e_visc},
+    {SPHDEM_FIELD_ENERGY, FD_DEVISCF, 1, &SphDemParticles::de_visc_dt},
 };
 }  // namespace
 
@@ -832,6 +836,17 @@ int sphdem_adjoint_backward(sphdem_handle h, const double *dL_dr, const double *
         grads->viscosity = h->cfg.visc == SPHDEM_VISC_ARTIFICIAL ? g5[2] : g5[3];
         grads->drag_scale = g5[4];
         grads->valid = valid;
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+    return check_device(h);
+}
+
+int sphdem_output_vars(sphdem_handle h, SphDemOutputVars *out) {
+    if (!h || !out) return SPHDEM_ERR_INVALID;
+    try {
+        const int rc = output_vars(h, out);
+        if (rc) return rc;
     } catch (const std::string &e) {
         return fail(h, SPHDEM_ERR_CUDA, e);
     }

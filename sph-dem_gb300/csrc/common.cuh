@@ -39,6 +39,7 @@ enum FieldD : int {
     FD_N1 = 36, FD_N2 = 39, FD_N3 = 42,
     FD_MASS = 45, FD_DENS, FD_DDDT, FD_H, FD_PRESS, FD_PDR2, FD_OMEGA,
     FD_POR, FD_DPORDT, FD_SHEP, FD_RADIUS,
+    FD_U, FD_DUDT, FD_EVISCF, FD_DEVISCF,   /* calcEnergies: elastic and viscous energy per unit mass, rates */
     FD_IH, FD_IHN, FD_IHN2,   /* 1/h, 1/h^nd, 1/h^(nd+2): refreshed whenever h changes */
     NFD
 };

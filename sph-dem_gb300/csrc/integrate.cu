@@ -208,7 +208,9 @@ __global__ void k_end_drift(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
 }
 
 /* end() tail: dem kick(dt/2,dt/2) (sphIncompress.cpp:239), driftRest for
- * sph/sphBoundary (245) and calcEnergies' EOS refresh (249, 769-781) */
+ * sph/sphBoundary (245) and calcEnergies (249, sphIncompress.h:769-781): EOS
+ * refresh, elastic energy u += dt pdr2 dddt, and for sph the viscous energy
+ * eViscF += dt (-vhat . fv) */
 __global__ void k_end_tail(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -236,6 +238,15 @@ __global__ void k_end_tail(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
             h_derived(c, s, i);
         }
         eos(c, s, i);
+        const double dudt = s.row(FD_PDR2)[i] * s.row(FD_DDDT)[i];
+        s.row(FD_DUDT)[i] = dudt;
+        s.row(FD_U)[i] += dt * dudt;
+        if (t == T_SPH) {
+            double w = 0.0;
+            for (int d = 0; d < c.nd; d++) w += s.row(FD_VHAT + d)[i] * s.row(FD_FV + d)[i];
+            s.row(FD_DEVISCF)[i] = -w;
+            s.row(FD_EVISCF)[i] += dt * (-w);
+        }
     }
 }
 

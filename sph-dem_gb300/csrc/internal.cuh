@@ -146,6 +146,9 @@ void dem_end(sphdem_ctx *c);
  * tables (tag space, slot *slot of nb / oc / cnt) */
 void mixed_adj_pairs(sphdem_ctx *c, int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot);
 
+/* diagnostics.cu: calcOutputVars on the device (synchronises) */
+int output_vars(sphdem_ctx *c, SphDemOutputVars *out);
+
 /* adjoint.cu */
 void adjoint_free(sphdem_ctx *c);
 constexpr int ADJ_MODE_DEM = 1;   /* all-DEM handle: contacts, walls, leapfrog */

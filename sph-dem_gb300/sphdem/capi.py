@@ -30,6 +30,7 @@ FIELD_ALL = 0xFFFFFFFF
 FIELD_R, FIELD_V, FIELD_VHAT, FIELD_MASS = 1 << 0, 1 << 1, 1 << 2, 1 << 3
 FIELD_DENS, FIELD_H, FIELD_F, FIELD_DDDT = 1 << 4, 1 << 5, 1 << 6, 1 << 7
 FIELD_PRESS, FIELD_COUPLING, FIELD_OMEGA, FIELD_V0, FIELD_IAM = 1 << 8, 1 << 9, 1 << 10, 1 << 11, 1 << 12
+FIELD_ENERGY = 1 << 13
 
 D3 = C.c_double * 3
 I3 = C.c_int32 * 3
@@ -78,6 +79,7 @@ class SphDemParticles(C.Structure):
         ("porosity", P_F64), ("dporositydt", P_F64), ("shep_sum", P_F64), ("omega", P_F64),
         ("fdrag", P_F64), ("fvel", P_F64), ("grad_porosity", P_F64),
         ("v0", P_F64), ("vhat0", P_F64),
+        ("u", P_F64), ("dudt", P_F64), ("e_visc", P_F64), ("de_visc_dt", P_F64),
     ]
 
 
@@ -95,6 +97,22 @@ class SphDemGrads(C.Structure):
                 ("drag_scale", C.c_double), ("valid", C.c_uint32)]
 
 
+class SphDemOutputVars(C.Structure):
+    _fields_ = [("lin_mom", C.c_double * 3), ("ang_mom", C.c_double),
+                ("e_ke", C.c_double), ("e_elast", C.c_double), ("e_elast_exact", C.c_double),
+                ("ed_elast_dt", C.c_double), ("e_visc_f", C.c_double), ("ed_visc_f_dt", C.c_double),
+                ("e_ff", C.c_double), ("ed_ff_dt", C.c_double), ("e_visc_b", C.c_double),
+                ("e_b_force", C.c_double), ("e_total", C.c_double), ("max_v", C.c_double),
+                ("max_f", C.c_double), ("max_ff", C.c_double), ("rms_ff", C.c_double),
+                ("ave_dens", C.c_double), ("var_dens", C.c_double), ("ave_dens_from_mass", C.c_double),
+                ("n", C.c_int64), ("n_sph", C.c_int64)]
+
+    def as_dict(self) -> dict:
+        d = {k: getattr(self, k) for k, _ in self._fields_}
+        d["lin_mom"] = list(self.lin_mom)
+        return d
+
+
 class SphDemStats(C.Structure):
     _fields_ = [("n_particles", C.c_int64), ("n_alive", C.c_int64), ("n_list_pairs", C.c_int64),
                 ("list_depth", C.c_int64), ("n_sph_cells", C.c_int64), ("n_dem_cells", C.c_int64),
@@ -105,7 +123,7 @@ class SphDemStats(C.Structure):
 VEC_FIELDS = ("r", "v", "vhat", "norm1", "norm2", "norm3", "f", "fp", "fv", "fb",
               "fdrag", "fvel", "grad_porosity", "v0", "vhat0")
 SCA_FIELDS = ("mass", "dens", "h", "radius", "dddt", "press", "pdr2", "porosity",
-              "dporositydt", "shep_sum", "omega")
+              "dporositydt", "shep_sum", "omega", "u", "dudt", "e_visc", "de_visc_dt")
 
 
 def config_struct(cfg: dict, precision: int | None = None) -> SphDemConfig:
@@ -220,6 +238,7 @@ class Library:
         L.sphdem_cell_ids_noalloc.argtypes = [H, C.POINTER(C.c_int32)]
         D = C.POINTER(C.c_double)
         L.sphdem_adjoint_forward.argtypes = [H, C.c_int, C.c_int]
+        L.sphdem_output_vars.argtypes = [H, C.POINTER(SphDemOutputVars)]
         L.sphdem_adjoint_backward.argtypes = [H, D, D, D, C.POINTER(SphDemGrads), D, D, D]
         L.sphdem_batch_create.argtypes = [C.POINTER(H), C.c_int, C.POINTER(H)]
         L.sphdem_batch_destroy.argtypes = [H]
@@ -325,6 +344,12 @@ class Simulation:
         ms = C.c_double(0)
         self.L.check(self.L.lib.sphdem_time_steps(self.h, n, C.byref(ms)), self.h, "time_steps")
         return ms.value
+
+    def output_vars(self) -> dict:
+        """calcOutputVars of the current state (sphdem_output_vars)."""
+        o = SphDemOutputVars()
+        self.L.check(self.L.lib.sphdem_output_vars(self.h, C.byref(o)), self.h, "output_vars")
+        return o.as_dict()
 
     def adjoint_forward(self, nsteps: int, ckpt_every: int):
         self.L.check(self.L.lib.sphdem_adjoint_forward(self.h, nsteps, ckpt_every), self.h, "adjoint_forward")

@@ -66,6 +66,11 @@ def read_output(path) -> dict:
     out["cells"] = np.frombuffer(buf, "<i4", 3 * n, off).copy().reshape(n, 3)
     off += 12 * n
     out["time"], out["dt"] = struct.unpack_from("<dd", buf, off)
+    off += 16
+    if off + 8 <= len(buf):
+        (nov,) = struct.unpack_from("<q", buf, off)
+        off += 8
+        out["output_vars"] = np.frombuffer(buf, "<f8", nov, off).copy()
     return out
 
 

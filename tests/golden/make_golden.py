@@ -39,6 +39,8 @@ def make(name: str) -> str:
               "cells": out["cells"]}
     for k, v in out["fields"].items():
         arrays["field_" + k] = v
+    if "output_vars" in out:
+        arrays["output_vars"] = out["output_vars"]
     for k, (offs, idx) in out["pairs"].items():
         arrays["pairs_" + k + "_offs"] = offs
         arrays["pairs_" + k + "_idx"] = idx

@@ -24,7 +24,12 @@ FIELD_MAP = {"r": "r", "v": "v", "vhat": "vhat", "v0": "v0", "vhat0": "vhat0", "
              "press": "press", "pdr2": "pdr2", "porosity": "porosity",
              "dporositydt": "dporositydt", "gradPorosity": "grad_porosity",
              "shepSum": "shep_sum", "fdrag": "fdrag", "fvel": "fvel", "omega": "omega",
-             "mass": "mass"}
+             "mass": "mass", "u": "u", "dudt": "dudt", "eViscF": "e_visc", "deViscFdt": "de_visc_dt"}
+# calcOutputVars globals in the order the fixtures store them
+OUTPUT_VARS = ["lin_mom_x", "lin_mom_y", "lin_mom_z", "ang_mom", "e_ke", "e_elast", "e_elast_exact",
+               "ed_elast_dt", "e_visc_f", "ed_visc_f_dt", "e_ff", "ed_ff_dt", "e_visc_b", "e_b_force",
+               "e_total", "max_v", "max_f", "max_ff", "rms_ff", "ave_dens", "var_dens",
+               "ave_dens_from_mass", "n", "n_sph"]
 RTOL = 1e-11
 
 
@@ -40,11 +45,12 @@ def ran(request):
     assert case.n == int(g["meta_n"])
     o = OracleSim(case.cfg, case.particles)
     o.step(int(g["meta_nsteps"]))
-    return name, g, o, o.get(), o.globals()
+    ov = o.output_vars()   # on the lists of the last reset, before any rebuild below
+    return name, g, o, o.get(), o.globals(), ov
 
 
 def test_fields_match_reference(ran):
-    name, g, o, got, glob = ran
+    name, g, o, got, glob, ov = ran
     assert glob.time == pytest.approx(float(g["time"]), rel=1e-15)
     assert glob.dt == float(g["dt"])
     for k, ours in FIELD_MAP.items():
@@ -61,7 +67,7 @@ def test_fields_match_reference(ran):
 
 
 def test_pairs_and_cells_match_reference(ran):
-    name, g, o, got, glob = ran
+    name, g, o, got, glob, ov = ran
     o.rebuild()
     for kind, kname in PAIR_KIND_NAMES.items():
         key = "pairs_" + kname + "_offs"
@@ -72,6 +78,22 @@ def test_pairs_and_cells_match_reference(ran):
         ours = pair_set(po, pi)
         assert np.array_equal(ours, ref), f"{name}:{kname} {ours.size} vs {ref.size}"
     assert np.array_equal(o.cells(), g["cells"])
+
+
+def output_vars_vector(ov: dict) -> np.ndarray:
+    """A SphDemOutputVars dict in the fixtures' order."""
+    out = list(ov["lin_mom"])
+    out += [ov[k] for k in OUTPUT_VARS[3:]]
+    return np.array(out, dtype=np.float64)
+
+
+def test_output_vars_match_reference(ran):
+    name, g, o, got, glob, ov = ran
+    ref = g["output_vars"]
+    ours = output_vars_vector(ov)
+    assert ours.shape == ref.shape
+    for k, (a, b) in enumerate(zip(ours, ref)):
+        assert abs(a - b) <= 1e-9 * abs(b) + 1e-12, f"{name}:{OUTPUT_VARS[k]} ours {a!r} reference {b!r}"
 
 
 def test_golden_cases_are_not_trivial():
