@@ -157,6 +157,8 @@ typedef struct SphDemParticles {
 #define SPHDEM_FIELD_V0       (1u << 11)  /* v0, vhat0 */
 #define SPHDEM_FIELD_IAM      (1u << 12)
 #define SPHDEM_FIELD_ENERGY   (1u << 13)  /* u, dudt, e_visc, de_visc_dt */
+#define SPHDEM_FIELD_NORMALS  (1u << 14)  /* norm1, norm2, norm3 */
+#define SPHDEM_FIELD_RADIUS   (1u << 15)
 #define SPHDEM_FIELD_ALL      0xffffffffu
 
 /* Step globals: the CglobalVars members of the hot path, globalVars.h:196-220. */

@@ -737,6 +737,10 @@ const FieldMap kFields[] = {
     {SPHDEM_FIELD_OMEGA, FD_OMEGA, 1, &SphDemParticles::omega},
     {SPHDEM_FIELD_V0, FD_V0, 3, &SphDemParticles::v0},
     {SPHDEM_FIELD_V0, FD_VHAT0, 3, &SphDemParticles::vhat0},
+    {SPHDEM_FIELD_NORMALS, FD_N1, 3, &SphDemParticles::norm1},
+    {SPHDEM_FIELD_NORMALS, FD_N2, 3, &SphDemParticles::norm2},
+    {SPHDEM_FIELD_NORMALS, FD_N3, 3, &SphDemParticles::norm3},
+    {SPHDEM_FIELD_RADIUS, FD_RADIUS, 1, &SphDemParticles::radius},
     {SPHDEM_FIELD_ENERGY, FD_U, 1, &SphDemParticles::u},
     {SPHDEM_FIELD_ENERGY, FD_DUDT, 1, &SphDemParticles::dudt},
     {SPHDEM_FIELD_ENERGY, FD_EVISCF, 1, &SphDemParticles::e_visc},

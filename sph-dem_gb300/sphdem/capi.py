@@ -30,7 +30,7 @@ FIELD_ALL = 0xFFFFFFFF
 FIELD_R, FIELD_V, FIELD_VHAT, FIELD_MASS = 1 << 0, 1 << 1, 1 << 2, 1 << 3
 FIELD_DENS, FIELD_H, FIELD_F, FIELD_DDDT = 1 << 4, 1 << 5, 1 << 6, 1 << 7
 FIELD_PRESS, FIELD_COUPLING, FIELD_OMEGA, FIELD_V0, FIELD_IAM = 1 << 8, 1 << 9, 1 << 10, 1 << 11, 1 << 12
-FIELD_ENERGY = 1 << 13
+FIELD_ENERGY, FIELD_NORMALS, FIELD_RADIUS = 1 << 13, 1 << 14, 1 << 15
 
 D3 = C.c_double * 3
 I3 = C.c_int32 * 3
@@ -309,6 +309,9 @@ class Simulation:
         g = SphDemGlobals()
         self.L.check(self.L.lib.sphdem_get_globals(self.h, C.byref(g)), self.h, "get_globals")
         return g
+
+    def set_globals(self, g: SphDemGlobals):
+        self.L.check(self.L.lib.sphdem_set_globals(self.h, C.byref(g)), self.h, "set_globals")
 
     def stats(self) -> SphDemStats:
         st = SphDemStats()
