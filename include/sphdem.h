@@ -63,6 +63,11 @@ extern "C" {
 #define SPHDEM_F_LIQ_DEM          (1u << 3)  /* LIQ_DEM: DEM + coupling         */
 #define SPHDEM_F_FIXED_DT         (1u << 4)  /* dt == maxdt every step          */
 #define SPHDEM_F_DEM_ONLY_CONTACT (1u << 5)  /* reserved                        */
+#define SPHDEM_F_CORRECTED_GRADIENT (1u << 6) /* CORRECTED_GRADIENT (calcInvM, sph.h:394-434);
+                                                 FP64 precision, no LIQ_DEM */
+#define SPHDEM_F_DEM_BLOCK        (1u << 7)  /* DEM_BLOCK: every DEM particle takes the mean
+                                                 DEM force before the end kick
+                                                 (sphIncompress.cpp:231-238); needs LIQ_DEM */
 
 /* ---- precision of the pair kernels ------------------------------------- */
 #define SPHDEM_PREC_FP64   0   /* everything in FP64                                  */
@@ -115,6 +120,10 @@ typedef struct SphDemConfig {
     SphDemWall walls[SPHDEM_MAX_WALLS];
     double   drag_scale;           /* factor on the Di Felice drag force of calcParticleDrag
                                       (sph.h:1593-1598); 0 is read as 1, the reference's law */
+    int32_t  reinit_dens_every;    /* REINIT_DENS_EVERY_N_STEPS: density re-initialisation of
+                                      start() (sphIncompress.cpp:19-35) every that many steps;
+                                      0 = never */
+    int32_t  reinit_dens_at;       /* REINIT_DENS_AT_N_STEPS: and at that step (<= 0: never) */
 } SphDemConfig;
 
 /* Host-side particle arrays (structure of arrays).  Vector fields hold three
@@ -299,7 +308,8 @@ int sphdem_adjoint_backward(sphdem_handle h, const double *dL_dr, const double *
  * step whose branches are the members' own step sequences.  Members stay
  * usable on their own (get/set fields, stats); a batch call orders itself
  * after their pending work and their later calls after it.  Destroy the
- * batch before its members. */
+ * batch before its members.  A member with a density re-initialisation
+ * (reinit_dens_every / reinit_dens_at) gives SPHDEM_ERR_UNSUPPORTED. */
 typedef struct sphdem_batch_ctx *sphdem_batch;
 
 int sphdem_batch_create(const sphdem_handle *members, int n, sphdem_batch *out);

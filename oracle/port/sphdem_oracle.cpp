@@ -48,6 +48,7 @@ struct Part {
     double norm1[3], norm2[3], norm3[3];
     double mass, dens, dddt, h, press, pdr2, omega, porosity, dpordt, shep, radius;
     double u, dudt, eViscF, deViscFdt;   /* calcEnergies integrals (sphIncompress.h:769-781) */
+    double invM[9], sumGrad[3], sum;     /* CORRECTED_GRADIENT (particle.h:243-246) */
 };
 
 /* A bucket entry: particle index plus the periodic image it stands for. */
@@ -101,14 +102,27 @@ struct Sim {
     }
     bool var_h() const { return c.flags & SPHDEM_F_VAR_H_CORRECTION; }
     bool liq_dem() const { return c.flags & SPHDEM_F_LIQ_DEM; }
-    /* gradW, sph.h:322-342 (no CORRECTED_GRADIENT) */
+    bool corrected() const { return c.flags & SPHDEM_F_CORRECTED_GRADIENT; }
+    /* gradW, sph.h:322-342; with CORRECTED_GRADIENT the product
+     * invM_a ((dr F - sumGrad_a/sum_a)/sum_a) (vect.h:39-47 row by row) */
     void gradW(const Part &pa, const double *dr, double q, double h, double *out) const {
         double drF[3] = {0, 0, 0};
         if (q != 0) {
             const double fq = F(q, h);
             for (int i = 0; i < nd; i++) drF[i] = dr[i] * fq;
         }
-        for (int i = 0; i < nd; i++) out[i] = var_h() ? drF[i] / pa.omega : drF[i];
+        double ret[3] = {0, 0, 0};
+        if (corrected()) {
+            double t[3] = {0, 0, 0};
+            for (int i = 0; i < nd; i++) t[i] = (drF[i] - pa.sumGrad[i] / pa.sum) / pa.sum;
+            for (int i = 0; i < nd; i++) {
+                ret[i] = 0.0;
+                for (int j = 0; j < nd; j++) ret[i] += pa.invM[i * nd + j] * t[j];
+            }
+        } else {
+            for (int i = 0; i < nd; i++) ret[i] = drF[i];
+        }
+        for (int i = 0; i < nd; i++) out[i] = var_h() ? ret[i] / pa.omega : ret[i];
     }
     static bool is_boundary(int t) { return t == T_BOUNDARY || (t >= T_BOBJ1 && t <= T_BOBJ6); }
 
@@ -487,6 +501,115 @@ struct Sim {
             }
         }
         p.omega = 1 + p.h * p.omega / (p.dens * nd);
+    }
+
+    /* inverseSym, vect.h:49-111: adjugate over determinant, identity if singular */
+    void inverse_sym(double *a) const {
+        if (nd == 2) {
+            const double A = a[0], B = a[1], C = a[2], D = a[3];
+            const double det = (A * D - B * C);
+            if (det != 0.0) {
+                a[0] = D / det;
+                a[1] = -B / det;
+                a[2] = -C / det;
+                a[3] = A / det;
+            } else {
+                a[0] = 1.0; a[1] = 0.0; a[2] = 0.0; a[3] = 1.0;
+            }
+            return;
+        }
+        if (nd == 1) {   /* not defined by the reference (2D and 3D only) */
+            a[0] = a[0] != 0.0 ? 1.0 / a[0] : 1.0;
+            return;
+        }
+        const double A0 = a[0], B0 = a[1], C0 = a[2], D0 = a[3], E0 = a[4], F0 = a[5], G0 = a[6], H0 = a[7],
+                     K0 = a[8];
+        const double cA = (E0 * K0 - F0 * H0), cB = (F0 * G0 - D0 * K0), cC = (D0 * H0 - E0 * G0);
+        const double cD = (C0 * H0 - B0 * K0), cE = (A0 * K0 - C0 * G0), cF = (B0 * G0 - A0 * H0);
+        const double cG = (B0 * F0 - C0 * E0), cH = (C0 * D0 - A0 * F0), cK = (A0 * E0 - B0 * D0);
+        const double Z = A0 * (E0 * K0 - F0 * H0) + B0 * (F0 * G0 - K0 * D0) + C0 * (D0 * H0 - E0 * G0);
+        if (Z != 0) {
+            const double o[9] = {cA, cD, cG, cB, cE, cH, cC, cF, cK};
+            for (int k = 0; k < 9; k++) a[k] = o[k] / Z;
+        } else {
+            for (int k = 0; k < 9; k++) a[k] = (k % 4 == 0) ? 1.0 : 0.0;
+        }
+    }
+
+    /* calcInvM, sph.h:393-434 */
+    void calc_invm(Part &p, const std::vector<Entry> &nb) {
+        for (int k = 0; k < 9; k++) p.invM[k] = 0.0;
+        p.sum = (p.mass / p.dens) * Wk(0, p.h);
+        for (int i = 0; i < 3; i++) p.sumGrad[i] = 0.0;
+        if (nb.empty()) {
+            for (int i = 0; i < nd; i++) p.invM[nd * i + i] = 1.0;
+            return;
+        }
+        for (const Entry &e : nb) {
+            const Part &pn = ps[e.idx];
+            if (!sph_or_sphb(pn.iam)) continue;
+            double rb[3], dr[3] = {0, 0, 0};
+            epos(e, rb);
+            for (int i = 0; i < nd; i++) dr[i] = p.r[i] - rb[i];
+            const double r = len(dr);
+            const double dvol = pn.mass / pn.dens;
+            const double hav = 0.5 * (p.h + pn.h);
+            const double q = r / hav;
+            const double Fa = F(q, hav);
+            const double Wab = Wk(q, hav);
+            p.sum += dvol * Wab;
+            for (int i = 0; i < nd; i++) p.sumGrad[i] += (dvol * dr[i]) * Fa;
+        }
+        for (const Entry &e : nb) {
+            const Part &pn = ps[e.idx];
+            if (!sph_or_sphb(pn.iam)) continue;
+            double rb[3], dr[3] = {0, 0, 0}, g[3] = {0, 0, 0};
+            epos(e, rb);
+            for (int i = 0; i < nd; i++) dr[i] = p.r[i] - rb[i];
+            const double r = len(dr);
+            const double dvol = pn.mass / pn.dens;
+            const double hav = 0.5 * (p.h + pn.h);
+            const double Fa = F(r / hav, hav);
+            for (int i = 0; i < nd; i++) g[i] = (dr[i] * Fa - p.sumGrad[i] / p.sum) / p.sum;
+            for (int i = 0; i < nd; i++)
+                for (int j = 0; j < nd; j++) p.invM[i * nd + j] -= (pn.mass / pn.dens) * (g[i] * dr[j]);
+        }
+        inverse_sym(p.invM);
+    }
+
+    /* the density re-initialisation of start(), sphIncompress.cpp:19-35:
+     * a reset, then ten rounds of calcHFromDens (sph.h:1823-1825) and
+     * calcDensity (sph.h:1172-1184).  The neighbour lists are built on their
+     * first use, after the first calcHFromDens (dataLL.impl.h:230-240). */
+    void reinit_density() {
+        reset();
+        const int n = ps.size();
+        for (int it = 0; it < 10; it++) {
+            for (auto &p : ps)
+                if (p.alive && sph_or_sphb(p.iam)) p.h = c.hfac * std::pow(p.mass / p.dens, 1.0 / nd);
+            if (it == 0) {
+                nbrs.assign(n, std::vector<Entry>());
+                for (int k : order) calc_neighbours(k, nbrs[k]);
+            }
+            for (int k = 0; k < n; k++) {
+                Part &p = ps[k];
+                if (!p.alive || !sph_or_sphb(p.iam)) continue;
+                p.dens = p.mass * Wk(0, p.h);
+                for (const Entry &e : nbrs[k]) {
+                    const Part &pn = ps[e.idx];
+                    if (!sph_or_sphb(pn.iam)) continue;
+                    double rb[3], dr[3] = {0, 0, 0};
+                    epos(e, rb);
+                    for (int i = 0; i < nd; i++) dr[i] = p.r[i] - rb[i];
+                    const double r = len(dr);
+                    p.dens += pn.mass * Wk(r / p.h, p.h);
+                }
+            }
+        }
+    }
+    bool reinit_due() const {
+        return (c.reinit_dens_every > 0 && step % c.reinit_dens_every == 0) ||
+               (c.reinit_dens_at > 0 && step == c.reinit_dens_at);
     }
 
     void visc_force(Part &pa, const Part &pb, const double *dx, const double *gw, const double *dv, double r) {
@@ -879,6 +1002,7 @@ struct Sim {
         for (auto &p : ps)
             if (p.alive && sph_or_sphb(p.iam)) drift_rest(p, h);
         time += dt / 2;
+        if (reinit_due()) reinit_density();
         for (auto &p : ps)
             if (p.alive && sph_or_sphb(p.iam)) init_sums_middle(p);
     }
@@ -914,6 +1038,9 @@ struct Sim {
             for (auto &p : ps)
                 if (p.alive && is_boundary(p.iam)) p.porosity = 1.0;
         }
+        if (corrected())
+            for (int k = 0; k < n; k++)
+                if (ps[k].alive && sph_or_sphb(ps[k].iam)) calc_invm(ps[k], nbrs[k]);
         if (var_h())
             for (int k = 0; k < n; k++)
                 if (ps[k].alive && sph_or_sphb(ps[k].iam)) calc_omega(ps[k], nbrs[k]);
@@ -951,6 +1078,9 @@ struct Sim {
         time += dt / 2;
         reset();
         const int n = ps.size();
+        if (corrected())
+            for (int k = 0; k < n; k++)
+                if (ps[k].alive && sph_or_sphb(ps[k].iam)) calc_invm(ps[k], nbrs[k]);
         if (var_h())
             for (int k = 0; k < n; k++)
                 if (ps[k].alive && sph_or_sphb(ps[k].iam)) calc_omega(ps[k], nbrs[k]);
@@ -967,6 +1097,20 @@ struct Sim {
                 }
             for (int k = 0; k < n; k++)
                 if (ps[k].alive && ps[k].iam == T_DEM) calc_dem_contacts(ps[k], nbrs[k]);
+            if (c.flags & SPHDEM_F_DEM_BLOCK) {
+                /* DEM_BLOCK, sphIncompress.cpp:231-238: calcAvForce, mean, setAvForce
+                 * (sphIncompress.h:107-114), in traverse order */
+                double av[3] = {0, 0, 0}, cnt = 0;
+                for (int k : order)
+                    if (ps[k].alive && ps[k].iam == T_DEM) {
+                        for (int i = 0; i < 3; i++) av[i] += ps[k].f[i];
+                        cnt++;
+                    }
+                for (int i = 0; i < 3; i++) av[i] = av[i] / cnt;
+                for (auto &p : ps)
+                    if (p.alive && p.iam == T_DEM)
+                        for (int i = 0; i < 3; i++) p.f[i] = av[i];
+            }
             for (auto &p : ps)
                 if (p.alive && p.iam == T_DEM) kick(p, 0.5 * dt, 0.5 * dt);
         }

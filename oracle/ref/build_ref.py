@@ -80,11 +80,17 @@ def customconstants(case: cases.Case) -> str:
         lines.append("#define CONST_H")
     if flags & cases.F_VAR_H_CORRECTION:
         lines.append("#define VAR_H_CORRECTION")
+    if flags & cases.F_CORRECTED_GRADIENT:
+        lines.append("#define CORRECTED_GRADIENT")
+    if flags & cases.F_DEM_BLOCK:
+        lines.append("#define DEM_BLOCK")
+    every = int(c.get("reinit_dens_every", 0))
+    at = int(c.get("reinit_dens_at", 0))
     n = case.n
     lines += [
         "const int OUTSTEP = 1000000;", "const int RESTART_EVERY_N_STEPS = 1000000;",
-        "const int REINIT_DENS_EVERY_N_STEPS = 2000000000;",
-        "const int REINIT_DENS_AT_N_STEPS = -1;",
+        "const int REINIT_DENS_EVERY_N_STEPS = %d;" % (every if every > 0 else 2000000000),
+        "const int REINIT_DENS_AT_N_STEPS = %d;" % (at if at > 0 else -1),
         "const double MAXTIME = 1e30;",
         "const double DAMPTIME = %s;" % _f(c["damptime"]),
         "const double VREF = 1.0;", "const double REYNOLDS_NUMBER = 1.0;",
@@ -101,6 +107,7 @@ def customconstants(case: cases.Case) -> str:
         "const double APPROX_SMOOTH_GRID_SIZE = H;", "const double SMOOTH_GRID_SIZE = H;",
         "const double GRIDSEP = PSEP;", "#define MIN_ALPHA 0.1",
         "const double ORACLE_MAXDT = %s;" % _f(c["maxdt"]),
+        "const bool ORACLE_FIXED_DT = %s;" % ("true" if flags & cases.F_FIXED_DT else "false"),
     ]
     if flags & cases.F_LIQ_DEM:
         ndem = int((case.particles["iam"] == cases.DEM).sum())

@@ -138,7 +138,8 @@ int main(int argc, char **argv) {
     const double sec = (t1.tv_sec - t0.tv_sec) + 1e-6 * (t1.tv_usec - t0.tv_usec);
     fprintf(stderr, "ref_driver: n=%zu steps=%d sec=%.6f particle_steps_per_s=%.6e dt_changed=%d\n",
             ps.size(), nsteps, sec, ps.size() * (double)nsteps / (sec > 0 ? sec : 1e-30), dt_changed);
-    if (timing_only) return dt_changed ? 3 : 0;
+    /* a fixed-dt case must keep the reference's adaptive dt at maxdt */
+    if (timing_only) return (ORACLE_FIXED_DT && dt_changed) ? 3 : 0;
 
     /* tag -> position in ps (periodic exchange reorders ps) */
     std::vector<long long> row_of_tag(n + 1, -1);
@@ -292,5 +293,5 @@ int main(int argc, char **argv) {
     fwrite(&nov, 8, 1, out);
     fwrite(ov.data(), 8, ov.size(), out);
     fclose(out);
-    return dt_changed ? 3 : 0;
+    return (ORACLE_FIXED_DT && dt_changed) ? 3 : 0;
 }

@@ -916,6 +916,9 @@ std::string adjoint_supported(sphdem_ctx *c, int *mode) {
     const DevCfg &cfg = c->cfg;
     *mode = 0;
     if (!(cfg.flags & SPHDEM_F_FIXED_DT)) return "the adjoint needs a fixed time step";
+    if (cfg.flags & SPHDEM_F_CORRECTED_GRADIENT) return "the adjoint does not cover CORRECTED_GRADIENT";
+    if (cfg.flags & SPHDEM_F_DEM_BLOCK) return "the adjoint does not cover DEM_BLOCK";
+    if (reinit_configured(c->host_cfg)) return "the adjoint does not cover density re-initialisation";
     if (cfg.damptime > 0) return "the adjoint does not cover velocity damping";
     std::vector<int> iam(c->n);
     field_get_int(c, FI_IAM, iam.data());

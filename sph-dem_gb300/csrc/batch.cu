@@ -123,6 +123,10 @@ int sphdem_batch_create(const sphdem_handle *members, int n, sphdem_batch *out) 
     for (int i = 0; i < n; i++)
         for (int j = 0; j < i; j++)
             if (members[i] == members[j]) return SPHDEM_ERR_INVALID;
+    /* a density re-initialisation step rebuilds once more than the others,
+     * which one shared graph per step cannot follow */
+    for (int i = 0; i < n; i++)
+        if (sphdem::reinit_configured(members[i]->host_cfg)) return SPHDEM_ERR_UNSUPPORTED;
     sphdem_batch_ctx *b = new sphdem_batch_ctx;
     b->members.assign(members, members + n);
     b->ev_join.assign(n, nullptr);

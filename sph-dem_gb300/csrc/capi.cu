@@ -220,6 +220,12 @@ std::string validate(const SphDemConfig *cfg, const SphDemParticles *p, int64_t 
     if (cfg->n_walls < 0 || cfg->n_walls > SPHDEM_MAX_WALLS) return "n_walls out of range";
     for (int d = 0; d < cfg->ndim; d++)
         if (!(cfg->domain_max[d] > cfg->domain_min[d])) return "empty binning domain";
+    if (cfg->flags & SPHDEM_F_CORRECTED_GRADIENT) {
+        if (cfg->precision != SPHDEM_PREC_FP64) return "CORRECTED_GRADIENT is carried by the FP64 path only";
+        if (cfg->flags & SPHDEM_F_LIQ_DEM) return "CORRECTED_GRADIENT is not combined with LIQ_DEM";
+    }
+    if (cfg->reinit_dens_every < 0) return "reinit_dens_every must be >= 0";
+    if ((cfg->flags & SPHDEM_F_DEM_BLOCK) && !(cfg->flags & SPHDEM_F_LIQ_DEM)) return "DEM_BLOCK needs LIQ_DEM";
     if ((cfg->flags & SPHDEM_F_LIQ_DEM) && !(cfg->dem_search_radius > 0 && cfg->coupling_radius > 0))
         return "LIQ_DEM needs dem_search_radius and coupling_radius";
     if ((cfg->flags & SPHDEM_F_LIQ_DEM) && cfg->precision == SPHDEM_PREC_MIXED) {
@@ -277,7 +283,9 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->mx_bandq);
     cudaFree(c->mx_bandn);
     cudaFree(c->dcfg);
-    for (int k = 0; k < 2; k++)
+    cudaFree(c->cg);
+    cudaFree(c->hpred);
+    for (int k = 0; k < 4; k++)
         if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -315,6 +323,7 @@ void run_phase_mixed(sphdem_ctx *c, int phase) {
                 mixed::dddt(c);  /* Omega (VAR_H_CORRECTION) is summed inside the continuity pass */
             }
             if (liq) mixed::dem_end(c);
+            if (c->host_cfg.flags & SPHDEM_F_DEM_BLOCK) run_dem_block(c);
             run_end_tail(c);
             break;
     }
@@ -329,9 +338,11 @@ void run_phase(sphdem_ctx *c, int phase) {
     switch (phase) {
         case SPHDEM_HOOK_BEFORE_START:
             globals_op(c, OP_STEP_INC);
+            c->host_step++;
             break;
         case SPHDEM_PHASE_START:
             run_start(c);
+            if (reinit_due(c->host_cfg, c->host_step)) run_reinit_density(c);
             break;
         case SPHDEM_HOOK_BEFORE_MIDDLE:
             run_hook_before_middle(c);
@@ -343,6 +354,7 @@ void run_phase(sphdem_ctx *c, int phase) {
                 run_porosity(c);
                 run_dem_drag(c);
             }
+            if (corrected_gradient(c)) run_invm(c);
             run_omega_eos(c, c->cfg.var_h(), true);
             run_force(c);
             if (liq) run_dem_accel(c);
@@ -355,9 +367,11 @@ void run_phase(sphdem_ctx *c, int phase) {
         case SPHDEM_PHASE_END:
             run_end_drift(c);
             rebuild(c);
+            if (corrected_gradient(c)) run_invm(c);
             if (c->cfg.var_h()) run_omega_eos(c, true, false);
             run_dddt(c);
             if (liq) run_dem_end(c);
+            if (c->host_cfg.flags & SPHDEM_F_DEM_BLOCK) run_dem_block(c);
             run_end_tail(c);
             break;
         case SPHDEM_HOOK_AFTER_END:
@@ -474,6 +488,9 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
         SPHDEM_CUDA_CHECK(cudaMalloc(&b.fill, (size_t)b.cells_cap * sizeof(int)));
         SPHDEM_CUDA_CHECK(cudaMalloc(&b.bsum, ((size_t)b.cells_cap / 4096 + 2) * sizeof(int)));
         setup_rebuild_buffers(c);
+        if (cfg->flags & SPHDEM_F_CORRECTED_GRADIENT)
+            SPHDEM_CUDA_CHECK(cudaMalloc(&c->cg, (size_t)CG_ROWS * capacity * sizeof(double)));
+        if (reinit_configured(*cfg)) SPHDEM_CUDA_CHECK(cudaMalloc(&c->hpred, capacity * sizeof(double)));
 
         /* globals as the CdataLL constructor leaves them (dataLL.cpp:8-40) */
         DevGlobals hg;
@@ -588,18 +605,26 @@ int sphdem_step(sphdem_handle h, int nsteps) {
                 run_full_step(h);
                 continue;
             }
-            cudaGraphExec_t &ge = h->graph[h->flipped ? 1 : 0];
+            /* a step that re-initialises the density rebuilds once more, so
+             * it has its own graphs and may leave the other parity behind */
+            const int key = (h->flipped ? 1 : 0) | (reinit_due(h->host_cfg, h->host_step + 1) ? 2 : 0);
+            cudaGraphExec_t &ge = h->graph[key];
             if (!ge) {
                 cudaGraph_t graph;
                 h->in_capture = true;
                 SPHDEM_CUDA_CHECK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-                const bool flipped0 = h->flipped;
-                run_full_step(h);
+                run_full_step(h);   /* advances host_step and the parity */
                 h->in_capture = false;
                 SPHDEM_CUDA_CHECK(cudaStreamEndCapture(h->stream, &graph));
-                if (h->flipped != flipped0) throw std::string("a step must rebuild an even number of times");
+                h->graph_end_flip[key] = h->flipped;
                 SPHDEM_CUDA_CHECK(cudaGraphInstantiate(&ge, graph, 0));
                 cudaGraphDestroy(graph);
+            } else {
+                h->host_step++;
+                if (h->flipped != h->graph_end_flip[key]) {
+                    std::swap(h->A, h->B);
+                    h->flipped = h->graph_end_flip[key];
+                }
             }
             SPHDEM_CUDA_CHECK(cudaGraphLaunch(ge, h->stream));
         }
@@ -703,6 +728,7 @@ int sphdem_set_globals(sphdem_handle h, const SphDemGlobals *in) {
     hg.step = in->sph_step;
     if (cudaMemcpy(h->g, &hg, sizeof(hg), cudaMemcpyHostToDevice) != cudaSuccess)
         return fail(h, SPHDEM_ERR_CUDA, "cannot write globals");
+    h->host_step = in->sph_step;
     cudaDeviceSynchronize();
     return SPHDEM_OK;
 }

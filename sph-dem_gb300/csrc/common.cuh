@@ -118,6 +118,7 @@ struct DevGlobals {
     int n_total_cells;                /* SPH + DEM buckets (+1 dead bucket) */
     int n_alive;
     long long n_deleted;
+    double dem_avf[3];                /* DEM_BLOCK: mean DEM force of the end phase */
     unsigned int err;                 /* SPHDEM error bits (1 << code) */
     int err_info;
 };
@@ -318,6 +319,40 @@ __device__ __forceinline__ void scan_cells(const CellCoord &cc, const int *dims,
                 const int b0 = start[base + lin], b1 = start[base + lin + 1];
                 for (int b = b0; b < b1; b++) body(b, sh);
             }
+}
+
+/* h = HFAC (m/rho)^(1/NDIM) (sphIncompress.h:698-700).  The FP64 path calls
+ * pow like the reference; the mixed path takes an FP32 estimate of
+ * x^(-1/NDIM) and one FP64 Newton step (relative error ~1e-14), because FP64
+ * pow costs hundreds of FP64 operations on this GPU. */
+__device__ __forceinline__ double smoothing_length(const DevCfg &c, double x) {
+    if (c.precision != SPHDEM_PREC_MIXED) return c.hfac * pow(x, 1.0 / c.nd);
+    if (c.nd == 1) return c.hfac * x;
+    if (c.nd == 2) {
+        double z = (double)rsqrtf((float)x);
+        z = z * (1.5 - 0.5 * x * z * z);
+        return c.hfac * x * z;
+    }
+    double z = (double)(1.0f / cbrtf((float)x));
+    z = z * (4.0 - x * z * z * z) * (1.0 / 3.0);
+    return c.hfac * x * z * z;
+}
+
+/* 1/h by an FP32 estimate and one FP64 Newton step in the mixed path */
+__device__ __forceinline__ double recip(const DevCfg &c, double h) {
+    if (c.precision != SPHDEM_PREC_MIXED) return 1.0 / h;
+    double y = (double)(1.0f / (float)h);
+    return y * (2.0 - h * y);
+}
+
+__device__ __forceinline__ void h_derived(const DevCfg &c, const DevState &s, int64_t i) {
+    const double h = s.row(FD_H)[i];
+    const double ih = recip(c, h);
+    double ihn = ih;
+    for (int d = 1; d < c.nd; d++) ihn *= ih;
+    s.row(FD_IH)[i] = ih;
+    s.row(FD_IHN)[i] = ihn;
+    s.row(FD_IHN2)[i] = ihn * ih * ih;
 }
 
 }  // namespace sphdem

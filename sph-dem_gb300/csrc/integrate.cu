@@ -45,40 +45,6 @@ __global__ void k_globals_op(DevCfg c, DevGlobals *g, int op) {
     }
 }
 
-/* h = HFAC (m/rho)^(1/NDIM) (sphIncompress.h:698-700).  The FP64 path calls
- * pow like the reference; the mixed path takes an FP32 estimate of
- * x^(-1/NDIM) and one FP64 Newton step (relative error ~1e-14), because FP64
- * pow costs hundreds of FP64 operations on this GPU. */
-__device__ __forceinline__ double smoothing_length(const DevCfg &c, double x) {
-    if (c.precision != SPHDEM_PREC_MIXED) return c.hfac * pow(x, 1.0 / c.nd);
-    if (c.nd == 1) return c.hfac * x;
-    if (c.nd == 2) {
-        double z = (double)rsqrtf((float)x);
-        z = z * (1.5 - 0.5 * x * z * z);
-        return c.hfac * x * z;
-    }
-    double z = (double)(1.0f / cbrtf((float)x));
-    z = z * (4.0 - x * z * z * z) * (1.0 / 3.0);
-    return c.hfac * x * z * z;
-}
-
-/* 1/h by an FP32 estimate and one FP64 Newton step in the mixed path */
-__device__ __forceinline__ double recip(const DevCfg &c, double h) {
-    if (c.precision != SPHDEM_PREC_MIXED) return 1.0 / h;
-    double y = (double)(1.0f / (float)h);
-    return y * (2.0 - h * y);
-}
-
-__device__ __forceinline__ void h_derived(const DevCfg &c, const DevState &s, int64_t i) {
-    const double h = s.row(FD_H)[i];
-    const double ih = recip(c, h);
-    double ihn = ih;
-    for (int d = 1; d < c.nd; d++) ihn *= ih;
-    s.row(FD_IH)[i] = ih;
-    s.row(FD_IHN)[i] = ihn;
-    s.row(FD_IHN2)[i] = ihn * ih * ih;
-}
-
 __device__ __forceinline__ void eos(const DevCfg &c, const DevState &s, int64_t i) {
     const double dens = s.row(FD_DENS)[i];
     double press;
@@ -219,7 +185,9 @@ __global__ void k_end_tail(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
     if (c.liq_dem() && t == T_DEM) {
         const double k = 0.5 * dt + 0.5 * dt;
         const bool damp = g->time < c.damptime;
+        const bool block = c.flags & SPHDEM_F_DEM_BLOCK;
         for (int d = 0; d < c.nd; d++) {
+            if (block) s.row(FD_F + d)[i] = g->dem_avf[d];   /* setAvForce, sphIncompress.h:112-114 */
             const double f = s.row(FD_F + d)[i];
             double v = s.row(FD_V0 + d)[i] + k * f;
             double vh = s.row(FD_VHAT0 + d)[i] + k * f;
@@ -247,6 +215,33 @@ __global__ void k_end_tail(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
             s.row(FD_DEVISCF)[i] = -w;
             s.row(FD_EVISCF)[i] += dt * (-w);
         }
+    }
+}
+
+/* DEM_BLOCK: calcAvForce over the DEM particles (sphIncompress.h:107-110) and
+ * the mean (sphIncompress.cpp:232-236).  One block, a fixed reduction tree:
+ * the same sum on every run. */
+constexpr int AVF_BLK = 1024;
+__global__ void __launch_bounds__(AVF_BLK) k_dem_block(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
+    __shared__ double sh[4][AVF_BLK / 32];
+    double acc[4] = {0, 0, 0, 0};
+    for (int64_t i = threadIdx.x; i < n; i += AVF_BLK) {
+        if (s.irow(FI_IAM)[i] != T_DEM) continue;
+        for (int d = 0; d < c.nd; d++) acc[d] += s.row(FD_F + d)[i];
+        acc[3] += 1.0;
+    }
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int k = 0; k < 4; k++) {
+        double v = acc[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) sh[k][w] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t[4] = {0, 0, 0, 0};
+        for (int k = 0; k < 4; k++)
+            for (int j = 0; j < AVF_BLK / 32; j++) t[k] += sh[k][j];
+        for (int d = 0; d < 3; d++) g->dem_avf[d] = t[3] > 0 ? t[d] / t[3] : 0.0;
     }
 }
 
@@ -334,6 +329,9 @@ void run_middle_tail(sphdem_ctx *c) {
 }
 void run_end_drift(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "end_drift", k_end_drift, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, c->g, c->n);
+}
+void run_dem_block(sphdem_ctx *c) {
+    SPHDEM_LAUNCH(c, "dem_block", k_dem_block, 1, AVF_BLK, 0, c->cfg, c->A, c->g, c->n);
 }
 void run_end_tail(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "end_tail", k_end_tail, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, c->g, c->n);

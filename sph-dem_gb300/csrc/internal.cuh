@@ -53,8 +53,15 @@ struct sphdem_ctx {
     sphdem::Buffers buf;
     cudaStream_t stream = nullptr;
     std::string err;
-    /* CUDA graph of one full step, per state parity */
-    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    /* CUDA graphs of one full step, keyed by the state parity at its start
+     * (bit 0) and whether the step re-initialises the density (bit 1), with
+     * the parity each leaves behind */
+    cudaGraphExec_t graph[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool graph_end_flip[4] = {false, false, false, false};
+    long long host_step = 0;  /* host copy of the device step counter (sphStep) */
+    /* CORRECTED_GRADIENT rows (CG_ROWS x cap) and the density re-initialisation's
+     * first smoothing length (cap) */
+    double *cg = nullptr, *hpred = nullptr;
     bool in_capture = false;
     /* timing */
     bool timing = false;
@@ -92,6 +99,17 @@ struct sphdem_ctx {
 
 namespace sphdem {
 
+/* CORRECTED_GRADIENT rows per particle: invM (nd x nd, row-major),
+ * sumGrad/sum, sum */
+enum : int { CG_M = 0, CG_C = 9, CG_S = 12, CG_ROWS = 13 };
+inline bool corrected_gradient(const sphdem_ctx *c) { return c->host_cfg.flags & SPHDEM_F_CORRECTED_GRADIENT; }
+inline bool reinit_configured(const SphDemConfig &c) { return c.reinit_dens_every > 0 || c.reinit_dens_at > 0; }
+/* start() of step `step` re-initialises the density (sphIncompress.cpp:20) */
+inline bool reinit_due(const SphDemConfig &c, long long step) {
+    return (c.reinit_dens_every > 0 && step % c.reinit_dens_every == 0) ||
+           (c.reinit_dens_at > 0 && step == c.reinit_dens_at);
+}
+
 /* launch bracket: records events around a launch when timing is enabled */
 void launch_begin(sphdem_ctx *c, const char *name);
 void launch_end(sphdem_ctx *c);
@@ -119,6 +137,9 @@ void run_omega_eos(sphdem_ctx *c, bool omega, bool eos);
 void run_force(sphdem_ctx *c);         /* calcForce + accelCondition        */
 void run_dem_accel(sphdem_ctx *c);
 void run_dddt(sphdem_ctx *c);          /* calcDddtDudt                      */
+void run_invm(sphdem_ctx *c);
+void run_dem_block(sphdem_ctx *c);     /* DEM_BLOCK: mean DEM force     */          /* calcInvM (CORRECTED_GRADIENT)     */
+void run_reinit_density(sphdem_ctx *c); /* reset + ten rounds of calcHFromDens and calcDensity */
 void run_dem_end(sphdem_ctx *c);       /* calcFPI + calcDEMContacts         */
 
 void zero_dem_shep(sphdem_ctx *c);

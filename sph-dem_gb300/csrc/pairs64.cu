@@ -12,6 +12,12 @@
  *   k_dddt      calcDddtDudt                      sphIncompress.h:783-851
  *   k_dem_end   calcFPI + calcParticleDrag + calcDEMContacts
  *                                                 sph.h:1708-1792, 1575-1631, 1676-1706
+ *   k_invm      calcInvM + inverseSym (CORRECTED_GRADIENT)
+ *                                                 sph.h:393-434, vect.h:49-111
+ *   k_reinit_h, k_reinit_dens
+ *               the density re-initialisation of start(): ten rounds of
+ *               calcHFromDens + calcDensity       sphIncompress.cpp:19-35,
+ *                                                 sph.h:1823-1825, 1172-1184
  *
  * Neighbour sets are those of the reference exactly: the same 3^d bucket
  * stencil, the FP64 predicate |r_a-r_b|^2 <= (2 max(h_a,h_b))^2 evaluated
@@ -248,7 +254,194 @@ __device__ __forceinline__ void calc_normal(const DevCfg &c, const DevState &s, 
         for (int d = 0; d < 3; d++) normp[d] = n2[d];
 }
 
-__global__ void k_force(DevCfg c, DevState s, const int *start, const int *skey, DevGlobals *g, int64_t n) {
+/* ---------------------------------------------------------------------- */
+/* CORRECTED_GRADIENT: per sph / sphBoundary particle, rows CG_M.. of the
+ * matrix invM (nd x nd, row-major), CG_C.. of sumGrad/sum and CG_S of sum */
+struct CgRow {
+    double m[9], cs[3], sum;
+};
+
+__device__ __forceinline__ void cg_load(const double *cg, int64_t cap, int64_t a, int nd, CgRow &o) {
+    for (int k = 0; k < nd * nd; k++) o.m[k] = cg[(CG_M + k) * cap + a];
+    for (int d = 0; d < nd; d++) o.cs[d] = cg[(CG_C + d) * cap + a];
+    o.sum = cg[CG_S * cap + a];
+}
+
+/* gradW with CORRECTED_GRADIENT (sph.h:325-326): invM ((dr F - sumGrad/sum)/sum),
+ * the product row by row from 0 (vect.h:39-47) */
+__device__ __forceinline__ void cg_apply(const CgRow &w, const double *dx, double F, int nd, double *out) {
+    double t[3] = {0, 0, 0};
+    for (int d = 0; d < nd; d++) t[d] = (dx[d] * F - w.cs[d]) / w.sum;
+    for (int i = 0; i < nd; i++) {
+        double v = 0.0;
+        for (int j = 0; j < nd; j++) v += w.m[i * nd + j] * t[j];
+        out[i] = v;
+    }
+}
+
+/* inverseSym (vect.h:49-111): adjugate over determinant; identity when the
+ * determinant is 0.  1D (which the reference does not define) inverts the
+ * scalar. */
+__device__ void inverse_sym(double *a, int nd) {
+    if (nd == 1) {
+        a[0] = a[0] != 0.0 ? 1.0 / a[0] : 1.0;
+        return;
+    }
+    if (nd == 2) {
+        const double A = a[0], B = a[1], C = a[2], D = a[3];
+        const double det = dsub(dmul(A, D), dmul(B, C));
+        if (det != 0.0) {
+            a[0] = D / det;
+            a[1] = -B / det;
+            a[2] = -C / det;
+            a[3] = A / det;
+        } else {
+            a[0] = 1.0;
+            a[1] = 0.0;
+            a[2] = 0.0;
+            a[3] = 1.0;
+        }
+        return;
+    }
+    const double A0 = a[0], B0 = a[1], C0 = a[2], D0 = a[3], E0 = a[4], F0 = a[5], G0 = a[6], H0 = a[7], K0 = a[8];
+    const double cA = dsub(dmul(E0, K0), dmul(F0, H0)), cB = dsub(dmul(F0, G0), dmul(D0, K0));
+    const double cC = dsub(dmul(D0, H0), dmul(E0, G0)), cD = dsub(dmul(C0, H0), dmul(B0, K0));
+    const double cE = dsub(dmul(A0, K0), dmul(C0, G0)), cF = dsub(dmul(B0, G0), dmul(A0, H0));
+    const double cG = dsub(dmul(B0, F0), dmul(C0, E0)), cH = dsub(dmul(C0, D0), dmul(A0, F0));
+    const double cK = dsub(dmul(A0, E0), dmul(B0, D0));
+    const double Z = dadd(dadd(dmul(A0, cA), dmul(B0, dsub(dmul(F0, G0), dmul(K0, D0)))), dmul(C0, cC));
+    if (Z != 0.0) {
+        const double o[9] = {cA, cD, cG, cB, cE, cH, cC, cF, cK};
+        for (int k = 0; k < 9; k++) a[k] = o[k] / Z;
+    } else {
+        for (int k = 0; k < 9; k++) a[k] = (k % 4 == 0) ? 1.0 : 0.0;
+    }
+}
+
+/* calcInvM (sph.h:393-434) of every sph / sphBoundary particle over the
+ * neighbours of the last rebuild: sum = (m/rho) W(0,h) + sum dvol W(r/hav,hav),
+ * sumGrad = sum dvol dr F(r/hav,hav), M = -sum dvol (dr F - sumGrad/sum)/sum (x) dr,
+ * invM = M^-1 (identity without neighbours) */
+__global__ void k_invm(DevCfg c, DevState s, const int *start, const int *skey, const DevGlobals *g, double *cg,
+                       int64_t n) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    if (!is_sph_or_sphb(s.irow(FI_IAM)[a])) return;
+    const GridInfo gi = load_grid(g);
+    const int nd = c.nd;
+    double ra[3] = {0, 0, 0};
+    for (int d = 0; d < nd; d++) ra[d] = s.row(FD_R + d)[a];
+    const double ha = s.row(FD_H)[a];
+    double sum = (s.row(FD_MASS)[a] / s.row(FD_DENS)[a]) * (s.row(FD_IHN)[a] * wK(0.0, c.wcon));
+    double sg[3] = {0, 0, 0}, m[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    int nn = 0;
+    const CellCoord cc = decode_cell(skey[a], gi.sdims, nd);
+    /* F(q, hav) and W(q, hav) of a pair (sph.h:74-80, 306-308) */
+    auto kern = [&](double r, double hb, double &F, double &W) {
+        const double hav = 0.5 * (ha + hb);
+        const double q = r / hav, ih = 1.0 / hav;
+        double ihn = ih;
+        for (int d = 1; d < nd; d++) ihn *= ih;
+        F = (ihn * ih * ih) * wdK(q, c.wcon) / q;
+        W = ihn * wK(q, c.wcon);
+    };
+    scan_cells(cc, gi.sdims, c.periodic, nd, start, 0, [&](int b, const int *sh) {
+        if (b == a && !(sh[0] | sh[1] | sh[2])) return;
+        double dx[3], r2;
+        if (!pair_geom(c, s, b, sh, ra, ha, dx, r2)) return;
+        nn++;
+        if (!is_sph_or_sphb(s.irow(FI_IAM)[b])) return;
+        const double dvol = s.row(FD_MASS)[b] / s.row(FD_DENS)[b];
+        double F, W;
+        kern(sqrt(r2), s.row(FD_H)[b], F, W);
+        sum += dvol * W;
+        for (int d = 0; d < nd; d++) sg[d] += (dvol * dx[d]) * F;
+    });
+    if (nn == 0) {
+        for (int i = 0; i < nd; i++) m[i * nd + i] = 1.0;
+    } else {
+        scan_cells(cc, gi.sdims, c.periodic, nd, start, 0, [&](int b, const int *sh) {
+            if (b == a && !(sh[0] | sh[1] | sh[2])) return;
+            double dx[3], r2;
+            if (!pair_geom(c, s, b, sh, ra, ha, dx, r2)) return;
+            if (!is_sph_or_sphb(s.irow(FI_IAM)[b])) return;
+            const double dvol = s.row(FD_MASS)[b] / s.row(FD_DENS)[b];
+            double F, W;
+            kern(sqrt(r2), s.row(FD_H)[b], F, W);
+            double gw[3] = {0, 0, 0};
+            for (int d = 0; d < nd; d++) gw[d] = (dx[d] * F - sg[d] / sum) / sum;
+            for (int i = 0; i < nd; i++)
+                for (int j = 0; j < nd; j++) m[i * nd + j] -= dvol * dmul(gw[i], dx[j]);
+        });
+        inverse_sym(m, nd);
+    }
+    const int64_t cap = s.cap;
+    for (int k = 0; k < nd * nd; k++) cg[(CG_M + k) * cap + a] = m[k];
+    for (int d = 0; d < nd; d++) cg[(CG_C + d) * cap + a] = sg[d] / sum;
+    cg[CG_S * cap + a] = sum;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Density re-initialisation (sphIncompress.cpp:19-35).  The neighbour lists
+ * of the reference are built lazily after the first calcHFromDens, so the
+ * neighbour predicate uses that first h (kept in hp) through all ten
+ * rounds, while calcDensity uses each round's own h. */
+__global__ void k_reinit_h(DevCfg c, DevState s, double *hp, int64_t n) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    if (!is_sph_or_sphb(s.irow(FI_IAM)[a])) return;
+    const double m = s.row(FD_MASS)[a], rho = s.row(FD_DENS)[a];
+    const double x = c.precision == SPHDEM_PREC_MIXED ? m * recip(c, rho) : m / rho;
+    const double h = smoothing_length(c, x);
+    s.row(FD_H)[a] = h;
+    hp[a] = h;
+}
+
+__global__ void k_reinit_dens(DevCfg c, DevState s, const int *start, const int *skey, const DevGlobals *g,
+                              const double *hp, int64_t n) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    if (!is_sph_or_sphb(s.irow(FI_IAM)[a])) return;
+    const GridInfo gi = load_grid(g);
+    const int nd = c.nd;
+    double ra[3] = {0, 0, 0};
+    for (int d = 0; d < nd; d++) ra[d] = s.row(FD_R + d)[a];
+    const double ma = s.row(FD_MASS)[a], hpa = hp[a];
+    double h = s.row(FD_H)[a], rho = s.row(FD_DENS)[a];
+    const CellCoord cc = decode_cell(skey[a], gi.sdims, nd);
+    for (int round = 0; round < 10; round++) {
+        if (round > 0) {
+            const double x = c.precision == SPHDEM_PREC_MIXED ? ma * recip(c, rho) : ma / rho;
+            h = smoothing_length(c, x);
+        }
+        const double ih = recip(c, h);
+        double ihn = ih;
+        for (int d = 1; d < nd; d++) ihn *= ih;
+        double sum = ma * (ihn * wK(0.0, c.wcon));
+        scan_cells(cc, gi.sdims, c.periodic, nd, start, 0, [&](int b, const int *sh) {
+            const bool shifted = (sh[0] | sh[1] | sh[2]) != 0;
+            if (b == a && !shifted) return;
+            if (!is_sph_or_sphb(s.irow(FI_IAM)[b])) return;
+            double dx[3] = {0, 0, 0};
+            for (int d = 0; d < nd; d++)
+                dx[d] = dsub(ra[d], image_pos(s.row(FD_R + d)[b], sh[d], c.rmin[d], c.rmax[d]));
+            const double r2 = exact_len2(dx, nd);
+            const double hb = hp[b];
+            const double t = 2.0 * (hpa > hb ? hpa : hb);
+            if (r2 > dmul(t, t)) return;
+            if (shifted && !image_exists(s.irow(FI_GCODE)[b], sh, nd)) return;
+            const double q = c.precision == SPHDEM_PREC_MIXED ? sqrt(r2) * ih : sqrt(r2) / h;
+            sum += s.row(FD_MASS)[b] * (ihn * wK(q, c.wcon));
+        });
+        rho = sum;
+    }
+    s.row(FD_H)[a] = h;
+    h_derived(c, s, a);
+    s.row(FD_DENS)[a] = rho;
+}
+
+__global__ void k_force(DevCfg c, DevState s, const int *start, const int *skey, DevGlobals *g, const double *cg,
+                        int64_t n) {
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double ndt = DBL_MAX;
     if (a < n && is_sph_or_sphb(s.irow(FI_IAM)[a])) {
@@ -268,6 +461,8 @@ __global__ void k_force(DevCfg c, DevState s, const int *start, const int *skey,
         const double densa = s.row(FD_DENS)[a], pdr2a = s.row(FD_PDR2)[a], ma = s.row(FD_MASS)[a];
         const double oma = c.var_h() ? s.row(FD_OMEGA)[a] : 1.0;
         const bool no_anti = c.flags & SPHDEM_F_NO_ANTICLUMPING;
+        CgRow cw;
+        if (cg) cg_load(cg, s.cap, a, c.nd, cw);
         const CellCoord cc = decode_cell(skey[a], gi.sdims, c.nd);
         scan_cells(cc, gi.sdims, c.periodic, c.nd, start, 0, [&](int b, const int *sh) {
             if (b == a && !(sh[0] | sh[1] | sh[2])) return;
@@ -282,13 +477,22 @@ __global__ void k_force(DevCfg c, DevState s, const int *start, const int *skey,
             if (qa != 0) Fa = ihn2a * wdK(qa, c.wcon) / qa;
             if (qb != 0) Fb = ihn2b * wdK(qb, c.wcon) / qb;
             double gA[3] = {0, 0, 0}, gB[3] = {0, 0, 0};
+            double wa[3] = {0, 0, 0}, wb[3] = {0, 0, 0};
+            if (cg) {
+                cg_apply(cw, dx, Fa, c.nd, wa);
+                cg_apply(cw, dx, Fb, c.nd, wb);
+            } else {
+                for (int d = 0; d < c.nd; d++) {
+                    wa[d] = dx[d] * Fa;
+                    wb[d] = dx[d] * Fb;
+                }
+            }
             for (int d = 0; d < c.nd; d++) {
-                const double ga = dx[d] * Fa, gb = dx[d] * Fb;
                 if (c.var_h()) {
-                    gA[d] = ga / oma;
-                    gB[d] = gb / oma;
+                    gA[d] = wa[d] / oma;
+                    gB[d] = wb[d] / oma;
                 } else {
-                    gA[d] = gB[d] = 0.5 * (ga + gb);
+                    gA[d] = gB[d] = 0.5 * (wa[d] + wb[d]);
                 }
             }
             const double densb = s.row(FD_DENS)[b], mb = s.row(FD_MASS)[b];
@@ -421,7 +625,8 @@ __global__ void k_dem_accel(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
 }
 
 /* ---------------------------------------------------------------------- */
-__global__ void k_dddt(DevCfg c, DevState s, const int *start, const int *skey, const DevGlobals *g, int64_t n) {
+__global__ void k_dddt(DevCfg c, DevState s, const int *start, const int *skey, const DevGlobals *g,
+                       const double *cg, int64_t n) {
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (a >= n) return;
     if (!is_sph_or_sphb(s.irow(FI_IAM)[a])) return;
@@ -434,6 +639,8 @@ __global__ void k_dddt(DevCfg c, DevState s, const int *start, const int *skey, 
     const double ha = s.row(FD_H)[a], iha = s.row(FD_IH)[a], ihn2a = s.row(FD_IHN2)[a];
     const double oma = c.var_h() ? s.row(FD_OMEGA)[a] : 1.0;
     double dddt = s.row(FD_DDDT)[a];
+    CgRow cw;
+    if (cg) cg_load(cg, s.cap, a, c.nd, cw);
     const CellCoord cc = decode_cell(skey[a], gi.sdims, c.nd);
     scan_cells(cc, gi.sdims, c.periodic, c.nd, start, 0, [&](int b, const int *sh) {
         if (b == a && !(sh[0] | sh[1] | sh[2])) return;
@@ -445,14 +652,21 @@ __global__ void k_dddt(DevCfg c, DevState s, const int *start, const int *skey, 
         const double qa = r * iha;
         double Fa = 0.0;
         if (qa != 0) Fa = ihn2a * wdK(qa, c.wcon) / qa;
-        double gw[3] = {0, 0, 0};
+        double gw[3] = {0, 0, 0}, wa[3] = {0, 0, 0};
+        if (cg) cg_apply(cw, dx, Fa, c.nd, wa);
+        else
+            for (int d = 0; d < c.nd; d++) wa[d] = dx[d] * Fa;
         if (c.var_h()) {
-            for (int d = 0; d < c.nd; d++) gw[d] = dx[d] * Fa / oma;
+            for (int d = 0; d < c.nd; d++) gw[d] = wa[d] / oma;
         } else {
             const double qb = r * s.row(FD_IH)[b];
             double Fb = 0.0;
             if (qb != 0) Fb = s.row(FD_IHN2)[b] * wdK(qb, c.wcon) / qb;
-            for (int d = 0; d < c.nd; d++) gw[d] = 0.5 * (dx[d] * Fa + dx[d] * Fb);
+            double wb[3] = {0, 0, 0};
+            if (cg) cg_apply(cw, dx, Fb, c.nd, wb);
+            else
+                for (int d = 0; d < c.nd; d++) wb[d] = dx[d] * Fb;
+            for (int d = 0; d < c.nd; d++) gw[d] = 0.5 * (wa[d] + wb[d]);
         }
         double dv[3] = {0, 0, 0};
         for (int d = 0; d < c.nd; d++) dv[d] = va[d] - s.row(FD_VHAT + d)[b];
@@ -600,14 +814,24 @@ void run_omega_eos(sphdem_ctx *c, bool omega, bool eos) {
 }
 void run_force(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "force_fp64", k_force, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, c->buf.start, c->buf.skey,
-                  c->g, c->n);
+                  c->g, corrected_gradient(c) ? c->cg : nullptr, c->n);
+}
+void run_invm(sphdem_ctx *c) {
+    SPHDEM_LAUNCH(c, "invm_fp64", k_invm, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, c->buf.start, c->buf.skey, c->g,
+                  c->cg, c->n);
+}
+void run_reinit_density(sphdem_ctx *c) {
+    rebuild(c);
+    SPHDEM_LAUNCH(c, "reinit_h", k_reinit_h, grid_for(c->n, 256), 256, 0, c->cfg, c->A, c->hpred, c->n);
+    SPHDEM_LAUNCH(c, "reinit_dens_fp64", k_reinit_dens, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, c->buf.start,
+                  c->buf.skey, c->g, c->hpred, c->n);
 }
 void run_dem_accel(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "dem_accel", k_dem_accel, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, c->g, c->n);
 }
 void run_dddt(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "dddt_fp64", k_dddt, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, c->buf.start, c->buf.skey,
-                  c->g, c->n);
+                  c->g, corrected_gradient(c) ? c->cg : nullptr, c->n);
 }
 void run_dem_end(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "dem_end_fp64", k_dem_end, grid_for(c->n, BLK), BLK, 0, c->cfg, c->A, c->buf.start, c->g, c->n);

@@ -17,7 +17,7 @@
 #if !defined(WENDLAND)
 #error "the device path implements the Wendland C2 kernel only (#define WENDLAND)"
 #endif
-#if defined(LUBRICATION) || defined(HERTZ) || defined(HERTZ_KUWABARA) || defined(CORRECTED_GRADIENT)
+#if defined(LUBRICATION) || defined(HERTZ) || defined(HERTZ_KUWABARA) || defined(REINIT_DENS_MLS)
 #error "option not implemented by the device path"
 #endif
 
@@ -49,6 +49,12 @@ inline SphDemConfig sphdem_case_config(int precision, bool fixed_dt) {
 #ifdef LIQ_DEM
     c.flags |= SPHDEM_F_LIQ_DEM;
 #endif
+#ifdef CORRECTED_GRADIENT
+    c.flags |= SPHDEM_F_CORRECTED_GRADIENT; /* FP64 precision only */
+#endif
+#if defined(LIQ_DEM) && defined(DEM_BLOCK)
+    c.flags |= SPHDEM_F_DEM_BLOCK;
+#endif
     if (fixed_dt) c.flags |= SPHDEM_F_FIXED_DT;
     c.pi = PI;
     for (int d = 0; d < NDIM; d++) {
@@ -73,6 +79,9 @@ inline SphDemConfig sphdem_case_config(int precision, bool fixed_dt) {
     c.bfac = BFAC;
     c.maxdt = MAXTIME / OUTSTEP; /* run.cpp:87 */
     c.damptime = DAMPTIME;
+    /* both constants are required, as sphIncompress.cpp:20 reads both */
+    c.reinit_dens_every = REINIT_DENS_EVERY_N_STEPS;
+    c.reinit_dens_at = REINIT_DENS_AT_N_STEPS;
 #ifdef LIQ_DEM
     c.dem_radius = DEM_RADIUS;
     c.dem_dens = DEM_DENS;

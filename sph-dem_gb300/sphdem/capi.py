@@ -60,6 +60,7 @@ class SphDemConfig(C.Structure):
         ("gravity_sph", D3), ("gravity_dem", D3),
         ("walls", SphDemWall * 6),
         ("drag_scale", C.c_double),
+        ("reinit_dens_every", C.c_int32), ("reinit_dens_at", C.c_int32),
     ]
 
 
@@ -134,7 +135,12 @@ def config_struct(cfg: dict, precision: int | None = None) -> SphDemConfig:
                 s.walls[i].point = D3(*w["point"])
                 s.walls[i].normal = D3(*w["normal"])
             continue
-        val = cfg.get(name, 1.0) if name == "drag_scale" else cfg[name]
+        if name == "drag_scale":
+            val = cfg.get(name, 1.0)
+        elif name in ("reinit_dens_every", "reinit_dens_at"):
+            val = cfg.get(name, 0)
+        else:
+            val = cfg[name]
         if ctype in (D3, I3):
             setattr(s, name, ctype(*val))
         else:

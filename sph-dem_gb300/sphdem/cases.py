@@ -37,6 +37,8 @@ F_NO_ANTICLUMPING = 1 << 1
 F_VAR_H_CORRECTION = 1 << 2
 F_LIQ_DEM = 1 << 3
 F_FIXED_DT = 1 << 4
+F_CORRECTED_GRADIENT = 1 << 6
+F_DEM_BLOCK = 1 << 7
 
 PREC_FP64, PREC_MIXED = 0, 1
 
@@ -69,6 +71,7 @@ def _base_cfg(ndim: int) -> dict:
         dem_search_radius=0.0, dem_vol=0.0, coupling_radius=0.0,
         dem_timestep=1e30, liq_dem_timestep=1e30,
         time_drop_particle=1e30, freeze_dem_until=-1.0, drag_scale=1.0,
+        reinit_dens_every=0, reinit_dens_at=0,
         gravity_sph=[0.0, 0.0, 0.0], gravity_dem=[0.0, 0.0, 0.0],
         walls=[],
     )
@@ -117,12 +120,17 @@ def dambreak2d(dx: float = 0.01, width: float = 1.0, height: float = 2.0,
                tank=(4.0, 3.0), seed: int = 1, jitter: float = 0.01,
                nsteps: int = 1000, layers: int = 3,
                visc_model: int = VISC_ARTIFICIAL, const_h: bool = True,
-               anticlumping: bool = False, viscosity: float = 1e-6) -> Case:
+               anticlumping: bool = False, viscosity: float = 1e-6,
+               var_h: bool = False, corrected_gradient: bool = False,
+               reinit_every: int = 0, reinit_at: int = 0, fixed_dt: bool = True) -> Case:
     """Weakly-compressible 2D dam break: a width x height water column at rest
     in a tank[0] x tank[1] tank with three walls of `layers` fixed
     sphBoundary layers.  Wendland C2, h = 1.3 dx (CONST_H), Tait EOS
     gamma = 7, rho0 = 1000, c0 = 10 sqrt(2 g height), artificial viscosity
-    alpha = 0.1, gravity -9.81, dt = 0.25 h / c0."""
+    alpha = 0.1, gravity -9.81, dt = 0.25 h / c0.  Options: VAR_H_CORRECTION,
+    CORRECTED_GRADIENT, and the density re-initialisation of start() every
+    `reinit_every` steps and at step `reinit_at` (0: never); fixed_dt=False
+    lets dt follow the reference's time-step conditions."""
     ndim = 2
     rho0 = 1000.0
     c0 = 10.0 * math.sqrt(2.0 * 9.81 * height)
@@ -131,7 +139,9 @@ def dambreak2d(dx: float = 0.01, width: float = 1.0, height: float = 2.0,
     cfg.update(
         visc_model=visc_model,
         flags=(F_CONST_H if const_h else 0) | (0 if anticlumping else F_NO_ANTICLUMPING)
-        | F_FIXED_DT,
+        | (F_VAR_H_CORRECTION if var_h else 0) | (F_CORRECTED_GRADIENT if corrected_gradient else 0)
+        | (F_FIXED_DT if fixed_dt else 0),
+        reinit_dens_every=reinit_every, reinit_dens_at=reinit_at,
         rmin=[0.0, 0.0, 0.0], rmax=[tank[0], tank[1], 0.0],
         hfac=1.3, psep=dx, h=h, dens=rho0, refd=rho0, gamma=7.0,
         spsound=c0, prb=c0 * c0 * rho0 / 7.0, viscosity=viscosity,
@@ -272,7 +282,8 @@ def sediment3d(nx: int = 80, L: float = 0.2, height: float = 0.4,
                rho_s: float = 2500.0, k: float = 1e4, restitution: float = 0.5,
                viscosity: float = 1e-6, seed: int = 3, nsteps: int = 1000,
                dt: float | None = None, floor: str = "boundary", var_h: bool = True,
-               dem_top_margin: float | None = None) -> Case:
+               dem_top_margin: float | None = None, reinit_every: int = 0,
+               dem_block: bool = False) -> Case:
     """Coupled SPH-DEM sedimentation in a periodic-x/y box L x L x height with
     a bottom wall.  Fluid lattice as sediment3D/setup.cpp:65-108 (staggered
     odd layers, one `boundary` layer at k=0), h = 1.5 dx, Morris viscosity
@@ -285,7 +296,10 @@ def sediment3d(nx: int = 80, L: float = 0.2, height: float = 0.4,
     h without VAR_H_CORRECTION: the coupled form the adjoint covers.
     dem_top_margin keeps the DEM centres that far below the free surface
     (default R): spheres at the surface see about half a kernel of fluid, the
-    0.5 threshold of calcFPI's Shepard normalisation (sph.h:1759-1760)."""
+    0.5 threshold of calcFPI's Shepard normalisation (sph.h:1759-1760).
+    reinit_every > 0 re-initialises the fluid density every that many steps
+    (sediment3D's REINIT_DENS_EVERY_N_STEPS); dem_block moves the DEM
+    particles as one block under their mean force (sediment3D's DEM_BLOCK)."""
     ndim = 3
     psep = L / nx
     nz = int(round(height / psep))
@@ -371,9 +385,10 @@ def sediment3d(nx: int = 80, L: float = 0.2, height: float = 0.4,
     cfg = _base_cfg(ndim)
     cfg.update(
         visc_model=VISC_MORRIS,
-        flags=(F_LIQ_DEM | F_VAR_H_CORRECTION | F_NO_ANTICLUMPING | F_FIXED_DT) if var_h
-        else (F_LIQ_DEM | F_CONST_H | F_NO_ANTICLUMPING | F_FIXED_DT),
-        periodic=[1, 1, 0],
+        flags=((F_LIQ_DEM | F_VAR_H_CORRECTION | F_NO_ANTICLUMPING | F_FIXED_DT) if var_h
+               else (F_LIQ_DEM | F_CONST_H | F_NO_ANTICLUMPING | F_FIXED_DT))
+        | (F_DEM_BLOCK if dem_block else 0),
+        periodic=[1, 1, 0], reinit_dens_every=reinit_every,
         rmin=[0.0, 0.0, 0.0], rmax=[L, L, height],
         hfac=1.5, psep=psep, h=h, dens=rho0, refd=rho0, gamma=7.0,
         spsound=c0, prb=c0 * c0 * rho0 / 7.0, viscosity=viscosity,
@@ -432,12 +447,30 @@ def workload(name: str, **kw) -> Case:
                                                         visc_model=VISC_MONAGHAN,
                                                         anticlumping=True, const_h=False,
                                                         viscosity=1e-2),
+        # damBreak's customConstants.h as written: the above plus
+        # CORRECTED_GRADIENT and density re-initialisation every step
+        "dambreak2d_own_small": lambda: dambreak2d(dx=0.05, nsteps=30, visc_model=VISC_MONAGHAN,
+                                                   anticlumping=True, const_h=False, viscosity=1e-2,
+                                                   corrected_gradient=True, reinit_every=1,
+                                                   fixed_dt=False),
+        # the corrected gradient under VAR_H_CORRECTION, re-initialisation
+        # every 7 steps and at step 3
+        "dambreak2d_cg_varh_small": lambda: dambreak2d(dx=0.05, nsteps=20, const_h=False, var_h=True,
+                                                       corrected_gradient=True, reinit_every=7,
+                                                       reinit_at=3, seed=5, fixed_dt=False),
         "dem_small": lambda: dem_settling3d(lattice=(6, 6, 10), box=(0.0138, 0.0138, 0.023),
                                             spread=0.0, nsteps=600, vel_amp=0.3),
         "dem_small_poly": lambda: dem_settling3d(lattice=(6, 6, 10), box=(0.0144, 0.0144, 0.024),
                                                  nsteps=600, vel_amp=0.3),
         "sediment3d_small": lambda: sediment3d(nx=10, L=0.04, height=0.08, n_dem=100,
                                                nsteps=20),
+        # coupled, DEM moving as one block under the mean DEM force
+        "sediment3d_block_small": lambda: sediment3d(nx=10, L=0.04, height=0.08, n_dem=100, nsteps=20,
+                                                     dem_block=True, seed=6),
+        # coupled, periodic: density re-initialisation every 4 steps (the
+        # surface particles' h grows by ~1/3, so the box is 8.75 h_max wide)
+        "sediment3d_reinit_small": lambda: sediment3d(nx=15, L=0.06, height=0.05, n_dem=100, nsteps=12,
+                                                      reinit_every=4),
         "sediment3d_adjoint_small": lambda: sediment3d(nx=10, L=0.04, height=0.08, n_dem=60, nsteps=30,
                                                        floor="sphb3", var_h=False, viscosity=1e-4),
     }

@@ -27,7 +27,9 @@ from sphdem.state import read_output  # noqa: E402
 
 import build_ref  # noqa: E402
 
-WORKLOADS = ["dambreak2d_small", "dambreak2d_monaghan_small", "dem_small", "sediment3d_small"]
+WORKLOADS = ["dambreak2d_small", "dambreak2d_monaghan_small", "dem_small", "sediment3d_small",
+             "dambreak2d_own_small", "dambreak2d_cg_varh_small", "sediment3d_reinit_small",
+             "sediment3d_block_small"]
 
 
 def make(name: str) -> str:

@@ -18,7 +18,9 @@ from sphdem.state import pair_set
 from oracle.port_api import OracleSim
 
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
-WORKLOADS = ["dambreak2d_small", "dambreak2d_monaghan_small", "dem_small", "sediment3d_small"]
+WORKLOADS = ["dambreak2d_small", "dambreak2d_monaghan_small", "dem_small", "sediment3d_small",
+             "dambreak2d_own_small", "dambreak2d_cg_varh_small", "sediment3d_reinit_small",
+             "sediment3d_block_small"]
 FIELD_MAP = {"r": "r", "v": "v", "vhat": "vhat", "v0": "v0", "vhat0": "vhat0", "f": "f",
              "fp": "fp", "fv": "fv", "fb": "fb", "dens": "dens", "dddt": "dddt", "h": "h",
              "press": "press", "pdr2": "pdr2", "porosity": "porosity",
