@@ -230,6 +230,25 @@ int sphdem_get_globals(sphdem_handle h, SphDemGlobals *out);
 int sphdem_get_stats(sphdem_handle h, SphDemStats *out);
 int sphdem_set_globals(sphdem_handle h, const SphDemGlobals *in);
 
+/* Insert in->n particles between phases (CdataLL::insertNewParticle,
+ * dataLL.cpp:238-261, called from a case hook).  iam, r, mass, dens and h
+ * are required; v, vhat (default v), radius, normals and concave are read if
+ * given, every other field starts as sphdem_create leaves it.  Each new
+ * particle takes the lowest free tag-order index -- a slot left by a deleted
+ * particle, else the next index past the last -- written to out_idx[j] when
+ * out_idx is not NULL.  Past the capacity given at creation nothing is
+ * inserted and the call returns SPHDEM_ERR_CAPACITY (the reference exits at
+ * MAX_NUM_PARTICLES_PER_CPU).  The new particles join the bucket lists at the
+ * next rebuild, which every phase's neighbour passes follow. */
+int sphdem_insert_particles(sphdem_handle h, const SphDemParticles *in, int64_t *out_idx);
+
+/* Mark particles (tag-order indices) for deletion (CdataLL::markForDeletion,
+ * dataLL.cpp:263-266: tag = -111).  They take part in the step as usual
+ * until the next rebuild removes them (dataLL.cpp:377-380); their slots are
+ * then free for insertion.  An index out of range or of a deleted particle
+ * gives SPHDEM_ERR_INVALID and marks nothing. */
+int sphdem_mark_for_deletion(sphdem_handle h, const int64_t *idx, int64_t k);
+
 /* Rebuild the bucket lists at the current positions (CdataLL::reset,
  * dataLL.cpp:140-236): periodic wrap, out-of-domain deletion, h_max tracking,
  * bin, sort by cell, permute. */

@@ -42,6 +42,7 @@ struct V3 {
 struct Part {
     int iam, tag;
     bool concave, alive;
+    bool marked;           /* markForDeletion (tag -111): removed by the next reset */
     double r[3], v[3], vhat[3], v0[3], vhat0[3];
     double f[3], fp[3], fv[3], fb[3], ff[3];
     double fdrag[3], fvel[3], gradPor[3];
@@ -235,6 +236,14 @@ struct Sim {
         for (size_t pos = 0; pos < order.size();) {
             const int k = order[pos];
             Part &p = ps[k];
+            if (p.marked) {
+                /* updateDomain deletes tag -111 first (dataLL.cpp:377-380) */
+                p.alive = false;
+                p.marked = false;
+                order[pos] = order.back();
+                order.pop_back();
+                continue;
+            }
             int oc[3] = {1, 1, 1};
             bool lost = false, out = false;
             for (int i = 0; i < nd; i++) {
@@ -1192,6 +1201,28 @@ struct Sim {
 
 std::string g_err;
 
+/* a particle as the Cparticle constructor and the case set it (particle.h:60-120) */
+void init_part(Part &p, const SphDemParticles *in, int64_t k) {
+    std::memset(&p, 0, sizeof(Part));
+    p.alive = true;
+    p.iam = in->iam[k];
+    p.tag = in->tag ? in->tag[k] : (int)k + 1;
+    p.concave = in->concave ? in->concave[k] != 0 : true;
+    for (int i = 0; i < 3; i++) {
+        p.r[i] = in->r[3 * k + i];
+        p.v[i] = in->v ? in->v[3 * k + i] : 0.0;
+        p.vhat[i] = in->vhat ? in->vhat[3 * k + i] : p.v[i];
+        p.norm1[i] = in->norm1 ? in->norm1[3 * k + i] : 0.0;
+        p.norm2[i] = in->norm2 ? in->norm2[3 * k + i] : 0.0;
+        p.norm3[i] = in->norm3 ? in->norm3[3 * k + i] : 0.0;
+    }
+    p.mass = in->mass[k];
+    p.dens = in->dens[k];
+    p.h = in->h[k];
+    p.radius = in->radius ? in->radius[k] : 0.0;
+    p.porosity = 1.0;
+}
+
 void load(Sim &s, const SphDemConfig *cfg, const SphDemParticles *in) {
     s.c = *cfg;
     s.nd = cfg->ndim;
@@ -1199,27 +1230,7 @@ void load(Sim &s, const SphDemConfig *cfg, const SphDemParticles *in) {
     s.maxdt = cfg->maxdt;
     s.dt = cfg->maxdt;
     s.ps.resize(in->n);
-    for (int64_t k = 0; k < in->n; k++) {
-        Part &p = s.ps[k];
-        std::memset(&p, 0, sizeof(Part));
-        p.alive = true;
-        p.iam = in->iam[k];
-        p.tag = in->tag ? in->tag[k] : (int)k + 1;
-        p.concave = in->concave ? in->concave[k] != 0 : true;
-        for (int i = 0; i < 3; i++) {
-            p.r[i] = in->r[3 * k + i];
-            p.v[i] = in->v ? in->v[3 * k + i] : 0.0;
-            p.vhat[i] = in->vhat ? in->vhat[3 * k + i] : p.v[i];
-            p.norm1[i] = in->norm1 ? in->norm1[3 * k + i] : 0.0;
-            p.norm2[i] = in->norm2 ? in->norm2[3 * k + i] : 0.0;
-            p.norm3[i] = in->norm3 ? in->norm3[3 * k + i] : 0.0;
-        }
-        p.mass = in->mass[k];
-        p.dens = in->dens[k];
-        p.h = in->h[k];
-        p.radius = in->radius ? in->radius[k] : 0.0;
-        p.porosity = 1.0;
-    }
+    for (int64_t k = 0; k < in->n; k++) init_part(s.ps[k], in, k);
     s.init_grids();
     s.reset();
 }
@@ -1276,6 +1287,35 @@ int oracle_phase(void *h, int phase) {
 
 /* CdataLL::reset at the current positions (the pair exports read the
  * buckets of the last reset). */
+/* insertNewParticle (dataLL.cpp:238-261): appended to the container
+ * (traversal) order; the index is the lowest dead slot, else the next */
+int oracle_insert(void *h, const SphDemParticles *in, int64_t *out_idx) {
+    Sim *s = static_cast<Sim *>(h);
+    size_t cursor = 0;
+    for (int64_t j = 0; j < in->n; j++) {
+        while (cursor < s->ps.size() && s->ps[cursor].alive) cursor++;
+        const size_t slot = cursor < s->ps.size() ? cursor++ : s->ps.size();
+        if (slot == s->ps.size()) s->ps.emplace_back();
+        init_part(s->ps[slot], in, j);
+        s->order.push_back((int)slot);
+        if (out_idx) out_idx[j] = (int64_t)slot;
+    }
+    return 0;
+}
+
+/* markForDeletion (dataLL.cpp:263-266) */
+int oracle_mark_for_deletion(void *h, const int64_t *idx, int64_t k) {
+    Sim *s = static_cast<Sim *>(h);
+    for (int64_t j = 0; j < k; j++) {
+        if (idx[j] < 0 || idx[j] >= (int64_t)s->ps.size() || !s->ps[idx[j]].alive) {
+            g_err = "bad deletion index";
+            return 1;
+        }
+    }
+    for (int64_t j = 0; j < k; j++) s->ps[idx[j]].marked = true;
+    return 0;
+}
+
 int oracle_rebuild(void *h) {
     Sim *s = static_cast<Sim *>(h);
     try {

@@ -32,6 +32,8 @@ def lib():
         L.oracle_step.argtypes = [H, C.c_int]
         L.oracle_phase.argtypes = [H, C.c_int]
         L.oracle_rebuild.argtypes = [H]
+        L.oracle_insert.argtypes = [H, C.POINTER(SphDemParticles), C.POINTER(C.c_int64)]
+        L.oracle_mark_for_deletion.argtypes = [H, C.POINTER(C.c_int64), C.c_int64]
         L.oracle_get.argtypes = [H, C.POINTER(SphDemParticles)]
         L.oracle_pairs.argtypes = [H, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                    C.c_int64, C.POINTER(C.c_int64)]
@@ -73,6 +75,22 @@ class OracleSim:
         rc = self.L.oracle_rebuild(self.h)
         if rc:
             raise RuntimeError("oracle_rebuild: " + self.L.oracle_last_error().decode())
+
+    def insert(self, particles: dict) -> np.ndarray:
+        k = int(particles["iam"].shape[0])
+        buf = ParticleBuffers(k, particles)
+        out = np.zeros(max(k, 1), np.int64)
+        self.L.oracle_insert(self.h, buf.ref(), out.ctypes.data_as(C.POINTER(C.c_int64)))
+        out = out[:k]
+        if k:
+            self.n = max(self.n, int(out.max()) + 1)
+        return out
+
+    def mark_for_deletion(self, idx):
+        idx = np.ascontiguousarray(idx, np.int64).reshape(-1)
+        rc = self.L.oracle_mark_for_deletion(self.h, idx.ctypes.data_as(C.POINTER(C.c_int64)), int(idx.size))
+        if rc:
+            raise RuntimeError("oracle_mark_for_deletion: " + self.L.oracle_last_error().decode())
 
     def get(self) -> ParticleBuffers:
         out = ParticleBuffers(self.n)

@@ -100,7 +100,7 @@ def customconstants(case: cases.Case) -> str:
         "const double SPSOUND = %s;" % _f(c["spsound"]),
         "const double PRB = %s;" % _f(c["prb"]),
         "const int NX = 10;", "const int NY = 10;", "const int NZ = 10;",
-        "const int MAX_NUM_PARTICLES_PER_CPU = %d;" % (n + 64),
+        "const int MAX_NUM_PARTICLES_PER_CPU = %d;" % (n + case.n_inserted + 64),
         "const double PSEP = %s;" % _f(c["psep"]),
         "const double BFAC = %s;" % _f(c["bfac"]),
         "const double H = %s;" % _f(c["h"]),
@@ -234,7 +234,7 @@ def run(case: cases.Case, nsteps: int | None = None, exe: str | None = None) -> 
     exe = exe or os.path.join(d, "ref_driver")
     state = os.path.join(d, "init.state")
     out = os.path.join(d, "out.bin")
-    write_state(state, case.particles)
+    write_state(state, case.particles, case.events)
     steps = case.nsteps if nsteps is None else nsteps
     res = subprocess.run([exe, state, out, str(steps)], capture_output=True, text=True)
     sys.stderr.write(res.stderr)

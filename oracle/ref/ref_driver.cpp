@@ -52,6 +52,74 @@ struct Field {
     std::vector<double> data;
 };
 
+/* particle arrays of the state file (tag order) */
+struct Block {
+    std::vector<int> iam, tag, concave;
+    std::vector<double> r, v, mass, dens, h, radius, n1, n2, n3;
+};
+
+static void read_block(std::ifstream &in, long long n, bool with_tag, Block &b) {
+    b.iam.resize(n);
+    b.tag.resize(n);
+    b.concave.resize(n);
+    b.r.resize(3 * n);
+    b.v.resize(3 * n);
+    b.mass.resize(n);
+    b.dens.resize(n);
+    b.h.resize(n);
+    b.radius.resize(n);
+    b.n1.resize(3 * n);
+    b.n2.resize(3 * n);
+    b.n3.resize(3 * n);
+    rd(in, b.iam.data(), n);
+    if (with_tag) rd(in, b.tag.data(), n);
+    rd(in, b.concave.data(), n);
+    rd(in, b.r.data(), 3 * n);
+    rd(in, b.v.data(), 3 * n);
+    rd(in, b.mass.data(), n);
+    rd(in, b.dens.data(), n);
+    rd(in, b.h.data(), n);
+    rd(in, b.radius.data(), n);
+    rd(in, b.n1.data(), 3 * n);
+    rd(in, b.n2.data(), 3 * n);
+    rd(in, b.n3.data(), 3 * n);
+}
+
+static Cparticle to_particle(const Block &b, long long i, int tag) {
+    Cparticle p;
+    p.iam = (enum iamTypes)b.iam[i];
+    p.tag = tag;
+    p.concave = b.concave[i] != 0;
+    for (int d = 0; d < NDIM; d++) {
+        p.r[d] = b.r[3 * i + d];
+        p.v[d] = b.v[3 * i + d];
+        p.norm1[d] = b.n1[3 * i + d];
+        p.norm2[d] = b.n2[3 * i + d];
+#ifdef _3D_
+        p.norm3[d] = b.n3[3 * i + d];
+#endif
+    }
+    p.vhat = p.v;
+    p.mass = b.mass[i];
+    p.dens = b.dens[i];
+    p.h = b.h[i];
+    /* members the Cparticle constructor leaves unset (particle.h:67-131) and
+     * the step never writes for every type: zero, as in fresh memory */
+    p.deViscFdt = 0.0;
+    p.fb = 0.0;
+    p.ff = 0.0;
+    return p;
+}
+
+/* one scheduled change: insert a block (kind 1) or mark tag-order indices
+ * for deletion (kind 2) */
+struct Event {
+    long long step = 0;
+    int kind = 0;
+    Block add;
+    std::vector<long long> del;
+};
+
 static void put_name(FILE *f, const std::string &s) {
     char buf[16];
     memset(buf, 0, 16);
@@ -71,44 +139,37 @@ int main(int argc, char **argv) {
     if (memcmp(magic, "SPDMST01", 8) != 0) fail("bad magic");
     long long n;
     rd(in, &n, 1);
-    std::vector<int> iam(n), tag(n), concave(n);
-    std::vector<double> r(3 * n), v(3 * n), mass(n), dens(n), h(n), radius(n);
-    std::vector<double> n1(3 * n), n2(3 * n), n3(3 * n);
-    rd(in, iam.data(), n);
-    rd(in, tag.data(), n);
-    rd(in, concave.data(), n);
-    rd(in, r.data(), 3 * n);
-    rd(in, v.data(), 3 * n);
-    rd(in, mass.data(), n);
-    rd(in, dens.data(), n);
-    rd(in, h.data(), n);
-    rd(in, radius.data(), n);
-    rd(in, n1.data(), 3 * n);
-    rd(in, n2.data(), 3 * n);
-    rd(in, n3.data(), 3 * n);
+    Block init;
+    read_block(in, n, true, init);
+
+    /* optional schedule of insertions and deletions (SPDMEV01), applied
+     * after afterEnd of their step as a case's own afterEnd hook would */
+    std::vector<Event> events;
+    if (in.peek() != EOF) {
+        rd(in, magic, 8);
+        if (memcmp(magic, "SPDMEV01", 8) != 0) fail("bad event magic");
+        long long ne;
+        rd(in, &ne, 1);
+        events.resize(ne);
+        for (long long e = 0; e < ne; e++) {
+            long long hdr[3];
+            rd(in, hdr, 3);
+            events[e].step = hdr[0];
+            events[e].kind = (int)hdr[1];
+            if (events[e].kind == 1) {
+                read_block(in, hdr[2], false, events[e].add);
+            } else if (events[e].kind == 2) {
+                events[e].del.resize(hdr[2]);
+                rd(in, events[e].del.data(), hdr[2]);
+            } else {
+                fail("bad event kind");
+            }
+        }
+    }
 
     vector<Cparticle> ps;
     ps.reserve(std::max<long long>(MAX_NUM_PARTICLES_PER_CPU, n + 64));
-    for (long long i = 0; i < n; i++) {
-        Cparticle p;
-        p.iam = (enum iamTypes)iam[i];
-        p.tag = tag[i];
-        p.concave = concave[i] != 0;
-        for (int d = 0; d < NDIM; d++) {
-            p.r[d] = r[3 * i + d];
-            p.v[d] = v[3 * i + d];
-            p.norm1[d] = n1[3 * i + d];
-            p.norm2[d] = n2[3 * i + d];
-#ifdef _3D_
-            p.norm3[d] = n3[3 * i + d];
-#endif
-        }
-        p.vhat = p.v;
-        p.mass = mass[i];
-        p.dens = dens[i];
-        p.h = h[i];
-        ps.push_back(p);
-    }
+    for (long long i = 0; i < n; i++) ps.push_back(to_particle(init, i, init.tag[i]));
 
     CglobalVars g;
     Nmisc::setupEntireDomain(g.procDomain, g.procNeighbrs);
@@ -121,6 +182,8 @@ int main(int argc, char **argv) {
     CcustomSim customSim(data, g.time);
 
     int dt_changed = 0;
+    long long ntot = n;          /* tags handed out so far */
+    std::vector<int> pending;    /* tags marked for deletion, not yet deleted */
     timeval t0, t1;
     gettimeofday(&t0, NULL);
     for (int k = 0; k < nsteps; k++) {
@@ -133,6 +196,47 @@ int main(int argc, char **argv) {
         solver.end();
         customSim.afterEnd(g.time);
         if (g.dt != ORACLE_MAXDT) dt_changed++;
+        for (const Event &ev : events) {
+            if (ev.step != g.sphStep) continue;
+            /* a marked particle (tag -111) keeps its slot until the reset
+             * that deletes it */
+            bool marked_present = false;
+            for (const Cparticle &p : ps) marked_present |= p.tag == -111;
+            if (!marked_present) pending.clear();
+            if (ev.kind == 2) {
+                for (long long idx : ev.del) {
+                    bool found = false;
+                    for (Cparticle &p : ps)
+                        if (p.tag == idx + 1) {
+                            data->markForDeletion(p);
+                            found = true;
+                            break;
+                        }
+                    if (!found) fail("deletion of a particle that is not there");
+                    pending.push_back((int)idx + 1);
+                }
+            } else {
+                /* tags in the library's slot order: the lowest free tag, else the next */
+                std::vector<char> used(ntot + 2 + ev.add.iam.size(), 0);
+                for (const Cparticle &p : ps)
+                    if (p.tag >= 1) used[p.tag] = 1;
+                for (int t : pending) used[t] = 1;
+                long long cursor = 1;
+                for (size_t i = 0; i < ev.add.iam.size(); i++) {
+                    while (cursor <= ntot && used[cursor]) cursor++;
+                    long long t;
+                    if (cursor <= ntot) {
+                        t = cursor;
+                        used[cursor] = 1;
+                    } else {
+                        t = ++ntot;
+                        cursor = ntot + 1;
+                    }
+                    Cparticle p = to_particle(ev.add, (long long)i, (int)t);
+                    data->insertNewParticle(p);
+                }
+            }
+        }
     }
     gettimeofday(&t1, NULL);
     const double sec = (t1.tv_sec - t0.tv_sec) + 1e-6 * (t1.tv_usec - t0.tv_usec);
@@ -141,19 +245,23 @@ int main(int argc, char **argv) {
     /* a fixed-dt case must keep the reference's adaptive dt at maxdt */
     if (timing_only) return (ORACLE_FIXED_DT && dt_changed) ? 3 : 0;
 
-    /* tag -> position in ps (periodic exchange reorders ps) */
+    /* tag -> position in ps (periodic exchange reorders ps); a tag without a
+     * particle was deleted and is written as zeros with alive = 0 */
+    n = ntot;
     std::vector<long long> row_of_tag(n + 1, -1);
     for (size_t i = 0; i < ps.size(); i++) {
         if (ps[i].tag < 1 || ps[i].tag > n) fail("tag out of range");
         row_of_tag[ps[i].tag] = i;
     }
-    for (long long t = 1; t <= n; t++)
-        if (row_of_tag[t] < 0) fail("particle lost (deleted?)");
+    if (events.empty())
+        for (long long t = 1; t <= n; t++)
+            if (row_of_tag[t] < 0) fail("particle lost (deleted?)");
 
     std::vector<Field> fields;
     auto vec_field = [&](const char *name, vect Cparticle::*m) {
         Field f{name, 3, std::vector<double>(3 * n, 0.0)};
         for (long long t = 1; t <= n; t++) {
+            if (row_of_tag[t] < 0) continue;
             const Cparticle &p = ps[row_of_tag[t]];
             for (int d = 0; d < NDIM; d++) f.data[3 * (t - 1) + d] = (p.*m)[d];
         }
@@ -161,9 +269,15 @@ int main(int argc, char **argv) {
     };
     auto sca_field = [&](const char *name, double Cparticle::*m) {
         Field f{name, 1, std::vector<double>(n, 0.0)};
-        for (long long t = 1; t <= n; t++) f.data[t - 1] = ps[row_of_tag[t]].*m;
+        for (long long t = 1; t <= n; t++)
+            if (row_of_tag[t] >= 0) f.data[t - 1] = ps[row_of_tag[t]].*m;
         fields.push_back(f);
     };
+    {
+        Field f{"alive", 1, std::vector<double>(n, 0.0)};
+        for (long long t = 1; t <= n; t++) f.data[t - 1] = row_of_tag[t] >= 0 ? 1.0 : 0.0;
+        fields.push_back(f);
+    }
     vec_field("r", &Cparticle::r);
     vec_field("v", &Cparticle::v);
     vec_field("vhat", &Cparticle::vhat);
@@ -217,7 +331,12 @@ int main(int argc, char **argv) {
     Rel sdrel{"couple_sd", std::vector<std::vector<int> >(n)};
     Rel dsrel{"couple_ds", std::vector<std::vector<int> >(n)};
     int duplicates = 0;
+    /* the reset moved particles: map tags again */
+    std::fill(row_of_tag.begin(), row_of_tag.end(), -1);
+    for (size_t i = 0; i < ps.size(); i++)
+        if (ps[i].tag >= 1 && ps[i].tag <= n) row_of_tag[ps[i].tag] = i;
     for (long long t = 1; t <= n; t++) {
+        if (row_of_tag[t] < 0) continue;
         Cparticle &p = ps[row_of_tag[t]];
         std::vector<Cparticle *> nb;
         data->calcNeighbours(nb, p);
@@ -277,6 +396,7 @@ int main(int argc, char **argv) {
     }
     std::vector<int> cells(3 * n, 0);
     for (long long t = 1; t <= n; t++) {
+        if (row_of_tag[t] < 0) continue;
         Cparticle &p = ps[row_of_tag[t]];
         vectInt c;
 #ifdef LIQ_DEM

@@ -28,6 +28,7 @@ struct sphdem_batch_ctx {
     cudaStream_t stream = nullptr;
     cudaGraphExec_t graph = nullptr;
     std::vector<char> graph_parity;   /* members' buffer parity the graph was captured at */
+    std::vector<long long> graph_gen; /* members' population generation at capture */
     cudaEvent_t ev_fork = nullptr;
     std::vector<cudaEvent_t> ev_join;
     std::string err;
@@ -86,13 +87,19 @@ void capture(sphdem_batch_ctx *b) {
     cudaGraphDestroy(graph);
     check_cuda(e, "instantiate");
     b->graph_parity.resize(b->members.size());
-    for (size_t i = 0; i < b->members.size(); i++) b->graph_parity[i] = b->members[i]->flipped;
+    b->graph_gen.resize(b->members.size());
+    for (size_t i = 0; i < b->members.size(); i++) {
+        b->graph_parity[i] = b->members[i]->flipped;
+        b->graph_gen[i] = b->members[i]->population_gen;
+    }
 }
 
 bool parity_changed(const sphdem_batch_ctx *b) {
     if (!b->graph) return true;
     for (size_t i = 0; i < b->members.size(); i++)
-        if ((char)b->members[i]->flipped != b->graph_parity[i]) return true;
+        if ((char)b->members[i]->flipped != b->graph_parity[i] ||
+            b->members[i]->population_gen != b->graph_gen[i])
+            return true;
     return false;
 }
 

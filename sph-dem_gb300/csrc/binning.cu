@@ -33,7 +33,7 @@ namespace {
 
 constexpr int BLK = 256;
 
-__global__ void k_migrate(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
+__global__ void k_migrate(DevCfg c, DevState s, DevGlobals *g, unsigned char *mark, int64_t n) {
     __shared__ unsigned long long bmax;
     if (threadIdx.x == 0) bmax = 0ull;
     __syncthreads();
@@ -41,6 +41,11 @@ __global__ void k_migrate(DevCfg c, DevState s, DevGlobals *g, int64_t n) {
     double h = -1.0;
     if (i < n) {
         int *iam = s.irow(FI_IAM);
+        if (mark[i]) {
+            /* markForDeletion (tag -111) is honoured first (dataLL.cpp:377-380) */
+            mark[i] = 0;
+            iam[i] = T_DEAD;
+        }
         if (iam[i] != T_DEAD) {
             int oc[3] = {1, 1, 1};
             bool lost = false, out = false;
@@ -446,7 +451,7 @@ void rebuild(sphdem_ctx *c) {
     const int64_t n = c->n;
     const int gb = grid_for(n, BLK);
     Buffers &b = c->buf;
-    SPHDEM_LAUNCH(c, "rebuild_migrate", k_migrate, gb, BLK, 0, c->cfg, c->A, c->g, n);
+    SPHDEM_LAUNCH(c, "rebuild_migrate", k_migrate, gb, BLK, 0, c->cfg, c->A, c->g, c->delmark, n);
     SPHDEM_LAUNCH(c, "rebuild_ghost", k_ghost, gb, BLK, 0, c->cfg, c->A, c->g, n);
     SPHDEM_LAUNCH(c, "rebuild_finalize", k_finalize, 1, 32, 0, c->cfg, c->g);
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(b.cnt, 0, (size_t)b.cells_cap * sizeof(int), c->stream));

@@ -285,6 +285,7 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->dcfg);
     cudaFree(c->cg);
     cudaFree(c->hpred);
+    cudaFree(c->delmark);
     for (int k = 0; k < 4; k++)
         if (c->graph[k]) cudaGraphExecDestroy(c->graph[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -491,6 +492,8 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
         if (cfg->flags & SPHDEM_F_CORRECTED_GRADIENT)
             SPHDEM_CUDA_CHECK(cudaMalloc(&c->cg, (size_t)CG_ROWS * capacity * sizeof(double)));
         if (reinit_configured(*cfg)) SPHDEM_CUDA_CHECK(cudaMalloc(&c->hpred, capacity * sizeof(double)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&c->delmark, capacity));
+        SPHDEM_CUDA_CHECK(cudaMemset(c->delmark, 0, capacity));
 
         /* globals as the CdataLL constructor leaves them (dataLL.cpp:8-40) */
         DevGlobals hg;
@@ -635,6 +638,30 @@ int sphdem_step(sphdem_handle h, int nsteps) {
     const int rc = check_device(h);
     collect_times(h);
     return rc;
+}
+
+int sphdem_insert_particles(sphdem_handle h, const SphDemParticles *in, int64_t *out_idx) {
+    if (!h || !in || in->n < 0) return SPHDEM_ERR_INVALID;
+    if (in->n > 0 && (!in->iam || !in->r || !in->mass || !in->dens || !in->h))
+        return fail(h, SPHDEM_ERR_INVALID, "iam, r, mass, dens and h are required");
+    int rc;
+    try {
+        rc = insert_particles(h, in, out_idx);
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+    return rc != SPHDEM_OK ? rc : check_device(h);
+}
+
+int sphdem_mark_for_deletion(sphdem_handle h, const int64_t *idx, int64_t k) {
+    if (!h || k < 0 || (k > 0 && !idx)) return SPHDEM_ERR_INVALID;
+    int rc;
+    try {
+        rc = mark_for_deletion(h, idx, k);
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+    return rc != SPHDEM_OK ? rc : check_device(h);
 }
 
 int sphdem_rebuild(sphdem_handle h) {

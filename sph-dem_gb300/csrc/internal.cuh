@@ -62,6 +62,9 @@ struct sphdem_ctx {
     /* CORRECTED_GRADIENT rows (CG_ROWS x cap) and the density re-initialisation's
      * first smoothing length (cap) */
     double *cg = nullptr, *hpred = nullptr;
+    /* particles marked for deletion (state order), removed by the next rebuild */
+    unsigned char *delmark = nullptr;
+    long long population_gen = 0;   /* bumped by every insertion (captured graphs hold n) */
     bool in_capture = false;
     /* timing */
     bool timing = false;
@@ -166,6 +169,10 @@ void dem_end(sphdem_ctx *c);
 /* pairs32.cu: the mixed lists of the last rebuild as the adjoint's pair
  * tables (tag space, slot *slot of nb / oc / cnt) */
 void mixed_adj_pairs(sphdem_ctx *c, int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot);
+
+/* population.cu: insertNewParticle / markForDeletion (synchronise) */
+int insert_particles(sphdem_ctx *c, const SphDemParticles *in, int64_t *out_idx);
+int mark_for_deletion(sphdem_ctx *c, const int64_t *idx, int64_t k);
 
 /* diagnostics.cu: calcOutputVars on the device (synchronises) */
 int output_vars(sphdem_ctx *c, SphDemOutputVars *out);

@@ -31,6 +31,7 @@ const double BFAC = 1.0;
 const int OUTSTEP = 10;
 const double MAXTIME = 5.986414282632196e-05 * OUTSTEP;
 const double DAMPTIME = 0.0;
+const int MAX_NUM_PARTICLES_PER_CPU = 2456;
 const int REINIT_DENS_EVERY_N_STEPS = 50000000;
 const int REINIT_DENS_AT_N_STEPS = 50000000;
 const double TIME_DROP_PARTICLE = 1e+30;

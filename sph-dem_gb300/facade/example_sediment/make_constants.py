@@ -51,6 +51,7 @@ def constants(name: str = "sediment3d_small") -> str:
         f"const int OUTSTEP = {outstep};",
         f"const double MAXTIME = {r(c['maxdt'])} * OUTSTEP;",
         f"const double DAMPTIME = {r(c['damptime'])};",
+        f"const int MAX_NUM_PARTICLES_PER_CPU = {case.n + 256};",
         f"const int REINIT_DENS_EVERY_N_STEPS = {int(c['reinit_dens_every']) or 50000000};",
         f"const int REINIT_DENS_AT_N_STEPS = {int(c['reinit_dens_at']) or 50000000};",
         f"const double TIME_DROP_PARTICLE = {r(c['time_drop_particle'])};",

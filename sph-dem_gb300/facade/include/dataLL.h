@@ -8,11 +8,16 @@
  * mutable fields (r, v, vhat, f/fp/fv/fb, dens, h) and the globals back.
  * traverse / neighboursGroup run the case functors on the mirror
  * (dataLL.h:125-176); neighbour lists come from the device's own list
- * (sphdem_pairs) and are fetched once per pull.
+ * (sphdem_pairs) and are fetched once per pull.  insertNewParticle and
+ * markForDeletion (dataLL.cpp:238-266) queue on the mirror and reach the
+ * device at push(): marked particles leave at its next rebuild, inserted
+ * ones take the lowest free slots (sphdem_insert_particles), and the
+ * mirror grows to the device's particle count.
  */
 #ifndef DATALL_H
 #define DATALL_H
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -41,8 +46,16 @@ class CdataLL {
 
     /* device -> mirror (all fields, globals); neighbour lists on demand */
     void pull();
-    /* mirror -> device (mutable fields, globals) */
+    /* mirror -> device (mutable fields, globals, deletions, insertions) */
     void push();
+
+    /* CdataLL::insertNewParticle (dataLL.cpp:238-261) */
+    void insertNewParticle(Cparticle &newP) { pending_insert.push_back(newP); }
+    /* CdataLL::markForDeletion (dataLL.cpp:263-266) */
+    void markForDeletion(Cparticle &p) { p.tag = -111; }
+    /* CdataLL::deleteParticles (dataLL.cpp:272-283): marked particles leave at
+     * the device's next rebuild, which every neighbour pass follows */
+    void deleteParticles() {}
 
     template <void Thefunct(Cparticle &, CglobalVars &)>
     void traverse() {
@@ -77,6 +90,7 @@ class CdataLL {
    private:
     particleContainer &ps;
     sphdem_handle h;
+    vector<Cparticle> pending_insert;
     vector<vector<Cparticle *> > nbrs;
     bool lists_valid = false;
     vector<double> vr, vv, vvh, vv0, vvh0, vf, vfp, vfv, vfb, vfd, vfvel, vgp, vn1, vn2, vn3;
@@ -168,6 +182,49 @@ inline void CdataLL::push() {
     g.time = globals.time;
     g.maxdt = globals.maxdt;
     check(sphdem_set_globals(h, &g), "sphdem_set_globals");
+    vector<int64_t> del;
+    for (size_t i = 0; i < ps.size(); i++)
+        if (ps[i].tag == -111 && viam[i] >= 0) del.push_back((int64_t)i);
+    if (!del.empty()) check(sphdem_mark_for_deletion(h, del.data(), (int64_t)del.size()), "sphdem_mark_for_deletion");
+    if (!pending_insert.empty()) {
+        const size_t k = pending_insert.size();
+        vector<int32_t> iam(k);
+        vector<uint8_t> conc(k);
+        vector<double> r(3 * k, 0.0), v(3 * k, 0.0), vh(3 * k, 0.0), n1(3 * k, 0.0), n2(3 * k, 0.0), n3(3 * k, 0.0);
+        vector<double> m(k), d(k), hh(k), rad(k);
+        for (size_t j = 0; j < k; j++) {
+            const Cparticle &q = pending_insert[j];
+            iam[j] = (int32_t)q.iam;
+            conc[j] = q.concave ? 1 : 0;
+            for (int a = 0; a < NDIM; a++) {
+                r[3 * j + a] = q.r[a];
+                v[3 * j + a] = q.v[a];
+                vh[3 * j + a] = q.vhat[a];
+                n1[3 * j + a] = q.norm1[a];
+                n2[3 * j + a] = q.norm2[a];
+                n3[3 * j + a] = q.norm3[a];
+            }
+            m[j] = q.mass;
+            d[j] = q.dens;
+            hh[j] = q.h;
+            rad[j] = q.radius;
+        }
+        SphDemParticles in;
+        std::memset(&in, 0, sizeof in);
+        in.n = (int64_t)k;
+        in.iam = iam.data(); in.concave = conc.data();
+        in.r = r.data(); in.v = v.data(); in.vhat = vh.data();
+        in.norm1 = n1.data(); in.norm2 = n2.data(); in.norm3 = n3.data();
+        in.mass = m.data(); in.dens = d.data(); in.h = hh.data(); in.radius = rad.data();
+        vector<int64_t> slot(k);
+        check(sphdem_insert_particles(h, &in, slot.data()), "sphdem_insert_particles");
+        size_t n = ps.size();
+        for (int64_t s : slot) n = std::max(n, (size_t)s + 1);
+        ps.resize(n);
+        for (size_t j = 0; j < k; j++) ps[slot[j]] = pending_insert[j];
+        pending_insert.clear();
+        lists_valid = false;
+    }
 }
 
 inline void CdataLL::lists() {

@@ -12,6 +12,7 @@
  * The final state is written as r, v, vhat, f, dens, h per particle (tag
  * order) after a 16-byte header ("SPDMFAC1", n).
  */
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <cstdlib>
@@ -100,7 +101,9 @@ int main(int argc, char *argv[]) {
     const int nsteps = std::atoi(argv[2]);
     SphDemConfig cfg = sphdem_case_config(mixed ? SPHDEM_PREC_MIXED : SPHDEM_PREC_FP64, fixed_dt);
     sphdem_handle h = nullptr;
-    if (sphdem_create(&cfg, &init, init.n, &h) != SPHDEM_OK) {
+    /* room for the particles the case's hooks insert (dataLL.cpp:241) */
+    const int64_t capacity = std::max<int64_t>(init.n, MAX_NUM_PARTICLES_PER_CPU);
+    if (sphdem_create(&cfg, &init, capacity, &h) != SPHDEM_OK) {
         std::cerr << "sphdem_create failed" << std::endl;
         return -1;
     }
@@ -121,6 +124,7 @@ int main(int argc, char *argv[]) {
     };
     int outstep = 0;
     for (int s = 0; s < nsteps; s++) {
+        phase(SPHDEM_HOOK_BEFORE_START, "step");   /* globals.sphStep++ (run.cpp:104) */
         data.pull();
         customSim.beforeStart(globals.time);
         data.push();

@@ -238,6 +238,8 @@ class Library:
         L.sphdem_get_globals.argtypes = [H, C.POINTER(SphDemGlobals)]
         L.sphdem_set_globals.argtypes = [H, C.POINTER(SphDemGlobals)]
         L.sphdem_rebuild.argtypes = [H]
+        L.sphdem_insert_particles.argtypes = [H, C.POINTER(SphDemParticles), C.POINTER(C.c_int64)]
+        L.sphdem_mark_for_deletion.argtypes = [H, C.POINTER(C.c_int64), C.c_int64]
         L.sphdem_pairs.argtypes = [H, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                    C.c_int64, C.POINTER(C.c_int64)]
         L.sphdem_cell_ids.argtypes = [H, C.POINTER(C.c_int32)]
@@ -302,6 +304,24 @@ class Simulation:
 
     def rebuild(self):
         self.L.check(self.L.lib.sphdem_rebuild(self.h), self.h, "sphdem_rebuild")
+
+    def insert(self, particles: dict) -> np.ndarray:
+        """sphdem_insert_particles: the tag-order index each new particle took."""
+        k = int(particles["iam"].shape[0])
+        buf = ParticleBuffers(k, particles)
+        out = np.zeros(max(k, 1), np.int64)
+        self.L.check(self.L.lib.sphdem_insert_particles(self.h, buf.ref(), out.ctypes.data_as(C.POINTER(C.c_int64))),
+                     self.h, "sphdem_insert_particles")
+        out = out[:k]
+        if k:
+            self.n = max(self.n, int(out.max()) + 1)
+        return out
+
+    def mark_for_deletion(self, idx):
+        idx = np.ascontiguousarray(idx, np.int64).reshape(-1)
+        self.L.check(self.L.lib.sphdem_mark_for_deletion(self.h, idx.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                         int(idx.size)),
+                     self.h, "sphdem_mark_for_deletion")
 
     def get(self, mask: int = FIELD_ALL, out: ParticleBuffers | None = None) -> ParticleBuffers:
         out = out or ParticleBuffers(self.n)

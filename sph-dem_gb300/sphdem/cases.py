@@ -52,10 +52,17 @@ class Case:
     particles: dict
     nsteps: int
     notes: dict = field(default_factory=dict)
+    # insertions and deletions after a step's last hook: {"step": s,
+    # "insert": particle block} or {"step": s, "delete": tag-order indices}
+    events: list = field(default_factory=list)
 
     @property
     def n(self) -> int:
         return int(self.particles["iam"].shape[0])
+
+    @property
+    def n_inserted(self) -> int:
+        return sum(int(e["insert"]["iam"].shape[0]) for e in self.events if "insert" in e)
 
 
 def _base_cfg(ndim: int) -> dict:
@@ -427,6 +434,63 @@ def dambreak_ensemble(n_instances: int = 256, seed: int = 5, n_min: int = 2000, 
     return out
 
 
+def advance(sim, case: Case, nsteps: int | None = None, start: int = 0) -> None:
+    """Step `sim` (anything with step / insert / mark_for_deletion: a
+    capi.Simulation, the oracle) through steps start+1 .. start+nsteps of the
+    case, applying its insertions and deletions after the steps they follow,
+    as a case's afterEnd hook would."""
+    end = start + (case.nsteps if nsteps is None else nsteps)
+    s = start
+    for t in sorted({e["step"] for e in case.events if start < e["step"] <= end}):
+        sim.step(t - s)
+        s = t
+        for e in case.events:
+            if e["step"] == t:
+                if "insert" in e:
+                    sim.insert(e["insert"])
+                else:
+                    sim.mark_for_deletion(e["delete"])
+    if end > s:
+        sim.step(end - s)
+
+
+def dambreak2d_flow(dx: float = 0.05, nsteps: int = 30, seed: int = 7) -> Case:
+    """The small dam break with particles leaving and entering between steps:
+    after step 8 every 13th fluid particle is marked for deletion; after step
+    12 a row of fluid particles enters above the column, falling at 1 m/s
+    (taking the freed slots); after step 20 every 17th fluid particle more
+    and two wall particles go; after step 22 five more rows enter (more than
+    the free slots, so the last ones are appended)."""
+    case = dambreak2d(dx=dx, nsteps=nsteps, seed=seed)
+    ps = case.particles
+    fluid = np.nonzero(ps["iam"] == SPH)[0]
+    k = fluid - fluid[0]
+    rng = np.random.default_rng(seed + 100)
+    rho0, nx = case.cfg["dens"], int(round(1.0 / dx))
+    top = float(ps["r"][fluid, 1].max())
+
+    def rows(y0: float, nrows: int) -> dict:
+        ii, jj = np.meshgrid(np.arange(nx), np.arange(nrows), indexing="ij")
+        m = nx * nrows
+        blk = _empty_particles(m)
+        blk["r"][:, 0] = (ii.ravel() + 0.5) * dx
+        blk["r"][:, 1] = y0 + jj.ravel() * dx
+        blk["r"][:, :2] += rng.uniform(-0.01 * dx, 0.01 * dx, size=(m, 2))
+        blk["v"][:, 1] = -1.0
+        blk["iam"][:] = SPH
+        blk["mass"][:] = dx * dx * rho0
+        blk["dens"][:] = rho0
+        blk["h"][:] = 1.3 * dx
+        return blk
+
+    del1 = fluid[k % 13 == 0]
+    del2 = np.concatenate([fluid[(k % 17 == 5) & (k % 13 != 0)], [0, 1]])
+    case.events = [{"step": 8, "delete": del1}, {"step": 12, "insert": rows(top + dx, 1)},
+                   {"step": 20, "delete": del2}, {"step": 22, "insert": rows(top + 2 * dx, 5)}]
+    case.notes["events"] = "8: -%d, 12: +%d, 20: -%d, 22: +%d" % (del1.size, nx, del2.size, 5 * nx)
+    return case
+
+
 def workload(name: str, **kw) -> Case:
     """The five configurations at full size, plus the small variants used as
     golden-fixture and parity cases."""
@@ -464,6 +528,9 @@ def workload(name: str, **kw) -> Case:
                                                  nsteps=600, vel_amp=0.3),
         "sediment3d_small": lambda: sediment3d(nx=10, L=0.04, height=0.08, n_dem=100,
                                                nsteps=20),
+        # particles deleted and inserted between steps (insertNewParticle,
+        # markForDeletion)
+        "dambreak2d_flow_small": lambda: dambreak2d_flow(),
         # coupled, DEM moving as one block under the mean DEM force
         "sediment3d_block_small": lambda: sediment3d(nx=10, L=0.04, height=0.08, n_dem=100, nsteps=20,
                                                      dem_block=True, seed=6),

@@ -1,7 +1,10 @@
 """Binary particle-state files shared by the reference driver, the CPU oracle
 and the tests.
 
-Input state (``SPDMST01``): the initial particles of a case, in tag order.
+Input state (``SPDMST01``): the initial particles of a case, in tag order,
+optionally followed by a schedule of insertions and deletions (``SPDMEV01``:
+per event its step, kind 1 = insert a particle block / 2 = mark tag-order
+indices for deletion, and the payload), applied after the step's last hook.
 Output state (``SPDMOUT1``): per-particle fields in tag order, the neighbour
 relations as CSR over tag order (rows sorted ascending), the bucket index of
 every particle and the final time / dt.
@@ -13,23 +16,43 @@ import struct
 import numpy as np
 
 IN_MAGIC = b"SPDMST01"
+EV_MAGIC = b"SPDMEV01"
 OUT_MAGIC = b"SPDMOUT1"
 
 
-def write_state(path, ps: dict) -> None:
+def _write_block(fh, ps: dict, with_tag: bool) -> None:
+    fh.write(np.ascontiguousarray(ps["iam"], "<i4").tobytes())
+    if with_tag:
+        fh.write(np.ascontiguousarray(ps["tag"], "<i4").tobytes())
+    fh.write(np.ascontiguousarray(ps["concave"], "<i4").tobytes())
+    for k in ("r", "v"):
+        fh.write(np.ascontiguousarray(ps[k], "<f8").tobytes())
+    for k in ("mass", "dens", "h", "radius"):
+        fh.write(np.ascontiguousarray(ps[k], "<f8").tobytes())
+    for k in ("norm1", "norm2", "norm3"):
+        fh.write(np.ascontiguousarray(ps[k], "<f8").tobytes())
+
+
+def write_state(path, ps: dict, events=()) -> None:
+    """events: dicts {"step": s, "insert": particle block} or
+    {"step": s, "delete": tag-order indices}."""
     n = ps["iam"].shape[0]
     with open(path, "wb") as fh:
         fh.write(IN_MAGIC)
         fh.write(struct.pack("<q", n))
-        fh.write(np.ascontiguousarray(ps["iam"], "<i4").tobytes())
-        fh.write(np.ascontiguousarray(ps["tag"], "<i4").tobytes())
-        fh.write(np.ascontiguousarray(ps["concave"], "<i4").tobytes())
-        for k in ("r", "v"):
-            fh.write(np.ascontiguousarray(ps[k], "<f8").tobytes())
-        for k in ("mass", "dens", "h", "radius"):
-            fh.write(np.ascontiguousarray(ps[k], "<f8").tobytes())
-        for k in ("norm1", "norm2", "norm3"):
-            fh.write(np.ascontiguousarray(ps[k], "<f8").tobytes())
+        _write_block(fh, ps, True)
+        if events:
+            fh.write(EV_MAGIC)
+            fh.write(struct.pack("<q", len(events)))
+            for ev in events:
+                if "insert" in ev:
+                    blk = ev["insert"]
+                    fh.write(struct.pack("<qqq", ev["step"], 1, blk["iam"].shape[0]))
+                    _write_block(fh, blk, False)
+                else:
+                    idx = np.ascontiguousarray(ev["delete"], "<i8")
+                    fh.write(struct.pack("<qqq", ev["step"], 2, idx.shape[0]))
+                    fh.write(idx.tobytes())
 
 
 def read_output(path) -> dict:

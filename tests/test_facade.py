@@ -88,3 +88,89 @@ def test_case_hooks_match_device_hooks(tmp_path, precision):
         err = np.abs(a[k] - b[k]).max() / scale
         print(precision, k, err)
         assert err <= tol, f"{k}: {err}"
+
+
+HOOK_H = """#ifndef CUSTOMSIM_H
+#define CUSTOMSIM_H
+#include "customConstants.h"
+#include "customSimBase.h"
+#include "dataLL.h"
+#include "sph.h"
+#include "vect.h"
+class CcustomSim : public CcustomSimBase {
+   public:
+    CcustomSim(CdataLL *_data, double _time) : CcustomSimBase(_data, _time) {}
+    void beforeMiddle(double newTime);
+    void beforeEnd(double newTime);
+    void afterEnd(double newTime);
+};
+#endif
+"""
+
+# after the second step: every 50th fluid particle is marked for deletion and
+# three spheres are inserted, through the reference's own CdataLL calls
+HOOK_CPP = """
+void CcustomSim::afterEnd(double newTime) {
+    static int step = 0;
+    if (++step != 2) return;
+    particleContainer &ps = data->getParticles();
+    int k = 0;
+    for (size_t i = 0; i < ps.size(); i++)
+        if (ps[i].iam == sph && (k++ % 50) == 0) data->markForDeletion(ps[i]);
+    for (int j = 0; j < 3; j++) {
+        Cparticle p;
+        p.iam = dem;
+        p.r = vect(0.01 * (j + 1), 0.02, 0.072);
+        p.mass = DEM_VOL * DEM_DENS;
+        p.dens = DEM_DENS;
+        p.h = DEM_RADIUS;
+        p.radius = DEM_RADIUS;
+        data->insertNewParticle(p);
+    }
+}
+"""
+
+
+@pytest.mark.gpu
+def test_case_hook_insertion_and_deletion(tmp_path):
+    """insertNewParticle / markForDeletion in a case hook, through the
+    façade, against the same changes made through the C ABI."""
+    import shutil
+    import __graft_entry__
+    __graft_entry__.build()
+    src = os.path.join(FACADE, "example_sediment")
+    case_dir = tmp_path / "case"
+    shutil.copytree(src, case_dir, ignore=shutil.ignore_patterns("__pycache__"))
+    (case_dir / "customSim.h").write_text(HOOK_H)
+    with open(case_dir / "customSim.cpp", "a") as fh:
+        fh.write(HOOK_CPP)
+    exe = build_case(str(case_dir), str(tmp_path / "run_case"))
+    case = cases.workload("sediment3d_small")
+    init = tmp_path / "init.spdm"
+    state.write_state(str(init), case.particles)
+    final = tmp_path / "final.bin"
+    res = subprocess.run([exe, str(init), "5", str(final), "--fixed-dt"], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0, res.stderr[-2000:]
+    a = read_final(str(final))
+
+    lib = capi.Library()
+    sim = capi.Simulation(lib, case.cfg, case.particles, capacity=case.n + 256)
+    sim.step(2)
+    fluid = np.nonzero(case.particles["iam"] == cases.SPH)[0]
+    sim.mark_for_deletion(fluid[::50])
+    R = case.cfg["dem_radius"]
+    blk = {"iam": np.full(3, cases.DEM, np.int32), "r": np.array([[0.01 * (j + 1), 0.02, 0.072] for j in range(3)]),
+           "mass": np.full(3, case.cfg["dem_vol"] * case.cfg["dem_dens"]), "dens": np.full(3, case.cfg["dem_dens"]),
+           "h": np.full(3, R), "radius": np.full(3, R)}
+    idx = sim.insert(blk)
+    assert list(idx) == [case.n, case.n + 1, case.n + 2]   # no slot is free before the next rebuild
+    sim.step(3)
+    b = sim.get()
+    live = b["iam"] >= 0
+    assert (~live).sum() == fluid[::50].size
+    assert a["r"].shape[0] == b.n
+    for k in ("r", "vhat", "dens"):
+        scale = np.abs(b[k][live]).max()
+        err = np.abs(a[k][live] - b[k][live]).max() / scale
+        assert err <= 1e-12, f"{k}: {err}"
