@@ -558,7 +558,8 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
                 int maxn = std::max(32, (int)(1.6 * m) + 16);
                 maxn = (maxn + 31) / 32 * 32;
                 c->mx_maxn = maxn;
-                SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_nbr, (size_t)maxn * capacity * sizeof(int)));
+                /* list tiles of 32 particles x 8 entries */
+                SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_nbr, (size_t)maxn * ((capacity + 31) / 32 * 32) * sizeof(int)));
             }
         }
         int rc = check_device(c);

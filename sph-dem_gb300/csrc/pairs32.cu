@@ -421,6 +421,32 @@ __device__ __noinline__ bool exact_from_code(const DevCfg &c, const DevState &s,
     return exact_neighbour<ND>(c, s, a, e & B_MASK, sh);
 }
 
+/* FP64 decision of list entry e of particle a, its bucket from the key row */
+template <int ND>
+__device__ __noinline__ bool exact_from_key(const DevCfg &c, const DevState &s, const DevGlobals *g,
+                                            const int *skey, int a, int e) {
+    const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
+    int cc[3] = {0, 0, 0};
+    decode<ND>(skey[a], dims, cc);
+    return exact_from_code<ND>(c, s, g, a, e, cc);
+}
+
+/* Neighbour lists: slot j of particle a, in tiles of 32 particles x 8
+ * entries -- each particle's 8 entries contiguous, the 32 particles' groups
+ * back to back -- so a warp of consecutive particles reads 8 entries each
+ * with two coalesced int4 loads and the build writes a particle's entries in
+ * runs.  maxn (the list depth) is a multiple of 8. */
+__device__ __forceinline__ int64_t nl_at(int64_t a, int j, int64_t maxn) {
+    return ((a >> 5) * maxn + (j & ~7)) * 32 + ((a & 31) << 3) + (j & 7);
+}
+
+/* lane bits [lo, hi), 0 <= lo <= hi <= 32 */
+__device__ __forceinline__ unsigned lane_range(int lo, int hi) {
+    const unsigned up = hi >= 32 ? 0xffffffffu : ((1u << hi) - 1u);
+    const unsigned dn = lo >= 32 ? 0xffffffffu : ((1u << lo) - 1u);
+    return up & ~dn;
+}
+
 template <int ND, bool COUNT>
 __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s, const int *__restrict__ start,
                                                          const int *__restrict__ skey, DevGlobals *__restrict__ g,
@@ -430,8 +456,8 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
                                                          int *__restrict__ bandn) {
     constexpr int Z = ND - 1;
     constexpr unsigned FULL = 0xffffffffu;
-    __shared__ float4 s_pos[NL_WARPS][NL_CAP];
-    __shared__ int s_ent[NL_WARPS][NL_CAP];
+    __shared__ float4 s_pos[NL_WARPS][NL_CAP + 32];
+    __shared__ int s_ent[NL_WARPS][NL_CAP + 32];
     __shared__ unsigned char s_zr[NL_WARPS][NL_CAP];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
@@ -473,7 +499,6 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
         float4 pa0 = make_float4(0.f, 0.f, 0.f, 0.f);
         if (act) pa0 = P0[a];
         int cnt = 0, nb = 0;
-        int *outp = nbr + a;
         unsigned pending = __ballot_sync(FULL, act);
         while (pending) {
             /* a run: lanes in the leader's column within 3 buckets of it */
@@ -512,42 +537,117 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
             zt_hi += supp;
             int nst = 0;
 
+            /* Test the staged candidates 32 at a time, branch-free: one bit per
+             * candidate that passes the widened FP32 test (the staged set is
+             * padded to a multiple of 32 with far-away entries; each staged w
+             * holds the candidate's own threshold K_HI h_b^2 + EPS).  The warp
+             * then writes the passing entries of all its lanes together: the
+             * t-th entry of the chunk goes to the lane whose prefix of pass
+             * counts covers t, and each particle's entries land in consecutive
+             * slots of its 8-entry list tiles, so the stores coalesce.  The
+             * particle itself and band candidates outside the particle's own
+             * stencil leave a hole (-1), which every reader skips. */
+            const float thr_a = fmaf(ha2, K_HI, EPS);
+            const int my_zr = lane_zr;
             auto evaluate = [&]() {
+                if (lane < ((32 - (nst & 31)) & 31)) {
+                    cpos[nst + lane] = make_float4(-1e30f, -1e30f, -1e30f, 0.f);
+                    cent[nst + lane] = 0;
+                }
                 __syncwarp();
-#pragma unroll 4
-                for (int j = 0; j < nst; j++) {
-                    const float4 q = cpos[j];
-                    const float dx = pv[0] - q.x;
-                    const float dy = ND > 1 ? pv[1] - q.y : 0.f;
-                    const float dz = ND > 2 ? pv[2] - q.z : 0.f;
-                    const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-                    const float m2 = fmaxf(ha2, q.w);
-                    if (!(r2 <= fmaf(m2, K_HI, EPS))) continue;
-                    const int dzc = (int)czr[j] - lane_zr;
-                    int e = cent[j] + (dzc + 1) * zstride;
-                    if ((e ^ a) == self_e) continue; /* the particle itself */
+                for (int j0 = 0; j0 < nst; j0 += 32) {
+                    unsigned pm = 0u;
+#pragma unroll 8
+                    for (int jj = 0; jj < 32; jj++) {
+                        const float4 q = cpos[j0 + jj];
+                        const float dx = pv[0] - q.x;
+                        const float dy = ND > 1 ? pv[1] - q.y : 0.f;
+                        const float dz = ND > 2 ? pv[2] - q.z : 0.f;
+                        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                        pm |= (r2 <= fmaxf(thr_a, q.w) ? 1u : 0u) << jj;
+                    }
+                    const int c_i = __popc(pm);
                     if (COUNT) {
-                        cnt++;
+                        cnt += c_i;
                         continue;
                     }
-                    if (r2 >= fmaf(m2, K_LO, -EPS)) {
-                        /* buckets are at least 2h wide, so a candidate outside this
-                         * particle's own 3^d stencil is at least 2h away: it can only
-                         * pass the FP32 test inside the band, and is no neighbour */
-                        if ((unsigned)(dzc + 1) > 2u) continue;
-                        if (cnt < maxn) {
-                            if (nb < NL_QB) {
-                                bandq[(int64_t)a * NL_QB + nb] = make_int2(e, cnt);
-                                e |= (int)0x80000000u;
-                            } else if (!exact_from_code<ND>(c, s, g, a, e, cc)) {
-                                continue; /* record full: decided here (slow but exact) */
-                            }
-                            nb++;
-                        }
+                    int incl = c_i;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int v = __shfl_up_sync(FULL, incl, o);
+                        if (lane >= o) incl += v;
                     }
-                    if (cnt < maxn) *outp = e;
-                    outp += ld;
-                    cnt++;
+                    const int T = __shfl_sync(FULL, incl, 31);
+                    const int my_ex = incl - c_i;
+                    for (int base = 0; base < T; base += 32) {
+                        const int t = base + lane;
+                        /* owner: the first lane whose inclusive count exceeds t */
+                        int i = 0;
+#pragma unroll
+                        for (int step = 16; step > 0; step >>= 1) {
+                            const int v = __shfl_sync(FULL, incl, i + step - 1);
+                            if (v <= t) i += step;
+                        }
+                        const unsigned pmi = __shfl_sync(FULL, pm, i);
+                        const int exi = __shfl_sync(FULL, my_ex, i);
+                        const int cni = __shfl_sync(FULL, cnt | (nb << 16), i);
+                        const int zri = __shfl_sync(FULL, my_zr, i);
+                        const float pxi = __shfl_sync(FULL, pv[0], i);
+                        const float pyi = __shfl_sync(FULL, pv[1], i);
+                        const float pzi = __shfl_sync(FULL, pv[2], i);
+                        const float h2i = __shfl_sync(FULL, ha2, i);
+                        const bool on = t < T;
+                        int e = -1, slot = 0, j = 0;
+                        const int ai = t0 + i;
+                        bool band = false;
+                        if (on) {
+                            /* the r-th set bit of the owner's mask */
+                            const int r = t - exi;
+                            unsigned m = pmi;
+                            int bit = 0, rr = r;
+#pragma unroll
+                            for (int w2 = 16; w2 > 0; w2 >>= 1) {
+                                const int cl = __popc(m & ((1u << w2) - 1u));
+                                if (rr >= cl) {
+                                    rr -= cl;
+                                    m >>= w2;
+                                    bit += w2;
+                                }
+                            }
+                            j = j0 + bit;
+                            slot = (cni & 0xffff) + r;
+                            e = (int)((unsigned)cent[j] + (unsigned)(1 - zri) * (unsigned)zstride);
+                            if (e == (ai | self_e)) {
+                                e = -1; /* the particle itself */
+                            } else {
+                                const float4 q = cpos[j];
+                                const float dx = pxi - q.x;
+                                const float dy = ND > 1 ? pyi - q.y : 0.f;
+                                const float dz = ND > 2 ? pzi - q.z : 0.f;
+                                const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+                                band = r2 >= fmaf(fmaxf(h2i, q.w * (1.f / K_HI)), K_LO, -2.f * EPS);
+                            }
+                        }
+                        const unsigned bb = __ballot_sync(FULL, band);
+                        if (band) {
+                            /* buckets are at least 2h wide, so a candidate outside this
+                             * particle's own 3^d stencil is at least 2h away: it can only
+                             * pass the FP32 test inside the band, and is no neighbour */
+                            const bool in_stencil = (unsigned)((int)czr[j] - zri + 1) <= 2u;
+                            const int qb = (cni >> 16) + __popc(bb & lane_range(max(exi - base, 0), lane));
+                            if (qb < NL_QB) {
+                                bandq[(int64_t)ai * NL_QB + qb] =
+                                    in_stencil && slot < maxn ? make_int2(e, slot) : make_int2(-1, -1);
+                                e = in_stencil ? (e | (int)0x80000000u) : -1;
+                            } else if (!in_stencil || !exact_from_key<ND>(c, s, g, skey, ai, e)) {
+                                e = -1; /* record full: decided here (slow but exact) */
+                            }
+                        }
+                        if (on && slot < maxn) nbr[nl_at(ai, slot, maxn)] = e;
+                        /* band records of this lane's own entries in this round */
+                        nb += __popc(bb & lane_range(min(max(my_ex - base, 0), 32), min(max(my_ex + c_i - base, 0), 32)));
+                    }
+                    cnt += c_i;
                 }
                 __syncwarp();
                 nst = 0;
@@ -669,8 +769,10 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
                     if (Z > 0) qv[0] += ox;
                     if (Z > 1) qv[1] += oy;
                     qv[Z] += (float)zrel * cz;
-                    cpos[pos] = make_float4(qv[0], qv[1], qv[2], pb.w * pb.w);
-                    cent[pos] = k | code;
+                    cpos[pos] = make_float4(qv[0], qv[1], qv[2], fmaf(pb.w * pb.w, K_HI, EPS));
+                    /* k | code of the candidate's bucket relative to the run's
+                     * first bucket - 1; evaluate adds the lane's own offset */
+                    cent[pos] = (int)((unsigned)(k | code) + (unsigned)(zrel + 1) * (unsigned)zstride);
                     czr[pos] = (unsigned char)(zrel + 1);
                 }
                 nst += __popc(m);
@@ -719,13 +821,14 @@ __global__ void k_band_fix(DevCfg c, DevState s, const DevGlobals *__restrict__ 
         const float4 pa = P0[a], al = P0lo[a];
         for (int k = 0; k < nb; k++) {
             const int2 it = bandq[(int64_t)a * NL_QB + k];
+            if (it.y < 0) continue; /* a blank record */
             const int e = it.x, b = e & B_MASK;
             int o[3];
             nl_decode_code(e >> B_BITS, o);
             int dec = nl_refine<ND>(pa, al, P0[b], P0lo[b], o, cell, cell_lo, 1e-13f * cmax * cmax);
             /* an FP64 tie: the reference's predicate on the periodic image */
             if (dec == 0) dec = exact_from_code<ND>(c, s, g, a, e, cc) ? 1 : -1;
-            nbr[(int64_t)it.y * ld + a] = dec > 0 ? e : -1;
+            nbr[nl_at(a, it.y, ld)] = dec > 0 ? e : -1;
         }
     }
 }
@@ -780,9 +883,18 @@ __global__ void __launch_bounds__(BLK) k_omega_eos(DevCfg c, DevState s, const D
         Kahan om;
         om.init(-P1[a].w * pd_coef * wK32(0.f, wcon));
         const int cnt = ncnt[a];
+        /* 8 entries at a time from the particle's list tiles (two int4 loads) */
+        const int4 *tile = reinterpret_cast<const int4 *>(nbr + nl_at(a, 0, ld));
+        int4 q0 = make_int4(-1, -1, -1, -1), q1 = q0;
 #pragma unroll 2
         for (int j = 0; j < cnt; j++) {
-            const int e = nbr[(int64_t)j * ld + a];
+            if ((j & 7) == 0) {
+                q0 = __ldg(tile + (j >> 3) * 64);
+                q1 = __ldg(tile + (j >> 3) * 64 + 1);
+            }
+            const int e = q0.x;
+            q0 = make_int4(q0.y, q0.z, q0.w, q1.x);
+            q1 = make_int4(q1.y, q1.z, q1.w, -1);
             if (e < 0) continue;
             const int b = e & B_MASK;
             const float4 pb = P0[b];
@@ -938,9 +1050,18 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
             fa[k].init(0.f);
         }
         const int cnt = ncnt[a];
+        /* 8 entries at a time from the particle's list tiles (two int4 loads) */
+        const int4 *tile = reinterpret_cast<const int4 *>(nbr + nl_at(a, 0, ld));
+        int4 q0 = make_int4(-1, -1, -1, -1), q1 = q0;
 #pragma unroll 2
         for (int j = 0; j < cnt; j++) {
-            const int e = nbr[(int64_t)j * ld + a];
+            if ((j & 7) == 0) {
+                q0 = __ldg(tile + (j >> 3) * 64);
+                q1 = __ldg(tile + (j >> 3) * 64 + 1);
+            }
+            const int e = q0.x;
+            q0 = make_int4(q0.y, q0.z, q0.w, q1.x);
+            q1 = make_int4(q1.y, q1.z, q1.w, -1);
             if (e < 0) continue;
             const int b = e & B_MASK;
             const float4 pb = P0[b], vb = P1[b], xb = P2[b];
@@ -1065,9 +1186,18 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
     Kahan acc;
     acc.init(0.f);
     const int cnt = ncnt[a];
+    /* 8 entries at a time from the particle's list tiles (two int4 loads) */
+    const int4 *tile = reinterpret_cast<const int4 *>(nbr + nl_at(a, 0, ld));
+    int4 q0 = make_int4(-1, -1, -1, -1), q1 = q0;
 #pragma unroll 2
     for (int j = 0; j < cnt; j++) {
-        const int e = nbr[(int64_t)j * ld + a];
+        if ((j & 7) == 0) {
+            q0 = __ldg(tile + (j >> 3) * 64);
+            q1 = __ldg(tile + (j >> 3) * 64 + 1);
+        }
+        const int e = q0.x;
+        q0 = make_int4(q0.y, q0.z, q0.w, q1.x);
+        q1 = make_int4(q1.y, q1.z, q1.w, -1);
         if (e < 0) continue;
         const int b = e & B_MASK;
         const int tb = tg[b] & 0xff;
@@ -1838,13 +1968,13 @@ __global__ void k_list_export(DevState s, const int *tg, const int *nbr, const i
     const int m = ncnt[a];
     if (!idx) {
         int v = 0;
-        for (int j = 0; j < m; j++) v += nbr[(int64_t)j * ld + a] >= 0;
+        for (int j = 0; j < m; j++) v += nbr[nl_at(a, j, ld)] >= 0;
         cnt[tag] = v;
         return;
     }
     int k = 0;
     for (int j = 0; j < m; j++) {
-        const int e = nbr[(int64_t)j * ld + a];
+        const int e = nbr[nl_at(a, j, ld)];
         if (e >= 0) idx[offs[tag] + k++] = s.irow(FI_TAG)[e & B_MASK];
     }
 }
@@ -1864,7 +1994,7 @@ __global__ void k_adj_pairs(DevState s, const DevGlobals *__restrict__ g, const 
     const bool live = a < n && is_sph_or_sphb(tg[a] & 0xff);
     const int m = live ? ncnt[a] : 0;
     int k = 0;
-    for (int j = 0; j < m; j++) k += nbr[(int64_t)j * ld + a] >= 0;
+    for (int j = 0; j < m; j++) k += nbr[nl_at(a, j, ld)] >= 0;
     const int lane = threadIdx.x & 31;
     int incl = k;
     for (int o = 1; o < 32; o <<= 1) {
@@ -1885,7 +2015,7 @@ __global__ void k_adj_pairs(DevState s, const DevGlobals *__restrict__ g, const 
     decode<ND>(skey[a], dims, cc);
     int q = 0;
     for (int j = 0; j < m && q < room; j++) {
-        const int e = nbr[(int64_t)j * ld + a];
+        const int e = nbr[nl_at(a, j, ld)];
         if (e < 0) continue;
         int o[3];
         nl_decode_code(e >> B_BITS, o);
@@ -1938,20 +2068,20 @@ int nlist_blocks(int64_t particles) {
 }  // namespace
 
 void mixed_list_export(sphdem_ctx *c, int *cnt, const long long *offs, int *idx) {
-    k_list_export<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->A, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap, c->n,
+    k_list_export<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->A, c->mx_tg, c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn, c->n,
                                                               cnt, offs, idx);
 }
 
 void mixed_adj_pairs(sphdem_ctx *c, int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot) {
     const int g = grid_for(c->n, 128);
     if (c->cfg.nd == 3)
-        k_adj_pairs<3><<<g, 128, 0, c->stream>>>(c->A, c->g, c->buf.skey, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap,
+        k_adj_pairs<3><<<g, 128, 0, c->stream>>>(c->A, c->g, c->buf.skey, c->mx_tg, c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn,
                                                  c->n, nb, oc, cnt, cap, slot);
     else if (c->cfg.nd == 2)
-        k_adj_pairs<2><<<g, 128, 0, c->stream>>>(c->A, c->g, c->buf.skey, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap,
+        k_adj_pairs<2><<<g, 128, 0, c->stream>>>(c->A, c->g, c->buf.skey, c->mx_tg, c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn,
                                                  c->n, nb, oc, cnt, cap, slot);
     else
-        k_adj_pairs<1><<<g, 128, 0, c->stream>>>(c->A, c->g, c->buf.skey, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap,
+        k_adj_pairs<1><<<g, 128, 0, c->stream>>>(c->A, c->g, c->buf.skey, c->mx_tg, c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn,
                                                  c->n, nb, oc, cnt, cap, slot);
 }
 
@@ -2005,7 +2135,7 @@ void nlist(sphdem_ctx *c) {
 #undef L_
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "band_fix", k_band_fix<ND>, grid_for(c->n, 256), 256, 0, c->cfg, c->A, c->g, c->buf.start,  \
-                  c->buf.skey, c->mx_pos, c->mx_poslo, c->mx_bandq, c->mx_bandn, c->mx_nbr, c->cap)
+                  c->buf.skey, c->mx_pos, c->mx_poslo, c->mx_bandq, c->mx_bandn, c->mx_nbr, (int64_t)c->mx_maxn)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
@@ -2033,7 +2163,7 @@ void omega_eos(sphdem_ctx *c, bool omega, bool eos) {
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, omega ? "omega_eos32" : "eos32", k_omega_eos<ND>, grid_for(c->n, c->blk_pair), c->blk_pair, 0, \
                   c->cfg, c->A, \
-                  c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap, c->n,         \
+                  c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_tg, c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn, c->n,         \
                   (int)omega, (int)eos, c->mx_om)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
@@ -2043,7 +2173,7 @@ void force(sphdem_ctx *c) {
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "force32", k_force<ND>, grid_for(c->n, c->blk_pair), c->blk_pair, 0, c->cfg, c->dcfg, c->A,   \
                   c->g, c->mx_pos, \
-                  c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap, c->n, c->mx_nb)
+                  c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn, c->n, c->mx_nb)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
@@ -2052,7 +2182,7 @@ void dddt(sphdem_ctx *c) {
 #define L_(ND)                                                                                                  \
     SPHDEM_LAUNCH(c, "dddt32", k_dddt<ND>, grid_for(c->n, c->blk_pair), c->blk_pair, 0, c->cfg, c->A, c->g,      \
                   c->mx_pos, c->mx_vel, \
-                  c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt, c->cap, c->n)
+                  c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn, c->n)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
