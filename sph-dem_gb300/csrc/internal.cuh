@@ -76,7 +76,7 @@ struct sphdem_ctx {
     float4 *mx_pos = nullptr, *mx_vel = nullptr, *mx_aux = nullptr;
     int *mx_tg = nullptr;       /* type | ghost code << 8 */
     float *mx_om = nullptr;     /* Omega (VAR_H_CORRECTION) */
-    int *mx_nbr = nullptr;      /* column-major lists, mx_maxn x cap */
+    int *mx_nbr = nullptr;      /* lists in tiles of 32 particles x 8 slots, mx_maxn x cap (rounded to 32) */
     int *mx_ncnt = nullptr;
     int mx_maxn = 0;
     float4 *mx_q0 = nullptr, *mx_q1 = nullptr, *mx_q2 = nullptr;  /* FPI fields of fluid particles */

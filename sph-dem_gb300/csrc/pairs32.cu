@@ -14,9 +14,9 @@
  *                FP32 with a proven error bound; candidates inside the bound
  *                go to k_band_fix (double-float, then the reference's FP64
  *                predicate, particle.h:236-238, for true ties).  Periodic
- *                images only where the reference holds a ghost.  Column-major
- *                storage (entry j of all particles contiguous):
- *                b | stencil code << 26.
+ *                images only where the reference holds a ghost.  Entries
+ *                b | stencil code << 26 in tiles of 32 particles x 8 slots
+ *                (nl_at).
  *   k_omega_eos  calcOmega over the list + the FP64 EOS (its (rho/rho0)^7-1
  *                cancels too much for FP32)
  *   k_force      calcForce + the Courant/viscous/accel dt conditions
