@@ -845,7 +845,9 @@ void replay_sph_step(sphdem_ctx *c) {
     SPHDEM_CUDA_CHECK(cudaGraphLaunch(ge, c->stream));
 }
 
-void backward_dem(sphdem_ctx *c, AdjointData *a, int steps, double dt, int cap) {
+/* the steps of a segment with their taps (the states after each step, the
+ * contacts / pair tables of each step), from the segment's first state */
+void replay_dem(sphdem_ctx *c, AdjointData *a, int steps, int cap) {
     const int64_t n = c->n;
     for (int j = 1; j <= steps; j++) {
         one_step(c);
@@ -854,6 +856,10 @@ void backward_dem(sphdem_ctx *c, AdjointData *a, int steps, double dt, int cap) 
                                                             a->pairs + (size_t)(j - 1) * cap, a->pair_cnt + j - 1,
                                                             cap);
     }
+}
+
+void backward_dem(sphdem_ctx *c, AdjointData *a, int steps, double dt, int cap) {
+    const int64_t n = c->n;
     for (int j = steps; j >= 1; j--) {
         const double *s0 = a->seg + (size_t)(j - 1) * n * ADJ_NC, *s1 = a->seg + (size_t)j * n * ADJ_NC;
         k_vjp_particles<<<grid_for(n, ABLK), ABLK, 0, c->stream>>>(c->cfg, n, dt, s0, s1, a->mass, a->rad, a->adj,
@@ -865,13 +871,18 @@ void backward_dem(sphdem_ctx *c, AdjointData *a, int steps, double dt, int cap) 
     }
 }
 
-void backward_sph(sphdem_ctx *c, AdjointData *a, int steps, double dt) {
-    const int64_t n = c->n, cap = a->pair_cap;
+void replay_sph(sphdem_ctx *c, AdjointData *a, int steps) {
+    const int64_t n = c->n;
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->slot, 0, sizeof(int), c->stream));
     /* a particle that stops being SPH/SPHB (deleted) keeps an empty list */
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_mid, 0, (size_t)a->K * n * sizeof(int2), c->stream));
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_end, 0, (size_t)a->K * n * sizeof(int2), c->stream));
+    if (a->mode == ADJ_MODE_COUPLED) cpl_reset_segment(c, a);
     for (int j = 1; j <= steps; j++) replay_sph_step(c);
+}
+
+void backward_sph(sphdem_ctx *c, AdjointData *a, int steps, double dt) {
+    const int64_t n = c->n, cap = a->pair_cap;
     for (int j = steps; j >= 1; j--) {
         const double *s0 = a->seg + (size_t)(j - 1) * n * ADJ_NC, *s1 = a->seg + (size_t)j * n * ADJ_NC;
         const int *nbm = a->nb_mid + (size_t)(j - 1) * cap, *nbe = a->nb_end + (size_t)(j - 1) * cap;
@@ -901,13 +912,54 @@ void backward_sph(sphdem_ctx *c, AdjointData *a, int steps, double dt) {
 }
 
 void backward_cpl(sphdem_ctx *c, AdjointData *a, int steps, double dt) {
-    const int64_t n = c->n;
-    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->slot, 0, sizeof(int), c->stream));
-    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_mid, 0, (size_t)a->K * n * sizeof(int2), c->stream));
-    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_end, 0, (size_t)a->K * n * sizeof(int2), c->stream));
-    cpl_reset_segment(c, a);
-    for (int j = 1; j <= steps; j++) replay_sph_step(c);
     for (int j = steps; j >= 1; j--) cpl_backward_step(c, a, j, dt);
+}
+
+/* buffers of one segment's tape and of the reverse sweep */
+void alloc_backward(sphdem_ctx *c, AdjointData *a) {
+    if (a->seg) return;
+    const int64_t n = c->n;
+    const int K = a->K;
+    const size_t sbytes = (size_t)n * ADJ_NC * sizeof(double);
+    const int cap = ADJ_MAX_CONTACTS * (int)n;
+    const bool sph = a->mode == ADJ_MODE_SPH, cpl = a->mode == ADJ_MODE_COUPLED;
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->seg, (size_t)(K + 1) * sbytes));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->pair_cnt, (size_t)K * sizeof(int)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->adj, sbytes));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->racc, n * 3 * sizeof(double)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->vmacc, n * 3 * sizeof(double)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->fbar, n * 3 * sizeof(double)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->grads, ADJ_NGRAD * sizeof(double)));
+    if (sph || cpl) {
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->nb_mid, (size_t)K * a->pair_cap * sizeof(int)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->nb_end, (size_t)K * a->pair_cap * sizeof(int)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->oc_mid, (size_t)K * n * sizeof(int2)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->oc_end, (size_t)K * n * sizeof(int2)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->cnt_end, (size_t)K * sizeof(int)));
+        if (cpl)
+            cpl_alloc(c, a);
+        else if (c->cfg.precision == SPHDEM_PREC_MIXED)
+            SPHDEM_CUDA_CHECK(cudaMalloc(&a->rec, (size_t)n * ADJ_NREC * sizeof(float4)));
+        else
+            SPHDEM_CUDA_CHECK(cudaMalloc(&a->aux, (size_t)n * ADJ_AUX * sizeof(double)));
+    } else {
+        SPHDEM_CUDA_CHECK(cudaMalloc(&a->pairs, (size_t)K * cap * sizeof(int4)));
+    }
+}
+
+/* the tape of segment sg: from its checkpoint (already the handle's state),
+ * the steps with their taps */
+void tape_segment(sphdem_ctx *c, AdjointData *a, int sg, int steps) {
+    const size_t sbytes = (size_t)c->n * ADJ_NC * sizeof(double);
+    const int K = a->K;
+    SPHDEM_CUDA_CHECK(cudaMemcpyAsync(a->seg, a->ckpt[sg], sbytes, cudaMemcpyDeviceToDevice, c->stream));
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->pair_cnt, 0, K * sizeof(int), c->stream));
+    if (a->mode == ADJ_MODE_SPH || a->mode == ADJ_MODE_COUPLED) {
+        SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cnt_end, 0, K * sizeof(int), c->stream));
+        replay_sph(c, a, steps);
+    } else {
+        replay_dem(c, a, steps, ADJ_MAX_CONTACTS * (int)c->n);
+    }
 }
 
 }  // namespace
@@ -994,6 +1046,16 @@ int adjoint_forward(sphdem_ctx *c, int nsteps, int K, int mode) {
         save_state(c, a->ckpt[s]);
         a->ckpt_g[s] = read_globals(c);
         const int steps = std::min(K, nsteps - s * K);
+        if (s == nseg - 1) {
+            /* the backward pass starts with the last segment: record its tape
+             * now instead of replaying it then */
+            alloc_backward(c, a);
+            tape_segment(c, a, s, steps);
+            a->taped = s;
+            const int rc = device_status(c);
+            if (rc) return rc;
+            continue;
+        }
         const int rc = sphdem_step(c, steps);
         if (rc) return rc;
     }
@@ -1012,30 +1074,7 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
     const size_t sbytes = (size_t)n * ADJ_NC * sizeof(double);
     const int cap = ADJ_MAX_CONTACTS * (int)n;
     const bool sph = a->mode == ADJ_MODE_SPH, cpl = a->mode == ADJ_MODE_COUPLED;
-    if (!a->seg) {
-        SPHDEM_CUDA_CHECK(cudaMalloc(&a->seg, (size_t)(K + 1) * sbytes));
-        SPHDEM_CUDA_CHECK(cudaMalloc(&a->pair_cnt, (size_t)K * sizeof(int)));
-        SPHDEM_CUDA_CHECK(cudaMalloc(&a->adj, sbytes));
-        SPHDEM_CUDA_CHECK(cudaMalloc(&a->racc, n * 3 * sizeof(double)));
-        SPHDEM_CUDA_CHECK(cudaMalloc(&a->vmacc, n * 3 * sizeof(double)));
-        SPHDEM_CUDA_CHECK(cudaMalloc(&a->fbar, n * 3 * sizeof(double)));
-        SPHDEM_CUDA_CHECK(cudaMalloc(&a->grads, ADJ_NGRAD * sizeof(double)));
-        if (sph || cpl) {
-            SPHDEM_CUDA_CHECK(cudaMalloc(&a->nb_mid, (size_t)K * a->pair_cap * sizeof(int)));
-            SPHDEM_CUDA_CHECK(cudaMalloc(&a->nb_end, (size_t)K * a->pair_cap * sizeof(int)));
-            SPHDEM_CUDA_CHECK(cudaMalloc(&a->oc_mid, (size_t)K * n * sizeof(int2)));
-            SPHDEM_CUDA_CHECK(cudaMalloc(&a->oc_end, (size_t)K * n * sizeof(int2)));
-            SPHDEM_CUDA_CHECK(cudaMalloc(&a->cnt_end, (size_t)K * sizeof(int)));
-            if (cpl)
-                cpl_alloc(c, a);
-            else if (c->cfg.precision == SPHDEM_PREC_MIXED)
-                SPHDEM_CUDA_CHECK(cudaMalloc(&a->rec, (size_t)n * ADJ_NREC * sizeof(float4)));
-            else
-                SPHDEM_CUDA_CHECK(cudaMalloc(&a->aux, (size_t)n * ADJ_AUX * sizeof(double)));
-        } else {
-            SPHDEM_CUDA_CHECK(cudaMalloc(&a->pairs, (size_t)K * cap * sizeof(int4)));
-        }
-    }
+    alloc_backward(c, a);
     /* seeds: adjoint of the final (r, v, vh) in tag order; f, dens, dddt 0 */
     {
         std::vector<double> h((size_t)n * ADJ_NC, 0.0);
@@ -1054,11 +1093,12 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
     bool overflow = false;
     for (int sg = nseg - 1; sg >= 0 && !overflow; sg--) {
         const int steps = std::min(K, a->nsteps - sg * K);
-        restore_state(c, a->ckpt[sg], a->ckpt_g[sg]);
-        SPHDEM_CUDA_CHECK(cudaMemcpyAsync(a->seg, a->ckpt[sg], sbytes, cudaMemcpyDeviceToDevice, c->stream));
-        SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->pair_cnt, 0, K * sizeof(int), c->stream));
+        if (sg != a->taped) {
+            restore_state(c, a->ckpt[sg], a->ckpt_g[sg]);
+            tape_segment(c, a, sg, steps);
+        }
+        a->taped = -1;   /* the buffers now hold this segment's tape */
         if (sph || cpl) {
-            SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cnt_end, 0, K * sizeof(int), c->stream));
             if (cpl) backward_cpl(c, a, steps, dt);
             else backward_sph(c, a, steps, dt);
         } else {

@@ -44,6 +44,7 @@ struct PairTable {
 struct AdjointData {
     int mode = 0;
     int nsteps = 0, K = 0;
+    int taped = -1;                 /* segment whose tape the buffers hold from the forward pass */
     int64_t n = 0;
     std::vector<double *> ckpt;     /* state at steps 0, K, 2K, ... and the final state */
     std::vector<DevGlobals> ckpt_g;
