@@ -182,7 +182,8 @@ __device__ __noinline__ bool exact_pair(const DevCfg *__restrict__ cp, const Dev
 }
 
 /* ---------------------------------------------------------------------- */
-/* P0 = (offset from own bucket origin, h), P1 = (vhat, mass),
+/* P0 = (offset from own bucket origin, h), P1 = (vhat, mass; negated for
+ * particles that are neither sph / sphBoundary nor DEM),
  * P2 = (dens, pdr2, porosity, 1/h), tg = type | gcode << 8 */
 /* reference DEM bucket indices packed 10 bits per axis (biased by 512) */
 constexpr int CP_BIAS = 512;
@@ -227,7 +228,11 @@ __global__ void k_pack(DevCfg c, DevState s, const int *__restrict__ skey, const
 #pragma unroll
     for (int d = 0; d < ND; d++) vh[d] = (float)s.row(FD_VHAT + d)[i];
     P0[i] = make_float4(off[0], off[1], off[2], (float)s.row(FD_H)[i]);
-    P1[i] = make_float4(vh[0], vh[1], vh[2], (float)s.row(FD_MASS)[i]);
+    /* the mass of a particle that is neither sph / sphBoundary nor DEM is
+     * stored negated: list readers take a neighbour's type from the sign and
+     * load the type row only for those (walls) */
+    const float mpk = (float)s.row(FD_MASS)[i];
+    P1[i] = make_float4(vh[0], vh[1], vh[2], (is_sph_or_sphb(t) || dem) ? mpk : -mpk);
     /* a DEM particle's pdr2 slot holds its radius (the contact pre-test) */
     const double rad = s.row(FD_RADIUS)[i] > 0 ? s.row(FD_RADIUS)[i] : c.dem_radius;
     P2[i] = make_float4((float)s.row(FD_DENS)[i], (float)(t == T_DEM ? rad : s.row(FD_PDR2)[i]),
@@ -898,7 +903,7 @@ __global__ void __launch_bounds__(BLK) k_omega_eos(DevCfg c, DevState s, const D
             if (e < 0) continue;
             const int b = e & B_MASK;
             const float4 pb = P0[b];
-            const float mb = P1[b].w;
+            const float mb = fabsf(P1[b].w);
             const int tb = tg[b] & 0xff;
             float d[3];
             nb_delta_t<ND>(e, shift, pa, pb, d);
@@ -1065,7 +1070,8 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
             if (e < 0) continue;
             const int b = e & B_MASK;
             const float4 pb = P0[b], vb = P1[b], xb = P2[b];
-            const int tb = tg[b] & 0xff;
+            /* sph / sphBoundary unless the packed mass is negative */
+            const int tb = vb.w < 0.f ? (tg[b] & 0xff) : T_SPH;
             float d[3];
             nb_delta_t<ND>(e, shift, pa, pb, d);
             const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
@@ -1086,7 +1092,7 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
             } else {
                 cA = cB = cM = 0.5f * (Fa + Fb);
             }
-            const float densb = xb.x, mb = vb.w;
+            const float densb = xb.x, mb = fabsf(vb.w);
             const float hav = 0.5f * (ha + hb);
             const float dv0 = va.x - vb.x, dv1 = va.y - vb.y, dv2 = va.z - vb.z;
             if (sph && tb != T_DEM && tb != T_DEMB) {
@@ -1200,9 +1206,10 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
         q1 = make_int4(q1.y, q1.z, q1.w, -1);
         if (e < 0) continue;
         const int b = e & B_MASK;
-        const int tb = tg[b] & 0xff;
         const float4 pb = P0[b], vb = P1[b];
-        const float ihb = P2[b].w;
+        /* sph / sphBoundary unless the packed mass is negative */
+        const int tb = vb.w < 0.f ? (tg[b] & 0xff) : T_SPH;
+        const float mb = fabsf(vb.w);
         float d[3];
         nb_delta_t<ND>(e, shift, pa, pb, d);
         const float r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
@@ -1213,14 +1220,15 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
         float F;
         if (c.var_h()) {
             F = Fa;
-            if (is_sph_or_sphb(tb)) om.add(vb.w * (ihna * (-qa * wdK32(qa, wcon) * iha) - pd_coef * wK32(qa, wcon)));
+            if (is_sph_or_sphb(tb)) om.add(mb * (ihna * (-qa * wdK32(qa, wcon) * iha) - pd_coef * wK32(qa, wcon)));
         } else {
+            const float ihb = P2[b].w;
             const float qb = r * ihb;
             const float Fb = qb != 0.f ? powi<ND>(ihb) * ihb * ihb * wdK32(qb, wcon) * (pb.w * rinv) : 0.f;
             F = 0.5f * (Fa + Fb);
         }
         const float vdr = (va.x - vb.x) * d[0] + (va.y - vb.y) * d[1] + (va.z - vb.z) * d[2];
-        if (!(is_boundary(tb) || tb == T_DEM)) acc.add(vb.w * vdr * F);
+        if (!(is_boundary(tb) || tb == T_DEM)) acc.add(mb * vdr * F);
     }
     float roma = 1.f;
     if (c.var_h()) {
@@ -1881,7 +1889,7 @@ __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restr
                 if (shp != 0x15 && !img_ok<ND>(tgb >> 8, sh)) continue;
                 if ((tgb & 0xff) == T_BOUNDARY) continue;
                 const float4 vb = P1[b], xb = P2[b];
-                const float mb = vb.w;
+                const float mb = fabsf(vb.w);
                 const float q = sqrtf(r2) * xb.w;
                 const float Wab = powi<ND>(xb.w) * wK32(q, wcon);
                 const float dvW = (mb / xb.x) * Wab, mW = mb * Wab;
