@@ -210,17 +210,29 @@ __device__ __noinline__ int cpl_scan32(const DevCfg &c, const DevState &s, const
     return k;
 }
 
+/* One scan per fluid particle: its partners go to a small per-thread buffer,
+ * then one warp-aggregated reservation places them; a particle with more
+ * partners than the buffer holds scans again straight into the table. */
+constexpr int CPL_LOCAL = 16;
 __global__ void k_cp_cpl_table(DevCfg c, DevState s, const int *start, const DevGlobals *g, int64_t n,
                                const float4 *dpos, int *nb, int2 *oc, int *cnt, int64_t cap, const int *slot) {
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const bool live = a < n && is_fluid(s.irow(FI_IAM)[a]);
     const int j = slot ? *slot : 0;
-    const int k = live ? cpl_scan32(c, s, start, g->n_sph_cells, dpos, 0.5 * g->dt, a, nullptr, 0) : 0;
+    int lb[CPL_LOCAL];
+    const int k = live ? cpl_scan32(c, s, start, g->n_sph_cells, dpos, 0.5 * g->dt, a, nb ? lb : nullptr,
+                                    nb ? CPL_LOCAL : 0)
+                       : 0;
     const int64_t off = reserve(k, cnt + j);
     if (!nb || !live) return;
     const int64_t room = cap - off;
-    cpl_scan32(c, s, start, g->n_sph_cells, dpos, 0.5 * g->dt, a, nb + (int64_t)j * cap + off,
-                      room > 0 ? room : 0);
+    int *out = nb + (int64_t)j * cap + off;
+    if (k <= CPL_LOCAL) {
+        if (room >= k)
+            for (int q = 0; q < k; q++) out[q] = lb[q];
+    } else {
+        cpl_scan32(c, s, start, g->n_sph_cells, dpos, 0.5 * g->dt, a, out, room > 0 ? room : 0);
+    }
     oc[(int64_t)j * n + s.irow(FI_TAG)[a]] = make_int2((int)off, room >= k ? k : 0);
 }
 
