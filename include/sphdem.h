@@ -226,6 +226,16 @@ int sphdem_step(sphdem_handle h, int nsteps);
 
 int sphdem_get_fields(sphdem_handle h, uint32_t mask, SphDemParticles *out);
 int sphdem_set_fields(sphdem_handle h, uint32_t mask, const SphDemParticles *in);
+/* sphdem_get_fields without waiting (no counterpart in the reference, whose
+ * particles live in host memory): the fields are gathered into tag order on
+ * the handle's stream and copied into `out` on a separate copy stream, so the
+ * copy overlaps the steps that follow.  `out`'s arrays must stay valid and
+ * unread until sphdem_fields_wait returns; pinned host memory
+ * (sphdem_alloc_host) makes the copy truly asynchronous.  Two transfers
+ * overlap; a third waits on the device for the first to finish.  Integer
+ * fields (iam, tag) are not copied by this call. */
+int sphdem_get_fields_async(sphdem_handle h, uint32_t mask, const SphDemParticles *out);
+int sphdem_fields_wait(sphdem_handle h);
 int sphdem_get_globals(sphdem_handle h, SphDemGlobals *out);
 int sphdem_get_stats(sphdem_handle h, SphDemStats *out);
 int sphdem_set_globals(sphdem_handle h, const SphDemGlobals *in);

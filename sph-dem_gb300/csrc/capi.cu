@@ -283,6 +283,7 @@ void free_ctx(sphdem_ctx *c) {
     cudaFree(c->mx_bandq);
     cudaFree(c->mx_bandn);
     cudaFree(c->dcfg);
+    fields_async_free(c);
     cudaFree(c->cg);
     cudaFree(c->hpred);
     cudaFree(c->delmark);
@@ -818,6 +819,33 @@ int sphdem_get_fields(sphdem_handle h, uint32_t mask, SphDemParticles *out) {
         return fail(h, SPHDEM_ERR_CUDA, e);
     }
     return SPHDEM_OK;
+}
+
+int sphdem_get_fields_async(sphdem_handle h, uint32_t mask, const SphDemParticles *out) {
+    if (!h || !out) return SPHDEM_ERR_INVALID;
+    if (out->n != h->n) return fail(h, SPHDEM_ERR_INVALID, "particle count mismatch");
+    std::vector<FieldCopy> fc;
+    for (const FieldMap &fm : kFields) {
+        if (!(mask & fm.bit)) continue;
+        double *dst = out->*fm.ptr;
+        if (dst) fc.push_back(FieldCopy{fm.row, fm.ncomp, dst});
+    }
+    try {
+        fields_get_async(h, fc.data(), (int)fc.size());
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+    return SPHDEM_OK;
+}
+
+int sphdem_fields_wait(sphdem_handle h) {
+    if (!h) return SPHDEM_ERR_INVALID;
+    try {
+        fields_wait(h);
+    } catch (const std::string &e) {
+        return fail(h, SPHDEM_ERR_CUDA, e);
+    }
+    return check_device(h);
 }
 
 int sphdem_set_fields(sphdem_handle h, uint32_t mask, const SphDemParticles *in) {

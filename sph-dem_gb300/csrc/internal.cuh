@@ -98,6 +98,14 @@ struct sphdem_ctx {
     sphdem::DevCfg *dcfg = nullptr;  /* device copy of cfg for out-of-line helpers */
     /* staging buffer for field transfers in tag order */
     double *stage = nullptr;
+    /* asynchronous field transfers: two device staging buffers, the copy
+     * stream, and per buffer the events of its gather and of its copy */
+    cudaStream_t copy_stream = nullptr;
+    double *astage[2] = {nullptr, nullptr};
+    size_t astage_cap[2] = {0, 0};
+    cudaEvent_t ev_gathered[2] = {nullptr, nullptr}, ev_copied[2] = {nullptr, nullptr};
+    bool astage_used[2] = {false, false};
+    int acur = 0;
 };
 
 namespace sphdem {
@@ -198,6 +206,15 @@ void phase_sequence(sphdem_ctx *c, int phase);
 int device_status(sphdem_ctx *c);
 
 /* fields.cu */
+struct FieldCopy {
+    int row, ncomp;
+    double *host;
+};
+/* gather the fields on the handle's stream, copy them on the copy stream;
+ * returns without waiting */
+void fields_get_async(sphdem_ctx *c, const FieldCopy *fc, int nf);
+void fields_wait(sphdem_ctx *c);
+void fields_async_free(sphdem_ctx *c);
 void field_get(sphdem_ctx *c, int row, int ncomp, double *host);
 void field_set(sphdem_ctx *c, int row, int ncomp, const double *host);
 void field_get_int(sphdem_ctx *c, int row, int *host);

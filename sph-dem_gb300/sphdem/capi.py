@@ -238,6 +238,8 @@ class Library:
         L.sphdem_get_globals.argtypes = [H, C.POINTER(SphDemGlobals)]
         L.sphdem_set_globals.argtypes = [H, C.POINTER(SphDemGlobals)]
         L.sphdem_rebuild.argtypes = [H]
+        L.sphdem_get_fields_async.argtypes = [H, C.c_uint32, C.POINTER(SphDemParticles)]
+        L.sphdem_fields_wait.argtypes = [H]
         L.sphdem_insert_particles.argtypes = [H, C.POINTER(SphDemParticles), C.POINTER(C.c_int64)]
         L.sphdem_mark_for_deletion.argtypes = [H, C.POINTER(C.c_int64), C.c_int64]
         L.sphdem_pairs.argtypes = [H, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
@@ -304,6 +306,14 @@ class Simulation:
 
     def rebuild(self):
         self.L.check(self.L.lib.sphdem_rebuild(self.h), self.h, "sphdem_rebuild")
+
+    def get_async(self, mask: int, out: "ParticleBuffers") -> "ParticleBuffers":
+        """sphdem_get_fields_async: `out` is filled once fields_wait() returns."""
+        self.L.check(self.L.lib.sphdem_get_fields_async(self.h, mask, out.ref()), self.h, "get_fields_async")
+        return out
+
+    def fields_wait(self):
+        self.L.check(self.L.lib.sphdem_fields_wait(self.h), self.h, "fields_wait")
 
     def insert(self, particles: dict) -> np.ndarray:
         """sphdem_insert_particles: the tag-order index each new particle took."""
