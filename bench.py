@@ -84,7 +84,7 @@ def run_profile(args):
                       "band_candidates": st.n_band_candidates, "band_queue_capacity": st.band_queue_capacity}))
 
 
-def workload_config(case, nsteps):
+def workload_config(case, nsteps, world: int = 1):
     n = case.n
     nd = int((case.particles["iam"] == 11).sum())
     return {
@@ -95,8 +95,44 @@ def workload_config(case, nsteps):
         "viscosity_kinematic": case.cfg["viscosity"], "steps": nsteps,
         "precision": "mixed (FP32 pair math on FP64-cell-origin offsets, FP64 integration)",
         "l2_policy": "inputs larger than L2 (state > 1 GB, L2 129 MB)",
-        "parallelism": "single GPU",
+        "parallelism": "single GPU" if world == 1 else f"{world} independent replicas, one per GPU",
     }
+
+
+# --------------------------------------------------------------------------
+# N > 1: independent replicas, one per GPU (the step does not shard); the
+# timed region is bracketed by barriers and its time is the maximum over ranks
+def dist_setup(world: int):
+    """torch.distributed for N > 1 replicas: NCCL on GPUs, gloo otherwise
+    (env:// rendezvous from the launcher).  None for a single process."""
+    if world <= 1:
+        return None
+    import torch
+    import torch.distributed as dist
+    if not dist.is_initialized():
+        dist.init_process_group(backend="nccl" if torch.cuda.is_available() else "gloo")
+    return dist
+
+
+def barrier(dist) -> None:
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(x: float, dist) -> float:
+    """The largest x over all ranks (the slowest rank's time)."""
+    if dist is None:
+        return x
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_rate(units_per_rank: float, world: int, seconds_max: float) -> float:
+    """Whole-job rate: the units all ranks processed over the slowest rank's time."""
+    return units_per_rank * world / seconds_max
 
 
 class ClockSampler:
@@ -335,12 +371,16 @@ def run_ours(args, rank, world):
     os.makedirs(out_dir, exist_ok=True)
 
     # ---- mixed precision, device-resident --------------------------------
+    dist = dist_setup(world)
     sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
     sim.step(args.warmup)
+    barrier(dist)
     with ClockSampler(os.path.join(out_dir, "bench_clocks.csv")) as clk:
-        ms = sim.time_steps(args.steps)
+        ms = sim.time_steps(args.steps)   # CUDA events on the handle's stream, synchronised
+    barrier(dist)
+    ms = max_over_ranks(ms, dist)
     clocks = clk.summary()
-    value = n * args.steps / (ms * 1e-3)
+    value = aggregate_rate(n * args.steps, world, ms * 1e-3)
     st = sim.stats()
 
     # per-kernel device times (CUDA events around each launch), 2 steps
@@ -394,6 +434,7 @@ def run_ours(args, rank, world):
     outbufs = [capi.ParticleBuffers(n, pinned=lib, fields=("r", "dens")) for _ in range(2)]
     import ctypes as C
     cfgs = capi.config_struct(case.cfg, cases.PREC_MIXED)
+    barrier(dist)
     t0 = time.perf_counter()
     h = C.c_void_p()
     lib.check(lib.lib.sphdem_create(C.byref(cfgs), init.ref(), n, C.byref(h)), None, "create")
@@ -402,9 +443,9 @@ def run_ours(args, rank, world):
         lib.check(lib.lib.sphdem_get_fields_async(h, capi.FIELD_R | capi.FIELD_DENS, outbufs[k % 2].ref()), h,
                   "get_fields_async")
     lib.check(lib.lib.sphdem_fields_wait(h), h, "fields_wait")
-    t_e2e = time.perf_counter() - t0
+    t_e2e = max_over_ranks(time.perf_counter() - t0, dist)
     lib.lib.sphdem_destroy(h)
-    e2e_value = n * e2e_steps / t_e2e
+    e2e_value = aggregate_rate(n * e2e_steps, world, t_e2e)
     h2d_bytes = n * (4 * 3 * 8 + 4 * 8 + 12)  # r, v, norms x3 (3 comps) + mass, dens, h, radius + ints
     d2h_bytes = n * (3 * 8 + 8)
 
@@ -421,7 +462,7 @@ def run_ours(args, rank, world):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64", "data": "synthetic (seeded)",
-        "config": workload_config(case, args.steps),
+        "config": workload_config(case, args.steps, world),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d_bytes / e2e_steps),
                 "d2h_bytes_per_step": int(d2h_bytes),
                 "what": "sphdem_create from pinned host arrays + per step sphdem_step + sphdem_get_fields_async(r, "
