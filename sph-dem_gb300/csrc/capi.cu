@@ -561,6 +561,8 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
                 c->mx_maxn = maxn;
                 /* list tiles of 32 particles x 8 entries */
                 SPHDEM_CUDA_CHECK(cudaMalloc(&c->mx_nbr, (size_t)maxn * ((capacity + 31) / 32 * 32) * sizeof(int)));
+                /* the lists of the creation's rebuild, for exports before any step */
+                mixed::nlist(c);
             }
         }
         int rc = check_device(c);
