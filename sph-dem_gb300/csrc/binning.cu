@@ -401,19 +401,29 @@ __global__ void k_rank(const int *key, const int *start, const int *slot, const 
     skey[s0 + rank] = k;
 }
 
+/* one thread per particle and a group of rows (blockIdx.y): the permutation
+ * is read once per group, and the group's loads are all in flight together */
+constexpr int GATHER_ROWS = 8;
 __global__ void k_gather(DevState src, DevState dst, const int *perm, const int *fd, int nfd,
                          const int *fi, int nfi, int64_t n) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= n) return;
     int p = perm[k];
     if (p < 0 || p >= n) p = 0;  /* never out of bounds, whatever the sort left */
-    const int f = blockIdx.y;
-    if (f < nfd) {
-        const int row = fd[f];
-        dst.row(row)[k] = src.row(row)[p];
-    } else if (f - nfd < nfi) {
-        const int row = fi[f - nfd];
-        dst.irow(row)[k] = src.irow(row)[p];
+    const int f0 = blockIdx.y * GATHER_ROWS;
+    double v[GATHER_ROWS];
+    int iv[GATHER_ROWS];
+#pragma unroll
+    for (int q = 0; q < GATHER_ROWS; q++) {
+        const int f = f0 + q;
+        if (f < nfd) v[q] = src.row(fd[f])[p];
+        else if (f - nfd < nfi) iv[q] = src.irow(fi[f - nfd])[p];
+    }
+#pragma unroll
+    for (int q = 0; q < GATHER_ROWS; q++) {
+        const int f = f0 + q;
+        if (f < nfd) dst.row(fd[f])[k] = v[q];
+        else if (f - nfd < nfi) dst.irow(fi[f - nfd])[k] = iv[q];
     }
 }
 
@@ -465,7 +475,7 @@ void rebuild(sphdem_ctx *c) {
                   c->A.row(FD_R + c->cfg.nd - 1), b.slot_tag, b.slot_z, n);
     SPHDEM_LAUNCH(c, "rebuild_rank", k_rank, gb, BLK, 0, b.key, b.start, b.slot, b.slot_tag, b.slot_z, b.perm,
                   b.skey, c->g, n);
-    dim3 gg(gb, b.n_fields_d + b.n_fields_i);
+    dim3 gg(gb, (b.n_fields_d + b.n_fields_i + GATHER_ROWS - 1) / GATHER_ROWS);
     SPHDEM_LAUNCH(c, "rebuild_gather", k_gather, gg, BLK, 0, c->A, c->B, b.perm, b.fields_d,
                   b.n_fields_d, b.fields_i, b.n_fields_i, n);
     std::swap(c->A, c->B);
