@@ -2058,6 +2058,19 @@ int resident_blocks(int64_t particles) {
     return (int)std::max<int64_t>(1, std::min<int64_t>(resident, need));
 }
 
+template <int ND>
+int dem_end_blocks(int64_t particles) {
+    static int resident = 0;
+    if (!resident) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dem_end<ND>, BLK, 0);
+        resident = std::max(1, sms * per_sm);
+    }
+    return std::max(1, std::min(resident, warp_blocks((int)std::min<int64_t>(particles, 1 << 22))));
+}
+
 /* list build: grid-stride over 32-particle slices, one wave of resident blocks */
 template <int ND, bool COUNT>
 int nlist_blocks(int64_t particles) {
@@ -2215,9 +2228,11 @@ void dem_drag(sphdem_ctx *c) {
 
 void dem_end(sphdem_ctx *c) {
     pack_fpi(c);
-    const int blocks = warp_blocks((int)std::min<int64_t>(c->n, 1 << 22));
+    /* one warp per DEM particle, grid-stride over the DEM range: one wave of
+     * resident blocks (a grid sized by the particle count would launch
+     * mostly empty warps) */
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "dem_end32", k_dem_end<ND>, blocks, BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->buf.skey,  \
+    SPHDEM_LAUNCH(c, "dem_end32", k_dem_end<ND>, dem_end_blocks<ND>(c->n), BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->buf.skey,  \
                   c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_q0, c->mx_q1, c->mx_q2, c->mx_tg, c->mx_ds)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
