@@ -491,6 +491,60 @@ def dambreak2d_flow(dx: float = 0.05, nsteps: int = 30, seed: int = 7) -> Case:
     return case
 
 
+def sediment3d_flow(nsteps: int = 16) -> Case:
+    """The small coupled sedimentation box with particles leaving and
+    entering between steps: after step 4 five DEM spheres enter near the top
+    (a sphere inflow) and every 40th fluid particle is marked for deletion;
+    after step 9 two of the new spheres and one of the first ones leave and
+    three more fluid particles enter."""
+    case = sediment3d(nx=10, L=0.04, height=0.08, n_dem=100, nsteps=nsteps, seed=8)
+    ps, c = case.particles, case.cfg
+    R, L = case.notes["dem_radius"], c["rmax"][0]
+    fluid = np.nonzero(ps["iam"] == SPH)[0]
+    dem = np.nonzero(ps["iam"] == DEM)[0]
+
+    def spheres(xyz):
+        m = len(xyz)
+        blk = _empty_particles(m)
+        blk["r"][:] = np.asarray(xyz, float)
+        blk["iam"][:] = DEM
+        blk["mass"][:] = c["dem_vol"] * c["dem_dens"]
+        blk["dens"][:] = c["dem_dens"]
+        blk["h"][:] = R
+        blk["radius"][:] = R
+        blk["v"][:, 2] = -0.05
+        return blk
+
+    def droplets(xyz):
+        m = len(xyz)
+        blk = _empty_particles(m)
+        blk["r"][:] = np.asarray(xyz, float)
+        blk["iam"][:] = SPH
+        blk["mass"][:] = ps["mass"][fluid[0]]
+        blk["dens"][:] = c["dens"]
+        blk["h"][:] = c["h"]
+        return blk
+
+    # five free places near the top: clear of the seeded spheres by 1.1 diameters
+    old = ps["r"][dem]
+    chosen = []
+    for zt in (0.072, 0.066, 0.060):
+        for fy in (0.5, 0.2, 0.8):
+            for fx in (0.15, 0.32, 0.49, 0.66, 0.83):
+                p = np.array([L * fx, L * fy, zt])
+                near = np.vstack([old] + [np.array(chosen)] if chosen else [old]) - p
+                near[:, :2] -= L * np.round(near[:, :2] / L)
+                if len(chosen) < 5 and np.linalg.norm(near, axis=1).min() > 2.2 * R:
+                    chosen.append(p)
+    new1 = spheres(chosen)
+    new2 = droplets([[L * 0.3, L * 0.31, 0.05], [L * 0.6, L * 0.62, 0.05], [L * 0.45, L * 0.77, 0.05]])
+    n0 = case.n
+    case.events = [{"step": 4, "insert": new1}, {"step": 4, "delete": fluid[::40]},
+                   {"step": 9, "delete": np.array([n0 + 1, n0 + 3, dem[7]])}, {"step": 9, "insert": new2}]
+    case.notes["events"] = "4: +5 DEM, -%d fluid; 9: -3 DEM, +3 fluid" % fluid[::40].size
+    return case
+
+
 def workload(name: str, **kw) -> Case:
     """The five configurations at full size, plus the small variants used as
     golden-fixture and parity cases."""
@@ -531,6 +585,8 @@ def workload(name: str, **kw) -> Case:
         # particles deleted and inserted between steps (insertNewParticle,
         # markForDeletion)
         "dambreak2d_flow_small": lambda: dambreak2d_flow(),
+        # coupled, with DEM spheres and fluid particles entering and leaving
+        "sediment3d_flow_small": lambda: sediment3d_flow(),
         # coupled, DEM moving as one block under the mean DEM force
         "sediment3d_block_small": lambda: sediment3d(nx=10, L=0.04, height=0.08, n_dem=100, nsteps=20,
                                                      dem_block=True, seed=6),

@@ -29,7 +29,7 @@ import build_ref  # noqa: E402
 
 WORKLOADS = ["dambreak2d_small", "dambreak2d_monaghan_small", "dem_small", "sediment3d_small",
              "dambreak2d_own_small", "dambreak2d_cg_varh_small", "sediment3d_reinit_small",
-             "sediment3d_block_small", "dambreak2d_flow_small"]
+             "sediment3d_block_small", "dambreak2d_flow_small", "sediment3d_flow_small"]
 
 
 def make(name: str) -> str:

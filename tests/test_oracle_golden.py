@@ -20,7 +20,7 @@ from oracle.port_api import OracleSim
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
 WORKLOADS = ["dambreak2d_small", "dambreak2d_monaghan_small", "dem_small", "sediment3d_small",
              "dambreak2d_own_small", "dambreak2d_cg_varh_small", "sediment3d_reinit_small",
-             "sediment3d_block_small", "dambreak2d_flow_small"]
+             "sediment3d_block_small", "dambreak2d_flow_small", "sediment3d_flow_small"]
 FIELD_MAP = {"r": "r", "v": "v", "vhat": "vhat", "v0": "v0", "vhat0": "vhat0", "f": "f",
              "fp": "fp", "fv": "fv", "fb": "fb", "dens": "dens", "dddt": "dddt", "h": "h",
              "press": "press", "pdr2": "pdr2", "porosity": "porosity",
@@ -83,7 +83,8 @@ def test_pairs_and_cells_match_reference(ran):
         ref = pair_set(g[key], g["pairs_" + kname + "_idx"])
         ours = pair_set(po, pi)
         assert np.array_equal(ours, ref), f"{name}:{kname} {ours.size} vs {ref.size}"
-    assert np.array_equal(o.cells(), g["cells"])
+    alive = g["field_alive"] > 0 if "field_alive" in g else np.ones(g["cells"].shape[0], bool)
+    assert np.array_equal(o.cells()[alive], g["cells"][alive])
 
 
 def output_vars_vector(ov: dict) -> np.ndarray:
