@@ -307,6 +307,13 @@ def measure_adjoint(lib, capi, cases, nsteps=100, ckpt=10):
     out["coupled"] = _time_adjoint(lib, capi, cases, cpl, cpl_steps, cpl_ckpt, cpl_seed, precisions=("mixed",))
     out["coupled"]["workload"] = (f"coupled SPH-DEM, {cpl.n} particles ({cpl.notes['n_fluid']} fluid, "
                                   f"{cpl.notes['n_dem']} DEM), {cpl_steps} steps, checkpoint every {cpl_ckpt}")
+    # the same with one segment (checkpoint interval = run length): the whole
+    # tape is recorded in the forward pass and nothing is replayed -- the
+    # cost of the taps and the reverse sweep alone
+    out["coupled_one_segment"] = _time_adjoint(lib, capi, cases, cpl, cpl_steps, cpl_steps, cpl_seed,
+                                               precisions=("mixed",))
+    out["coupled_one_segment"]["workload"] = (f"as coupled, {cpl_steps} steps in one checkpoint segment "
+                                              f"(tape recorded in the forward pass, no replay)")
     out["ratio"] = max(out["dem"]["mixed"]["ratio"], out["fluid"]["mixed"]["ratio"],
                        out["coupled"]["mixed"]["ratio"])
     return out
