@@ -649,8 +649,11 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
                             }
                         }
                         if (on && slot < maxn) nbr[nl_at(ai, slot, maxn)] = e;
-                        /* band records of this lane's own entries in this round */
-                        nb += __popc(bb & lane_range(min(max(my_ex - base, 0), 32), min(max(my_ex + c_i - base, 0), 32)));
+                        /* band records of this lane's own entries in this round
+                         * (bb is warp-uniform and almost always empty) */
+                        if (bb)
+                            nb += __popc(bb & lane_range(min(max(my_ex - base, 0), 32),
+                                                         min(max(my_ex + c_i - base, 0), 32)));
                     }
                     cnt += c_i;
                 }
