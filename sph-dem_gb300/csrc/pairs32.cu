@@ -492,6 +492,9 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
 
     for (int t0 = (blockIdx.x * NL_WARPS + w) * 32; t0 < n_t; t0 += NL_WARPS * gridDim.x * 32) {
         const int a = t0 + lane;
+        /* the warp's 32 particles share one column of list tiles: entry j of
+         * particle t0 + i sits at tiles + (j & ~7) * 32 + i * 8 + (j & 7) */
+        int *const tiles = nbr + (int64_t)(t0 >> 5) * maxn * 32;
         bool act = false;
         int key = 0;
         if (a < n_t) {
@@ -648,7 +651,7 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
                                 e = -1; /* record full: decided here (slow but exact) */
                             }
                         }
-                        if (on && slot < maxn) nbr[nl_at(ai, slot, maxn)] = e;
+                        if (on && slot < maxn) tiles[((slot & ~7) << 5) + (i << 3) + (slot & 7)] = e;
                         /* band records of this lane's own entries in this round
                          * (bb is warp-uniform and almost always empty) */
                         if (bb)
