@@ -464,6 +464,7 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
     __shared__ float4 s_pos[NL_WARPS][NL_CAP + 32];
     __shared__ int s_ent[NL_WARPS][NL_CAP + 32];
     __shared__ unsigned char s_zr[NL_WARPS][NL_CAP];
+    __shared__ float4 s_own[NL_WARPS][32];
     const int lane = threadIdx.x & 31;
     const int w = threadIdx.x >> 5;
     float4 *cpos = s_pos[w];
@@ -556,6 +557,8 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
              * particle itself and band candidates outside the particle's own
              * stencil leave a hole (-1), which every reader skips. */
             const float thr_a = fmaf(ha2, K_HI, EPS);
+            s_own[w][lane] = make_float4(pv[0], pv[1], pv[2], ha2);
+            __syncwarp();
             const int my_zr = lane_zr;
             auto evaluate = [&]() {
                 if (lane < ((32 - (nst & 31)) & 31)) {
@@ -600,10 +603,8 @@ __global__ void __launch_bounds__(NL_WARPS * 32, 3) k_nlist(DevCfg c, DevState s
                         const int exi = __shfl_sync(FULL, my_ex, i);
                         const int cni = __shfl_sync(FULL, cnt | (nb << 16), i);
                         const int zri = __shfl_sync(FULL, my_zr, i);
-                        const float pxi = __shfl_sync(FULL, pv[0], i);
-                        const float pyi = __shfl_sync(FULL, pv[1], i);
-                        const float pzi = __shfl_sync(FULL, pv[2], i);
-                        const float h2i = __shfl_sync(FULL, ha2, i);
+                        const float4 own = s_own[w][i];
+                        const float pxi = own.x, pyi = own.y, pzi = own.z, h2i = own.w;
                         const bool on = t < T;
                         int e = -1, slot = 0, j = 0;
                         const int ai = t0 + i;
