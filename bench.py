@@ -8,21 +8,29 @@ viscosity, Omega correction, porosity-weighted Tait EOS, Di Felice drag,
 linear spring-dashpot contacts, fixed dt.  Synthetic, seeded inputs.
 
   value     particle-steps/s of the mixed-precision path, state resident in
-            HBM (1.05M particles x ~1 GB of state, larger than L2), K steps
-            timed with CUDA events around replays of the captured step graph
+            HBM (1.08M particles, ~2.7 GB of state and lists, larger than
+            L2), K steps timed with CUDA events around replays of the
+            captured step graph
   e2e       the same metric through the C ABI with host buffers: create the
             simulation from pinned host arrays, then every step run it and
             read positions and densities back into pinned host arrays
-  fp64      the plain-FP64 GPU path on the same input (a few steps)
-  error     mixed vs FP64 after the same steps: max |drho|/rho0 and
-            max |df| / max |f|
-  roofline  the dominant kernel (force pass) from live per-launch CUDA
-            events; HBM fraction of its compulsory bytes and FP32-pipe
-            fraction of its pair FLOPs
+  fp64      the plain-FP64 GPU path on the same input (--fp64-steps steps)
+  error_vs_fp64  mixed vs FP64 after --error-steps steps from the same
+            input: max |drho| / rho0 and max |df| / max |f| (fluid), DEM
+            position error / R
+  roofline  the dominant kernel (largest device time per step) from live
+            per-launch CUDA events: HBM fraction of its algorithmic bytes
+            and, for the pair passes, FP32-pipe fraction of its pair FLOPs
+  configs   the other configurations at full size: the 2D dam break
+            (mixed and FP64 rates, error after 1000 steps) and the 50k-sphere
+            DEM settling (mixed and FP64 rates, error after 2000 steps)
   cpu_baseline  the CPU oracle port (a restatement of the reference's own
             C++ step) on a 1/16 periodic sub-box of the same workload
 
   python bench.py [--steps K] [--warmup W] [--gpus N] [--impl reference]
+
+With --gpus N > 1 and no launcher environment (RANK / WORLD_SIZE), the
+script starts its own N worker processes, one per GPU.
 """
 from __future__ import annotations
 
@@ -32,8 +40,10 @@ import math
 import multiprocessing as mp
 import os
 import statistics
+import socket
 import subprocess
 import sys
+import tempfile
 import time
 
 REPO = os.path.dirname(os.path.abspath(__file__))
@@ -63,8 +73,8 @@ def workload_case(small: bool = False, quarter: bool = False):
 
 
 def run_profile(args):
-    """Mixed path only: warm-up steps then `steps` graph replays; the command
-    the ncu captures under profiles/ run."""
+    """Mixed path only: warm-up steps then `steps` graph replays (the command
+    to run under a profiler)."""
     import __graft_entry__
     __graft_entry__.build()
     from sphdem import capi, cases
@@ -193,14 +203,30 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0, "sm_max_mhz": 2070.0}, "fallback"
 
 
-FORCE32_DRAM_BYTES_PER_PARTICLE = (163.309824e6 + 12.316928e6) / 270100
-
-
-def force_bytes_per_particle(avg_pairs: float) -> float:
-    """Compulsory bytes of k_force32 per target particle: packed inputs
-    (3 float4 = 48 B), type word, list length, Omega (4 B each), the list
-    itself (4 B per pair), and read+write of f, fp, fv, fb (FP64, 3 comps)."""
-    return 48 + 4 + 4 + 4 + 4.0 * avg_pairs + 4 * 3 * 8 * 2
+# Algorithmic bytes and FLOPs of one launch of each list pass (mixed
+# precision, 3D), per the compulsory-traffic rule: every field a pass needs
+# read once and every field it produces written once, plus 4 B per list entry
+# the pass reads or writes.  `owners` = sph + sphBoundary particles (the list
+# owners), `entries` = list entries of one build, `fluid` = sph particles.
+#   nlist32   reads each owner's packed position (16 B), writes its count
+#             (4 B) and its list (4 B per entry)
+#   force32   reads cell id + offset (4 + 12), vhat (12), rho, pdr2, m, h,
+#             type (4 each), porosity and Omega (4 each) and writes f (12):
+#             68 B per owner, + 4 B per entry; ~80 FLOP per entry
+#   dddt32    reads cell id + offset, vhat, m, h, type, Omega, writes dddt:
+#             52 B per owner, + 4 B per entry; ~40 FLOP per entry
+PASS_MODELS = {
+    "nlist32": lambda owners, entries: (20.0 * owners + 4.0 * entries, None),
+    "force32": lambda owners, entries: (68.0 * owners + 4.0 * entries, 80.0 * entries),
+    "dddt32": lambda owners, entries: (52.0 * owners + 4.0 * entries, 40.0 * entries),
+}
+# DRAM bytes (read + write) of one launch per particle of the whole state,
+# from ncu captures of the 270k sub-box of the same workload (traffic grows
+# in proportion to the particle count at fixed density)
+PASS_DRAM_BYTES_PER_PARTICLE = {
+    "force32": (163.309824e6 + 12.316928e6) / 270100,
+    "nlist32": (37.5e6 + 121.9e6) / 270100,
+}
 
 
 # --------------------------------------------------------------------------
@@ -347,15 +373,39 @@ def run_adjoint_profile(args):
                       "grad_viscosity": g.viscosity, "grad_drag_scale": g.drag_scale}), flush=True)
 
 
+def full_box_step_1core(warm: int = 1):
+    """One step of the CPU oracle port on the full 1.08M-particle workload on
+    one core (after `warm` warm-up steps): checks that the per-particle cost
+    of the 1/16 sub-box sample carries over to the full box."""
+    from oracle.port_api import OracleSim
+    case = workload_case()
+    t0 = time.perf_counter()
+    o = OracleSim(case.cfg, case.particles)
+    t_setup = time.perf_counter() - t0
+    o.step(warm)
+    t0 = time.perf_counter()
+    o.step(1)
+    t = time.perf_counter() - t0
+    return {"n": case.n, "setup_s": t_setup, "step_s": t, "particle_steps_per_s": case.n / t}
+
+
 def run_reference_arm(args, rank, world):
+    """The reference's CPU step (the oracle port, a restatement of its C++
+    step pinned to the compiled reference) on all host cores: one process per
+    core, each on a 1/16 periodic sub-box of the workload (16 sub-boxes make
+    the full 1.08M-particle box), W warm-up and K timed steps each; the value
+    is the particles of all processes times K over the slowest process's
+    time.  Then one full-box step on one core checks the per-particle cost."""
     if rank != 0:
         return
     procs = os.cpu_count() or 1
-    steps = max(1, min(args.steps, 2))
-    value, n, s, t = cpu_baseline(steps=steps, warm=1, procs=procs)
+    value, n, s, t = cpu_baseline(steps=args.steps, warm=args.warmup, procs=procs)
     sample = (f"CPU oracle port (restatement of the reference's C++ step, single-threaded per "
-              f"process) on a 1/16 periodic sub-box of the workload ({n} particles), "
-              f"{procs} independent processes x {s} steps after 1 warm-up step")
+              f"process) on 1/16 periodic sub-boxes of the workload ({n} particles each, "
+              f"{procs} processes = {procs / 16:.2f} full boxes), {s} timed steps after {args.warmup} "
+              f"warm-up steps each")
+    full = None if args.no_full_box else full_box_step_1core()
+    per_core_sub = value / procs
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / s,
@@ -363,26 +413,95 @@ def run_reference_arm(args, rank, world):
         "data": "synthetic (seeded)", "config": workload_config(workload_case(), args.steps),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "per_core_sub_box": per_core_sub,
+        "full_box_check": None if full is None else dict(
+            full, sub_box_per_core_over_full_box=per_core_sub / full["particle_steps_per_s"]),
     }
     print(json.dumps(line), flush=True)
+
+
+def select_device(world: int) -> None:
+    """One GPU per rank: the launcher's LOCAL_RANK, set as the current device
+    of the CUDA runtime the library uses (and of torch, whose NCCL calls need
+    it)."""
+    if world <= 1:
+        return
+    import ctypes as C
+    local = int(os.environ.get("LOCAL_RANK", os.environ.get("RANK", "0")))
+    rt = C.CDLL("libcudart.so.13")
+    rc = rt.cudaSetDevice(local)
+    if rc != 0:
+        raise RuntimeError(f"cudaSetDevice({local}) failed with {rc}")
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+    except ImportError:
+        pass
+
+
+def _kernel_split(sim, steps=2):
+    """Per-kernel device ms per step and launches per step over `steps` steps."""
+    sim.kernel_times_reset(True)
+    sim.step(steps)
+    kt = sim.kernel_times()
+    sim.kernel_times_reset(False)
+    return {k: (m / steps, c / steps) for k, (m, c) in kt.items()}
+
+
+def _errors(a, b, cases, rho0, R):
+    """Mixed (a) against FP64 (b), tag order: fluid density and force, DEM
+    position."""
+    iam = b["iam"]
+    fl = (iam == cases.SPH) | (iam == cases.SPH_BOUNDARY)
+    dem = iam == cases.DEM
+    out = {}
+    if fl.any():
+        out["max_abs_drho_over_rho0"] = float(np.abs(a["dens"][fl] - b["dens"][fl]).max() / rho0)
+        out["max_abs_df_over_max_f"] = float(np.abs(a["f"][fl] - b["f"][fl]).max() / np.abs(b["f"][fl]).max())
+    if dem.any():
+        out["dem_max_abs_dr_over_R"] = float(np.abs(a["r"][dem] - b["r"][dem]).max() / R)
+        out["dem_max_abs_df_over_max_f"] = float(np.abs(a["f"][dem] - b["f"][dem]).max()
+                                                 / max(np.abs(b["f"][dem]).max(), 1e-300))
+    return out
+
+
+def measure_config(lib, capi, cases, case, mixed_steps, fp64_steps, err_steps, R):
+    """Mixed and FP64 rates (graph replays timed with CUDA events) of one
+    configuration and the mixed error against FP64 after err_steps steps."""
+    n = case.n
+    mixed = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    fp64 = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_FP64)
+    ms_m = mixed.time_steps(mixed_steps)
+    ms_f = fp64.time_steps(fp64_steps)
+    mixed.step(err_steps - mixed_steps - 1)
+    fp64.step(err_steps - fp64_steps - 1)
+    a, b = mixed.get(), fp64.get()
+    mixed.close()
+    fp64.close()
+    return {"n_particles": n,
+            "mixed": {"value": n * mixed_steps / (ms_m * 1e-3), "unit": UNIT, "steps": mixed_steps},
+            "fp64": {"value": n * fp64_steps / (ms_f * 1e-3), "unit": UNIT, "steps": fp64_steps},
+            "mixed_over_fp64": (ms_f / fp64_steps) / (ms_m / mixed_steps),
+            "error_vs_fp64": dict(_errors(a, b, cases, case.cfg["dens"], R), steps=err_steps)}
 
 
 def run_ours(args, rank, world):
     import __graft_entry__
     __graft_entry__.build()
+    select_device(world)
     from sphdem import capi, cases
     lib = capi.Library()
     case = workload_case()
     n = case.n
-    out_dir = os.path.join(REPO, "gpurun_out")
-    os.makedirs(out_dir, exist_ok=True)
+    scratch = tempfile.mkdtemp(prefix="sphdem_bench_")
 
     # ---- mixed precision, device-resident --------------------------------
     dist = dist_setup(world)
     sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
     sim.step(args.warmup)
     barrier(dist)
-    with ClockSampler(os.path.join(out_dir, "bench_clocks.csv")) as clk:
+    with ClockSampler(os.path.join(scratch, "clocks.csv")) as clk:
         ms = sim.time_steps(args.steps)   # CUDA events on the handle's stream, synchronised
     barrier(dist)
     ms = max_over_ranks(ms, dist)
@@ -390,48 +509,82 @@ def run_ours(args, rank, world):
     value = aggregate_rate(n * args.steps, world, ms * 1e-3)
     st = sim.stats()
 
-    # per-kernel device times (CUDA events around each launch), 2 steps
-    sim.kernel_times_reset(True)
-    sim.step(2)
-    kt = sim.kernel_times()
-    sim.kernel_times_reset(False)
-    launches_per_step = sum(c for _, c in kt.values()) / 2.0
-    total_ms = sum(m for m, _ in kt.values())
-    top = sorted(kt.items(), key=lambda kv: -kv[1][0])
-    force_ms, force_launches = kt.get("force32", (float("nan"), 1))
-    force_ms_per_launch = force_ms / max(1, force_launches)
+    # per-kernel device times (CUDA events around each launch on the
+    # handle's stream), 2 steps
+    split = _kernel_split(sim, 2)
+    launches_per_step = sum(c for _, c in split.values())
+    total_ms = sum(m for m, _ in split.values())
+    top = sorted(split.items(), key=lambda kv: -kv[1][0])
 
+    # ---- roofline of the dominant list pass -------------------------------
     peaks, peak_kind = measured_peaks()
-    avg_pairs = st.n_list_pairs / max(1, case.notes["n_fluid"] + case.notes["n_boundary"])
-    targets = case.notes["n_fluid"]
-    alg_bytes = force_bytes_per_particle(avg_pairs) * targets
-    achieved_gbs = alg_bytes / (force_ms_per_launch * 1e-3) / 1e9
-    sm_mhz = clocks.get("sm_max_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    fp32_peak = SM_COUNT * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
-    flops = FORCE_FLOP_PER_PAIR * st.n_list_pairs
-    achieved_tf = flops / (force_ms_per_launch * 1e-3) / 1e12
-    # DRAM bytes of one force32 launch from an ncu capture, per particle of the
-    # whole state (traffic grows in proportion to the particle count at fixed
-    # density; the capture is the 270k sub-box, profiles/force32_sediment3d_quarter.md)
-    traffic = FORCE32_DRAM_BYTES_PER_PARTICLE * n
+    owners = case.notes["n_fluid"] + case.notes["n_boundary"]
+    entries = float(st.n_list_pairs)
+    dom = next((k for k, _ in top if k in PASS_MODELS), None)
+    roof = None
+    if dom is not None:
+        ms_step, launches = split[dom]
+        ms_launch = ms_step / max(launches, 1e-9)
+        alg_bytes, flops = PASS_MODELS[dom](owners, entries)
+        achieved = alg_bytes / (ms_launch * 1e-3) / 1e9
+        sm_mhz = clocks.get("sm_max_mhz") or peaks.get("sm_max_mhz", 2070.0)
+        fp32_peak = SM_COUNT * FP32_LANES * 2 * sm_mhz * 1e6 / 1e12
+        traffic = PASS_DRAM_BYTES_PER_PARTICLE.get(dom)
+        roof = {
+            "kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"),
+            "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs", 6800.0),
+            "traffic": None if traffic is None else traffic * n,
+            "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes, "ms_per_launch": ms_launch,
+            "launches_per_step": launches, "share_of_step": ms_step / total_ms,
+            "list_entries": entries, "owners": owners,
+            "h_max": st.h_max, "search_radius": st.search_radius, "n_sph_cells": st.n_sph_cells,
+            "band_candidates": st.n_band_candidates,
+        }
+        if flops is not None:
+            achieved_tf = flops / (ms_launch * 1e-3) / 1e12
+            roof["fp32_pipe"] = {"achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
+                                 "frac": achieved_tf / fp32_peak,
+                                 "peak_basis": f"{SM_COUNT} SMs x {FP32_LANES} lanes x 2 x {sm_mhz:.0f} MHz"}
+    passes = {}
+    for k in PASS_MODELS:
+        if k in split:
+            ms_step, launches = split[k]
+            b_, f_ = PASS_MODELS[k](owners, entries)
+            ms_launch = ms_step / max(launches, 1e-9)
+            passes[k] = {"ms_per_launch": ms_launch, "launches_per_step": launches,
+                         "hbm_frac": b_ / (ms_launch * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0)}
 
-    # ---- mixed vs FP64 on the same input ---------------------------------
-    fp64_steps = max(1, min(args.fp64_steps, args.steps))
+    # ---- FP64 path and mixed-vs-FP64 error on the same input -------------
+    fp64_steps = max(1, args.fp64_steps)
+    err_steps = max(args.error_steps, fp64_steps + 2, args.warmup + args.steps + 3)
     ref = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_FP64)
     ref.step(1)
-    ms64 = ref.time_steps(fp64_steps)  # steps 2 .. fp64_steps+2 (one more inside for the graph)
+    ms64 = ref.time_steps(fp64_steps)   # advances fp64_steps + 1 steps
     fp64_value = n * fp64_steps / (ms64 * 1e-3)
-    ref_steps = 2 + fp64_steps
-    cmp = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
-    cmp.step(ref_steps)
-    a = cmp.get(capi.FIELD_DENS | capi.FIELD_F)
-    b = ref.get(capi.FIELD_DENS | capi.FIELD_F)
-    err_dens = float(np.abs(a["dens"] - b["dens"]).max() / case.cfg["dens"])
-    err_f = float(np.abs(a["f"] - b["f"]).max() / np.abs(b["f"]).max())
+    ref.step(err_steps - fp64_steps - 2)
+    done = int(sim.globals().sph_step)
+    sim.step(err_steps - done)
+    a, b = sim.get(capi.FIELD_DENS | capi.FIELD_F | capi.FIELD_R | capi.FIELD_IAM), \
+        ref.get(capi.FIELD_DENS | capi.FIELD_F | capi.FIELD_R | capi.FIELD_IAM)
+    err = dict(_errors(a, b, cases, case.cfg["dens"], case.notes["dem_radius"]), steps=err_steps,
+               against="the FP64 GPU path from the same input (pinned to the CPU oracle on the small cases)")
     ref.close()
-    cmp.close()
 
-    # ---- adjoint / forward on the DEM-only and dam-break workloads --------
+    # ---- the other configurations at full size ---------------------------
+    configs = None
+    if not args.no_configs:
+        db = cases.workload("dambreak2d")
+        dem = cases.workload("dem_settling3d")
+        configs = {
+            "dambreak2d": dict(measure_config(lib, capi, cases, db, 200, 50, 1000, db.cfg["psep"]),
+                               workload=f"2D dam break, {db.notes['n_fluid']} fluid + {db.notes['n_boundary']} "
+                                        f"wall particles, dx 0.01, artificial viscosity, dt 0.25 h/c0"),
+            "dem_settling3d": dict(measure_config(lib, capi, cases, dem, 200, 200, 2000, dem.cfg["dem_radius"]),
+                                   workload="DEM settling, 50,000 spheres radius 1 mm x U[0.9, 1.1], walled "
+                                            "0.1 x 0.1 x 0.3 m box, k 1e4, e 0.5, dt 1e-5"),
+        }
+
+    # ---- adjoint / forward ------------------------------------------------
     adjoint = measure_adjoint(lib, capi, cases) if not args.no_adjoint else None
 
     # ---- end to end through the C ABI with host buffers -------------------
@@ -477,23 +630,14 @@ def run_ours(args, rank, world):
                         "sphdem_fields_wait at the end; wall clock"},
         "fp64": {"value": fp64_value, "unit": UNIT, "steps": fp64_steps,
                  "mixed_over_fp64": value / fp64_value},
-        "error_vs_fp64": {"steps": ref_steps, "max_abs_drho_over_rho0": err_dens,
-                          "max_abs_df_over_max_f": err_f},
+        "error_vs_fp64": err,
+        "configs": configs,
         "adjoint_over_forward": adjoint["ratio"] if adjoint else None,
         "adjoint": adjoint,
-        "roofline": {
-            "kernel": "force32", "bound": "hbm", "achieved": achieved_gbs, "peak": peaks.get("hbm_gbs"),
-            "unit": "GB/s", "frac": achieved_gbs / peaks.get("hbm_gbs", 6800.0), "traffic": traffic,
-            "peak_kind": peak_kind, "alg_bytes_per_launch": alg_bytes,
-            "ms_per_launch": force_ms_per_launch, "avg_list_pairs": avg_pairs,
-            "h_max": st.h_max, "search_radius": st.search_radius, "n_sph_cells": st.n_sph_cells,
-            "band_candidates": st.n_band_candidates,
-            "fp32_pipe": {"achieved": achieved_tf, "peak": fp32_peak, "unit": "TFLOP/s",
-                          "frac": achieved_tf / fp32_peak,
-                          "peak_basis": f"{SM_COUNT} SMs x {FP32_LANES} lanes x 2 x {sm_mhz:.0f} MHz"},
-        },
-        "kernels_ms_per_step": {k: v[0] / 2.0 for k, v in top[:12]},
-        "kernel_share": {k: v[0] / total_ms for k, v in top[:12]},
+        "roofline": roof,
+        "passes": passes,
+        "kernels_ms_per_step": {k: v[0] for k, v in top[:14]},
+        "kernel_share": {k: v[0] / total_ms for k, v in top[:14]},
         "gpu_launches": int(round(launches_per_step * args.steps)),
         "clocks": clocks,
         "cpu_baseline": cpu,
@@ -553,16 +697,41 @@ def run_ensemble(args):
     print(json.dumps(line), flush=True)
 
 
+def replica_env(rank: int, world: int, port: int, base: dict | None = None) -> dict:
+    """Environment of worker `rank` of `world` self-started replicas (the
+    variables torch.distributed.run would set; rendezvous on 127.0.0.1)."""
+    env = dict(os.environ if base is None else base)
+    env.update(RANK=str(rank), LOCAL_RANK=str(rank), WORLD_SIZE=str(world), LOCAL_WORLD_SIZE=str(world),
+               MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    return env
+
+
+def spawn_replicas(world: int) -> int:
+    """bench.py --gpus N without a launcher: start N copies of this command,
+    one per GPU; rank 0 prints the line.  Returns the worst exit code."""
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    procs = [subprocess.Popen([sys.executable, os.path.abspath(__file__), *sys.argv[1:]],
+                              env=replica_env(r, world, port)) for r in range(world)]
+    return max(p.wait() for p in procs)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--fp64-steps", type=int, default=20)
+    ap.add_argument("--error-steps", type=int, default=100,
+                    help="steps after which the mixed path is compared with the FP64 path")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-configs", action="store_true", help="skip the dam-break and DEM-settling legs")
+    ap.add_argument("--no-full-box", action="store_true", help="reference arm: skip the full-box step")
     ap.add_argument("--profile", action="store_true", help="mixed path only (for profiler captures)")
     ap.add_argument("--quarter", action="store_true", help="with --profile: 1/4 sub-box of the workload")
     ap.add_argument("--ensemble", action="store_true", help="batched dam-break ensemble instead")
@@ -572,8 +741,12 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    launched = "RANK" in os.environ and "WORLD_SIZE" in os.environ
+    if args.gpus > 1 and not launched and args.impl == "ours" and not (
+            args.profile or args.ensemble or args.adjoint_profile):
+        sys.exit(spawn_replicas(args.gpus))
+    rank = int(os.environ.get("RANK", "0")) if launched else 0
+    world = int(os.environ.get("WORLD_SIZE", "1")) if launched else 1
     if args.adjoint_profile:
         run_adjoint_profile(args)
     elif args.profile:
@@ -583,8 +756,6 @@ def main():
     elif args.impl == "reference":
         run_reference_arm(args, rank, world)
     else:
-        if world > 1:
-            os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("LOCAL_RANK", "0"))
         run_ours(args, rank, world)
 
 

@@ -366,9 +366,10 @@ int sphdem_batch_last_error(sphdem_batch b, char *buf, size_t len);
  * cudaFree.  It stages through one static device array of
  * SPHDEM_CELL_IDS_NOALLOC_MAX x 3 int32 per device, shared by every call on
  * that device: calls that overlap in time race on it.  Larger simulations
- * return SPHDEM_ERR_CAPACITY.  The first call on a device sets up the array's
- * address (and may load the module there): make it before any stream capture
- * on that device.  Same output as sphdem_cell_ids. */
+ * return SPHDEM_ERR_CAPACITY.  Every call looks the array's address up on the
+ * handle's device; the first call on a device may load the module there, so
+ * make it before any stream capture on that device.  Same output as
+ * sphdem_cell_ids. */
 int sphdem_cell_ids_noalloc(sphdem_handle h, int32_t *cell_xyz);
 
 /* Per-kernel device time accumulated with CUDA events since the last reset

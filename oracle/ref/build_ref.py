@@ -26,7 +26,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REF_SRC = "/root/reference"
+sys.path.insert(0, REPO)
+from oracle.refroot import REF_ROOT as REF_SRC  # noqa: E402
 OUT_ROOT = os.path.join(REPO, "oracle", "_ref")
 sys.path.insert(0, os.path.join(REPO, "sph-dem_gb300"))
 

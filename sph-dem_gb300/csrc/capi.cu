@@ -889,10 +889,12 @@ int sphdem_pairs(sphdem_handle h, int kind, int64_t *offsets, int32_t *idx, int6
 int sphdem_cell_ids(sphdem_handle h, int32_t *cells) {
     if (!h || !cells) return SPHDEM_ERR_INVALID;
     try {
-        return export_cells(h, cells);
+        const int rc = export_cells(h, cells);
+        if (rc) return rc;
     } catch (const std::string &e) {
         return fail(h, SPHDEM_ERR_CUDA, e);
     }
+    return check_device(h);
 }
 
 int sphdem_adjoint_forward(sphdem_handle h, int nsteps, int ckpt_every) {
@@ -944,10 +946,12 @@ int sphdem_output_vars(sphdem_handle h, SphDemOutputVars *out) {
 int sphdem_cell_ids_noalloc(sphdem_handle h, int32_t *cells) {
     if (!h || !cells) return SPHDEM_ERR_INVALID;
     try {
-        return export_cells_noalloc(h, cells);
+        const int rc = export_cells_noalloc(h, cells);
+        if (rc) return rc;
     } catch (const std::string &e) {
         return fail(h, SPHDEM_ERR_CUDA, e);
     }
+    return check_device(h);
 }
 
 int sphdem_kernel_times_reset(sphdem_handle h, int enable) {

@@ -6,7 +6,6 @@
  * lists after a reset.
  */
 #include <algorithm>
-#include <mutex>
 
 #include "internal.cuh"
 
@@ -203,9 +202,10 @@ int export_cells(sphdem_ctx *c, int32_t *cells) {
  * - Capacity: SPHDEM_CELL_IDS_NOALLOC_MAX particles (3 int32 each, 3 MiB of
  *   static device memory per device that loads this module); larger
  *   simulations are rejected with SPHDEM_ERR_CAPACITY.
- * - The first call on a device looks the array's device address up with
- *   cudaGetSymbolAddress (this can load the module on that device); make that
- *   first call before any stream capture on the device.
+ * - Every call looks the array's device address up with cudaGetSymbolAddress
+ *   on the handle's device (cheap; the first call on a device can load the
+ *   module there), so no address outlives a device reset.  Make the first
+ *   call on a device before any stream capture on it.
  * - Every call on a device shares the one array: calls that overlap in time
  *   (from several threads, or several handles on one device) race on it.
  *   Nothing in it needs to start at zero: k_cells writes all 3n entries
@@ -214,10 +214,6 @@ int export_cells(sphdem_ctx *c, int32_t *cells) {
 namespace {
 
 static __device__ __align__(256) int32_t g_cells_scratch[3 * SPHDEM_CELL_IDS_NOALLOC_MAX];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mu;
-int32_t *g_scratch_ptr[kMaxDevices] = {};
 
 }  // namespace
 
@@ -232,24 +228,17 @@ int export_cells_noalloc(sphdem_ctx *c, int32_t *cells) {
     cudaPointerAttributes attr{};
     SPHDEM_CUDA_CHECK(cudaPointerGetAttributes(&attr, c->g));
     const int dev = attr.device;
-    if (dev < 0 || dev >= kMaxDevices) {
-        c->err = "sphdem_cell_ids_noalloc: device index out of range";
+    if (dev < 0) {
+        c->err = "sphdem_cell_ids_noalloc: the handle's device could not be resolved";
         return SPHDEM_ERR_UNSUPPORTED;
     }
     int prev = -1;
     SPHDEM_CUDA_CHECK(cudaGetDevice(&prev));
     if (prev != dev) SPHDEM_CUDA_CHECK(cudaSetDevice(dev));
-    int32_t *scratch = nullptr;
-    cudaError_t e = cudaSuccess;
-    {
-        std::lock_guard<std::mutex> lock(g_scratch_mu);
-        if (!g_scratch_ptr[dev]) {
-            void *p = nullptr;
-            e = cudaGetSymbolAddress(&p, g_cells_scratch);
-            if (e == cudaSuccess) g_scratch_ptr[dev] = static_cast<int32_t *>(p);
-        }
-        scratch = g_scratch_ptr[dev];
-    }
+    /* the array's address on this device, looked up with the device current */
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_cells_scratch);
+    int32_t *scratch = static_cast<int32_t *>(p);
     if (e == cudaSuccess && n > 0) {
         k_cells<<<grid_for(n, BLK), BLK, 0, c->stream>>>(c->cfg, c->A, c->g, n, scratch);
         e = cudaGetLastError();

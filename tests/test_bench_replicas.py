@@ -52,3 +52,18 @@ def test_single_process_needs_no_process_group():
     assert bench.dist_setup(1) is None
     assert bench.max_over_ranks(2.5, None) == 2.5
     assert bench.aggregate_rate(100.0, 1, 2.0) == 50.0
+
+
+def test_self_started_replicas_get_one_rank_each():
+    """bench.py --gpus N without a launcher starts N workers itself: each
+    gets its own RANK / LOCAL_RANK (its GPU), the same WORLD_SIZE and a
+    127.0.0.1 rendezvous."""
+    sys.path.insert(0, REPO)
+    import bench
+    envs = [bench.replica_env(r, 4, 29500, base={"PATH": "/bin"}) for r in range(4)]
+    assert [e["RANK"] for e in envs] == ["0", "1", "2", "3"]
+    assert [e["LOCAL_RANK"] for e in envs] == ["0", "1", "2", "3"]
+    assert {e["WORLD_SIZE"] for e in envs} == {"4"}
+    assert {e["MASTER_ADDR"] for e in envs} == {"127.0.0.1"}
+    assert {e["MASTER_PORT"] for e in envs} == {"29500"}
+    assert all(e["PATH"] == "/bin" for e in envs)

@@ -9,6 +9,7 @@ import sys
 import numpy as np
 import pytest
 
+from oracle.refroot import REF_ROOT
 from sphdem import capi, cases, state
 
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -38,7 +39,7 @@ def test_example_constants_in_step(tmp_path):
         assert fh.read() == make_constants.constants()
 
 
-REF_CASE = "/root/reference/sediment3D"
+REF_CASE = os.path.join(REF_ROOT, "sediment3D")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_CASE), reason="reference sources not present")

@@ -11,9 +11,9 @@ import os
 import numpy as np
 import pytest
 
+from oracle.refroot import REF_ROOT as REF
 from sphdem import cases, io_vtk
 
-REF = "/root/reference"
 SHIPPED = ["singleDEM", "singleDEM3D", "singleDEMdrop3d"]
 
 

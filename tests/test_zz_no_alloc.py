@@ -5,6 +5,11 @@ Integer output, so the bar is equality.  Collected last on purpose: it must
 hold after every other test has used the device, and alone in a fresh
 process.
 """
+import ctypes as C
+import os
+import subprocess
+import sys
+
 import numpy as np
 import pytest
 
@@ -40,6 +45,60 @@ def test_noalloc_matches_cell_ids(lib, name, precision):
         np.testing.assert_array_equal(sim.cell_ids_noalloc(), sim.cell_ids())
     finally:
         sim.close()
+
+
+def _free_device_bytes() -> int:
+    """cudaMemGetInfo's free bytes, through the CUDA runtime libsphdem.so loads."""
+    rt = C.CDLL("libcudart.so.13")
+    free, total = C.c_size_t(0), C.c_size_t(0)
+    assert rt.cudaMemGetInfo(C.byref(free), C.byref(total)) == 0
+    return free.value
+
+
+def test_noalloc_takes_no_device_memory(lib):
+    """After the first call (which may load the module, and with it the static
+    array, on the device), further calls leave the device's free memory as it
+    was: the entry point allocates nothing."""
+    case = cases.workload("sediment3d_small")
+    sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    try:
+        sim.step(2)
+        first = sim.cell_ids_noalloc()
+        free0 = _free_device_bytes()
+        for _ in range(5):
+            again = sim.cell_ids_noalloc()
+            np.testing.assert_array_equal(again, first)
+        assert _free_device_bytes() == free0
+    finally:
+        sim.close()
+
+
+FRESH = r"""
+import sys
+sys.path[:0] = {paths!r}
+import numpy as np
+from sphdem import capi, cases
+lib = capi.Library()
+case = cases.workload("sediment3d_small")
+sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+sim.step(3)
+a = sim.cell_ids_noalloc()
+b = sim.cell_ids_noalloc()
+ref = sim.cell_ids()
+assert (a == ref).all() and (b == ref).all()
+sim.close()
+print("fresh-process noalloc ok")
+"""
+
+
+def test_noalloc_first_call_in_fresh_process(lib, repo_root):
+    """The entry point as the first device export of a process that has run
+    nothing else: two calls in a row, then the allocating export."""
+    paths = [os.path.join(repo_root, "sph-dem_gb300"), repo_root]
+    res = subprocess.run([sys.executable, "-c", FRESH.format(paths=paths)], capture_output=True, text=True,
+                         timeout=600)
+    assert res.returncode == 0, res.stderr[-4000:]
+    assert "fresh-process noalloc ok" in res.stdout
 
 
 def test_noalloc_rejects_large(lib):
