@@ -15,15 +15,23 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIBDIR = os.path.dirname(HERE)
 
 
+def zlib_flags() -> list:
+    """-lz where zlib's header is installed (the restart reader then also
+    reads zlib-compressed pieces, and the writer compresses)."""
+    probe = subprocess.run(["g++", "-E", "-x", "c++", "-", "-o", os.devnull], input="#include <zlib.h>\n",
+                           capture_output=True, text=True)
+    return ["-lz"] if probe.returncode == 0 else []
+
+
 def build_case(case_dir: str, out: str, extra=()) -> str:
     case_dir = os.path.abspath(case_dir)
-    srcs = [os.path.join(HERE, "run_facade.cpp")]
+    srcs = [os.path.join(HERE, "run_facade.cpp"), os.path.join(HERE, "io_data_vtk.cpp")]
     for f in ("customSim.cpp", "customOutput.cpp"):
         p = os.path.join(case_dir, f)
         if os.path.exists(p):
             srcs.append(p)
     cmd = ["g++", "-std=gnu++17", "-O2", "-w", f"-I{case_dir}", f"-I{os.path.join(HERE, 'include')}",
-           *srcs, f"-L{LIBDIR}", "-lsphdem", f"-Wl,-rpath,{LIBDIR}", "-o", out, *extra]
+           *srcs, f"-L{LIBDIR}", "-lsphdem", f"-Wl,-rpath,{LIBDIR}", "-o", out, *zlib_flags(), *extra]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("case build failed:\n" + res.stderr[-6000:])

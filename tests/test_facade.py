@@ -175,3 +175,140 @@ def test_case_hook_insertion_and_deletion(tmp_path):
         scale = np.abs(b[k][live]).max()
         err = np.abs(a[k][live] - b[k][live]).max() / scale
         assert err <= 1e-12, f"{k}: {err}"
+
+
+# ---------------------------------------------------------------------------
+# restart files through the façade's C++ reader and writer (Cio_data_vtk)
+VTK_TOOL = r"""
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include "io_data_vtk.h"
+/* vtk_tool <in.vtu> <out fields bin> <out piece.vtu> <float64 points 0/1> */
+int main(int argc, char **argv) {
+    particleContainer ps;
+    if (!Cio_data_vtk::readPiece(argv[1], ps)) return 1;
+    std::ofstream out(argv[2], std::ios::binary);
+    for (const Cparticle &p : ps) {
+        double rec[16] = {0};
+        for (int d = 0; d < NDIM; d++) {
+            rec[d] = p.r[d];
+            rec[3 + d] = p.v[d];
+            rec[6 + d] = p.vhat[d];
+            rec[9 + d] = p.norm1[d];
+        }
+        rec[12] = p.mass;
+        rec[13] = p.dens;
+        rec[14] = p.h;
+        rec[15] = p.iam + 1000.0 * p.tag;
+        out.write(reinterpret_cast<const char *>(rec), sizeof rec);
+    }
+    return Cio_data_vtk::writePiece(argv[3], ps, std::atoi(argv[4]) != 0) ? 0 : 2;
+}
+"""
+
+
+def _vtk_tool(tmp_path, ndim):
+    d = tmp_path / f"tool{ndim}"
+    d.mkdir(exist_ok=True)
+    (d / "customConstants.h").write_text(f"#ifndef CC_H\n#define CC_H\nconst int NDIM = {ndim};\n#endif\n")
+    (d / "vtk_tool.cpp").write_text(VTK_TOOL)
+    sys.path.insert(0, FACADE)
+    from build_case import zlib_flags
+    exe = str(d / "vtk_tool")
+    res = subprocess.run(["g++", "-std=gnu++17", "-O1", f"-I{d}", f"-I{os.path.join(FACADE, 'include')}",
+                          str(d / "vtk_tool.cpp"), os.path.join(FACADE, "io_data_vtk.cpp"), "-o", exe,
+                          *zlib_flags()], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr[-3000:]
+    return exe
+
+
+@pytest.mark.parametrize("name", ["dambreak2d_small", "sediment3d_small"])
+@pytest.mark.parametrize("exact", [False, True])
+def test_cpp_restart_reader_and_writer(tmp_path, name, exact):
+    """A restart piece written by sphdem.io_vtk reads back through the C++
+    reader field for field, and the C++ writer's piece reads back through
+    sphdem.io_vtk (Float32 points as the reference writes them, Float64 for
+    the exact form)."""
+    from sphdem import io_vtk
+    case = cases.workload(name)
+    nd = case.cfg["ndim"]
+    ps = {k: np.asarray(v) for k, v in case.particles.items()}
+    n = case.n
+    rng = np.random.default_rng(2)
+    ps["tag"] = np.arange(1, n + 1, dtype=np.int32)
+    ps["v"] = np.zeros((n, 3))
+    ps["v"][:, :nd] = rng.normal(size=(n, nd))
+    ps["vhat"] = ps["v"] * 0.5
+    io_vtk.write_restart(str(tmp_path / "case"), 0, ps, nd, exact=exact)
+    exe = _vtk_tool(tmp_path, nd)
+    fields, back = tmp_path / "fields.bin", tmp_path / "back.vtu"
+    res = subprocess.run([exe, str(tmp_path / "caseRestart0000000_0.vtu"), str(fields), str(back),
+                          "1" if exact else "0"], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stderr[-2000:]
+    rec = np.fromfile(str(fields), "<f8").reshape(n, 16)
+    r_want = ps["r"][:, :nd] if exact else ps["r"][:, :nd].astype(np.float32).astype(np.float64)
+    np.testing.assert_array_equal(rec[:, 0:nd], r_want)
+    np.testing.assert_array_equal(rec[:, 3:3 + nd], ps["v"][:, :nd])
+    np.testing.assert_array_equal(rec[:, 6:6 + nd], ps["vhat"][:, :nd])
+    np.testing.assert_array_equal(rec[:, 9:9 + nd], np.asarray(ps["norm1"])[:, :nd])
+    np.testing.assert_array_equal(rec[:, 12], ps["mass"])
+    np.testing.assert_array_equal(rec[:, 13], ps["dens"])
+    np.testing.assert_array_equal(rec[:, 14], ps["h"])
+    np.testing.assert_array_equal(rec[:, 15], ps["iam"] + 1000.0 * ps["tag"])
+    d = io_vtk.read_vtu(str(back))
+    assert d["n"] == n and d["points_type"] == ("Float64" if exact else "Float32")
+    np.testing.assert_array_equal(d["points"][:, :nd], r_want)
+    for k in ("dens", "h", "mass"):
+        np.testing.assert_array_equal(d["arrays"][k], ps[k])
+    np.testing.assert_array_equal(d["arrays"]["tag"], ps["tag"])
+    np.testing.assert_array_equal(d["arrays"]["v"][:, :nd], ps["v"][:, :nd])
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_ROOT, "singleDEM3D")), reason="reference files not present")
+def test_cpp_reader_on_the_reference_restart_files(tmp_path):
+    """The restart piece the reference shipped (written by VTK) reads through
+    the C++ reader as it reads through sphdem.io_vtk."""
+    from sphdem import io_vtk
+    import glob
+    pieces = sorted(glob.glob(os.path.join(REF_ROOT, "singleDEM3D", "*Restart*_0.vtu")))
+    if not pieces:
+        pytest.skip("no restart piece shipped")
+    exe = _vtk_tool(tmp_path, 3)
+    fields, back = tmp_path / "fields.bin", tmp_path / "back.vtu"
+    res = subprocess.run([exe, pieces[0], str(fields), str(back), "0"], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stderr[-2000:]
+    d = io_vtk.read_vtu(pieces[0])
+    rec = np.fromfile(str(fields), "<f8").reshape(d["n"], 16)
+    np.testing.assert_array_equal(rec[:, 0:3], d["points"])
+    np.testing.assert_array_equal(rec[:, 13], d["arrays"]["dens"])
+    np.testing.assert_array_equal(rec[:, 15], d["arrays"]["iam"] + 1000.0 * d["arrays"]["tag"])
+
+
+@pytest.mark.gpu
+def test_case_runs_from_a_restart_piece(tmp_path):
+    """run_facade started from the restart piece a case's setup writes
+    (<base>Restart0000000_0.vtu, Float64 points) gives the state the SPDMST01
+    start gives, and its own final restart reads back."""
+    import __graft_entry__
+    from sphdem import io_vtk
+    __graft_entry__.build()
+    exe = build_case(os.path.join(FACADE, "example_sediment"), str(tmp_path / "run_example"))
+    case = cases.workload("sediment3d_small")
+    ps = dict(case.particles)
+    ps["tag"] = np.arange(1, case.n + 1, dtype=np.int32)
+    pvtu = io_vtk.write_restart(str(tmp_path / "init"), 0, ps, 3, exact=True)
+    spdm = tmp_path / "init.spdm"
+    state.write_state(str(spdm), case.particles)
+    outs = []
+    for src in (str(spdm), str(tmp_path / "initRestart0000000_0.vtu"), pvtu):
+        final = tmp_path / f"final{len(outs)}.bin"
+        res = subprocess.run([exe, src, "4", str(final), "--fixed-dt", "--restart-out", str(tmp_path / "out")],
+                             capture_output=True, text=True, timeout=300)
+        assert res.returncode == 0, res.stderr[-2000:]
+        outs.append(read_final(str(final)))
+    for o in outs[1:]:
+        for k in ("r", "vhat", "dens"):
+            np.testing.assert_array_equal(o[k], outs[0][k])
+    d = io_vtk.read_vtu(str(tmp_path / "outRestart0000004_0.vtu"))
+    np.testing.assert_array_equal(d["points"], outs[0]["r"])
