@@ -373,16 +373,18 @@ def run_adjoint_profile(args):
                       "grad_viscosity": g.viscosity, "grad_drag_scale": g.drag_scale}), flush=True)
 
 
-def full_box_step_1core(warm: int = 1):
+def full_box_step_1core(warm: int = 0):
     """One step of the CPU oracle port on the full 1.08M-particle workload on
-    one core (after `warm` warm-up steps): checks that the per-particle cost
-    of the 1/16 sub-box sample carries over to the full box."""
+    one core (after `warm` warm-up steps; the oracle builds its lists at
+    creation, outside the timed step): checks that the per-particle cost of
+    the 1/16 sub-box sample carries over to the full box."""
     from oracle.port_api import OracleSim
     case = workload_case()
     t0 = time.perf_counter()
     o = OracleSim(case.cfg, case.particles)
     t_setup = time.perf_counter() - t0
-    o.step(warm)
+    if warm:
+        o.step(warm)
     t0 = time.perf_counter()
     o.step(1)
     t = time.perf_counter() - t0
@@ -561,13 +563,28 @@ def run_ours(args, rank, world):
     ref.step(1)
     ms64 = ref.time_steps(fp64_steps)   # advances fp64_steps + 1 steps
     fp64_value = n * fp64_steps / (ms64 * 1e-3)
-    ref.step(err_steps - fp64_steps - 2)
-    done = int(sim.globals().sph_step)
-    sim.step(err_steps - done)
-    a, b = sim.get(capi.FIELD_DENS | capi.FIELD_F | capi.FIELD_R | capi.FIELD_IAM), \
-        ref.get(capi.FIELD_DENS | capi.FIELD_F | capi.FIELD_R | capi.FIELD_IAM)
-    err = dict(_errors(a, b, cases, case.cfg["dens"], case.notes["dem_radius"]), steps=err_steps,
-               against="the FP64 GPU path from the same input (pinned to the CPU oracle on the small cases)")
+    # a fresh mixed handle from the same input, compared at checkpoints every
+    # 20 steps up to err_steps (the maxima over particles at each)
+    cmp = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    at = fp64_steps + 2
+    cmp.step(at)
+    mask = capi.FIELD_DENS | capi.FIELD_F | capi.FIELD_R | capi.FIELD_IAM
+    checkpoints = []
+    while True:
+        e = _errors(cmp.get(mask), ref.get(mask), cases, case.cfg["dens"], case.notes["dem_radius"])
+        checkpoints.append(dict(e, steps=at))
+        if at >= err_steps:
+            break
+        k = min(20, err_steps - at)
+        cmp.step(k)
+        ref.step(k)
+        at += k
+    err = dict(checkpoints[-1],
+               against="the FP64 GPU path from the same input (pinned to the CPU oracle on the small cases)",
+               checkpoints=checkpoints,
+               note="the suspension amplifies any difference at an e-folding time of ~30 steps; the FP64 path "
+                    "run from inputs one bit apart separates as far within ~700 steps (tests/test_gpu_precision.py)")
+    cmp.close()
     ref.close()
 
     # ---- the other configurations at full size ---------------------------
@@ -582,6 +599,7 @@ def run_ours(args, rank, world):
             "dem_settling3d": dict(measure_config(lib, capi, cases, dem, 200, 200, 2000, dem.cfg["dem_radius"]),
                                    workload="DEM settling, 50,000 spheres radius 1 mm x U[0.9, 1.1], walled "
                                             "0.1 x 0.1 x 0.3 m box, k 1e4, e 0.5, dt 1e-5"),
+            "ensemble_dambreak256": measure_ensemble(lib, capi, cases, args.instances, args.steps, args.warmup),
         }
 
     # ---- adjoint / forward ------------------------------------------------
@@ -644,6 +662,53 @@ def run_ours(args, rank, world):
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def measure_ensemble(lib, capi, cases, instances, steps, warmup, err_steps=1000, err_every=16):
+    """The batched dam-break ensemble: `instances` independent 2D dam breaks
+    of uneven size stepped by one CUDA graph per step (sphdem_batch_*),
+    against the same instances each graph-replayed alone; and the mixed
+    path's error against the FP64 path after err_steps steps on every
+    err_every-th instance (both precisions batched)."""
+    ens = cases.dambreak_ensemble(instances, seed=5)
+    n_total = sum(c.n for c in ens)
+    t0 = time.time()
+    sims = [capi.Simulation(lib, c.cfg, c.particles, precision=cases.PREC_MIXED) for c in ens]
+    batch = capi.Batch(lib, sims)
+    chosen = batch.tune(steps_per_trial=2)
+    setup_s = time.time() - t0
+    batch.step(warmup)
+    ms_batch = batch.time_steps(steps)
+    ms_seq = sum(sim.time_steps(steps) for sim in sims)
+    batch.close()
+    for sim in sims:
+        sim.close()
+    pick = list(range(0, instances, err_every))
+    runs = {}
+    for prec in (cases.PREC_MIXED, cases.PREC_FP64):
+        ss = [capi.Simulation(lib, ens[k].cfg, ens[k].particles, precision=prec) for k in pick]
+        b = capi.Batch(lib, ss)
+        b.step(err_steps)
+        runs[prec] = [x.get(capi.FIELD_DENS | capi.FIELD_F | capi.FIELD_IAM) for x in ss]
+        b.close()
+        for x in ss:
+            x.close()
+    errs = [_errors(a, f, cases, ens[k].cfg["dens"], 1.0)
+            for k, a, f in zip(pick, runs[cases.PREC_MIXED], runs[cases.PREC_FP64])]
+    return {
+        "workload": f"{instances} independent 2D dam breaks, fluid count log-uniform in [2k, 40k], "
+                    f"column height U[1.0, 2.5], seed 5",
+        "n_particles_total": n_total, "n_instances": instances,
+        "min_particles": min(c.n for c in ens), "max_particles": max(c.n for c in ens),
+        "batched": {"value": n_total * steps / (ms_batch * 1e-3), "unit": UNIT, "ms_per_step": ms_batch / steps},
+        "sequential": {"value": n_total * steps / (ms_seq * 1e-3), "unit": UNIT, "ms_per_step": ms_seq / steps},
+        "batched_over_sequential": ms_seq / ms_batch,
+        "autotuner": {"blk_pair_64": sum(1 for x in chosen if x[0] == 64),
+                      "grid_div_4": sum(1 for x in chosen if x[1] == 4), "setup_s": setup_s},
+        "error_vs_fp64": {"steps": err_steps, "instances": len(pick),
+                          "max_abs_drho_over_rho0": max(e["max_abs_drho_over_rho0"] for e in errs),
+                          "max_abs_df_over_max_f": max(e["max_abs_df_over_max_f"] for e in errs)},
+    }
 
 
 def run_ensemble(args):

@@ -221,7 +221,6 @@ std::string validate(const SphDemConfig *cfg, const SphDemParticles *p, int64_t 
     for (int d = 0; d < cfg->ndim; d++)
         if (!(cfg->domain_max[d] > cfg->domain_min[d])) return "empty binning domain";
     if (cfg->flags & SPHDEM_F_CORRECTED_GRADIENT) {
-        if (cfg->precision != SPHDEM_PREC_FP64) return "CORRECTED_GRADIENT is carried by the FP64 path only";
         if (cfg->flags & SPHDEM_F_LIQ_DEM) return "CORRECTED_GRADIENT is not combined with LIQ_DEM";
     }
     if (cfg->reinit_dens_every < 0) return "reinit_dens_every must be >= 0";
@@ -302,6 +301,8 @@ void run_phase_mixed(sphdem_ctx *c, int phase) {
             rebuild(c);
             mixed::pack(c);
             if (lists) mixed::nlist(c);
+            /* calcInvM in FP64 once per rebuild; the pair passes apply it in FP32 */
+            if (corrected_gradient(c)) run_invm(c);
             if (liq) {
                 mixed::zero_shep(c);
                 mixed::porosity(c);
@@ -320,6 +321,7 @@ void run_phase_mixed(sphdem_ctx *c, int phase) {
             run_end_drift(c);
             rebuild(c);
             mixed::pack(c, false);
+            if (corrected_gradient(c)) run_invm(c);
             if (lists) {
                 mixed::nlist(c);
                 mixed::dddt(c);  /* Omega (VAR_H_CORRECTION) is summed inside the continuity pass */

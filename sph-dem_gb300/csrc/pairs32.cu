@@ -1020,14 +1020,61 @@ __device__ __noinline__ void boundary32(const DevCfg *__restrict__ cp, const flo
     for (int k = 0; k < 3; k++) fbx[k] = sc * np[k];
 }
 
+/* Physics classes the force pass is specialised on (so that the unused
+ * viscosity forms, accumulators and branches compile away): the coupled
+ * sedimentation form (Morris viscosity, VAR_H_CORRECTION, no anticlumping),
+ * the dam-break form (artificial viscosity, constant h, no anticlumping),
+ * and every other combination read from the configuration. */
+enum : int { PHYS_GENERIC = 0, PHYS_MORRIS_VARH = 1, PHYS_ARTIFICIAL = 2, PHYS_CG = 3 };
+
+/* CORRECTED_GRADIENT in FP32 (sph.h:325-326): the corrected gradient of a
+ * pair is invM_a ((dr F - sumGrad_a/sum_a) / sum_a); invM_a, sumGrad_a and
+ * sum_a come from calcInvM (FP64, k_invm) once per rebuild and enter each
+ * owner's pair loop as M = invM_a / sum_a and cs = sumGrad_a / sum_a. */
 template <int ND>
+struct Cg32 {
+    float m[ND * ND], cs[ND];
+    __device__ __forceinline__ void load(const double *cg, int64_t cap, int64_t a) {
+        const double sum = cg[CG_S * cap + a];
+#pragma unroll
+        for (int k = 0; k < ND * ND; k++) m[k] = (float)(cg[(CG_M + k) * cap + a] / sum);
+#pragma unroll
+        for (int d = 0; d < ND; d++) cs[d] = (float)cg[(CG_C + d) * cap + a];
+    }
+    /* out = M (d F - cs) */
+    __device__ __forceinline__ void apply(const float *d, float F, float *out) const {
+        float t[ND];
+#pragma unroll
+        for (int k = 0; k < ND; k++) t[k] = d[k] * F - cs[k];
+#pragma unroll
+        for (int i = 0; i < ND; i++) {
+            float v = 0.f;
+#pragma unroll
+            for (int j = 0; j < ND; j++) v = fmaf(m[i * ND + j], t[j], v);
+            out[i] = v;
+        }
+    }
+};
+
+inline int phys_class(const DevCfg &c) {
+    const bool anti = !(c.flags & SPHDEM_F_NO_ANTICLUMPING);
+    if (!anti && c.visc == SPHDEM_VISC_MORRIS && c.var_h()) return PHYS_MORRIS_VARH;
+    if (!anti && c.visc == SPHDEM_VISC_ARTIFICIAL && !c.var_h()) return PHYS_ARTIFICIAL;
+    return PHYS_GENERIC;
+}
+
+template <int ND, int PHYS>
 __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restrict__ cp, DevState s, DevGlobals *__restrict__ g,
                                                const float4 *__restrict__ P0, const float4 *__restrict__ P1,
                                                const float4 *__restrict__ P2, float *__restrict__ om32,
                                                const int *__restrict__ tg, const int *__restrict__ nbr,
                                                const int *__restrict__ ncnt, int64_t ld, int64_t n,
-                                               const float4 *__restrict__ NB) {
+                                               const float4 *__restrict__ NB, const double *__restrict__ cgrows) {
+    constexpr bool CG = PHYS == PHYS_CG;
     const float4 *shift = stencil_shifts(c, g);
+    const int visc = PHYS == PHYS_MORRIS_VARH ? SPHDEM_VISC_MORRIS
+                     : (PHYS == PHYS_ARTIFICIAL ? SPHDEM_VISC_ARTIFICIAL : c.visc);
+    const bool var_h = PHYS == PHYS_MORRIS_VARH ? true : (PHYS == PHYS_ARTIFICIAL ? false : c.var_h());
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     float ndt = FLT_MAX;
     const int ta = a < n ? (tg[a] & 0xff) : -1;
@@ -1045,12 +1092,14 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
         Kahan om;
         om.init(-ma * pd_coef * wK32(0.f, wcon));
         const bool sph = ta == T_SPH;
-        const bool anti = !(c.flags & SPHDEM_F_NO_ANTICLUMPING);
+        const bool anti = PHYS == PHYS_GENERIC && !(c.flags & SPHDEM_F_NO_ANTICLUMPING);
         const float visc_nu = (float)c.viscosity, c0 = (float)c.spsound;
         const float liq_visc = (float)(2.0 * c.viscosity * c.dens);
         const float alpha_mon = (float)c.alpha_mon, alpha_art = (float)c.alpha_art;
-        const float vdc = c.visc == SPHDEM_VISC_MONAGHAN ? 0.06f : 0.125f;
+        const float vdc = visc == SPHDEM_VISC_MONAGHAN ? 0.06f : 0.125f;
         const float k_anti_inv = c.k_anti != 0 ? (float)(1.0 / c.k_anti) : 0.f;
+        Cg32<ND> cgw;
+        if constexpr (CG) cgw.load(cgrows, s.cap, a);
         Kahan fp[ND], fv[ND], fb[ND], fa[ND];
         Kahan fq;  /* anticlumping: the same term on every component, not scaled by 1/Omega */
         fq.init(0.f);
@@ -1091,7 +1140,7 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
             const float Fa = qa != 0.f ? ihn2a * wdK32(qa, wcon) * (ha * rinv) : 0.f;
             const float Fb = qb != 0.f ? ihn2b * wdK32(qb, wcon) * (hb * rinv) : 0.f;
             float cA, cB, cM;  /* gA = d*cA, gB = d*cB, 0.5(gA+gB) = d*cM (times Omega_a with VAR_H) */
-            if (c.var_h()) {
+            if (var_h) {
                 cA = Fa;
                 cB = Fb;
                 cM = 0.5f * (cA + cB);
@@ -1099,33 +1148,49 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
             } else {
                 cA = cB = cM = 0.5f * (Fa + Fb);
             }
+            /* corrected gradients: vectors gA, gB and their mean (times Omega_a with VAR_H) */
+            float gAv[3] = {0.f, 0.f, 0.f}, gBv[3] = {0.f, 0.f, 0.f}, gMv[3] = {0.f, 0.f, 0.f};
+            if constexpr (CG) {
+                float wa[ND], wb[ND];
+                cgw.apply(d, Fa, wa);
+                cgw.apply(d, Fb, wb);
+#pragma unroll
+                for (int k = 0; k < ND; k++) {
+                    gAv[k] = var_h ? wa[k] : 0.5f * (wa[k] + wb[k]);
+                    gBv[k] = var_h ? wb[k] : 0.5f * (wa[k] + wb[k]);
+                    gMv[k] = 0.5f * (gAv[k] + gBv[k]);
+                }
+            }
             const float densb = xb.x, mb = fabsf(vb.w);
             const float hav = 0.5f * (ha + hb);
             const float dv0 = va.x - vb.x, dv1 = va.y - vb.y, dv2 = va.z - vb.z;
             if (sph && tb != T_DEM && tb != T_DEMB) {
                 const float vdr = d[0] * dv0 + d[1] * dv1 + d[2] * dv2;
                 float vsig = 0.f;
-                if (c.visc == SPHDEM_VISC_MORRIS) {
+                if (visc == SPHDEM_VISC_MORRIS) {
                     const float visc = c.liq_dem() ? liq_visc / (densa * densb)
                                                    : visc_nu * (densa + densb) / (densa * densb);
                     vsig = 2.f * c0;
-                    const float sc = mb * visc * (r2 * cM) / (r2 + 0.01f * hav * hav);
+                    const float dg = CG ? d[0] * gMv[0] + d[1] * gMv[1] + d[2] * gMv[2] : r2 * cM;
+                    const float sc = mb * visc * dg / (r2 + 0.01f * hav * hav);
                     const float dvv[3] = {dv0, dv1, dv2};
 #pragma unroll
                     for (int k = 0; k < ND; k++) fv[k].add(dvv[k] * sc);
-                } else if (c.visc == SPHDEM_VISC_MONAGHAN) {
+                } else if (visc == SPHDEM_VISC_MONAGHAN) {
                     const float viss = vdr * rinv;
                     if (!c.liq_dem()) vsig = 2.f * c0 + 2.f * fabsf(viss);
-                    const float sc = mb * (viss * vsig * alpha_mon / (densa + densb)) * cM;
+                    const float sv = mb * (viss * vsig * alpha_mon / (densa + densb));
+                    const float sc = sv * cM;
 #pragma unroll
-                    for (int k = 0; k < ND; k++) fv[k].add(sc * d[k]);
-                } else if (c.visc == SPHDEM_VISC_ARTIFICIAL) {
+                    for (int k = 0; k < ND; k++) fv[k].add(CG ? sv * gMv[k] : sc * d[k]);
+                } else if (visc == SPHDEM_VISC_ARTIFICIAL) {
                     if (vdr < 0.f) {
                         const float viss = vdr * rinv;
                         const float avsig = 2.f * c0 - 4.f * viss;
-                        const float sc = mb * (viss * avsig * alpha_art / (densa + densb)) * cM;
+                        const float sv = mb * (viss * avsig * alpha_art / (densa + densb));
+                        const float sc = sv * cM;
 #pragma unroll
-                        for (int k = 0; k < ND; k++) fa[k].add(sc * d[k]);
+                        for (int k = 0; k < ND; k++) fa[k].add(CG ? sv * gMv[k] : sc * d[k]);
                         vsig = fmaxf(vsig, avsig);
                     }
                 }
@@ -1146,12 +1211,13 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
                 }
                 const float pc = pdr2a * cA + pdr2b * cB;
 #pragma unroll
-                for (int k = 0; k < ND; k++) fp[k].add(-mb * (pc * d[k]));
+                for (int k = 0; k < ND; k++)
+                    fp[k].add(CG ? -mb * (pdr2a * gAv[k] + pdr2b * gBv[k]) : -mb * (pc * d[k]));
                 if (anti) fq.add(-mb * antic);
             }
         }
         float roma = 1.f;
-        if (c.var_h()) {
+        if (var_h) {
             /* Omega = 1 + h*sum/(rho*NDIM): an O(1) number, FP32 is ample */
             const float omega = 1.f + ha * om.s / (densa * ND);
             s.row(FD_OMEGA)[a] = omega;
@@ -1177,12 +1243,13 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
     block_min_atomic(ndt, &g->new_dt_bits);
 }
 
-template <int ND>
+template <int ND, bool CG>
 __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlobals *__restrict__ g,
                                               const float4 *__restrict__ P0, const float4 *__restrict__ P1,
                                               const float4 *__restrict__ P2, float *__restrict__ om32,
                                               const int *__restrict__ tg, const int *__restrict__ nbr,
-                                              const int *__restrict__ ncnt, int64_t ld, int64_t n) {
+                                              const int *__restrict__ ncnt, int64_t ld, int64_t n,
+                                              const double *__restrict__ cgrows) {
     const float4 *shift = stencil_shifts(c, g);
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (a >= n) return;
@@ -1198,6 +1265,8 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
     om.init(-va.w * pd_coef * wK32(0.f, wcon));
     Kahan acc;
     acc.init(0.f);
+    Cg32<ND> cgw;
+    if constexpr (CG) cgw.load(cgrows, s.cap, a);
     const int cnt = ncnt[a];
     /* 8 entries at a time from the particle's list tiles (two int4 loads) */
     const int4 *tile = reinterpret_cast<const int4 *>(nbr + nl_at(a, 0, ld));
@@ -1224,17 +1293,30 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
         const float r = r2 * rinv;
         const float qa = r * iha;
         const float Fa = qa != 0.f ? ihn2a * wdK32(qa, wcon) * (ha * rinv) : 0.f;
-        float F;
+        float F, Fb = 0.f;
         if (c.var_h()) {
             F = Fa;
             if (is_sph_or_sphb(tb)) om.add(mb * (ihna * (-qa * wdK32(qa, wcon) * iha) - pd_coef * wK32(qa, wcon)));
         } else {
             const float ihb = P2[b].w;
             const float qb = r * ihb;
-            const float Fb = qb != 0.f ? powi<ND>(ihb) * ihb * ihb * wdK32(qb, wcon) * (pb.w * rinv) : 0.f;
+            Fb = qb != 0.f ? powi<ND>(ihb) * ihb * ihb * wdK32(qb, wcon) * (pb.w * rinv) : 0.f;
             F = 0.5f * (Fa + Fb);
         }
-        const float vdr = (va.x - vb.x) * d[0] + (va.y - vb.y) * d[1] + (va.z - vb.z) * d[2];
+        const float dv[3] = {va.x - vb.x, va.y - vb.y, va.z - vb.z};
+        float vdr;
+        if constexpr (CG) {
+            /* corrected gradient of a (and of b's kernel) applied with a's invM */
+            float wa[ND], wb[ND];
+            cgw.apply(d, Fa, wa);
+            if (!c.var_h()) cgw.apply(d, Fb, wb);
+            vdr = 0.f;
+#pragma unroll
+            for (int k = 0; k < ND; k++) vdr += dv[k] * (c.var_h() ? wa[k] : 0.5f * (wa[k] + wb[k]));
+            F = 1.f;
+        } else {
+            vdr = dv[0] * d[0] + dv[1] * d[1] + dv[2] * d[2];
+        }
         if (!(is_boundary(tb) || tb == T_DEM)) acc.add(mb * vdr * F);
     }
     float roma = 1.f;
@@ -2198,21 +2280,51 @@ void omega_eos(sphdem_ctx *c, bool omega, bool eos) {
 }
 
 void force(sphdem_ctx *c) {
+    const int phys = phys_class(c->cfg);
+    const double *cgrows = corrected_gradient(c) ? c->cg : nullptr;
+#define LP_(ND, P)                                                                                              \
+    SPHDEM_LAUNCH(c, "force32", (k_force<ND, P>), grid_for(c->n, c->blk_pair), c->blk_pair, 0, c->cfg, c->dcfg,  \
+                  c->A, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt,          \
+                  (int64_t)c->mx_maxn, c->n, c->mx_nb, cgrows)
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "force32", k_force<ND>, grid_for(c->n, c->blk_pair), c->blk_pair, 0, c->cfg, c->dcfg, c->A,   \
-                  c->g, c->mx_pos, \
-                  c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn, c->n, c->mx_nb)
+    do {                                                                                                        \
+        if (cgrows) {                                                                                           \
+            LP_(ND, PHYS_CG);                                                                                   \
+            break;                                                                                              \
+        }                                                                                                       \
+        if constexpr (ND > 1) {                                                                                 \
+            if (phys == PHYS_MORRIS_VARH) {                                                                     \
+                LP_(ND, PHYS_MORRIS_VARH);                                                                      \
+                break;                                                                                          \
+            }                                                                                                   \
+            if (phys == PHYS_ARTIFICIAL) {                                                                      \
+                LP_(ND, PHYS_ARTIFICIAL);                                                                       \
+                break;                                                                                          \
+            }                                                                                                   \
+        }                                                                                                       \
+        LP_(ND, PHYS_GENERIC);                                                                                  \
+    } while (0)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
+#undef LP_
 }
 
 void dddt(sphdem_ctx *c) {
-#define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "dddt32", k_dddt<ND>, grid_for(c->n, c->blk_pair), c->blk_pair, 0, c->cfg, c->A, c->g,      \
-                  c->mx_pos, c->mx_vel, \
-                  c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn, c->n)
+    const double *cgrows = corrected_gradient(c) ? c->cg : nullptr;
+#define LD_(ND, CGF)                                                                                            \
+    SPHDEM_LAUNCH(c, "dddt32", (k_dddt<ND, CGF>), grid_for(c->n, c->blk_pair), c->blk_pair, 0, c->cfg, c->A,     \
+                  c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt,                \
+                  (int64_t)c->mx_maxn, c->n, cgrows)
+#define L_(ND)                \
+    do {                      \
+        if (cgrows)           \
+            LD_(ND, true);    \
+        else                  \
+            LD_(ND, false);   \
+    } while (0)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
+#undef LD_
 }
 
 void porosity(sphdem_ctx *c) {

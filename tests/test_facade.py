@@ -307,8 +307,11 @@ def test_case_runs_from_a_restart_piece(tmp_path):
                              capture_output=True, text=True, timeout=300)
         assert res.returncode == 0, res.stderr[-2000:]
         outs.append(read_final(str(final)))
+    # the FP64 Shepard scatter sums with atomics, so two runs of the coupled
+    # step agree to rounding, not bit for bit
     for o in outs[1:]:
         for k in ("r", "vhat", "dens"):
-            np.testing.assert_array_equal(o[k], outs[0][k])
+            scale = np.abs(outs[0][k]).max()
+            assert np.abs(o[k] - outs[0][k]).max() <= 1e-12 * scale, k
     d = io_vtk.read_vtu(str(tmp_path / "outRestart0000004_0.vtu"))
-    np.testing.assert_array_equal(d["points"], outs[0]["r"])
+    np.testing.assert_array_equal(d["points"], outs[-1]["r"])

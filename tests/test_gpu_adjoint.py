@@ -304,3 +304,109 @@ def test_adjoint_rejects_unsupported_fluid(lib):
     with pytest.raises(capi.SphDemError, match="UNSUPPORTED"):
         sim.adjoint_forward(4, 2)
     sim.close()
+
+
+# ---------------------------------------------------------------------------
+# The differentiated coupled workload at its own size: 100k fluid + 5k DEM
+# (sediment3d_adjoint: periodic x/y, three fixed floor layers, constant h),
+# loss = mean final DEM height + (fluid kinetic energy)^2, gradients w.r.t.
+# the viscosity, the drag scale, the restitution (through the dashpot
+# coefficient gamma(e)) and all initial DEM positions along 32 seeded random
+# directions, against FP64 central differences.  The run is CFG4_STEPS steps
+# with a checkpoint every CFG4_K: the flow separates two runs whose inputs
+# differ in one bit by a decade every ~60 steps (tests/test_gpu_precision.py),
+# so differences over the full 500 steps leave the linear regime.
+
+CFG4_STEPS, CFG4_K = 20, 10
+
+
+def cfg4_case():
+    case = cases.workload("sediment3d_adjoint")
+    iam = np.asarray(case.particles["iam"])
+    rng = np.random.default_rng(10)
+    # spheres in touching pairs (2 % overlap), so that the contacts act from
+    # the first step, as in moving_coupled()
+    idx = np.flatnonzero(iam == cases.DEM)
+    R = case.cfg["dem_radius"]
+    r = np.asarray(case.particles["r"], dtype=np.float64).copy()
+    for a, b in zip(idx[0::2], idx[1::2]):
+        u = rng.normal(size=3)
+        u /= np.linalg.norm(u)
+        r[b] = r[a] + 1.98 * R * u
+    case.particles["r"] = r
+    v = np.zeros((case.n, 3))
+    fl, dem = iam == cases.SPH, iam == cases.DEM
+    v[fl] = rng.normal(0.0, 0.02, size=(fl.sum(), 3))
+    v[dem] = rng.normal(0.0, 0.05, size=(dem.sum(), 3))
+    case.particles["v"] = v
+    case.particles["vhat"] = v.copy()
+    return case
+
+
+def cfg4_loss(lib, case, cfg=None, r=None):
+    parts = copy.deepcopy(case.particles)
+    if r is not None:
+        parts["r"] = r
+    sim = capi.Simulation(lib, cfg or case.cfg, parts, precision=cases.PREC_FP64)
+    sim.step(CFG4_STEPS)
+    L = cpl_loss_and_seed(sim)[0]
+    sim.close()
+    return L
+
+
+def test_config4_coupled_adjoint_vs_central_differences(lib):
+    case = cfg4_case()
+    assert case.notes["n_dem"] == 5000 and case.notes["n_fluid"] > 98000
+    grads = {}
+    for prec in (cases.PREC_FP64, cases.PREC_MIXED):
+        sim = capi.Simulation(lib, case.cfg, case.particles, precision=prec)
+        sim.adjoint_forward(CFG4_STEPS, CFG4_K)
+        L0, dr, dv = cpl_loss_and_seed(sim)
+        g, dr0, _, _ = sim.adjoint_backward(dL_dr=dr, dL_dv=dv)
+        sim.close()
+        grads[prec] = (g, dr0)
+
+    # restitution e -> gamma(e) with the reduced mass the case used
+    e0 = 0.5
+    k = case.cfg["dem_k"]
+    m_red = 0.5 * case.cfg["dem_vol"] * case.cfg["dem_dens"]
+    de = 1e-6 * e0
+    dgam_de = (cases.dem_gamma_from_restitution(k, m_red, e0 + de)
+               - cases.dem_gamma_from_restitution(k, m_red, e0 - de)) / (2 * de)
+    fds = {}
+    for name, rel in (("viscosity", 1e-4), ("drag_scale", 1e-4)):
+        base = case.cfg.get(name, 1.0)
+        eps = rel * base
+        cp, cm = dict(case.cfg), dict(case.cfg)
+        cp[name], cm[name] = base + eps, base - eps
+        fds[name] = (cfg4_loss(lib, case, cfg=cp) - cfg4_loss(lib, case, cfg=cm)) / (2 * eps)
+    cp, cm = dict(case.cfg), dict(case.cfg)
+    cp["dem_gamma"] = cases.dem_gamma_from_restitution(k, m_red, e0 + de)
+    cm["dem_gamma"] = cases.dem_gamma_from_restitution(k, m_red, e0 - de)
+    fds["restitution"] = (cfg4_loss(lib, case, cfg=cp) - cfg4_loss(lib, case, cfg=cm)) / (2 * de)
+
+    rng = np.random.default_rng(4)
+    r0 = np.asarray(case.particles["r"], dtype=np.float64).copy()
+    dem = np.asarray(case.particles["iam"]) == cases.DEM
+    scale = np.abs(r0).max()
+    dirs, fd_dirs = [], []
+    for _ in range(32):
+        u = np.zeros_like(r0)
+        u[dem] = rng.normal(size=(dem.sum(), 3))
+        u /= np.linalg.norm(u)
+        eps = 1e-6 * scale
+        dirs.append(u)
+        fd_dirs.append((cfg4_loss(lib, case, r=r0 + eps * u) - cfg4_loss(lib, case, r=r0 - eps * u)) / (2 * eps))
+
+    for prec, (g, dr0) in grads.items():
+        label = "fp64" if prec == cases.PREC_FP64 else "mixed"
+        ad = {"viscosity": g.viscosity, "drag_scale": g.drag_scale, "restitution": g.dem_gamma * dgam_de}
+        for name, fd in fds.items():
+            print(label, name, "adjoint", ad[name], "fd", fd)
+            assert abs(ad[name] - fd) <= RTOL * abs(fd), f"{label} {name}: adjoint {ad[name]} fd {fd}"
+        worst = 0.0
+        for u, fd in zip(dirs, fd_dirs):
+            a = float((dr0 * u).sum())
+            worst = max(worst, abs(a - fd) / abs(fd))
+        print(label, "32 DEM position directions: worst relative difference", worst)
+        assert worst <= RTOL

@@ -104,7 +104,7 @@ def test_fp64_full_run_fields_pairs_cells(lib, name):
 # mixed precision: FP32 pair math on cell-relative offsets, FP64 integration
 MIXED_WORKLOADS = ["dambreak2d_small", "dambreak2d_monaghan_small", "dem_small", "sediment3d_small",
                    "sediment3d_reinit_small", "sediment3d_block_small", "dambreak2d_flow_small",
-                   "sediment3d_flow_small"]
+                   "sediment3d_flow_small", "dambreak2d_own_small", "dambreak2d_cg_varh_small"]
 # stated tolerances over the workloads' full step counts: density to 1e-5 of
 # its value, positions to 1e-6 of the largest coordinate, accelerations to
 # 1e-3 of the largest acceleration magnitude
@@ -173,9 +173,16 @@ def test_reinit_graph_and_phase_paths_agree(lib):
 
 
 def test_corrected_gradient_and_reinit_restrictions(lib):
+    """CORRECTED_GRADIENT runs on both paths but not with LIQ_DEM (the
+    reference's calcFPI would take a DEM particle's invM, which calcInvM never
+    sets); a batch takes no handle that re-initialises the density."""
     case = cases.workload("dambreak2d_own_small")
-    with pytest.raises(capi.SphDemError):
-        capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    cpl = cases.workload("sediment3d_small")
+    cfg = dict(cpl.cfg)
+    cfg["flags"] |= cases.F_CORRECTED_GRADIENT
+    for prec in (cases.PREC_MIXED, cases.PREC_FP64):
+        with pytest.raises(capi.SphDemError):
+            capi.Simulation(lib, cfg, cpl.particles, precision=prec)
     cfg = dict(case.cfg)
     cfg["flags"] &= ~cases.F_CORRECTED_GRADIENT
     sim = capi.Simulation(lib, cfg, case.particles, precision=cases.PREC_FP64)
