@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -335,7 +336,10 @@ void run_phase_mixed(sphdem_ctx *c, int phase) {
 
 void run_phase(sphdem_ctx *c, int phase) {
     const bool liq = c->cfg.liq_dem();
-    if (c->cfg.precision == SPHDEM_PREC_MIXED && (phase == SPHDEM_PHASE_MIDDLE || phase == SPHDEM_PHASE_END)) {
+    /* a DEM-only handle has no FP32 pair pass: its contacts are FP64 on both
+     * paths, so the mixed handle runs the FP64 phases */
+    if (c->cfg.precision == SPHDEM_PREC_MIXED && !c->mx_dem_only &&
+        (phase == SPHDEM_PHASE_MIDDLE || phase == SPHDEM_PHASE_END)) {
         run_phase_mixed(c, phase);
         return;
     }
@@ -553,6 +557,13 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
             SPHDEM_CUDA_CHECK(cudaMemset(c->mx_om, 0, capacity * sizeof(float)));
             SPHDEM_CUDA_CHECK(cudaMemset(c->mx_ncnt, 0, capacity * sizeof(int)));
             SPHDEM_CUDA_CHECK(cudaDeviceSynchronize());
+            mixed::prepare(c);
+            /* SPHDEM_FORCE_TILE=0: the force pass reads every neighbour record
+             * from global memory (the form the staged one is checked against) */
+            const char *ft = std::getenv("SPHDEM_FORCE_TILE");
+            c->force_tile = !(ft && ft[0] == '0');
+            c->mx_dem_only = true;
+            for (int64_t i = 0; i < init->n; i++) c->mx_dem_only = c->mx_dem_only && init->iam[i] == T_DEM;
             mixed::pack(c);
             const int m = mixed::nlist_max_count(c);
             if (m > 0) {

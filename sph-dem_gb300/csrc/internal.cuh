@@ -79,6 +79,7 @@ struct sphdem_ctx {
     int *mx_nbr = nullptr;      /* lists in tiles of 32 particles x 8 slots, mx_maxn x cap (rounded to 32) */
     int *mx_ncnt = nullptr;
     int mx_maxn = 0;
+    bool mx_dem_only = false;   /* every particle at creation is DEM: the FP64 phases run */
     float4 *mx_q0 = nullptr, *mx_q1 = nullptr, *mx_q2 = nullptr;  /* FPI fields of fluid particles */
     float4 *mx_dp = nullptr;    /* (m/shep, fdrag) of DEM particles */
     float4 *mx_poslo = nullptr; /* low FP32 halves of offsets and h (double-float) */
@@ -91,6 +92,7 @@ struct sphdem_ctx {
     sphdem::AdjointData *adj = nullptr; /* checkpoints and buffers of the adjoint */
     /* launch knobs chosen by the batch autotuner */
     int blk_pair = 128;         /* block size of the list-consumer passes (<= 128) */
+    bool force_tile = true;     /* force pass: neighbour records staged in shared memory */
     int grid_div = 1;           /* divides the resident-block grid of the slice passes */
     int2 *mx_bandq = nullptr;   /* per particle: list entries within the FP32 band */
     int *mx_bandn = nullptr;    /* per particle: how many are recorded */
@@ -163,6 +165,8 @@ namespace mixed {
 void pack(sphdem_ctx *c, bool coupling = true);
 void pack_fpi(sphdem_ctx *c);
 void nlist(sphdem_ctx *c);
+/* once per process, outside stream capture: kernel attributes of the step */
+void prepare(sphdem_ctx *c);
 void zero_shep(sphdem_ctx *c);
 int nlist_max_count(sphdem_ctx *c);
 int band_records_per_particle();

@@ -36,6 +36,7 @@
  */
 #include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <vector>
 
 #include "internal.cuh"
@@ -1020,6 +1021,172 @@ __device__ __noinline__ void boundary32(const DevCfg *__restrict__ cp, const flo
     for (int k = 0; k < 3; k++) fbx[k] = sc * np[k];
 }
 
+/* ---------------------------------------------------------------------- */
+/* Neighbour-record staging for the list consumers (TMA bulk copies).
+ *
+ * A block takes consecutive particles of the bucket order, so most of them
+ * lie in one column of buckets along the last axis, and their neighbours in
+ * the 3^(d-1) columns around it, over the block's bucket range on the last
+ * axis +- one bucket.  Each of those column ranges is a contiguous run of
+ * particle slots, so its packed records (P0, P1, P2) are copied global ->
+ * shared with one cp.async.bulk per array, completing on one mbarrier.  A
+ * list entry's stencil code names its neighbour column, so its record is
+ * found in shared memory when its slot lies in that column's staged range,
+ * else (another column of the block, a periodic image on the last axis, a
+ * range cut at the capacity) read from global memory. */
+constexpr int ST_CAP = 1536;    /* staged records per block (2 or 3 x 16 B each) */
+constexpr int ST_MAXSLOT = 9;   /* neighbour columns: 3^(d-1) */
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes, unsigned long long *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned parity) {
+    unsigned ok = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+/* bounded wait for phase 0 of the staging barrier: false after the limit */
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar) {
+    for (int it = 0; it < (1 << 22); it++)
+        if (mbar_try_wait(bar, 0)) return true;
+    return false;
+}
+
+struct Staged {
+    const float4 *S0, *S1, *S2;
+    const int *lo, *num, *base;
+    bool ok;
+};
+
+/* the neighbour column of a stencil code (3D: code / 3, 2D: code / 9) */
+template <int ND>
+__device__ __forceinline__ int st_slot(int code) {
+    return ND == 3 ? code / 3 : (ND == 2 ? code / 9 : 0);
+}
+
+/* Called by every thread of the block.  a0: the block's first slot, n_t:
+ * the particles in SPH buckets (sorted by bucket key). */
+template <int ND, int NARR>
+__device__ Staged stage_neighbours(const DevCfg &c, DevGlobals *g, const int *__restrict__ start,
+                                   const int *__restrict__ skey, const float4 *__restrict__ P0,
+                                   const float4 *__restrict__ P1, const float4 *__restrict__ P2, int64_t a0,
+                                   int n_t, float4 *smem) {
+    constexpr int Z = ND - 1;
+    constexpr int NS = ND == 3 ? 9 : (ND == 2 ? 3 : 1);
+    __shared__ int s_lo[ST_MAXSLOT], s_num[ST_MAXSLOT], s_base[ST_MAXSLOT];
+    __shared__ int s_col, s_zmin, s_zmax;
+    __shared__ __align__(8) unsigned long long s_bar;
+    const int dims[3] = {g->sdims[0], g->sdims[1], g->sdims[2]};
+    const int zdim = dims[Z];
+    if (threadIdx.x == 0) {
+        s_col = skey[a0] / zdim;
+        s_zmin = INT_MAX;
+        s_zmax = -1;
+        mbar_init(&s_bar, 1);
+    }
+    __syncthreads();
+    const int64_t a = a0 + threadIdx.x;
+    if (a < n_t) {
+        const int key = skey[a];
+        if (key / zdim == s_col) {
+            atomicMin(&s_zmin, key % zdim);
+            atomicMax(&s_zmax, key % zdim);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < NS) {
+        const int t = threadIdx.x;
+        int o[2] = {0, 0}, cc[2] = {0, 0};
+        if (ND == 3) {
+            o[0] = t / 3 - 1;
+            o[1] = t % 3 - 1;
+            cc[0] = s_col / dims[1];
+            cc[1] = s_col % dims[1];
+        } else if (ND == 2) {
+            o[0] = t - 1;
+            cc[0] = s_col;
+        }
+        bool ok = true;
+        int col = 0;
+#pragma unroll
+        for (int d = 0; d < Z; d++) {
+            int x = cc[d] + o[d];
+            if (x < 0 || x >= dims[d]) {
+                ok = ok && c.periodic[d];
+                x = x < 0 ? x + dims[d] : x - dims[d];
+            }
+            col = col * dims[d] + x;
+        }
+        const int zlo = max(s_zmin - 1, 0), zhi = min(s_zmax + 1, zdim - 1);
+        int lo = 0, num = 0;
+        if (ok && zlo <= zhi) {
+            lo = start[col * zdim + zlo];
+            num = start[col * zdim + zhi + 1] - lo;
+        }
+        s_lo[t] = lo;
+        s_num[t] = num;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int base = 0;
+        for (int t = 0; t < NS; t++) {
+            const int num = min(s_num[t], ST_CAP - base);
+            s_num[t] = num;
+            s_base[t] = base;
+            base += num;
+        }
+        mbar_expect_tx(&s_bar, (unsigned)(NARR * 16 * base));
+        for (int t = 0; t < NS; t++) {
+            const int num = s_num[t];
+            if (num <= 0) continue;
+            const unsigned bytes = (unsigned)(16 * num);
+            bulk_g2s(smem + s_base[t], P0 + s_lo[t], bytes, &s_bar);
+            bulk_g2s(smem + ST_CAP + s_base[t], P1 + s_lo[t], bytes, &s_bar);
+            if (NARR > 2) bulk_g2s(smem + 2 * ST_CAP + s_base[t], P2 + s_lo[t], bytes, &s_bar);
+        }
+    }
+    __syncthreads();
+    Staged st;
+    st.S0 = smem;
+    st.S1 = smem + ST_CAP;
+    st.S2 = smem + 2 * ST_CAP;
+    st.lo = s_lo;
+    st.num = s_num;
+    st.base = s_base;
+    bool ok = mbar_wait_bounded(&s_bar);
+    if (!ok) {
+        /* gave up: record it, and keep the block alive (again bounded) until
+         * the copies into its shared memory have landed */
+        set_err(g, SPHDEM_ERR_TIMEOUT, 1);
+        mbar_wait_bounded(&s_bar);
+    }
+    /* the whole block gives up together */
+    st.ok = !__syncthreads_or(!ok);
+    return st;
+}
+
 /* Physics classes the force pass is specialised on (so that the unused
  * viscosity forms, accumulators and branches compile away): the coupled
  * sedimentation form (Morris viscosity, VAR_H_CORRECTION, no anticlumping),
@@ -1063,15 +1230,25 @@ inline int phys_class(const DevCfg &c) {
     return PHYS_GENERIC;
 }
 
-template <int ND, int PHYS>
+template <int ND, int PHYS, bool TILE>
 __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restrict__ cp, DevState s, DevGlobals *__restrict__ g,
                                                const float4 *__restrict__ P0, const float4 *__restrict__ P1,
                                                const float4 *__restrict__ P2, float *__restrict__ om32,
                                                const int *__restrict__ tg, const int *__restrict__ nbr,
                                                const int *__restrict__ ncnt, int64_t ld, int64_t n,
-                                               const float4 *__restrict__ NB, const double *__restrict__ cgrows) {
+                                               const float4 *__restrict__ NB, const double *__restrict__ cgrows,
+                                               const int *__restrict__ start, const int *__restrict__ skey) {
     constexpr bool CG = PHYS == PHYS_CG;
     const float4 *shift = stencil_shifts(c, g);
+    extern __shared__ float4 st_smem[];
+    Staged st = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, false};
+    if constexpr (TILE) {
+        const int n_t = start[g->n_sph_cells];
+        const int64_t a0 = blockIdx.x * (int64_t)blockDim.x;
+        if (a0 >= n_t) return;  /* no list owner in this block */
+        st = stage_neighbours<ND, 3>(c, g, start, skey, P0, P1, P2, a0, n_t, st_smem);
+        if (!st.ok) return;
+    }
     const int visc = PHYS == PHYS_MORRIS_VARH ? SPHDEM_VISC_MORRIS
                      : (PHYS == PHYS_ARTIFICIAL ? SPHDEM_VISC_ARTIFICIAL : c.visc);
     const bool var_h = PHYS == PHYS_MORRIS_VARH ? true : (PHYS == PHYS_ARTIFICIAL ? false : c.var_h());
@@ -1125,7 +1302,25 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
             q1 = make_int4(q1.y, q1.z, q1.w, -1);
             if (e < 0) continue;
             const int b = e & B_MASK;
-            const float4 pb = P0[b], vb = P1[b], xb = P2[b];
+            float4 pb, vb, xb;
+            if constexpr (TILE) {
+                const int sl = st_slot<ND>(e >> B_BITS);
+                const int off = b - st.lo[sl];
+                if ((unsigned)off < (unsigned)st.num[sl]) {
+                    const int k = st.base[sl] + off;
+                    pb = st.S0[k];
+                    vb = st.S1[k];
+                    xb = st.S2[k];
+                } else {
+                    pb = P0[b];
+                    vb = P1[b];
+                    xb = P2[b];
+                }
+            } else {
+                pb = P0[b];
+                vb = P1[b];
+                xb = P2[b];
+            }
             /* sph / sphBoundary unless the packed mass is negative */
             const int tb = vb.w < 0.f ? (tg[b] & 0xff) : T_SPH;
             float d[3];
@@ -1243,14 +1438,27 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
     block_min_atomic(ndt, &g->new_dt_bits);
 }
 
-template <int ND, bool CG>
+/* VH: VAR_H_CORRECTION known at compile time (1 on, 0 off) or read from
+ * the configuration (-1) */
+template <int ND, bool CG, int VH, bool TILE>
 __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlobals *__restrict__ g,
                                               const float4 *__restrict__ P0, const float4 *__restrict__ P1,
                                               const float4 *__restrict__ P2, float *__restrict__ om32,
                                               const int *__restrict__ tg, const int *__restrict__ nbr,
                                               const int *__restrict__ ncnt, int64_t ld, int64_t n,
-                                              const double *__restrict__ cgrows) {
+                                              const double *__restrict__ cgrows,
+                                              const int *__restrict__ start, const int *__restrict__ skey) {
     const float4 *shift = stencil_shifts(c, g);
+    const bool var_h = VH < 0 ? c.var_h() : VH == 1;
+    extern __shared__ float4 st_smem[];
+    Staged st = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, false};
+    if constexpr (TILE) {
+        const int n_t = start[g->n_sph_cells];
+        const int64_t a0 = blockIdx.x * (int64_t)blockDim.x;
+        if (a0 >= n_t) return;  /* no list owner in this block */
+        st = stage_neighbours<ND, 2>(c, const_cast<DevGlobals *>(g), start, skey, P0, P1, P2, a0, n_t, st_smem);
+        if (!st.ok) return;
+    }
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (a >= n) return;
     if (!is_sph_or_sphb(tg[a] & 0xff)) return;
@@ -1282,7 +1490,21 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
         q1 = make_int4(q1.y, q1.z, q1.w, -1);
         if (e < 0) continue;
         const int b = e & B_MASK;
-        const float4 pb = P0[b], vb = P1[b];
+        float4 pb, vb;
+        if constexpr (TILE) {
+            const int sl = st_slot<ND>(e >> B_BITS);
+            const int off = b - st.lo[sl];
+            if ((unsigned)off < (unsigned)st.num[sl]) {
+                pb = st.S0[st.base[sl] + off];
+                vb = st.S1[st.base[sl] + off];
+            } else {
+                pb = P0[b];
+                vb = P1[b];
+            }
+        } else {
+            pb = P0[b];
+            vb = P1[b];
+        }
         /* sph / sphBoundary unless the packed mass is negative */
         const int tb = vb.w < 0.f ? (tg[b] & 0xff) : T_SPH;
         const float mb = fabsf(vb.w);
@@ -1294,7 +1516,7 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
         const float qa = r * iha;
         const float Fa = qa != 0.f ? ihn2a * wdK32(qa, wcon) * (ha * rinv) : 0.f;
         float F, Fb = 0.f;
-        if (c.var_h()) {
+        if (var_h) {
             F = Fa;
             if (is_sph_or_sphb(tb)) om.add(mb * (ihna * (-qa * wdK32(qa, wcon) * iha) - pd_coef * wK32(qa, wcon)));
         } else {
@@ -1309,10 +1531,10 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
             /* corrected gradient of a (and of b's kernel) applied with a's invM */
             float wa[ND], wb[ND];
             cgw.apply(d, Fa, wa);
-            if (!c.var_h()) cgw.apply(d, Fb, wb);
+            if (!var_h) cgw.apply(d, Fb, wb);
             vdr = 0.f;
 #pragma unroll
-            for (int k = 0; k < ND; k++) vdr += dv[k] * (c.var_h() ? wa[k] : 0.5f * (wa[k] + wb[k]));
+            for (int k = 0; k < ND; k++) vdr += dv[k] * (var_h ? wa[k] : 0.5f * (wa[k] + wb[k]));
             F = 1.f;
         } else {
             vdr = dv[0] * d[0] + dv[1] * d[1] + dv[2] * d[2];
@@ -1320,7 +1542,7 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
         if (!(is_boundary(tb) || tb == T_DEM)) acc.add(mb * vdr * F);
     }
     float roma = 1.f;
-    if (c.var_h()) {
+    if (var_h) {
         const float omega = 1.f + ha * om.s / (P2[a].x * ND);
         s.row(FD_OMEGA)[a] = omega;
         om32[a] = omega;
@@ -2282,10 +2504,23 @@ void omega_eos(sphdem_ctx *c, bool omega, bool eos) {
 void force(sphdem_ctx *c) {
     const int phys = phys_class(c->cfg);
     const double *cgrows = corrected_gradient(c) ? c->cg : nullptr;
+    /* neighbour records staged through shared memory (2D and 3D) */
+    const bool tile = c->cfg.nd > 1 && c->force_tile;
+    const size_t st_bytes = tile ? (size_t)3 * ST_CAP * sizeof(float4) : 0;
 #define LP_(ND, P)                                                                                              \
-    SPHDEM_LAUNCH(c, "force32", (k_force<ND, P>), grid_for(c->n, c->blk_pair), c->blk_pair, 0, c->cfg, c->dcfg,  \
-                  c->A, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt,          \
-                  (int64_t)c->mx_maxn, c->n, c->mx_nb, cgrows)
+    do {                                                                                                        \
+        if (tile) {                                                                                             \
+            SPHDEM_LAUNCH(c, "force32", (k_force<ND, P, true>), grid_for(c->n, c->blk_pair), c->blk_pair,      \
+                          st_bytes, c->cfg, c->dcfg, c->A, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_om,     \
+                          c->mx_tg, c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn, c->n, c->mx_nb, cgrows,        \
+                          c->buf.start, c->buf.skey);                                                          \
+        } else {                                                                                                \
+            SPHDEM_LAUNCH(c, "force32", (k_force<ND, P, false>), grid_for(c->n, c->blk_pair), c->blk_pair, 0,  \
+                          c->cfg, c->dcfg, c->A, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg,     \
+                          c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn, c->n, c->mx_nb, cgrows, c->buf.start,    \
+                          c->buf.skey);                                                                        \
+        }                                                                                                       \
+    } while (0)
 #define L_(ND)                                                                                                  \
     do {                                                                                                        \
         if (cgrows) {                                                                                           \
@@ -2309,18 +2544,60 @@ void force(sphdem_ctx *c) {
 #undef LP_
 }
 
+/* Kernel attributes the step needs, set once per process outside any
+ * stream capture: the dynamic shared memory of the staged force passes. */
+void prepare(sphdem_ctx *) {
+    static bool done = false;
+    if (done) return;
+    const int bytes = (int)(3 * ST_CAP * sizeof(float4));
+#define A_(ND, P) \
+    SPHDEM_CUDA_CHECK(cudaFuncSetAttribute(k_force<ND, P, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes))
+    A_(2, PHYS_GENERIC);
+    A_(2, PHYS_MORRIS_VARH);
+    A_(2, PHYS_ARTIFICIAL);
+    A_(2, PHYS_CG);
+    A_(3, PHYS_GENERIC);
+    A_(3, PHYS_MORRIS_VARH);
+    A_(3, PHYS_ARTIFICIAL);
+    A_(3, PHYS_CG);
+#undef A_
+    const int bytes2 = (int)(2 * ST_CAP * sizeof(float4));
+#define D_(ND, CGF, VH) \
+    SPHDEM_CUDA_CHECK(cudaFuncSetAttribute(k_dddt<ND, CGF, VH, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes2))
+    D_(2, true, -1);
+    D_(2, false, 1);
+    D_(2, false, 0);
+    D_(3, true, -1);
+    D_(3, false, 1);
+    D_(3, false, 0);
+#undef D_
+    done = true;
+}
+
 void dddt(sphdem_ctx *c) {
     const double *cgrows = corrected_gradient(c) ? c->cg : nullptr;
-#define LD_(ND, CGF)                                                                                            \
-    SPHDEM_LAUNCH(c, "dddt32", (k_dddt<ND, CGF>), grid_for(c->n, c->blk_pair), c->blk_pair, 0, c->cfg, c->A,     \
-                  c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg, c->mx_nbr, c->mx_ncnt,                \
-                  (int64_t)c->mx_maxn, c->n, cgrows)
-#define L_(ND)                \
-    do {                      \
-        if (cgrows)           \
-            LD_(ND, true);    \
-        else                  \
-            LD_(ND, false);   \
+    const bool vh = c->cfg.var_h();
+    const bool tile = c->cfg.nd > 1 && c->force_tile;
+    const size_t st_bytes = (size_t)2 * ST_CAP * sizeof(float4);
+#define LD_(ND, CGF, VH)                                                                                        \
+    do {                                                                                                        \
+        if (tile)                                                                                               \
+            SPHDEM_LAUNCH(c, "dddt32", (k_dddt<ND, CGF, VH, true>), grid_for(c->n, c->blk_pair), c->blk_pair,  \
+                          st_bytes, c->cfg, c->A, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg,    \
+                          c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn, c->n, cgrows, c->buf.start, c->buf.skey); \
+        else                                                                                                    \
+            SPHDEM_LAUNCH(c, "dddt32", (k_dddt<ND, CGF, VH, false>), grid_for(c->n, c->blk_pair), c->blk_pair, \
+                          0, c->cfg, c->A, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_om, c->mx_tg,           \
+                          c->mx_nbr, c->mx_ncnt, (int64_t)c->mx_maxn, c->n, cgrows, c->buf.start, c->buf.skey); \
+    } while (0)
+#define L_(ND)                       \
+    do {                             \
+        if (cgrows)                  \
+            LD_(ND, true, -1);       \
+        else if (vh)                 \
+            LD_(ND, false, 1);       \
+        else                         \
+            LD_(ND, false, 0);       \
     } while (0)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_

@@ -109,6 +109,12 @@ MIXED_WORKLOADS = ["dambreak2d_small", "dambreak2d_monaghan_small", "dem_small",
 # its value, positions to 1e-6 of the largest coordinate, accelerations to
 # 1e-3 of the largest acceleration magnitude
 MIXED_TOL = {"dens": 1e-5, "r": 1e-6, "f": 1e-3}
+# damBreak's own constants: the corrected gradient multiplies each pair's
+# gradient by the inverse moment matrix, whose condition number at particles
+# of the free surface (few neighbours) amplifies the FP32 rounding of the pair
+# offsets; with density re-initialisation every step (a summation over those
+# positions) the run keeps the spec bar of 1e-4 on density, not 1e-5
+MIXED_TOL_BY_CASE = {"dambreak2d_own_small": {"dens": 1e-4, "r": 1e-5, "f": 1e-3}}
 
 
 @pytest.mark.parametrize("name", MIXED_WORKLOADS)
@@ -151,7 +157,7 @@ def test_mixed_fields_within_tolerance(lib, name):
         "f": np.abs(a["f"] - b["f"]).max() / max(np.abs(b["f"]).max(), 1e-300),
     }
     print(name, "mixed vs oracle", {k: f"{v:.2e}" for k, v in errs.items()})
-    for k, tol in MIXED_TOL.items():
+    for k, tol in MIXED_TOL_BY_CASE.get(name, MIXED_TOL).items():
         assert errs[k] <= tol, f"{name}: {k} {errs[k]:.3e} > {tol}"
 
 
@@ -188,3 +194,27 @@ def test_corrected_gradient_and_reinit_restrictions(lib):
     sim = capi.Simulation(lib, cfg, case.particles, precision=cases.PREC_FP64)
     with pytest.raises(capi.SphDemError):
         capi.Batch(lib, [sim])
+
+
+@pytest.mark.parametrize("name", ["sediment3d_small", "dambreak2d_small", "dambreak2d_own_small"])
+def test_staged_force_pass_equals_plain_loads(lib, name, monkeypatch):
+    """The force pass with its neighbour records staged in shared memory by
+    bulk copies gives bit for bit the forces of the same pass reading every
+    record from global memory (SPHDEM_FORCE_TILE=0)."""
+    case = cases.workload(name)
+    out = []
+    for tile in ("1", "0"):
+        monkeypatch.setenv("SPHDEM_FORCE_TILE", tile)
+        sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+        for _ in range(4):
+            for p in range(7):
+                sim.phase(p)
+        out.append(sim.get(capi.FIELD_F | capi.FIELD_R | capi.FIELD_DENS))
+        sim.close()
+    for k in ("f", "r", "dens"):
+        if name.startswith("sediment"):
+            # the coupled step's Shepard scatter sums with atomics: rounding
+            scale = np.abs(out[1][k]).max()
+            assert np.abs(out[0][k] - out[1][k]).max() <= 1e-6 * scale, k
+        else:
+            np.testing.assert_array_equal(out[0][k], out[1][k], err_msg=k)
