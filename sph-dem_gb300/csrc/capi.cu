@@ -558,10 +558,12 @@ int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t 
             SPHDEM_CUDA_CHECK(cudaMemset(c->mx_ncnt, 0, capacity * sizeof(int)));
             SPHDEM_CUDA_CHECK(cudaDeviceSynchronize());
             mixed::prepare(c);
-            /* SPHDEM_FORCE_TILE=0: the force pass reads every neighbour record
-             * from global memory (the form the staged one is checked against) */
+            /* SPHDEM_FORCE_TILE=1: the force and continuity passes stage the
+             * neighbour records in shared memory by bulk copies (measured
+             * slower than reading them through L1 on the coupled workload,
+             * so off by default) */
             const char *ft = std::getenv("SPHDEM_FORCE_TILE");
-            c->force_tile = !(ft && ft[0] == '0');
+            c->force_tile = ft && ft[0] == '1';
             c->mx_dem_only = true;
             for (int64_t i = 0; i < init->n; i++) c->mx_dem_only = c->mx_dem_only && init->iam[i] == T_DEM;
             mixed::pack(c);

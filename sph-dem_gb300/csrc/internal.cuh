@@ -92,7 +92,7 @@ struct sphdem_ctx {
     sphdem::AdjointData *adj = nullptr; /* checkpoints and buffers of the adjoint */
     /* launch knobs chosen by the batch autotuner */
     int blk_pair = 128;         /* block size of the list-consumer passes (<= 128) */
-    bool force_tile = true;     /* force pass: neighbour records staged in shared memory */
+    bool force_tile = false;    /* force / continuity: neighbour records staged in shared memory */
     int grid_div = 1;           /* divides the resident-block grid of the slice passes */
     int2 *mx_bandq = nullptr;   /* per particle: list entries within the FP32 band */
     int *mx_bandn = nullptr;    /* per particle: how many are recorded */

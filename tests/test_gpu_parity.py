@@ -198,9 +198,10 @@ def test_corrected_gradient_and_reinit_restrictions(lib):
 
 @pytest.mark.parametrize("name", ["sediment3d_small", "dambreak2d_small", "dambreak2d_own_small"])
 def test_staged_force_pass_equals_plain_loads(lib, name, monkeypatch):
-    """The force pass with its neighbour records staged in shared memory by
-    bulk copies gives bit for bit the forces of the same pass reading every
-    record from global memory (SPHDEM_FORCE_TILE=0)."""
+    """The force and continuity passes with their neighbour records staged in
+    shared memory by bulk copies (SPHDEM_FORCE_TILE=1) give bit for bit the
+    results of the same passes reading every record through L1 (the
+    default)."""
     case = cases.workload(name)
     out = []
     for tile in ("1", "0"):
