@@ -704,7 +704,8 @@ def measure_ensemble(lib, capi, cases, instances, steps, warmup, err_steps=1000,
         "sequential": {"value": n_total * steps / (ms_seq * 1e-3), "unit": UNIT, "ms_per_step": ms_seq / steps},
         "batched_over_sequential": ms_seq / ms_batch,
         "autotuner": {"blk_pair_64": sum(1 for x in chosen if x[0] == 64),
-                      "grid_div_4": sum(1 for x in chosen if x[1] == 4), "setup_s": setup_s},
+                      "grid_div_4": sum(1 for x in chosen if x[1] == 4),
+                      "staged_tiles": sum(1 for x in chosen if x[2]), "setup_s": setup_s},
         "error_vs_fp64": {"steps": err_steps, "instances": len(pick),
                           "max_abs_drho_over_rho0": max(e["max_abs_drho_over_rho0"] for e in errs),
                           "max_abs_df_over_max_f": max(e["max_abs_df_over_max_f"] for e in errs)},
@@ -755,8 +756,9 @@ def run_ensemble(args):
                    "min_particles": min(c.n for c in ens), "max_particles": max(c.n for c in ens)},
         "sequential": {"value": n_total * args.steps / (ms_seq * 1e-3), "ms_per_step": ms_seq / args.steps},
         "batched_over_sequential": ms_seq / ms_batch,
-        "autotuner": {"blk_pair_64": sum(1 for b, _ in chosen if b == 64),
-                      "grid_div_4": sum(1 for _, d in chosen if d == 4), "setup_s": setup_s},
+        "autotuner": {"blk_pair_64": sum(1 for b, _, _ in chosen if b == 64),
+                      "grid_div_4": sum(1 for _, d, _ in chosen if d == 4),
+                      "staged_tiles": sum(1 for _, _, t in chosen if t), "setup_s": setup_s},
         "max_drho_over_rho0_vs_fp64": max(errs),
     }
     print(json.dumps(line), flush=True)

@@ -349,10 +349,14 @@ int sphdem_batch_step(sphdem_batch b, int nsteps);
 int sphdem_batch_time_steps(sphdem_batch b, int nsteps, double *ms);
 /* Autotuner: for every member, times steps_per_trial graph-replayed steps
  * alone for each candidate launch configuration (block size of the
- * list-consumer passes 64 / 128, grid of the slice passes full or 1/4) and
- * keeps the fastest.  This advances every member by 4 x (steps_per_trial + 1)
- * steps.  `chosen` (optional, 2 ints per member) receives block size and
- * grid divisor. */
+ * list-consumer passes 64 / 128, grid of the slice passes full or 1/4,
+ * neighbour tiles of the force and continuity passes staged in shared
+ * memory or read through L1 -- mixed 2D / 3D handles) and keeps the
+ * fastest.  Choices are remembered per (dimension, precision, feature
+ * flags, particle-count octave) for the process: a member of a class tuned
+ * before takes its choice untimed.  A timed member advances by up to
+ * 8 x (steps_per_trial + 1) steps.  `chosen` (optional, 3 ints per member)
+ * receives block size, grid divisor and staged tiles (0 / 1). */
 int sphdem_batch_tune(sphdem_batch b, int steps_per_trial, int *chosen);
 int sphdem_batch_last_error(sphdem_batch b, char *buf, size_t len);
 

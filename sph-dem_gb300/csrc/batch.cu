@@ -10,14 +10,20 @@
  * step and error flags; nothing is shared between them.
  *
  * The autotuner (sphdem_batch_tune) picks, per member, the block size of the
- * list-consumer passes and the grid of the slice passes by timing a few
- * graph-replayed steps of that member alone for every candidate.
+ * list-consumer passes, the grid of the slice passes and whether the force
+ * and continuity passes stage their neighbour tiles in shared memory, by
+ * timing a few graph-replayed steps of that member alone for every
+ * candidate; the choice is remembered per dimension, precision, feature
+ * flags and particle-count octave, and members of a class tuned before
+ * take it without timing.
  *
  * The reference runs one simulation per process; this file has no
  * counterpart there.
  */
 #include <algorithm>
 #include <cstdio>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -203,6 +209,34 @@ int sphdem_batch_time_steps(sphdem_batch b, int nsteps, double *ms) {
     return rc ? rc : check_members(b);
 }
 
+/* Tuned launch shapes, remembered per (dimension, precision, feature flags,
+ * particle-count octave) for the rest of the process: a member whose class
+ * was tuned before takes the same shape without timing. */
+struct TuneKey {
+    int nd, precision;
+    unsigned flags;
+    int octave;
+    bool operator<(const TuneKey &o) const {
+        if (nd != o.nd) return nd < o.nd;
+        if (precision != o.precision) return precision < o.precision;
+        if (flags != o.flags) return flags < o.flags;
+        return octave < o.octave;
+    }
+};
+struct TuneChoice {
+    int blk, div, tile;
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, TuneChoice> g_tune_cache;
+
+void drop_member_graphs(sphdem_ctx *m) {
+    for (cudaGraphExec_t &g : m->graph)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+}
+
 int sphdem_batch_tune(sphdem_batch b, int steps_per_trial, int *chosen) {
     if (!b || steps_per_trial <= 0) return SPHDEM_ERR_INVALID;
     static const int blk_opts[] = {64, 128};
@@ -211,36 +245,50 @@ int sphdem_batch_tune(sphdem_batch b, int steps_per_trial, int *chosen) {
         drop_graph(b);
         for (size_t i = 0; i < b->members.size(); i++) {
             sphdem_ctx *m = b->members[i];
-            double best = 1e300;
-            int best_blk = m->blk_pair, best_div = m->grid_div;
-            for (int blk : blk_opts)
-                for (int dv : div_opts) {
-                    m->blk_pair = blk;
-                    m->grid_div = dv;
-                    for (cudaGraphExec_t &g : m->graph)
-                        if (g) {
-                            cudaGraphExecDestroy(g);
-                            g = nullptr;
+            int octave = 0;
+            while ((int64_t(1) << (octave + 1)) <= m->n) octave++;
+            const TuneKey key{m->cfg.nd, m->cfg.precision, m->host_cfg.flags, octave};
+            TuneChoice best_c{m->blk_pair, m->grid_div, m->force_tile ? 1 : 0};
+            bool cached = false;
+            {
+                std::lock_guard<std::mutex> lock(g_tune_mu);
+                auto it = g_tune_cache.find(key);
+                if (it != g_tune_cache.end()) {
+                    best_c = it->second;
+                    cached = true;
+                }
+            }
+            if (!cached) {
+                /* staged neighbour tiles apply to the list passes of mixed
+                 * handles in 2D and 3D */
+                const int tiles = (m->cfg.precision == SPHDEM_PREC_MIXED && m->cfg.nd > 1 && m->mx_maxn > 0) ? 2 : 1;
+                double best = 1e300;
+                for (int blk : blk_opts)
+                    for (int dv : div_opts)
+                        for (int tl = 0; tl < tiles; tl++) {
+                            m->blk_pair = blk;
+                            m->grid_div = dv;
+                            m->force_tile = tl != 0;
+                            drop_member_graphs(m);
+                            double ms = 0.0;
+                            const int rc = sphdem_time_steps(m, steps_per_trial, &ms);
+                            if (rc) return batch_fail(b, rc, "tuning member " + std::to_string(i) + ": " + m->err);
+                            if (ms < best) {
+                                best = ms;
+                                best_c = TuneChoice{blk, dv, tl};
+                            }
                         }
-                    double ms = 0.0;
-                    const int rc = sphdem_time_steps(m, steps_per_trial, &ms);
-                    if (rc) return batch_fail(b, rc, "tuning member " + std::to_string(i) + ": " + m->err);
-                    if (ms < best) {
-                        best = ms;
-                        best_blk = blk;
-                        best_div = dv;
-                    }
-                }
-            m->blk_pair = best_blk;
-            m->grid_div = best_div;
-            for (cudaGraphExec_t &g : m->graph)
-                if (g) {
-                    cudaGraphExecDestroy(g);
-                    g = nullptr;
-                }
+                std::lock_guard<std::mutex> lock(g_tune_mu);
+                g_tune_cache[key] = best_c;
+            }
+            m->blk_pair = best_c.blk;
+            m->grid_div = best_c.div;
+            m->force_tile = best_c.tile != 0;
+            drop_member_graphs(m);
             if (chosen) {
-                chosen[2 * i] = best_blk;
-                chosen[2 * i + 1] = best_div;
+                chosen[3 * i] = best_c.blk;
+                chosen[3 * i + 1] = best_c.div;
+                chosen[3 * i + 2] = best_c.tile;
             }
         }
     } catch (const std::string &e) {

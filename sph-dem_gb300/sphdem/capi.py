@@ -454,9 +454,10 @@ class Batch:
         return ms.value
 
     def tune(self, steps_per_trial: int = 3):
-        chosen = (C.c_int * (2 * len(self.sims)))()
+        """sphdem_batch_tune: per member (block size, grid divisor, staged tiles)."""
+        chosen = (C.c_int * (3 * len(self.sims)))()
         self._check(self.L.lib.sphdem_batch_tune(self.h, steps_per_trial, chosen), "sphdem_batch_tune")
-        return [(chosen[2 * i], chosen[2 * i + 1]) for i in range(len(self.sims))]
+        return [(chosen[3 * i], chosen[3 * i + 1], chosen[3 * i + 2]) for i in range(len(self.sims))]
 
     def close(self):
         if getattr(self, "h", None):

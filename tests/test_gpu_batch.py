@@ -54,11 +54,13 @@ def test_batch_tune_then_step(lib):
     try:
         chosen = batch.tune(steps_per_trial=2)
         assert len(chosen) == len(ens)
-        assert all(blk in (64, 128) and div in (1, 4) for blk, div in chosen)
-        # tuning advanced every member by 4 x (2 + 1) steps
+        assert all(blk in (64, 128) and div in (1, 4) and tile in (0, 1) for blk, div, tile in chosen)
+        # tuning advanced each timed member by (2 + 1) steps per candidate; a
+        # member of a class tuned before is not timed
+        done = [int(m.globals().sph_step) for m in members]
         batch.step(3)
-        for s in alone:
-            s.step(4 * 3 + 3)
+        for s, k in zip(alone, done):
+            s.step(k + 3)
         for k, (m, s) in enumerate(zip(members, alone)):
             a, b = m.get(), s.get()
             for f in ("r", "dens"):
