@@ -4,23 +4,18 @@ walled 0.1 x 0.1 x 0.3 m box, linear spring-dashpot normal contacts
 (k = 1e4 N/m, restitution 0.5), gravity, dt = 1e-5 s, 2000 steps; the
 contact law of sph.h:1676-1706 with demNormal LINEAR (sph.h:1513-1515).
 
-Both paths run the same 2000 steps from the same input.  Every 500 steps:
+Both paths run the same 2000 steps from the same input.  A DEM-only
+handle has no FP32 pair pass (the contact law is FP64 on both paths), so
+the mixed handle runs the FP64 phases and the two runs agree bit for bit.
+Every 500 steps:
 
-- the contact relation of each path equals the exact pair set of the FP64
-  path on the same positions (two fresh handles, one per precision, made
-  from the mixed run's state and rebuilt twice), and both put every sphere
-  in the same reference bucket;
-- the mixed run's error against the FP64 run is printed: max |dr| / R,
-  max |dv| / max |v|, max |df| / max |f|.
-
-The bar on the trajectories: the two runs stay within 1e-6 R in position
-over the first 500 steps (the spheres fall freely and first touch the
-floor after about 0.01 s), and within the collision-driven divergence
-measured over the full 2000 steps (positions to 1e-2 R).  Contacts make
-the step discontinuous in time: a sphere pair that touches one step later
-in one run than in the other starts its dashpot force gamma |vn| one step
-later, so the two trajectories separate at the rate the granular collisions
-amplify that difference, not at the rate of FP32 rounding.
+- the contact relation of each precision equals the exact pair set of the
+  FP64 path on the same positions (two fresh handles, one per precision,
+  made from the mixed run's state and rebuilt twice), and both put every
+  sphere in the same reference bucket;
+- the mixed run's difference from the FP64 run is printed: max |dr| / R,
+  max |dv| / max |v|, max |df| / max |f|.  The spheres fall freely until
+  step ~1350 and then land on the floor.
 
 The reference has one global sphere radius (sph.h:1685); the polydisperse
 form (overlap = R_a + R_b - r) is pinned to the oracle on the small
@@ -85,5 +80,5 @@ def test_dem_settling_50k_mixed_vs_fp64(lib):
     for s, e_r, e_v, e_f, npairs in rows:
         print(f"step {s}: max|dr|/R {e_r:.2e}  max|dv|/max|v| {e_v:.2e}  max|df|/max|f| {e_f:.2e}  "
               f"contact pairs {npairs}")
-    assert rows[0][1] <= 1e-6
-    assert rows[-1][1] <= 1e-2
+    for s, e_r, e_v, e_f, _ in rows:
+        assert e_r == 0.0 and e_v == 0.0 and e_f == 0.0, f"step {s}: {e_r} {e_v} {e_f}"
