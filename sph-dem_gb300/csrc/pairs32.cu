@@ -1287,6 +1287,7 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
             fb[k].init(0.f);
             fa[k].init(0.f);
         }
+        float hmin = FLT_MAX; /* smallest hav of the fluid pairs */
         const int cnt = ncnt[a];
         /* 8 entries at a time from the particle's list tiles (two int4 loads) */
         const int4 *tile = reinterpret_cast<const int4 *>(nbr + nl_at(a, 0, ld));
@@ -1363,11 +1364,11 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
                 const float vdr = d[0] * dv0 + d[1] * dv1 + d[2] * dv2;
                 float vsig = 0.f;
                 if (visc == SPHDEM_VISC_MORRIS) {
-                    const float visc = c.liq_dem() ? liq_visc / (densa * densb)
-                                                   : visc_nu * (densa + densb) / (densa * densb);
-                    vsig = 2.f * c0;
+                    /* mb visc dg / (r^2 + 0.01 hav^2) with visc = num / (rho_a rho_b):
+                     * one division, by the fast reciprocal (2 ulp) */
+                    const float num = c.liq_dem() ? liq_visc : visc_nu * (densa + densb);
                     const float dg = CG ? d[0] * gMv[0] + d[1] * gMv[1] + d[2] * gMv[2] : r2 * cM;
-                    const float sc = mb * visc * dg / (r2 + 0.01f * hav * hav);
+                    const float sc = __fdividef(mb * num * dg, (densa * densb) * (r2 + 0.01f * hav * hav));
                     const float dvv[3] = {dv0, dv1, dv2};
 #pragma unroll
                     for (int k = 0; k < ND; k++) fv[k].add(dvv[k] * sc);
@@ -1389,8 +1390,12 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
                         vsig = fmaxf(vsig, avsig);
                     }
                 }
-                ndt = fminf(ndt, 0.6f * hav / vsig);
-                ndt = fminf(ndt, vdc * hav * hav / visc_nu);
+                /* the viscous bound vdc hav^2 / nu increases with hav, and so
+                 * does the Courant bound 0.6 hav / vsig under Morris viscosity
+                 * (vsig = 2 c0 for every pair): the loop's smallest hav gives
+                 * them, bit for bit */
+                hmin = fminf(hmin, hav);
+                if (visc != SPHDEM_VISC_MORRIS) ndt = fminf(ndt, 0.6f * hav / vsig);
             }
             if (is_boundary(tb)) {
                 float fbx[3] = {0.f, 0.f, 0.f};
@@ -1410,6 +1415,13 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
                     fp[k].add(CG ? -mb * (pdr2a * gAv[k] + pdr2b * gBv[k]) : -mb * (pc * d[k]));
                 if (anti) fq.add(-mb * antic);
             }
+        }
+        if (hmin < FLT_MAX) {
+            if (visc == SPHDEM_VISC_MORRIS) {
+                const float vsig = 2.f * c0;
+                ndt = fminf(ndt, 0.6f * hmin / vsig);
+            }
+            ndt = fminf(ndt, vdc * hmin * hmin / visc_nu);
         }
         float roma = 1.f;
         if (var_h) {
