@@ -63,6 +63,16 @@ struct Kahan {
     __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+/* A plain FP32 sum with the same interface, for sums whose rounding does
+ * not reach the results' tolerance: the calcOmega sum under
+ * VAR_H_CORRECTION, where Omega = 1 + h sum / (rho NDIM) is an O(1) factor
+ * known to ~1e-6 from ~100 terms. */
+struct Plain {
+    float s;
+    __device__ __forceinline__ void init(float v) { s = v; }
+    __device__ __forceinline__ void add(float x) { s += x; }
+};
+
 __device__ __forceinline__ float wK32(float q, float wcon) {
     if (q > 2.f) return 0.f;
     const float t = 2.f - q, t2 = t * t;
@@ -1266,7 +1276,7 @@ __global__ void __launch_bounds__(BLK) k_force(DevCfg c, const DevCfg *__restric
          * sph.h:438-451) is summed in this same loop and the gradient sums
          * are scaled once at the end */
         const float ihna = powi<ND>(iha), pd_coef = ND * ihna * iha;
-        Kahan om;
+        Plain om;
         om.init(-ma * pd_coef * wK32(0.f, wcon));
         const bool sph = ta == T_SPH;
         const bool anti = PHYS == PHYS_GENERIC && !(c.flags & SPHDEM_F_NO_ANTICLUMPING);
@@ -1481,7 +1491,7 @@ __global__ void __launch_bounds__(BLK) k_dddt(DevCfg c, DevState s, const DevGlo
     /* VAR_H_CORRECTION: the continuity sum carries 1/Omega_a only, so
      * Omega_a is summed in this loop and applied once at the end */
     const float ihna = powi<ND>(iha), pd_coef = ND * ihna * iha;
-    Kahan om;
+    Plain om;
     om.init(-va.w * pd_coef * wK32(0.f, wcon));
     Kahan acc;
     acc.init(0.f);
