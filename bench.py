@@ -258,10 +258,12 @@ def cpu_baseline(steps=2, warm=1, procs=1):
 
 
 # --------------------------------------------------------------------------
-def _time_adjoint(lib, capi, cases, case, nsteps, ckpt, seed_fn, precisions=("fp64", "mixed")):
+def _time_adjoint(lib, capi, cases, case, nsteps, ckpt, seed_fn, precisions=("fp64", "mixed"), tape_mem=0):
     """(plain forward, adjoint forward, adjoint backward) wall times of the
     same nsteps from the same state, FP64 and / or mixed (each call returns
-    after the device finished)."""
+    after the device finished).  tape_mem: sphdem_adjoint_set_tape_memory
+    (0: one segment's tape, earlier segments replayed in the backward pass;
+    -1: the tapes of every segment that fits in half of the free memory)."""
     out = {}
     for name in precisions:
         prec = cases.PREC_FP64 if name == "fp64" else cases.PREC_MIXED
@@ -274,6 +276,7 @@ def _time_adjoint(lib, capi, cases, case, nsteps, ckpt, seed_fn, precisions=("fp
         sim = capi.Simulation(lib, case.cfg, case.particles, precision=prec)
         sim.step(2)
         seeds = seed_fn(sim)
+        sim.adjoint_set_tape_memory(tape_mem)
         t0 = time.perf_counter()
         sim.adjoint_forward(nsteps, ckpt)
         t_af = time.perf_counter() - t0
@@ -330,16 +333,29 @@ def measure_adjoint(lib, capi, cases, nsteps=100, ckpt=10):
         seed[m, 2] = 1.0 / max(1, m.sum())
         return {"dL_dr": seed}
 
-    out["coupled"] = _time_adjoint(lib, capi, cases, cpl, cpl_steps, cpl_ckpt, cpl_seed, precisions=("mixed",))
+    # checkpoints every 50 steps; the tapes of the segments are kept in
+    # device memory from the forward pass (they fit: ~10 GB per 50 steps)
+    out["coupled"] = _time_adjoint(lib, capi, cases, cpl, cpl_steps, cpl_ckpt, cpl_seed, precisions=("mixed",),
+                                   tape_mem=-1)
     out["coupled"]["workload"] = (f"coupled SPH-DEM, {cpl.n} particles ({cpl.notes['n_fluid']} fluid, "
-                                  f"{cpl.notes['n_dem']} DEM), {cpl_steps} steps, checkpoint every {cpl_ckpt}")
-    # the same with one segment (checkpoint interval = run length): the whole
-    # tape is recorded in the forward pass and nothing is replayed -- the
-    # cost of the taps and the reverse sweep alone
+                                  f"{cpl.notes['n_dem']} DEM), {cpl_steps} steps, checkpoint every {cpl_ckpt}, "
+                                  f"segment tapes kept in device memory")
+    # the same with one segment's tape: the backward pass replays the first
+    # segment from its checkpoint
+    out["coupled_replay"] = _time_adjoint(lib, capi, cases, cpl, cpl_steps, cpl_ckpt, cpl_seed,
+                                          precisions=("mixed",), tape_mem=0)
+    out["coupled_replay"]["workload"] = (f"as coupled, one segment's tape kept (earlier segments replayed "
+                                         f"from their checkpoints)")
+    # the same with one segment (checkpoint interval = run length)
     out["coupled_one_segment"] = _time_adjoint(lib, capi, cases, cpl, cpl_steps, cpl_steps, cpl_seed,
                                                precisions=("mixed",))
     out["coupled_one_segment"]["workload"] = (f"as coupled, {cpl_steps} steps in one checkpoint segment "
                                               f"(tape recorded in the forward pass, no replay)")
+    # the differentiated run's own length: 500 steps, checkpoints every 50
+    out["coupled_500"] = _time_adjoint(lib, capi, cases, cpl, 500, 50, cpl_seed, precisions=("mixed",),
+                                       tape_mem=-1)
+    out["coupled_500"]["workload"] = ("as coupled, 500 steps, checkpoint every 50, segment tapes kept in "
+                                      "device memory")
     out["ratio"] = max(out["dem"]["mixed"]["ratio"], out["fluid"]["mixed"]["ratio"],
                        out["coupled"]["mixed"]["ratio"])
     return out

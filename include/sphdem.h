@@ -302,7 +302,12 @@ int sphdem_cell_ids(sphdem_handle h, int32_t *cell_xyz);
  *  - fluid handles of SPH and SPH-boundary particles (no LIQ_DEM) with
  *    artificial viscosity, CONST_H, NO_ANTICLUMPING, no VAR_H_CORRECTION and
  *    no periodic axes (the dam break): gradients `viscosity` =
- *    dL/d(alpha_artificial) and the initial state.
+ *    dL/d(alpha_artificial) and the initial state;
+ *  - coupled LIQ_DEM handles of SPH, SPH-boundary and DEM particles with
+ *    Morris viscosity, CONST_H, NO_ANTICLUMPING, no VAR_H_CORRECTION, gamma
+ *    = 7 (periodic axes allowed; sedimentation): gradients dem_k, dem_gamma,
+ *    `viscosity` = dL/d(kinematic viscosity), drag_scale and the initial
+ *    state.
  * Other handles get SPHDEM_ERR_UNSUPPORTED.
  *
  * sphdem_adjoint_forward runs nsteps ordinary steps from the current state,
@@ -326,6 +331,15 @@ typedef struct SphDemGrads {
 } SphDemGrads;
 
 int sphdem_adjoint_forward(sphdem_handle h, int nsteps, int ckpt_every);
+/* Device memory the adjoint may use to keep checkpoint segments' tapes (the
+ * per-step states and pair tables the reverse sweep reads) from the forward
+ * pass: bytes = 0 (the default) keeps one segment's tape, so the backward
+ * pass replays every earlier segment from its checkpoint; bytes > 0 keeps
+ * the tapes of as many of the last segments as fit, which the backward pass
+ * then does not replay; bytes < 0 takes half of the device memory free at
+ * sphdem_adjoint_forward.  Applies from the next sphdem_adjoint_forward.
+ * All-DEM handles always keep one segment's tape. */
+int sphdem_adjoint_set_tape_memory(sphdem_handle h, int64_t bytes);
 int sphdem_adjoint_backward(sphdem_handle h, const double *dL_dr, const double *dL_dv,
                             const double *dL_dvhat, SphDemGrads *grads,
                             double *dL_dr0, double *dL_dv0, double *dL_dvhat0);

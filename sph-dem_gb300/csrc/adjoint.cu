@@ -98,10 +98,12 @@ namespace {
 
 constexpr int ABLK = 256;
 
-__global__ void k_save(DevState s, int64_t n, double *dst, const int *slot) {
+/* with slot: the state after step *slot of the tape store, whose blocks of K
+ * steps each hold K + 1 states (the block's first state, then one per step) */
+__global__ void k_save(DevState s, int64_t n, double *dst, const int *slot, int K) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= n) return;
-    if (slot) dst += (int64_t)(*slot + 1) * n * ADJ_NC;
+    if (slot) dst += (int64_t)(*slot + 1 + *slot / K) * n * ADJ_NC;
     double *o = dst + (int64_t)s.irow(FI_TAG)[k] * ADJ_NC;
     for (int d = 0; d < 3; d++) {
         o[d] = s.row(FD_R + d)[k];
@@ -139,6 +141,10 @@ __global__ void k_restore(DevState s, int64_t n, const double *src) {
 
 __global__ void k_slot_inc(int *slot) {
     if (threadIdx.x == 0 && blockIdx.x == 0) *slot += 1;
+}
+
+__global__ void k_slot_set(int *slot, int v) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) *slot = v;
 }
 
 __global__ void k_save_const(DevCfg c, DevState s, int64_t n, double *mass, double *rad, int *typ, double *hh) {
@@ -768,8 +774,8 @@ __global__ void __launch_bounds__(128) k_sadj_mid32(DevCfg c, int64_t n, double 
     if ((threadIdx.x & 31) == 0 && Ab != 0.f) atomicAdd(&grads[2], (double)Ab);
 }
 
-void save_state(sphdem_ctx *c, double *dst, const int *slot = nullptr) {
-    k_save<<<grid_for(c->n, ABLK), ABLK, 0, c->stream>>>(c->A, c->n, dst, slot);
+void save_state(sphdem_ctx *c, double *dst, const int *slot = nullptr, int K = 1) {
+    k_save<<<grid_for(c->n, ABLK), ABLK, 0, c->stream>>>(c->A, c->n, dst, slot, K);
 }
 
 void restore_state(sphdem_ctx *c, const double *src, const DevGlobals &g) {
@@ -809,6 +815,8 @@ void replay_sph_step(sphdem_ctx *c) {
         const bool p0 = c->flipped;
         c->in_capture = true;
         SPHDEM_CUDA_CHECK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        /* mixed coupled handles: the forward coupling passes write the pair tables */
+        if (a->mode == ADJ_MODE_COUPLED) c->tap = cpl_forward_taps(c, a);
         try {
             for (int p = SPHDEM_HOOK_BEFORE_START; p <= SPHDEM_HOOK_AFTER_END; p++) {
                 phase_sequence(c, p);
@@ -824,15 +832,17 @@ void replay_sph_step(sphdem_ctx *c) {
                     if (a->mode == ADJ_MODE_COUPLED) cpl_taps_end(c, a);
                 }
             }
-            save_state(c, a->seg, a->slot);
+            save_state(c, a->seg, a->slot, a->K);
             k_slot_inc<<<1, 32, 0, c->stream>>>(a->slot);
         } catch (...) {
             c->in_capture = false;
+            c->tap = nullptr;
             cudaStreamEndCapture(c->stream, &graph);
             if (graph) cudaGraphDestroy(graph);
             throw;
         }
         c->in_capture = false;
+        c->tap = nullptr;
         SPHDEM_CUDA_CHECK(cudaStreamEndCapture(c->stream, &graph));
         if (c->flipped != p0) {
             cudaGraphDestroy(graph);
@@ -871,22 +881,25 @@ void backward_dem(sphdem_ctx *c, AdjointData *a, int steps, double dt, int cap) 
     }
 }
 
+/* the steps of a segment with their taps into tape block a->blk */
 void replay_sph(sphdem_ctx *c, AdjointData *a, int steps) {
     const int64_t n = c->n;
-    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->slot, 0, sizeof(int), c->stream));
+    const size_t s0 = (size_t)a->blk * a->K;
+    k_slot_set<<<1, 32, 0, c->stream>>>(a->slot, (int)s0);
     /* a particle that stops being SPH/SPHB (deleted) keeps an empty list */
-    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_mid, 0, (size_t)a->K * n * sizeof(int2), c->stream));
-    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_end, 0, (size_t)a->K * n * sizeof(int2), c->stream));
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_mid + s0 * n, 0, (size_t)a->K * n * sizeof(int2), c->stream));
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->oc_end + s0 * n, 0, (size_t)a->K * n * sizeof(int2), c->stream));
     if (a->mode == ADJ_MODE_COUPLED) cpl_reset_segment(c, a);
     for (int j = 1; j <= steps; j++) replay_sph_step(c);
 }
 
 void backward_sph(sphdem_ctx *c, AdjointData *a, int steps, double dt) {
     const int64_t n = c->n, cap = a->pair_cap;
+    const size_t sb = (size_t)a->blk * a->K, stb = (size_t)a->blk * (a->K + 1);
     for (int j = steps; j >= 1; j--) {
-        const double *s0 = a->seg + (size_t)(j - 1) * n * ADJ_NC, *s1 = a->seg + (size_t)j * n * ADJ_NC;
-        const int *nbm = a->nb_mid + (size_t)(j - 1) * cap, *nbe = a->nb_end + (size_t)(j - 1) * cap;
-        const int2 *ocm = a->oc_mid + (size_t)(j - 1) * n, *oce = a->oc_end + (size_t)(j - 1) * n;
+        const double *s0 = a->seg + (stb + j - 1) * n * ADJ_NC, *s1 = a->seg + (stb + j) * n * ADJ_NC;
+        const int *nbm = a->nb_mid + (sb + j - 1) * cap, *nbe = a->nb_end + (sb + j - 1) * cap;
+        const int2 *ocm = a->oc_mid + (sb + j - 1) * n, *oce = a->oc_end + (sb + j - 1) * n;
         if (a->rec) {
             k_sadj_pre32<<<grid_for(n, ABLK), ABLK, 0, c->stream>>>(c->cfg, n, dt, s0, s1, a->adj, a->mass, a->hh,
                                                                     a->typ, a->rec);
@@ -915,15 +928,36 @@ void backward_cpl(sphdem_ctx *c, AdjointData *a, int steps, double dt) {
     for (int j = steps; j >= 1; j--) cpl_backward_step(c, a, j, dt);
 }
 
-/* buffers of one segment's tape and of the reverse sweep */
+/* How many segments' tapes the store holds: the handle's tape memory
+ * (sphdem_adjoint_set_tape_memory) over the bytes of one segment's tape,
+ * between 1 and the segment count; DEM handles keep one. */
+int tape_blocks(sphdem_ctx *c, AdjointData *a, int nseg) {
+    if (a->mode == ADJ_MODE_DEM || nseg <= 1 || c->adj_tape_mem == 0) return 1;
+    const int64_t n = c->n, K = a->K;
+    int64_t blk = (K + 1) * n * ADJ_NC * (int64_t)sizeof(double) + 2 * K * (int64_t)sizeof(int) +
+                  K * (2 * a->pair_cap * (int64_t)sizeof(int) + 2 * n * (int64_t)sizeof(int2));
+    if (a->mode == ADJ_MODE_COUPLED)
+        blk += K * ((a->cpl.cap + a->fpi.cap + a->ct_cap) * (int64_t)sizeof(int) + 3 * n * (int64_t)sizeof(int2) +
+                    3 * (int64_t)sizeof(int) + n * 3 * (int64_t)sizeof(double));
+    int64_t budget = c->adj_tape_mem;
+    if (budget < 0) {   /* half of the device memory free now */
+        size_t fr = 0, tot = 0;
+        SPHDEM_CUDA_CHECK(cudaMemGetInfo(&fr, &tot));
+        budget = (int64_t)(fr / 2);
+    }
+    return (int)std::max<int64_t>(1, std::min<int64_t>(nseg, budget / blk));
+}
+
+/* buffers of the tape store (a->nblk blocks of one segment's tape) and of
+ * the reverse sweep */
 void alloc_backward(sphdem_ctx *c, AdjointData *a) {
     if (a->seg) return;
     const int64_t n = c->n;
-    const int K = a->K;
+    const int K = a->K * a->nblk;   /* step slots of the store */
     const size_t sbytes = (size_t)n * ADJ_NC * sizeof(double);
     const int cap = ADJ_MAX_CONTACTS * (int)n;
     const bool sph = a->mode == ADJ_MODE_SPH, cpl = a->mode == ADJ_MODE_COUPLED;
-    SPHDEM_CUDA_CHECK(cudaMalloc(&a->seg, (size_t)(K + 1) * sbytes));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->seg, (size_t)(K + a->nblk) * sbytes));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->pair_cnt, (size_t)K * sizeof(int)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->adj, sbytes));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->racc, n * 3 * sizeof(double)));
@@ -947,15 +981,17 @@ void alloc_backward(sphdem_ctx *c, AdjointData *a) {
     }
 }
 
-/* the tape of segment sg: from its checkpoint (already the handle's state),
- * the steps with their taps */
+/* the tape of segment sg into tape block a->blk: from its checkpoint
+ * (already the handle's state), the steps with their taps */
 void tape_segment(sphdem_ctx *c, AdjointData *a, int sg, int steps) {
     const size_t sbytes = (size_t)c->n * ADJ_NC * sizeof(double);
     const int K = a->K;
-    SPHDEM_CUDA_CHECK(cudaMemcpyAsync(a->seg, a->ckpt[sg], sbytes, cudaMemcpyDeviceToDevice, c->stream));
-    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->pair_cnt, 0, K * sizeof(int), c->stream));
+    const size_t sb = (size_t)a->blk * K;
+    SPHDEM_CUDA_CHECK(cudaMemcpyAsync(a->seg + (size_t)a->blk * (K + 1) * c->n * ADJ_NC, a->ckpt[sg], sbytes,
+                                      cudaMemcpyDeviceToDevice, c->stream));
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->pair_cnt + sb, 0, K * sizeof(int), c->stream));
     if (a->mode == ADJ_MODE_SPH || a->mode == ADJ_MODE_COUPLED) {
-        SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cnt_end, 0, K * sizeof(int), c->stream));
+        SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cnt_end + sb, 0, K * sizeof(int), c->stream));
         replay_sph(c, a, steps);
     } else {
         replay_dem(c, a, steps, ADJ_MAX_CONTACTS * (int)c->n);
@@ -1042,16 +1078,19 @@ int adjoint_forward(sphdem_ctx *c, int nsteps, int K, int mode) {
         a->pair_cap = (int64_t)n0 + n0 / 2 + 4096;
         if (mode == ADJ_MODE_COUPLED) cpl_count_tables(c, a);
     }
+    a->nblk = tape_blocks(c, a, nseg);
     for (int s = 0; s < nseg; s++) {
         save_state(c, a->ckpt[s]);
         a->ckpt_g[s] = read_globals(c);
         const int steps = std::min(K, nsteps - s * K);
-        if (s == nseg - 1) {
-            /* the backward pass starts with the last segment: record its tape
-             * now instead of replaying it then */
+        if (s >= nseg - a->nblk) {
+            /* the backward pass starts with the last segments: record the
+             * tapes of those the store holds now instead of replaying them
+             * then */
             alloc_backward(c, a);
+            a->blk = s - (nseg - a->nblk);
             tape_segment(c, a, s, steps);
-            a->taped = s;
+            a->taped = 1;
             const int rc = device_status(c);
             if (rc) return rc;
             continue;
@@ -1091,13 +1130,20 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
     const int nseg = (a->nsteps + K - 1) / K;
     const double dt = a->ckpt_g[0].dt;
     bool overflow = false;
+    const int kept0 = a->taped ? nseg - a->nblk : nseg;
+    a->taped = 0;   /* block 0 takes the replays below: a later call replays everything */
     for (int sg = nseg - 1; sg >= 0 && !overflow; sg--) {
         const int steps = std::min(K, a->nsteps - sg * K);
-        if (sg != a->taped) {
+        /* the last nblk segments were taped in the forward pass into blocks
+         * 0..nblk-1; the earlier ones are replayed into block 0, whose
+         * segment the sweep has passed by then */
+        if (sg >= kept0) {
+            a->blk = sg - kept0;
+        } else {
+            a->blk = 0;
             restore_state(c, a->ckpt[sg], a->ckpt_g[sg]);
             tape_segment(c, a, sg, steps);
         }
-        a->taped = -1;   /* the buffers now hold this segment's tape */
         if (sph || cpl) {
             if (cpl) backward_cpl(c, a, steps, dt);
             else backward_sph(c, a, steps, dt);
@@ -1107,10 +1153,12 @@ int adjoint_backward(sphdem_ctx *c, const double *seed_r, const double *seed_v, 
         SPHDEM_CUDA_CHECK(cudaGetLastError());
         /* list overflow check of this segment */
         std::vector<int> cnt(2 * K, 0);
-        SPHDEM_CUDA_CHECK(cudaMemcpyAsync(cnt.data(), a->pair_cnt, K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        const size_t sb = (size_t)a->blk * K;
+        SPHDEM_CUDA_CHECK(
+            cudaMemcpyAsync(cnt.data(), a->pair_cnt + sb, K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         if (sph || cpl)
             SPHDEM_CUDA_CHECK(
-                cudaMemcpyAsync(cnt.data() + K, a->cnt_end, K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+                cudaMemcpyAsync(cnt.data() + K, a->cnt_end + sb, K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
         SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
         const int64_t lim = (sph || cpl) ? a->pair_cap : cap;
         for (int v : cnt) overflow = overflow || v > lim;

@@ -29,6 +29,21 @@ constexpr int CP_NMID = 8;         /* coupled step: middle intermediates per par
 constexpr int CP_NREC32 = 8;       /* coupled step, mixed: float4 records per particle */
 constexpr int CP_FPI_PER = 384;    /* FPI partners per DEM particle per step (3D fluid at rest: ~122) */
 
+/* one step's transposed pair table: (offset, count) per partner tag, the
+ * owners' entries (owner tag | shift code of the owner's image) */
+struct TrTable {
+    int *nb = nullptr;
+    int *ix = nullptr;      /* index of the pair's entry in the owners' table */
+    int2 *oc = nullptr;
+};
+/* scratch of the transposition: counts, fill cursors, offsets, tile sums,
+ * the entries before ranking */
+struct TrScratch {
+    int *cnt = nullptr, *fill = nullptr, *off = nullptr, *tsum = nullptr;
+    int2 *tmp = nullptr;
+};
+constexpr int CP_NCOEF = 12;       /* coupled step: FPI coefficient record per DEM particle */
+
 /* a grouped pair table of every step of a segment: entries partner tag |
  * shift << 26 grouped by particle, (offset, count) per tag and step, entries
  * used per step */
@@ -44,7 +59,11 @@ struct PairTable {
 struct AdjointData {
     int mode = 0;
     int nsteps = 0, K = 0;
-    int taped = -1;                 /* segment whose tape the buffers hold from the forward pass */
+    /* tape store: nblk blocks of K step slots (K + 1 states) each; the
+     * forward pass tapes the last nblk segments into blocks 0..nblk-1 */
+    int nblk = 1;
+    int blk = 0;                    /* block the current segment's tape is in */
+    int taped = 0;                  /* the blocks hold the forward pass's tapes */
     int64_t n = 0;
     std::vector<double *> ckpt;     /* state at steps 0, K, 2K, ... and the final state */
     std::vector<DevGlobals> ckpt_g;
@@ -82,6 +101,13 @@ struct AdjointData {
     float4 *dpos = nullptr;         /* middle-phase DEM positions by state index (FP32) */
     int n_dem = 0;                  /* DEM particles at the forward pass */
     int *dem_tags = nullptr;        /* their tags */
+    TapTables tap;                  /* mixed: the tables above as the forward coupling passes fill them */
+    TrTable cplT, fpiT;             /* one step's coupling table by DEM particle, FPI table by fluid particle */
+    TrScratch trw;
+    double *coef = nullptr;         /* CP_NCOEF per particle (DEM): adjoints of its FPI sums */
+    /* one step's pair geometry per entry of the coupling / FPI tables: (d,
+     * W'/r) and W, FP32 on mixed handles, FP64 on FP64 handles */
+    void *g4_cpl = nullptr, *gw_cpl = nullptr, *g4_fpi = nullptr, *gw_fpi = nullptr;
 };
 
 /* G = (F(r, h_a) + F(r, h_b)) / 2 and dG/dr, F(r, h) = -10 C (2-q)^3 / h^(d+2)
@@ -170,6 +196,9 @@ void cpl_count_tables(sphdem_ctx *c, AdjointData *a);          /* sizes cpl / fp
 void cpl_alloc(sphdem_ctx *c, AdjointData *a);
 void cpl_free(AdjointData *a);
 void cpl_reset_segment(sphdem_ctx *c, AdjointData *a);         /* empty tables before a segment's replay */
+/* mixed handles: the forward coupling passes write the cpl / fpi / contact
+ * tables while the replay graph is captured (c->tap = the returned tables) */
+const TapTables *cpl_forward_taps(sphdem_ctx *c, AdjointData *a);
 void cpl_taps_middle(sphdem_ctx *c, AdjointData *a);           /* inside the replay graph, after MIDDLE */
 void cpl_taps_end(sphdem_ctx *c, AdjointData *a);              /* inside the replay graph, after END */
 void cpl_backward_step(sphdem_ctx *c, AdjointData *a, int j, double dt);  /* VJP of step j of the segment */

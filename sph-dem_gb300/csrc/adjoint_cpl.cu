@@ -27,13 +27,20 @@
  *
  * W_c(r) = C_c K(2r/Rc) is the coupling kernel, V the DEM volume increment,
  * kappa the drag scale and Phi the Di Felice law.  The reverse pass of one
- * step runs, in order: intermediates (k_cp_pre), porosity / Shepard / EOS
- * (k_cp_por), FPI + drag (k_cp_fpi), DEM walls + contacts (k_cp_dem),
- * continuity and the adjoint of f1 (k_cp_end), forces + EOS (k_cp_force),
- * porosity + DEM->fluid drag (k_cp_cpl_a), Shepard sums (k_cp_cpl_b) and the
- * adjoint of the state before the step (k_cp_assemble).  Scatters from one
- * particle kind into the other (fluid <-> DEM) are FP64 atomics; sums within
- * the fluid gather over the symmetric pair table.
+ * step runs, in order: the transposed coupling and FPI tables of the step
+ * (transpose), intermediates (k_cp_pre), porosity / EOS (k_cp_por), Shepard
+ * sums (k_cp_shep), FPI + drag (k_cp_fpi on the DEM side, k_cp_fpi_fluid on
+ * the fluid side), DEM walls + contacts (k_cp_dem), continuity and the
+ * adjoint of f1 (k_cp_end), forces + EOS (k_cp_force), porosity, DEM->fluid
+ * drag and Shepard terms (k_cp_cpl_dem, k_cp_cpl_fluid) and the adjoint of
+ * the state before the step (k_cp_assemble).  Every pair term is gathered by
+ * both of its particles (the fluid over the symmetric pair tables, fluid <->
+ * DEM over a table and its transpose), so no accumulator takes an atomic;
+ * only the five scalar gradients are reduced with one FP64 atomic per warp.
+ *
+ * Mixed-precision handles take the coupling, FPI and contact tables from
+ * the forward passes themselves (k_couple, k_dem_end write them while the
+ * replay graph runs); FP64 handles scan for them after each phase.
  *
  * Mixed-precision handles run the two fluid pair passes (continuity and
  * forces, ~100 pairs per particle in 3D) in FP32 on double-float position
@@ -45,6 +52,7 @@
  * recomputed r_s from the frame the pair tables were built in).
  */
 #include <algorithm>
+#include <cstdlib>
 #include <string>
 #include <vector>
 
@@ -88,8 +96,12 @@ enum : int {
 /* end-phase results (CP_NEND): total adjoint of r1, vh1, f1, fp, fv */
 enum : int { CE_R1 = 0, CE_VH1 = 3, CE_F = 6, CE_P = 9, CE_V = 12 };
 /* middle intermediates (CP_NMID): eps, clamped, pdr2, Shepard sum (DEM),
- * adjoint of vh_s */
-enum : int { CM_EPS = 0, CM_CLAMP = 1, CM_PDR2 = 2, CM_SHEP = 3, CM_VHS = 4 };
+ * adjoint of vh_s, 1 / Shepard sum (DEM; 0 for a zero sum) */
+enum : int { CM_EPS = 0, CM_CLAMP = 1, CM_PDR2 = 2, CM_SHEP = 3, CM_VHS = 4, CM_ISHEP = 7 };
+/* FPI coefficient record of a DEM particle (CP_NCOEF): drag on (1) or not
+ * (0), then the adjoints of its Shepard sum, of the porosity sum and of the
+ * fp, fv and velocity sums */
+enum : int { CF_ON = 0, CF_SUM = 1, CF_POR = 2, CF_FP = 3, CF_FV = 6, CF_VEL = 9 };
 
 __device__ __forceinline__ bool is_fluid(int t) { return t == T_SPH || t == T_SPHB; }
 
@@ -335,7 +347,7 @@ __device__ __forceinline__ void wc_kernel(const DevCfg &c, double r, double &W, 
     Wp = c.c_ihn * c.wcon * (-10.0 * q * t2 * t) * c.two_over_rc;
 }
 
-/* intermediates: middle positions, vh_s (fluid) / vh_m (DEM), rho_s */
+/* intermediates: middle positions, vh_s (fluid) / vh_m (DEM), rho_s, 1/rho_s */
 __global__ void k_cp_pre(int64_t n, double dt, const double *s0, const double *rm, const int *typ, double *aux) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -349,27 +361,114 @@ __global__ void k_cp_pre(int64_t n, double dt, const double *s0, const double *r
         o[3 + d] = (t == T_SPH || t == T_DEM) ? x[AS_VH + d] + hd * x[AS_F + d] : x[AS_VH + d];
     }
     o[6] = x[AS_DENS] + hd * x[AS_DDDT];
-    o[7] = 0.0;
+    o[7] = is_fluid(t) ? 1.0 / o[6] : 0.0;
 }
 
-/* porosity, EOS and the Shepard sums of the middle phase (forward) */
-__global__ void k_cp_por(DevCfg c, int64_t n, const double *aux, const double *mass, const int *typ, const int *nb,
-                         const int2 *oc, double *cmid) {
+/* ---- pair geometry of the coupling and FPI tables -------------------------
+ * Each coupling pair is visited by four reverse passes and each FPI pair by
+ * three; its displacement, kernel value and kernel slope are evaluated once
+ * per step into records of the pair's table entry: g4 = (d, W'/r), gw = W.
+ * M = float on mixed-precision handles (the displacement is an FP64
+ * difference rounded once), double on FP64 handles. */
+template <typename M> struct MT;
+template <> struct MT<float> {
+    using V4 = float4;
+    using Acc = Kf;
+    static __device__ __forceinline__ float4 make(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+    static __device__ __forceinline__ float root(float x) { return sqrtf(x); }
+};
+/* plain FP64 sum with Kf's interface */
+struct Kd {
+    double s = 0.0;
+    __device__ __forceinline__ void add(double x) { s += x; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <> struct MT<double> {
+    using V4 = double4;
+    using Acc = Kd;
+    static __device__ __forceinline__ double4 make(double a, double b, double c, double d) {
+        return make_double4(a, b, c, d);
+    }
+    static __device__ __forceinline__ double root(double x) { return sqrt(x); }
+};
+
+/* coupling pairs, one thread per fluid particle: d = r_a - r_i at the middle
+ * positions, W = W_c(r) = C_c K(2r/Rc) and W_c'(r) / r (sph.h:1246-1256) */
+template <typename M>
+__global__ void k_cp_geo_cpl(DevCfg c, int64_t n, const double *aux, const int *typ, const int *nb, const int2 *oc,
+                             typename MT<M>::V4 *g4, M *gw) {
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (a >= n || !is_fluid(typ[a])) return;
     const double *xa = aux + a * ADJ_AUX;
-    const double rho = xa[6], dvol = mass[a] / rho;
-    double e = 0.0;
+    const M tor = (M)c.two_over_rc, cw = (M)(c.c_ihn * c.wcon);
     const int2 o = oc[a];
     for (int k = 0; k < o.y; k++) {
+        const int e = o.x + k;
         int sh[3];
-        const int i = table_entry(nb[o.x + k], sh);
-        double d[3], r, W, Wp;
-        image_d(c, xa, aux + (int64_t)i * ADJ_AUX, sh, d, r);
-        wc_kernel(c, r, W, Wp);
-        e += c.por_incr * W;
-        atomicAdd(&cmid[(int64_t)i * CP_NMID + CM_SHEP], dvol * W);
+        const int i = table_entry(nb[e], sh);
+        M d[3] = {0, 0, 0}, r2 = 0;
+        for (int q = 0; q < c.nd; q++) {
+            d[q] = (M)(xa[q] - image_pos(aux[(int64_t)i * ADJ_AUX + q], sh[q], c.rmin[q], c.rmax[q]));
+            r2 += d[q] * d[q];
+        }
+        const M r = MT<M>::root(r2), qq = r * tor;
+        M W = 0, wpr = 0;
+        if (!(qq > (M)2)) {
+            const M t = (M)2 - qq, t2 = t * t;
+            W = cw * (t2 * t2) * ((M)1 + (M)2 * qq);
+            if (r > (M)0) wpr = cw * ((M)-10 * qq * t2 * t) * tor / r;
+        }
+        g4[e] = MT<M>::make(d[0], d[1], d[2], wpr);
+        gw[e] = W;
     }
+}
+
+/* FPI pairs, one warp per DEM particle: d = r_i - r_b at the end positions,
+ * W = W(r / h_b, h_b) and W' / r with the fluid particle's h (sph.h:1708-1792) */
+template <typename M>
+__global__ void k_cp_geo_fpi(DevCfg c, int n_dem, const int *dem_tags, const double *s1, const double *hh,
+                             const int *nb, const int2 *oc, typename MT<M>::V4 *g4, M *gw) {
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n_dem) return;
+    const int64_t i = dem_tags[w];
+    const double *xi = s1 + i * ADJ_NC;
+    const M wcon = (M)c.wcon;
+    const int2 o = oc[i];
+    for (int k = lane; k < o.y; k += 32) {
+        const int e = o.x + k;
+        int sh[3];
+        const int b = table_entry(nb[e], sh);
+        M d[3] = {0, 0, 0}, r2 = 0;
+        for (int q = 0; q < c.nd; q++) {
+            d[q] = (M)(xi[q] - image_pos(s1[(int64_t)b * ADJ_NC + q], sh[q], c.rmin[q], c.rmax[q]));
+            r2 += d[q] * d[q];
+        }
+        const M r = MT<M>::root(r2), ih = (M)1 / (M)hh[b], qq = r * ih;
+        M W = 0, wpr = 0;
+        if (!(qq > (M)2)) {
+            M ihn = 1;
+            for (int dd = 0; dd < c.nd; dd++) ihn *= ih;
+            const M t = (M)2 - qq, t2 = t * t;
+            W = ihn * wcon * (t2 * t2) * ((M)1 + (M)2 * qq);
+            if (r > (M)0) wpr = ihn * wcon * ((M)-10 * qq * t2 * t) * ih / r;
+        }
+        g4[e] = MT<M>::make(d[0], d[1], d[2], wpr);
+        gw[e] = W;
+    }
+}
+
+/* porosity and EOS of the middle phase (forward), per fluid particle */
+template <typename M>
+__global__ void k_cp_por(DevCfg c, int64_t n, const double *aux, const int *typ, const int2 *oc, const M *gw,
+                         double *cmid) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a >= n || !is_fluid(typ[a])) return;
+    const double rho = aux[a * ADJ_AUX + 6];
+    typename MT<M>::Acc sw;
+    const int2 o = oc[a];
+    for (int k = 0; k < o.y; k++) sw.add(gw[o.x + k]);
+    const double e = c.por_incr * sw.value();
     double eps = 1.0 - e;
     const bool clamp = eps < 0.37;
     if (clamp) eps = 0.37;
@@ -377,6 +476,29 @@ __global__ void k_cp_por(DevCfg c, int64_t n, const double *aux, const double *m
     cmid[a * CP_NMID + CM_EPS] = eps;
     cmid[a * CP_NMID + CM_CLAMP] = clamp ? 1.0 : 0.0;
     cmid[a * CP_NMID + CM_PDR2] = c.prb * (x2 * x2 * x2 * x - 1.0) / (rho * rho);
+}
+
+/* Shepard sums of the middle phase (forward, calcShepSum sph.h:1303-1320),
+ * one warp per DEM particle over its fluid partners (transposed coupling
+ * table): shep_i = sum_a (m_a / rho_a) W_c(r_ai); also 1 / shep_i */
+template <typename M>
+__global__ void k_cp_shep(int n_dem, const int *dem_tags, const double *aux, const double *mass, const int *nbT,
+                          const int *ixT, const int2 *ocT, const M *gw, double *cmid) {
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n_dem) return;
+    const int64_t i = dem_tags[w];
+    const int2 o = ocT[i];
+    typename MT<M>::Acc s;
+    for (int k = lane; k < o.y; k += 32) {
+        const int a = nbT[o.x + k] & ((1 << SH_SHIFT) - 1);
+        s.add((M)(mass[a] * aux[(int64_t)a * ADJ_AUX + 7]) * gw[ixT[o.x + k]]);
+    }
+    const double sum = warp_sum_d(s.value());
+    if (lane == 0) {
+        cmid[i * CP_NMID + CM_SHEP] = sum;
+        cmid[i * CP_NMID + CM_ISHEP] = sum != 0.0 ? 1.0 / sum : 0.0;
+    }
 }
 
 /* Di Felice drag Phi(dv, por) = 1/2 A C_d |dv| por^-chi dv (sph.h:1593-1598)
@@ -425,136 +547,194 @@ __device__ __noinline__ double difelice_vjp(const DevCfg &c, const double *dv, d
 
 /* FPI + Di Felice drag of each DEM particle (end phase), one warp per DEM
  * particle: the lanes split its fluid partners for the forward sums (warp
- * reductions), every lane then runs the drag VJP on the reduced values, and
- * the lanes split the partners again to scatter the adjoints into the fluid
- * accumulators (FP64 atomics).  Delta_i's adjoint is that of f1 + fdrag1. */
+ * reductions), every lane then runs the drag VJP on the reduced values and
+ * the lanes split the partners again for the particle's own position
+ * adjoint.  The adjoints of the normalised sums go to the particle's
+ * coefficient record (CF_*), from which k_cp_fpi_fluid gathers each fluid
+ * particle's share.  Delta_i's adjoint is that of f1 + fdrag1.  Pair math in
+ * M, per-particle math in FP64. */
+template <typename M>
 __global__ void k_cp_fpi(DevCfg c, int n_dem, const int *dem_tags, double dt, const double *s1, const double *aux,
-                         const double *cmid, const double *mass, const double *hh, const int *nb, const int2 *oc,
-                         const double *adj, double *cacc, double *grads) {
+                         const double *cmid, const double *mass, const int *nb, const int2 *oc,
+                         const typename MT<M>::V4 *g4, const M *gw, const double *adj, double *cacc, double *coef,
+                         double *grads) {
+    using Acc = typename MT<M>::Acc;
     const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (w >= n_dem) return;
     const int64_t i = dem_tags[w];
-    const double *xi = s1 + i * ADJ_NC, *ai = adj + i * ADJ_NC;
+    const double *ai = adj + i * ADJ_NC;
     const double *vhm = aux + i * ADJ_AUX + 3;
+    double *cf = coef + i * CP_NCOEF;
     const int2 o = oc[i];
-    double sum = 0.0, Npor = 0.0, Nfp[3] = {0, 0, 0}, Nfv[3] = {0, 0, 0}, Nvel[3] = {0, 0, 0};
+    Acc sum, Npor, Nfp[3], Nfv[3], Nvel[3];
     for (int k = lane; k < o.y; k += 32) {
-        int sh[3];
-        const int b = table_entry(nb[o.x + k], sh);
+        const M W = gw[o.x + k];
+        if (W == (M)0) continue;
+        const int b = nb[o.x + k] & ((1 << SH_SHIFT) - 1);
         const double *xb = s1 + (int64_t)b * ADJ_NC;
-        double d[3], r;
-        image_d(c, xi, xb, sh, d, r);
-        const double hb = hh[b], q = r / hb;
-        if (q > 2.0) continue;
-        double ihn = 1.0;
-        for (int dd = 0; dd < c.nd; dd++) ihn /= hb;
-        const double t = 2.0 - q, t2 = t * t;
-        const double W = ihn * c.wcon * (t2 * t2) * (1.0 + 2.0 * q);
-        const double mb = mass[b], dvol = mb / aux[(int64_t)b * ADJ_AUX + 6];
-        sum += dvol * W;
-        Npor += dvol * W * cmid[(int64_t)b * CP_NMID + CM_EPS];
+        const M mb = (M)mass[b], dW = (M)(mass[b] * aux[(int64_t)b * ADJ_AUX + 7]) * W, mW = mb * W;
+        sum.add(dW);
+        Npor.add(dW * (M)cmid[(int64_t)b * CP_NMID + CM_EPS]);
         for (int q3 = 0; q3 < c.nd; q3++) {
-            Nfp[q3] += mb * W * xb[AS_FP + q3];
-            Nfv[q3] += (mb * W + dvol * W) * xb[AS_FV + q3];
-            Nvel[q3] += dvol * W * xb[AS_VH + q3];
+            Nfp[q3].add(mW * (M)xb[AS_FP + q3]);
+            Nfv[q3].add((mW + dW) * (M)xb[AS_FV + q3]);
+            Nvel[q3].add(dW * (M)xb[AS_VH + q3]);
         }
     }
-    sum = warp_sum_d(sum);
-    Npor = warp_sum_d(Npor);
+    const double sumv = warp_sum_d(sum.value());
+    if (!(sumv > 0.5)) {             /* no drag, Delta = 0 (uniform over the warp) */
+        if (lane == 0) cf[CF_ON] = 0.0;
+        return;
+    }
+    double npor = warp_sum_d(Npor.value()), nfp[3], nfv[3], nvel[3];
     for (int q = 0; q < 3; q++) {
-        Nfp[q] = warp_sum_d(Nfp[q]);
-        Nfv[q] = warp_sum_d(Nfv[q]);
-        Nvel[q] = warp_sum_d(Nvel[q]);
+        nfp[q] = warp_sum_d(Nfp[q].value());
+        nfv[q] = warp_sum_d(Nfv[q].value());
+        nvel[q] = warp_sum_d(Nvel[q].value());
     }
-    if (!(sum > 0.5)) return;       /* no drag, Delta = 0 (uniform over the warp) */
-    const double mi = mass[i], rs = 1.0 / sum;
-    const double por = Npor * rs;
-    double fvel[3] = {0, 0, 0}, fpfb[3] = {0, 0, 0}, fvv[3] = {0, 0, 0}, dv[3] = {0, 0, 0}, Db[3] = {0, 0, 0};
-    for (int q = 0; q < c.nd; q++) {
-        fvel[q] = Nvel[q] * rs;
-        fpfb[q] = Nfp[q] * rs;
-        fvv[q] = Nfv[q] * rs;
-        dv[q] = por * (fvel[q] - vhm[q]);
-        Db[q] = ai[AS_F + q] + dt * (ai[AS_V + q] + ai[AS_VH + q]) + ai[AS_FDRAG + q];
-    }
-    /* Delta = (V/m)(fv + fpfb) + (rho0/m) kappa Phi */
-    double phi[3];
-    difelice(c, dv, por, phi);
-    double Pb[3] = {0, 0, 0}, dvb[3] = {0, 0, 0}, porb = 0.0, gkap = 0.0;
-    for (int q = 0; q < c.nd; q++) {
-        Pb[q] = (c.dens / mi) * c.drag_scale * Db[q];
-        gkap += (c.dens / mi) * Db[q] * phi[q];
-    }
-    const double gnu = difelice_vjp(c, dv, por, Pb, dvb, porb);
-    double fvelb[3] = {0, 0, 0}, ownvh[3] = {0, 0, 0};
-    for (int q = 0; q < c.nd; q++) {
-        fvelb[q] = por * dvb[q];
-        ownvh[q] = -por * dvb[q];
-        porb += (fvel[q] - vhm[q]) * dvb[q];
-    }
-    const double vm = c.dem_vol / mi;
-    double sumb = -porb * por;
-    double NfpB[3] = {0, 0, 0}, NfvB[3] = {0, 0, 0}, NvelB[3] = {0, 0, 0};
-    for (int q = 0; q < c.nd; q++) {
-        sumb -= vm * Db[q] * fpfb[q] + vm * Db[q] * fvv[q] + fvelb[q] * fvel[q];
-        NfpB[q] = vm * Db[q] * rs;
-        NfvB[q] = vm * Db[q] * rs;
-        NvelB[q] = fvelb[q] * rs;
-    }
-    sumb *= rs;
-    const double NporB = porb * rs;
-    double own_r[3] = {0, 0, 0};
-    for (int k = lane; k < o.y; k += 32) {
-        int sh[3];
-        const int b = table_entry(nb[o.x + k], sh);
-        const double *xb = s1 + (int64_t)b * ADJ_NC;
-        double d[3], r;
-        image_d(c, xi, xb, sh, d, r);
-        const double hb = hh[b], q = r / hb;
-        if (q > 2.0) continue;
-        double ihn = 1.0;
-        for (int dd = 0; dd < c.nd; dd++) ihn /= hb;
-        const double t = 2.0 - q, t2 = t * t;
-        const double W = ihn * c.wcon * (t2 * t2) * (1.0 + 2.0 * q);
-        const double Wp = ihn * c.wcon * (-10.0 * q * t2 * t) / hb;
-        const double mb = mass[b], rhob = aux[(int64_t)b * ADJ_AUX + 6], dvol = mb / rhob;
-        const double epsb = cmid[(int64_t)b * CP_NMID + CM_EPS];
-        double vfp = 0.0, vfv = 0.0, vvel = 0.0;
-        for (int q3 = 0; q3 < c.nd; q3++) {
-            vfp += NfpB[q3] * xb[AS_FP + q3];
-            vfv += NfvB[q3] * xb[AS_FV + q3];
-            vvel += NvelB[q3] * xb[AS_VH + q3];
-        }
-        const double Wb = dvol * (sumb + NporB * epsb + vvel) + mb * vfp + (mb + dvol) * vfv;
-        const double dvolb = W * (sumb + NporB * epsb + vvel + vfv);
-        double *acc = cacc + (int64_t)b * CP_NACC;
-        atomicAdd(&acc[CA_RHO], -dvolb * dvol / rhob);
-        atomicAdd(&acc[CA_EPS], dvol * W * NporB);
-        if (r > 0.0) {
-            for (int q3 = 0; q3 < c.nd; q3++) {
-                const double gq = Wb * Wp * d[q3] / r;
-                own_r[q3] += gq;
-                atomicAdd(&acc[CA_R1 + q3], -gq);
-            }
-        }
-        for (int q3 = 0; q3 < c.nd; q3++) {
-            atomicAdd(&acc[CA_FP + q3], mb * W * NfpB[q3]);
-            atomicAdd(&acc[CA_FV + q3], (mb + dvol) * W * NfvB[q3]);
-            atomicAdd(&acc[CA_VH1 + q3], dvol * W * NvelB[q3]);
-        }
-    }
-    for (int q = 0; q < 3; q++) own_r[q] = warp_sum_d(own_r[q]);
+    /* the particle's own FP64 math (drag law and its VJP, with its
+     * transcendentals) once per warp, on lane 0; the lanes take the adjoints
+     * of the sums from its coefficient record */
     if (lane == 0) {
+        const double mi = mass[i], rs = 1.0 / sumv;
+        const double por = npor * rs;
+        double fvel[3] = {0, 0, 0}, fpfb[3] = {0, 0, 0}, fvv[3] = {0, 0, 0}, dv[3] = {0, 0, 0}, Db[3] = {0, 0, 0};
+        for (int q = 0; q < c.nd; q++) {
+            fvel[q] = nvel[q] * rs;
+            fpfb[q] = nfp[q] * rs;
+            fvv[q] = nfv[q] * rs;
+            dv[q] = por * (fvel[q] - vhm[q]);
+            Db[q] = ai[AS_F + q] + dt * (ai[AS_V + q] + ai[AS_VH + q]) + ai[AS_FDRAG + q];
+        }
+        /* Delta = (V/m)(fv + fpfb) + (rho0/m) kappa Phi */
+        double phi[3];
+        difelice(c, dv, por, phi);
+        double Pb[3] = {0, 0, 0}, dvb[3] = {0, 0, 0}, porb = 0.0, gkap = 0.0;
+        for (int q = 0; q < c.nd; q++) {
+            Pb[q] = (c.dens / mi) * c.drag_scale * Db[q];
+            gkap += (c.dens / mi) * Db[q] * phi[q];
+        }
+        const double gnu = difelice_vjp(c, dv, por, Pb, dvb, porb);
+        double fvelb[3] = {0, 0, 0};
         double *acc = cacc + i * CP_NACC;
         for (int q = 0; q < c.nd; q++) {
-            acc[CA_R1 + q] += own_r[q];
-            acc[CA_VH1 + q] += ownvh[q];
+            fvelb[q] = por * dvb[q];
+            acc[CA_VH1 + q] += -por * dvb[q];
+            porb += (fvel[q] - vhm[q]) * dvb[q];
         }
+        const double vm = c.dem_vol / mi;
+        double sumb = -porb * por;
+        cf[CF_ON] = 1.0;
+        for (int q = 0; q < 3; q++) {
+            const bool on = q < c.nd;
+            if (on) sumb -= vm * Db[q] * fpfb[q] + vm * Db[q] * fvv[q] + fvelb[q] * fvel[q];
+            cf[CF_FP + q] = on ? vm * Db[q] * rs : 0.0;
+            cf[CF_FV + q] = on ? vm * Db[q] * rs : 0.0;
+            cf[CF_VEL + q] = on ? fvelb[q] * rs : 0.0;
+        }
+        cf[CF_SUM] = sumb * rs;
+        cf[CF_POR] = porb * rs;
         if (gnu != 0.0 || gkap != 0.0) {
             atomicAdd(&grads[3], gnu);
             atomicAdd(&grads[4], gkap);
         }
+    }
+    __syncwarp();
+    const M sumbM = (M)cf[CF_SUM], NporBM = (M)cf[CF_POR];
+    M NfpBM[3], NfvBM[3], NvelBM[3];
+    for (int q = 0; q < 3; q++) {
+        NfpBM[q] = (M)cf[CF_FP + q];
+        NfvBM[q] = (M)cf[CF_FV + q];
+        NvelBM[q] = (M)cf[CF_VEL + q];
+    }
+    Acc own_r[3];
+    for (int k = lane; k < o.y; k += 32) {
+        const typename MT<M>::V4 gd = g4[o.x + k];
+        if (gd.w == (M)0) continue;
+        const int b = nb[o.x + k] & ((1 << SH_SHIFT) - 1);
+        const double *xb = s1 + (int64_t)b * ADJ_NC;
+        const M mb = (M)mass[b], dvol = (M)(mass[b] * aux[(int64_t)b * ADJ_AUX + 7]);
+        const M epsb = (M)cmid[(int64_t)b * CP_NMID + CM_EPS];
+        M vfp = 0, vfv = 0, vvel = 0;
+        for (int q3 = 0; q3 < c.nd; q3++) {
+            vfp += NfpBM[q3] * (M)xb[AS_FP + q3];
+            vfv += NfvBM[q3] * (M)xb[AS_FV + q3];
+            vvel += NvelBM[q3] * (M)xb[AS_VH + q3];
+        }
+        const M Wb = dvol * (sumbM + NporBM * epsb + vvel) + mb * vfp + (mb + dvol) * vfv;
+        const M dd[3] = {gd.x, gd.y, gd.z};
+        for (int q3 = 0; q3 < c.nd; q3++) own_r[q3].add(Wb * gd.w * dd[q3]);
+    }
+    double own[3];
+    for (int q = 0; q < 3; q++) own[q] = warp_sum_d(own_r[q].value());
+    if (lane == 0) {
+        double *acc = cacc + i * CP_NACC;
+        for (int q = 0; q < c.nd; q++) acc[CA_R1 + q] += own[q];
+    }
+}
+
+/* the fluid side of k_cp_fpi: each fluid particle gathers, over its DEM FPI
+ * partners (transposed FPI table), the adjoints of its density, porosity,
+ * end position, velocity and force parts that the partners' normalised sums
+ * give it */
+template <typename M>
+__global__ void k_cp_fpi_fluid(int64_t n, int nd, const double *s1, const double *aux, const double *cmid,
+                               const double *mass, const int *typ, const int *nbT, const int *ixT, const int2 *ocT,
+                               const typename MT<M>::V4 *g4, const M *gw, const double *coef, double *cacc) {
+    using Acc = typename MT<M>::Acc;
+    const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (b >= n || !is_fluid(typ[b])) return;
+    const int2 o = ocT[b];
+    if (o.y == 0) return;
+    const double *xb = s1 + b * ADJ_NC;
+    const M mb = (M)mass[b], irho = (M)aux[b * ADJ_AUX + 7], dvol = (M)(mass[b] * aux[b * ADJ_AUX + 7]);
+    const M epsb = (M)cmid[b * CP_NMID + CM_EPS];
+    M fp[3] = {0, 0, 0}, fv[3] = {0, 0, 0}, vh[3] = {0, 0, 0};
+    for (int q = 0; q < nd; q++) {
+        fp[q] = (M)xb[AS_FP + q];
+        fv[q] = (M)xb[AS_FV + q];
+        vh[q] = (M)xb[AS_VH + q];
+    }
+    Acc arho, aeps, ar[3], afp[3], afv[3], avh[3];
+    for (int k = 0; k < o.y; k++) {
+        const int e = ixT[o.x + k];
+        const M W = gw[e];
+        if (W == (M)0) continue;
+        const int i = nbT[o.x + k] & ((1 << SH_SHIFT) - 1);
+        const double *cf = coef + (int64_t)i * CP_NCOEF;
+        if (cf[CF_ON] == 0.0) continue;
+        const typename MT<M>::V4 gd = g4[e];                   /* d = r_i - r_b */
+        const M sumb = (M)cf[CF_SUM], NporB = (M)cf[CF_POR];
+        M cfp[3], cfv[3], cvel[3], vfp = 0, vfv = 0, vvel = 0;
+        for (int q3 = 0; q3 < 3; q3++) {
+            cfp[q3] = (M)cf[CF_FP + q3];
+            cfv[q3] = (M)cf[CF_FV + q3];
+            cvel[q3] = (M)cf[CF_VEL + q3];
+            vfp += cfp[q3] * fp[q3];
+            vfv += cfv[q3] * fv[q3];
+            vvel += cvel[q3] * vh[q3];
+        }
+        const M Wb = dvol * (sumb + NporB * epsb + vvel) + mb * vfp + (mb + dvol) * vfv;
+        const M dvolb = W * (sumb + NporB * epsb + vvel + vfv);
+        arho.add(-dvolb * dvol * irho);
+        aeps.add(dvol * W * NporB);
+        const M dd[3] = {gd.x, gd.y, gd.z};
+        for (int q3 = 0; q3 < nd; q3++) {
+            ar[q3].add(-Wb * gd.w * dd[q3]);
+            afp[q3].add(mb * W * cfp[q3]);
+            afv[q3].add((mb + dvol) * W * cfv[q3]);
+            avh[q3].add(dvol * W * cvel[q3]);
+        }
+    }
+    double *acc = cacc + b * CP_NACC;
+    acc[CA_RHO] += arho.value();
+    acc[CA_EPS] += aeps.value();
+    for (int q = 0; q < nd; q++) {
+        acc[CA_R1 + q] += ar[q].value();
+        acc[CA_FP + q] += afp[q].value();
+        acc[CA_FV + q] += afv[q].value();
+        acc[CA_VH1 + q] += avh[q].value();
     }
 }
 
@@ -783,85 +963,286 @@ __global__ void k_cp_force(DevCfg c, int64_t n, const double *aux, const double 
     if ((threadIdx.x & 31) == 0 && gnu != 0.0) atomicAdd(&grads[3], gnu);
 }
 
-/* porosity and DEM -> fluid drag of the middle phase, per fluid particle */
-__global__ void k_cp_cpl_a(DevCfg c, int64_t n, const double *s0, const double *aux, const double *cmid,
-                           const double *cend, const double *mass, const int *typ, const int *nb, const int2 *oc,
-                           double *cacc) {
-    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (a >= n || !is_fluid(typ[a])) return;
-    const double *xa = aux + a * ADJ_AUX;
-    double *ac = cacc + a * CP_NACC;
-    const double eb = ac[CA_EBAR], rhoa = xa[6];
-    const double *F = cend + a * CP_NEND + CE_F;
+/* Porosity (e = sum V W_c), DEM -> fluid drag and Shepard sums of the middle
+ * phase, DEM side: one warp per DEM particle over its fluid partners
+ * (transposed coupling table).  The particle's adjoints of the lagged drag
+ * fdrag0 and of its Shepard sum come first (warp sums), then its position
+ * adjoint from both the drag / porosity terms and the Shepard terms. */
+template <typename M>
+__global__ void k_cp_cpl_dem(DevCfg c, int n_dem, const int *dem_tags, const double *s0, const double *aux,
+                             const double *cmid, const double *cend, const double *mass, const int *nbT,
+                             const int *ixT, const int2 *ocT, const typename MT<M>::V4 *g4, const M *gw,
+                             double *cacc) {
+    using Acc = typename MT<M>::Acc;
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n_dem) return;
+    const int64_t i = dem_tags[w];
+    const int2 o = ocT[i];
     const double f2d = c.nd == 2 ? 1.0 / (2.0 * c.dem_radius) : 1.0;
-    double rb[3] = {0, 0, 0}, rhob = 0.0;
-    const int2 o = oc[a];
-    for (int k = 0; k < o.y; k++) {
-        int sh[3];
-        const int i = table_entry(nb[o.x + k], sh);
-        double d[3], r, W, Wp;
-        image_d(c, xa, aux + (int64_t)i * ADJ_AUX, sh, d, r);
-        wc_kernel(c, r, W, Wp);
-        double Wbar = eb * c.por_incr;                          /* e = sum V W_c */
-        const double shep = cmid[(int64_t)i * CP_NMID + CM_SHEP];
+    const double shep = cmid[i * CP_NMID + CM_SHEP], ishep = cmid[i * CP_NMID + CM_ISHEP];
+    const M Ki = (M)(mass[i] * f2d * ishep), ishepM = (M)ishep, pinc = (M)c.por_incr;
+    M fd0[3] = {0, 0, 0};
+    for (int q = 0; q < c.nd; q++) fd0[q] = (M)s0[i * ADJ_NC + AS_FDRAG + q];
+    Acc fd0b[3], shepb, rs[3];
+    for (int k = lane; k < o.y; k += 32) {
+        const int e = ixT[o.x + k], a = nbT[o.x + k] & ((1 << SH_SHIFT) - 1);
+        const typename MT<M>::V4 gd = g4[e];                   /* d = r_a - r_i */
+        const M W = gw[e];
+        M Wbar = (M)cacc[(int64_t)a * CP_NACC + CA_EBAR] * pinc;   /* e = sum V W_c */
         if (shep != 0.0) {
-            const double *fd0 = s0 + (int64_t)i * ADJ_NC + AS_FDRAG;
-            const double mi = mass[i], sc = mi * f2d / (rhoa * shep), s = sc * W;
-            double Ff = 0.0;
-            double *ai = cacc + (int64_t)i * CP_NACC;
+            const double *F = cend + (int64_t)a * CP_NEND + CE_F;
+            const M sc = Ki * (M)aux[(int64_t)a * ADJ_AUX + 7], sw = sc * W;
+            M Ff = 0;
             for (int q = 0; q < c.nd; q++) {
-                Ff += F[q] * fd0[q];
-                atomicAdd(&ai[CA_FD0 + q], -s * F[q]);          /* fd_a = -sum s fdrag0_i */
+                const M Fq = (M)F[q];
+                Ff += Fq * fd0[q];
+                fd0b[q].add(-sw * Fq);                           /* fd_a = -sum s fdrag0_i */
             }
-            const double sb = -Ff;
-            Wbar += sb * sc;
-            rhob += -sb * s / rhoa;
-            atomicAdd(&ai[CA_SHEP], -sb * s / shep);
+            Wbar -= Ff * sc;
+            shepb.add(Ff * sw * ishepM);
         }
-        if (r > 0.0 && Wbar != 0.0) {
-            double *ai = cacc + (int64_t)i * CP_NACC;
-            for (int q = 0; q < c.nd; q++) {
-                const double gq = Wbar * Wp * d[q] / r;
-                rb[q] += gq;
-                atomicAdd(&ai[CA_RS + q], -gq);
-            }
+        const M gw2 = Wbar * gd.w;
+        rs[0].add(-gw2 * gd.x);
+        rs[1].add(-gw2 * gd.y);
+        rs[2].add(-gw2 * gd.z);
+    }
+    const double shepbv = warp_sum_d(shepb.value());
+    if (shepbv != 0.0) {
+        /* shep_i = sum_a (m_a / rho_a) W_c(r_ai) */
+        const M sb = (M)shepbv;
+        for (int k = lane; k < o.y; k += 32) {
+            const int e = ixT[o.x + k], a = nbT[o.x + k] & ((1 << SH_SHIFT) - 1);
+            const typename MT<M>::V4 gd = g4[e];
+            const M gw2 = sb * (M)(mass[a] * aux[(int64_t)a * ADJ_AUX + 7]) * gd.w;
+            rs[0].add(-gw2 * gd.x);
+            rs[1].add(-gw2 * gd.y);
+            rs[2].add(-gw2 * gd.z);
         }
     }
-    for (int q = 0; q < c.nd; q++) ac[CA_RS + q] += rb[q];
-    ac[CA_RHOS] += rhob;
+    double fb[3], rr[3];
+    for (int q = 0; q < 3; q++) {
+        fb[q] = warp_sum_d(fd0b[q].value());
+        rr[q] = warp_sum_d(rs[q].value());
+    }
+    if (lane == 0) {
+        double *ai = cacc + i * CP_NACC;
+        for (int q = 0; q < c.nd; q++) {
+            ai[CA_FD0 + q] += fb[q];
+            ai[CA_RS + q] += rr[q];
+        }
+        ai[CA_SHEP] += shepbv;
+    }
 }
 
-/* Shepard sums of the middle phase, per fluid particle */
-__global__ void k_cp_cpl_b(DevCfg c, int64_t n, const double *aux, const double *mass, const int *typ,
-                           const int *nb, const int2 *oc, double *cacc) {
+/* the same terms, fluid side: each fluid particle's position and density
+ * adjoints over its DEM partners (coupling table), with the partners'
+ * Shepard-sum adjoints from k_cp_cpl_dem */
+template <typename M>
+__global__ void k_cp_cpl_fluid(DevCfg c, int64_t n, const double *s0, const double *aux, const double *cmid,
+                               const double *cend, const double *mass, const int *typ, const int *nb, const int2 *oc,
+                               const typename MT<M>::V4 *g4, const M *gw, double *cacc) {
+    using Acc = typename MT<M>::Acc;
     const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (a >= n || !is_fluid(typ[a])) return;
-    const double *xa = aux + a * ADJ_AUX;
     double *ac = cacc + a * CP_NACC;
-    const double rhoa = xa[6], ma = mass[a];
-    double rb[3] = {0, 0, 0}, rhob = 0.0;
+    const M ebp = (M)(ac[CA_EBAR] * c.por_incr), irho = (M)aux[a * ADJ_AUX + 7], ma = (M)mass[a];
+    const M f2d = (M)(c.nd == 2 ? 1.0 / (2.0 * c.dem_radius) : 1.0);
+    M F[3] = {0, 0, 0};
+    for (int q = 0; q < c.nd; q++) F[q] = (M)cend[a * CP_NEND + CE_F + q];
+    Acc rb[3], rhob;
     const int2 o = oc[a];
     for (int k = 0; k < o.y; k++) {
-        int sh[3];
-        const int i = table_entry(nb[o.x + k], sh);
-        double *ai = cacc + (int64_t)i * CP_NACC;
-        const double sb = ai[CA_SHEP];
-        if (sb == 0.0) continue;
-        double d[3], r, W, Wp;
-        image_d(c, xa, aux + (int64_t)i * ADJ_AUX, sh, d, r);
-        wc_kernel(c, r, W, Wp);
-        rhob += -sb * ma * W / (rhoa * rhoa);
-        if (r > 0.0) {
-            const double Wbar = sb * ma / rhoa;
-            for (int q = 0; q < c.nd; q++) {
-                const double gq = Wbar * Wp * d[q] / r;
-                rb[q] += gq;
-                atomicAdd(&ai[CA_RS + q], -gq);
-            }
+        const int e = o.x + k, i = nb[e] & ((1 << SH_SHIFT) - 1);
+        const typename MT<M>::V4 gd = g4[e];                   /* d = r_a - r_i */
+        const M W = gw[e];
+        M Wbar = ebp;
+        const double ishep = cmid[(int64_t)i * CP_NMID + CM_ISHEP];
+        if (ishep != 0.0) {
+            const double *fd0 = s0 + (int64_t)i * ADJ_NC + AS_FDRAG;
+            const M sc = (M)mass[i] * f2d * irho * (M)ishep, sw = sc * W;
+            M Ff = 0;
+            for (int q = 0; q < c.nd; q++) Ff += F[q] * (M)fd0[q];
+            Wbar -= Ff * sc;
+            rhob.add(Ff * sw * irho);
         }
+        const double sbi = cacc[(int64_t)i * CP_NACC + CA_SHEP];
+        if (sbi != 0.0) {
+            const M t = (M)sbi * ma * irho;
+            rhob.add(-t * W * irho);
+            Wbar += t;
+        }
+        const M gw2 = Wbar * gd.w;
+        rb[0].add(gw2 * gd.x);
+        rb[1].add(gw2 * gd.y);
+        rb[2].add(gw2 * gd.z);
     }
-    for (int q = 0; q < c.nd; q++) ac[CA_RS + q] += rb[q];
-    ac[CA_RHOS] += rhob;
+    for (int q = 0; q < c.nd; q++) ac[CA_RS + q] += rb[q].value();
+    ac[CA_RHOS] += rhob.value();
+}
+
+/* ---- transposed pair tables: each partner's owners ------------------------
+ * For a table of owners o -> partners p (entry p | shift code), each
+ * partner's owners (key o | shift code, kept for a fixed order) and the
+ * index of the pair's entry in the owners' table (its geometry record),
+ * sorted by key so that the gathers over them sum in a fixed order.
+ * Counting (int atomics), an exclusive scan of the counts, filling,
+ * ranking.  Fluid-owned tables (coupling: few partners per owner) take a
+ * thread per owner; DEM-owned tables (FPI: ~100 partners per owner) a warp
+ * per DEM particle. */
+template <bool DEM_OWNERS>
+__global__ void k_tr_count(int64_t n, int n_dem, const int *dem_tags, const int *nb, const int2 *oc, int *tcnt) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t o = DEM_OWNERS ? ((t >> 5) < n_dem ? dem_tags[t >> 5] : -1) : (t < n ? t : -1);
+    if (o < 0) return;
+    const int step = DEM_OWNERS ? 32 : 1;
+    const int2 q = oc[o];
+    for (int k = DEM_OWNERS ? (threadIdx.x & 31) : 0; k < q.y; k += step)
+        atomicAdd(&tcnt[nb[q.x + k] & ((1 << SH_SHIFT) - 1)], 1);
+}
+
+template <bool DEM_OWNERS>
+__global__ void k_tr_fill(int64_t n, int n_dem, const int *dem_tags, const int *nb, const int2 *oc, const int *toff,
+                          int *tfill, int2 *tmp) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t o = DEM_OWNERS ? ((t >> 5) < n_dem ? dem_tags[t >> 5] : -1) : (t < n ? t : -1);
+    if (o < 0) return;
+    const int step = DEM_OWNERS ? 32 : 1;
+    const int2 q = oc[o];
+    for (int k = DEM_OWNERS ? (threadIdx.x & 31) : 0; k < q.y; k += step) {
+        int sh[3];
+        const int p = table_entry(nb[q.x + k], sh);
+        for (int d = 0; d < 3; d++) sh[d] = -sh[d];
+        tmp[toff[p] + atomicAdd(&tfill[p], 1)] = make_int2((int)o | shift_code(sh), q.x + k);
+    }
+}
+
+/* DEM partners (long lists): one warp per DEM particle, each entry to its
+ * rank among the partner's keys (keys are distinct) */
+__global__ void k_tr_rank_dem(int n_dem, const int *dem_tags, const int *toff, const int2 *tmp, int *tnb, int *tix,
+                              int2 *toc) {
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n_dem) return;
+    const int64_t p = dem_tags[w];
+    const int b0 = toff[p], m = toff[p + 1] - b0;
+    for (int k = lane; k < m; k += 32) {
+        const int2 v = tmp[b0 + k];
+        int r = 0;
+        for (int j = 0; j < m; j++) r += (unsigned)tmp[b0 + j].x < (unsigned)v.x;
+        tnb[b0 + r] = v.x;
+        tix[b0 + r] = v.y;
+    }
+    if (lane == 0) toc[p] = make_int2(b0, m);
+}
+
+/* fluid partners (a few entries each): one thread per particle, insertion
+ * sort by key */
+__global__ void k_tr_rank_fluid(int64_t n, const int *toff, const int2 *tmp, int *tnb, int *tix, int2 *toc) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const int b0 = toff[p], m = toff[p + 1] - b0;
+    for (int k = 0; k < m; k++) {
+        const int2 v = tmp[b0 + k];
+        int r = 0;
+        for (int j = 0; j < m; j++) r += (unsigned)tmp[b0 + j].x < (unsigned)v.x;
+        tnb[b0 + r] = v.x;
+        tix[b0 + r] = v.y;
+    }
+    toc[p] = make_int2(b0, m);
+}
+
+/* exclusive scan of cnt[0, n) into off[0, n], off[n] = total: tiles of
+ * SC_TILE counts per block, one block scanning the tile sums */
+constexpr int SC_THREADS = 256, SC_PER = 4, SC_TILE = SC_THREADS * SC_PER;
+
+__device__ int block_scan_excl(int v, int *total) {
+    __shared__ int ws[SC_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int t = lane < SC_THREADS / 32 ? ws[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        if (lane < SC_THREADS / 32) ws[lane] = t;
+    }
+    __syncthreads();
+    const int before = wid > 0 ? ws[wid - 1] : 0;
+    if (total) *total = ws[SC_THREADS / 32 - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_sc_tiles(const int *cnt, int64_t n, int *tsum) {
+    const int64_t base = (int64_t)blockIdx.x * SC_TILE + threadIdx.x * SC_PER;
+    int v = 0;
+    for (int k = 0; k < SC_PER; k++)
+        if (base + k < n) v += cnt[base + k];
+    int total = 0;
+    block_scan_excl(v, &total);
+    if (threadIdx.x == 0) tsum[blockIdx.x] = total;
+}
+
+constexpr int SC_SUMS_PER = 16;   /* one block scans up to SC_THREADS * 16 tile sums (4M counts) */
+__global__ void __launch_bounds__(SC_THREADS) k_sc_sums(int *tsum, int ntiles) {
+    const int base = threadIdx.x * SC_SUMS_PER;
+    int v[SC_SUMS_PER], acc = 0;
+    for (int k = 0; k < SC_SUMS_PER; k++) {
+        v[k] = base + k < ntiles ? tsum[base + k] : 0;
+        acc += v[k];
+    }
+    int run = block_scan_excl(acc, nullptr);
+    for (int k = 0; k < SC_SUMS_PER; k++) {
+        if (base + k < ntiles) tsum[base + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void __launch_bounds__(SC_THREADS) k_sc_down(const int *cnt, int64_t n, const int *tsum, int *off) {
+    const int64_t base = (int64_t)blockIdx.x * SC_TILE + threadIdx.x * SC_PER;
+    int v[SC_PER], acc = 0;
+    for (int k = 0; k < SC_PER; k++) {
+        v[k] = base + k < n ? cnt[base + k] : 0;
+        acc += v[k];
+    }
+    int run = block_scan_excl(acc, nullptr) + tsum[blockIdx.x];
+    for (int k = 0; k < SC_PER; k++) {
+        if (base + k < n) off[base + k] = run;
+        run += v[k];
+        if (base + k == n - 1) off[n] = run;
+    }
+}
+
+/* the transposed table of (nb, oc) into (tnb, tix, toc); DEM_OWNERS: the
+ * owners are the DEM particles (dem_tags), else every particle */
+template <bool DEM_OWNERS>
+void transpose(sphdem_ctx *c, AdjointData *a, const int *nb, const int2 *oc, TrTable &t) {
+    const int64_t n = c->n;
+    TrScratch &w = a->trw;
+    const int ntiles = (int)((n + SC_TILE - 1) / SC_TILE);
+    if (ntiles > SC_THREADS * SC_SUMS_PER) throw std::string("transpose: too many particles");
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(w.cnt, 0, (size_t)n * sizeof(int), c->stream));
+    SPHDEM_CUDA_CHECK(cudaMemsetAsync(w.fill, 0, (size_t)n * sizeof(int), c->stream));
+    const int nd = a->n_dem;
+    const int go = DEM_OWNERS ? grid_for((int64_t)std::max(1, nd) * 32, CB) : grid_for(n, CB);
+    SPHDEM_LAUNCH(c, "adj_tr_count", k_tr_count<DEM_OWNERS>, go, CB, 0, n, nd, a->dem_tags, nb, oc, w.cnt);
+    SPHDEM_LAUNCH(c, "adj_tr_scan", k_sc_tiles, ntiles, SC_THREADS, 0, w.cnt, n, w.tsum);
+    SPHDEM_LAUNCH(c, "adj_tr_scan", k_sc_sums, 1, SC_THREADS, 0, w.tsum, ntiles);
+    SPHDEM_LAUNCH(c, "adj_tr_scan", k_sc_down, ntiles, SC_THREADS, 0, w.cnt, n, w.tsum, w.off);
+    SPHDEM_LAUNCH(c, "adj_tr_fill", k_tr_fill<DEM_OWNERS>, go, CB, 0, n, nd, a->dem_tags, nb, oc, w.off, w.fill, w.tmp);
+    if (DEM_OWNERS)
+        SPHDEM_LAUNCH(c, "adj_tr_rank", k_tr_rank_fluid, grid_for(n, CB), CB, 0, n, w.off, w.tmp, t.nb, t.ix, t.oc);
+    else if (nd > 0)
+        SPHDEM_LAUNCH(c, "adj_tr_rank", k_tr_rank_dem, grid_for((int64_t)nd * 32, CB), CB, 0, nd, a->dem_tags, w.off,
+                      w.tmp, t.nb, t.ix, t.oc);
 }
 
 /* the adjoint of the state before the step */
@@ -1135,10 +1516,29 @@ void cpl_count_tables(sphdem_ctx *c, AdjointData *a) {
 }
 
 void cpl_alloc(sphdem_ctx *c, AdjointData *a) {
-    const int K = a->K;
+    const int K = a->K * a->nblk;   /* step slots of the tape store */
     const int64_t n = c->n;
     a->cpl.alloc(K, n);
     a->fpi.alloc(K, n);
+    /* one step's transposed coupling and FPI tables, their scratch, the pair
+     * geometry of both tables, and the DEM particles' FPI coefficient records */
+    const size_t ge = c->cfg.precision == SPHDEM_PREC_MIXED ? sizeof(float) : sizeof(double);
+    for (TrTable *t : {&a->cplT, &a->fpiT}) {
+        const int64_t cap = t == &a->cplT ? a->cpl.cap : a->fpi.cap;
+        SPHDEM_CUDA_CHECK(cudaMalloc(&t->nb, (size_t)cap * sizeof(int)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&t->ix, (size_t)cap * sizeof(int)));
+        SPHDEM_CUDA_CHECK(cudaMalloc(&t->oc, (size_t)n * sizeof(int2)));
+    }
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->g4_cpl, (size_t)a->cpl.cap * 4 * ge));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->gw_cpl, (size_t)a->cpl.cap * ge));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->g4_fpi, (size_t)a->fpi.cap * 4 * ge));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->gw_fpi, (size_t)a->fpi.cap * ge));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->trw.cnt, (size_t)n * sizeof(int)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->trw.fill, (size_t)n * sizeof(int)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->trw.off, (size_t)(n + 1) * sizeof(int)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->trw.tsum, (size_t)SC_THREADS * SC_SUMS_PER * sizeof(int)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->trw.tmp, (size_t)std::max(a->cpl.cap, a->fpi.cap) * sizeof(int2)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->coef, (size_t)n * CP_NCOEF * sizeof(double)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->ct.nb, (size_t)K * a->ct_cap * sizeof(int)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->ct.oc, (size_t)K * n * sizeof(int2)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->ct.cnt, (size_t)K * sizeof(int)));
@@ -1156,6 +1556,16 @@ void cpl_free(AdjointData *a) {
     a->cpl.free_all();
     a->fpi.free_all();
     a->ct.free_all();
+    for (int *p : {a->cplT.nb, a->cplT.ix, a->fpiT.nb, a->fpiT.ix, a->trw.cnt, a->trw.fill, a->trw.off, a->trw.tsum})
+        cudaFree(p);
+    for (void *p : {(void *)a->cplT.oc, (void *)a->fpiT.oc, (void *)a->trw.tmp, (void *)a->coef, a->g4_cpl, a->gw_cpl,
+                    a->g4_fpi, a->gw_fpi})
+        cudaFree(p);
+    a->g4_cpl = a->gw_cpl = a->g4_fpi = a->gw_fpi = nullptr;
+    a->cplT = TrTable{};
+    a->fpiT = TrTable{};
+    a->trw = TrScratch{};
+    a->coef = nullptr;
     cudaFree(a->rmid);
     cudaFree(a->cacc);
     cudaFree(a->cend);
@@ -1170,22 +1580,39 @@ void cpl_free(AdjointData *a) {
 }
 
 void cpl_reset_segment(sphdem_ctx *c, AdjointData *a) {
-    const size_t ocb = (size_t)a->K * c->n * sizeof(int2);
+    const size_t ocb = (size_t)a->K * c->n * sizeof(int2), sb = (size_t)a->blk * a->K;
     for (PairTable *t : {&a->cpl, &a->fpi, &a->ct}) {
-        SPHDEM_CUDA_CHECK(cudaMemsetAsync(t->oc, 0, ocb, c->stream));
-        SPHDEM_CUDA_CHECK(cudaMemsetAsync(t->cnt, 0, a->K * sizeof(int), c->stream));
+        SPHDEM_CUDA_CHECK(cudaMemsetAsync(t->oc + sb * c->n, 0, ocb, c->stream));
+        SPHDEM_CUDA_CHECK(cudaMemsetAsync(t->cnt + sb, 0, a->K * sizeof(int), c->stream));
     }
 }
 
+const TapTables *cpl_forward_taps(sphdem_ctx *c, AdjointData *a) {
+    if (c->cfg.precision != SPHDEM_PREC_MIXED || c->mx_maxn <= 0) return nullptr;
+    /* SPHDEM_ADJ_SCAN_TAPS=1: scan for the tables after each phase as FP64
+     * handles do (the tests compare both forms) */
+    const char *e = getenv("SPHDEM_ADJ_SCAN_TAPS");
+    if (e && e[0] == '1') return nullptr;
+    TapTables &t = a->tap;
+    t.cpl = TapTable{a->cpl.nb, a->cpl.oc, a->cpl.cnt, a->cpl.cap, 0};
+    t.fpi = TapTable{a->fpi.nb, a->fpi.oc, a->fpi.cnt, a->fpi.cap, CP_FPI_PER};
+    t.ct = TapTable{a->ct.nb, a->ct.oc, a->ct.cnt, a->ct.cap, ADJ_MAX_CONTACTS};
+    t.slot = a->slot;
+    return &t;
+}
+
 void cpl_taps_middle(sphdem_ctx *c, AdjointData *a) {
-    k_cp_dpos<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->A, c->g, c->n, a->dpos);
-    k_cp_cpl_table<<<grid_for(c->n, CB), CB, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->g, c->n, a->dpos,
-                                                             a->cpl.nb, a->cpl.oc, a->cpl.cnt, a->cpl.cap, a->slot);
+    if (!c->tap) {
+        k_cp_dpos<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->A, c->g, c->n, a->dpos);
+        k_cp_cpl_table<<<grid_for(c->n, CB), CB, 0, c->stream>>>(c->cfg, c->A, c->buf.start, c->g, c->n, a->dpos,
+                                                                 a->cpl.nb, a->cpl.oc, a->cpl.cnt, a->cpl.cap,
+                                                                 a->slot);
+    }
     k_cp_tap_r<<<grid_for(c->n, 256), 256, 0, c->stream>>>(c->A, c->n, a->rmid, a->slot);
 }
 
 void cpl_taps_end(sphdem_ctx *c, AdjointData *a) {
-    if (a->n_dem == 0) return;
+    if (a->n_dem == 0 || c->tap) return;
     k_cp_fpi_table<<<grid_for((int64_t)a->n_dem * 32, CB), CB, 0, c->stream>>>(
         c->cfg, c->A, c->buf.start, c->g, c->n, a->n_dem, CP_FPI_PER, a->fpi.nb, a->fpi.oc, a->fpi.cnt, a->fpi.cap,
         a->slot);
@@ -1197,9 +1624,10 @@ void cpl_taps_end(sphdem_ctx *c, AdjointData *a) {
 bool cpl_overflow(sphdem_ctx *c, AdjointData *a) {
     std::vector<int> v(3 * a->K);
     const PairTable *ts[3] = {&a->cpl, &a->fpi, &a->ct};
+    const size_t sb = (size_t)a->blk * a->K;
     for (int k = 0; k < 3; k++)
-        SPHDEM_CUDA_CHECK(
-            cudaMemcpyAsync(v.data() + k * a->K, ts[k]->cnt, a->K * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        SPHDEM_CUDA_CHECK(cudaMemcpyAsync(v.data() + k * a->K, ts[k]->cnt + sb, a->K * sizeof(int),
+                                          cudaMemcpyDeviceToHost, c->stream));
     SPHDEM_CUDA_CHECK(cudaStreamSynchronize(c->stream));
     for (int k = 0; k < 3; k++)
         for (int j = 0; j < a->K; j++)
@@ -1207,49 +1635,93 @@ bool cpl_overflow(sphdem_ctx *c, AdjointData *a) {
     return false;
 }
 
+namespace {
+
+/* the coupling passes of the reverse step with pair math in M */
+template <typename M>
+void cpl_backward_coupling(sphdem_ctx *c, AdjointData *a, int sl, const double *s0, const double *s1, double dt,
+                           bool after_forces) {
+    using V4 = typename MT<M>::V4;
+    const int64_t n = c->n;
+    const int nd = a->n_dem;
+    const int g = grid_for(n, CB), gd = grid_for((int64_t)std::max(1, nd) * 32, CB);
+    const int *nbc = a->cpl.nb + (size_t)sl * a->cpl.cap, *nbf = a->fpi.nb + (size_t)sl * a->fpi.cap;
+    const int2 *occ = a->cpl.oc + (size_t)sl * n, *ocf = a->fpi.oc + (size_t)sl * n;
+    V4 *g4c = (V4 *)a->g4_cpl, *g4f = (V4 *)a->g4_fpi;
+    M *gwc = (M *)a->gw_cpl, *gwf = (M *)a->gw_fpi;
+    if (!after_forces) {
+        /* pair geometry, the transposed tables, porosity / EOS, Shepard sums,
+         * FPI + drag */
+        SPHDEM_LAUNCH(c, "adj_geo_cpl", k_cp_geo_cpl<M>, g, CB, 0, c->cfg, n, a->aux, a->typ, nbc, occ, g4c, gwc);
+        transpose<false>(c, a, nbc, occ, a->cplT);
+        SPHDEM_LAUNCH(c, "adj_por", k_cp_por<M>, g, CB, 0, c->cfg, n, a->aux, a->typ, occ, gwc, a->cmid);
+        if (nd == 0) return;
+        SPHDEM_LAUNCH(c, "adj_geo_fpi", k_cp_geo_fpi<M>, gd, CB, 0, c->cfg, nd, a->dem_tags, s1, a->hh, nbf, ocf, g4f,
+                      gwf);
+        transpose<true>(c, a, nbf, ocf, a->fpiT);
+        SPHDEM_LAUNCH(c, "adj_shep", k_cp_shep<M>, gd, CB, 0, nd, a->dem_tags, a->aux, a->mass, a->cplT.nb, a->cplT.ix,
+                      a->cplT.oc, gwc, a->cmid);
+        SPHDEM_LAUNCH(c, "adj_fpi_dem", k_cp_fpi<M>, gd, CB, 0, c->cfg, nd, a->dem_tags, dt, s1, a->aux, a->cmid,
+                      a->mass, nbf, ocf, g4f, gwf, a->adj, a->cacc, a->coef, a->grads);
+        SPHDEM_LAUNCH(c, "adj_fpi_fluid", k_cp_fpi_fluid<M>, g, CB, 0, n, c->cfg.nd, s1, a->aux, a->cmid, a->mass,
+                      a->typ, a->fpiT.nb, a->fpiT.ix, a->fpiT.oc, g4f, gwf, a->coef, a->cacc);
+        return;
+    }
+    /* porosity, DEM -> fluid drag and Shepard terms, after the forces gave
+     * the adjoints of e and f */
+    if (nd > 0)
+        SPHDEM_LAUNCH(c, "adj_cpl_dem", k_cp_cpl_dem<M>, gd, CB, 0, c->cfg, nd, a->dem_tags, s0, a->aux, a->cmid,
+                      a->cend, a->mass, a->cplT.nb, a->cplT.ix, a->cplT.oc, g4c, gwc, a->cacc);
+    SPHDEM_LAUNCH(c, "adj_cpl_fluid", k_cp_cpl_fluid<M>, g, CB, 0, c->cfg, n, s0, a->aux, a->cmid, a->cend, a->mass,
+                  a->typ, nbc, occ, g4c, gwc, a->cacc);
+}
+
+}  // namespace
+
 void cpl_backward_step(sphdem_ctx *c, AdjointData *a, int j, double dt) {
     const int64_t n = c->n;
-    const double *s0 = a->seg + (size_t)(j - 1) * n * ADJ_NC, *s1 = a->seg + (size_t)j * n * ADJ_NC;
-    const double *rm = a->rmid + (size_t)(j - 1) * n * 3;
-    const int sl = j - 1;
+    /* step j of the segment in tape block a->blk */
+    const size_t stb = (size_t)a->blk * (a->K + 1);
+    const double *s0 = a->seg + (stb + j - 1) * n * ADJ_NC, *s1 = a->seg + (stb + j) * n * ADJ_NC;
+    const int sl = a->blk * a->K + j - 1;
+    const double *rm = a->rmid + (size_t)sl * n * 3;
     auto nbp = [&](const PairTable &t) { return t.nb + (size_t)sl * t.cap; };
     auto ocp = [&](const PairTable &t) { return t.oc + (size_t)sl * n; };
     const int *nbm = a->nb_mid + (size_t)sl * a->pair_cap, *nbe = a->nb_end + (size_t)sl * a->pair_cap;
     const int2 *ocm = a->oc_mid + (size_t)sl * n, *oce = a->oc_end + (size_t)sl * n;
-    const int g = grid_for(n, CB);
+    const int g = grid_for(n, CB), g256 = grid_for(n, 256);
+    const bool mixed = a->crec != nullptr;
     cudaStream_t st = c->stream;
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cacc, 0, (size_t)n * CP_NACC * sizeof(double), st));
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cmid, 0, (size_t)n * CP_NMID * sizeof(double), st));
-    k_cp_pre<<<grid_for(n, 256), 256, 0, st>>>(n, dt, s0, rm, a->typ, a->aux);
-    k_cp_por<<<g, CB, 0, st>>>(c->cfg, n, a->aux, a->mass, a->typ, nbp(a->cpl), ocp(a->cpl), a->cmid);
-    if (a->n_dem > 0)
-        k_cp_fpi<<<grid_for((int64_t)a->n_dem * 32, CB), CB, 0, st>>>(c->cfg, a->n_dem, a->dem_tags, dt, s1, a->aux,
-                                                                      a->cmid, a->mass, a->hh, nbp(a->fpi),
-                                                                      ocp(a->fpi), a->adj, a->cacc, a->grads);
-    k_cp_dem<<<g, CB, 0, st>>>(c->cfg, n, dt, s1, a->aux, a->mass, a->rad, a->typ, nbp(a->ct), ocp(a->ct), a->adj,
-                               a->cacc, a->grads);
-    if (a->crec) {
-        k_cp_pack32<<<grid_for(n, 256), 256, 0, st>>>(n, dt, a->aux, a->cmid, s1, a->adj, a->mass, a->hh, a->typ,
-                                                       a->crec);
+    SPHDEM_LAUNCH(c, "adj_pre", k_cp_pre, g256, 256, 0, n, dt, s0, rm, a->typ, a->aux);
+    if (mixed) cpl_backward_coupling<float>(c, a, sl, s0, s1, dt, false);
+    else cpl_backward_coupling<double>(c, a, sl, s0, s1, dt, false);
+    SPHDEM_LAUNCH(c, "adj_contacts", k_cp_dem, g, CB, 0, c->cfg, n, dt, s1, a->aux, a->mass, a->rad, a->typ,
+                  nbp(a->ct), ocp(a->ct), a->adj, a->cacc, a->grads);
+    if (mixed) {
+        SPHDEM_LAUNCH(c, "adj_pack32", k_cp_pack32, g256, 256, 0, n, dt, a->aux, a->cmid, s1, a->adj, a->mass, a->hh,
+                      a->typ, a->crec);
 #define L_(ND)                                                                                                   \
     do {                                                                                                         \
-        k_cp_end32<ND><<<g, CB, 0, st>>>(c->cfg, n, dt, a->typ, nbe, oce, a->adj, a->cacc, a->cend, a->crec);     \
-        k_cp_force32<ND><<<g, CB, 0, st>>>(c->cfg, n, a->typ, nbm, ocm, a->adj, a->aux, a->cend, a->crec, a->cmid, \
-                                           a->cacc, a->grads);                                                    \
+        SPHDEM_LAUNCH(c, "adj_end32", k_cp_end32<ND>, g, CB, 0, c->cfg, n, dt, a->typ, nbe, oce, a->adj, a->cacc, \
+                      a->cend, a->crec);                                                                         \
+        SPHDEM_LAUNCH(c, "adj_force32", k_cp_force32<ND>, g, CB, 0, c->cfg, n, a->typ, nbm, ocm, a->adj, a->aux,  \
+                      a->cend, a->crec, a->cmid, a->cacc, a->grads);                                             \
     } while (0)
         if (c->cfg.nd == 3) L_(3);
         else if (c->cfg.nd == 2) L_(2);
         else L_(1);
 #undef L_
+        cpl_backward_coupling<float>(c, a, sl, s0, s1, dt, true);
     } else {
-        k_cp_end<<<g, CB, 0, st>>>(c->cfg, n, dt, s1, a->mass, a->hh, a->typ, nbe, oce, a->adj, a->cacc, a->cend);
-        k_cp_force<<<g, CB, 0, st>>>(c->cfg, n, a->aux, a->mass, a->hh, a->typ, nbm, ocm, a->adj, a->cend, a->cmid,
-                                     a->cacc, a->grads);
+        SPHDEM_LAUNCH(c, "adj_end", k_cp_end, g, CB, 0, c->cfg, n, dt, s1, a->mass, a->hh, a->typ, nbe, oce, a->adj,
+                      a->cacc, a->cend);
+        SPHDEM_LAUNCH(c, "adj_force", k_cp_force, g, CB, 0, c->cfg, n, a->aux, a->mass, a->hh, a->typ, nbm, ocm,
+                      a->adj, a->cend, a->cmid, a->cacc, a->grads);
+        cpl_backward_coupling<double>(c, a, sl, s0, s1, dt, true);
     }
-    k_cp_cpl_a<<<g, CB, 0, st>>>(c->cfg, n, s0, a->aux, a->cmid, a->cend, a->mass, a->typ, nbp(a->cpl), ocp(a->cpl),
-                                 a->cacc);
-    k_cp_cpl_b<<<g, CB, 0, st>>>(c->cfg, n, a->aux, a->mass, a->typ, nbp(a->cpl), ocp(a->cpl), a->cacc);
-    k_cp_assemble<<<grid_for(n, 256), 256, 0, st>>>(n, dt, a->typ, a->cacc, a->cend, a->cmid, a->adj);
+    SPHDEM_LAUNCH(c, "adj_assemble", k_cp_assemble, g256, 256, 0, n, dt, a->typ, a->cacc, a->cend, a->cmid, a->adj);
 }
 
 }  // namespace sphdem

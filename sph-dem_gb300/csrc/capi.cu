@@ -924,6 +924,12 @@ int sphdem_adjoint_forward(sphdem_handle h, int nsteps, int ckpt_every) {
     }
 }
 
+int sphdem_adjoint_set_tape_memory(sphdem_handle h, int64_t bytes) {
+    if (!h) return SPHDEM_ERR_INVALID;
+    h->adj_tape_mem = bytes;
+    return SPHDEM_OK;
+}
+
 int sphdem_adjoint_backward(sphdem_handle h, const double *dL_dr, const double *dL_dv, const double *dL_dvhat,
                             SphDemGrads *grads, double *dL_dr0, double *dL_dv0, double *dL_dvhat0) {
     if (!h || !grads) return SPHDEM_ERR_INVALID;

@@ -41,6 +41,27 @@ struct Buffers {
     int *pair_cnt = nullptr;
 };
 
+/* A per-step pair table in tag space that the mixed-precision forward
+ * coupling passes fill while the adjoint's replay graph is captured: entries
+ * partner tag | image shift code << 26, grouped by owner, at nb[slot * cap +
+ * offset]; (offset, count) of each owner at oc[slot * n + tag]; cnt[slot]
+ * counts the entries of the step (owners reserve with atomics), or exceeds
+ * cap when the step's table overflowed.  `per` > 0: each owner has `per`
+ * fixed slots (DEM-owned tables, owner w of the DEM range at w * per). */
+struct TapTable {
+    int *nb = nullptr;
+    int2 *oc = nullptr;
+    int *cnt = nullptr;
+    int64_t cap = 0;
+    int per = 0;
+};
+struct TapTables {
+    TapTable cpl;   /* fluid -> DEM coupling pairs of the middle phase (porosity / drag passes) */
+    TapTable fpi;   /* DEM -> fluid pairs of calcFPI (end phase) */
+    TapTable ct;    /* DEM -> DEM contacts with positive overlap (end phase) */
+    const int *slot = nullptr;   /* device step index inside the segment */
+};
+
 }  // namespace sphdem
 
 struct sphdem_ctx {
@@ -90,6 +111,12 @@ struct sphdem_ctx {
     float4 *mx_ds = nullptr;    /* DEM particles: offset in their SPH bucket, bucket key */
     float4 *mx_nb = nullptr;    /* boundary particles: FP32 normals n1 (+concave), n2, n3 */
     sphdem::AdjointData *adj = nullptr; /* checkpoints and buffers of the adjoint */
+    /* device memory the adjoint may give its tape store (0: one segment's
+     * tape; < 0: half of the free memory at the forward pass) */
+    int64_t adj_tape_mem = 0;
+    /* set while the adjoint's replay graph is captured: the mixed coupling
+     * passes then also write these tables */
+    const sphdem::TapTables *tap = nullptr;
     /* launch knobs chosen by the batch autotuner */
     int blk_pair = 128;         /* block size of the list-consumer passes (<= 128) */
     bool force_tile = false;    /* force / continuity: neighbour records staged in shared memory */

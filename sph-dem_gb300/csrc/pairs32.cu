@@ -1606,7 +1606,27 @@ __device__ __forceinline__ bool coupling_rule_packed(int cs, int cd, int num, in
     return rP < lim_ceil || rM < lim_ceil;
 }
 
-template <int ND, int MODE>
+/* one warp-aggregated atomic reserves k entries per lane of cnt; every lane
+ * of the warp calls it; returns this lane's first entry */
+__device__ __forceinline__ int64_t tap_reserve(int k, int *cnt) {
+    const int lane = threadIdx.x & 31;
+    int incl = k;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    int base = 0;
+    if (lane == 31 && total > 0) base = atomicAdd(cnt, total);
+    base = __shfl_sync(0xffffffffu, base, 31);
+    return (int64_t)base + incl - k;
+}
+
+/* TAP (adjoint replay only): the coupling pairs each fluid particle takes
+ * go to the tap table tt of step *tslot -- mode 0 counts them and reserves
+ * the particle's entries, mode 1 (same pairs, same order) writes them. */
+template <int ND, int MODE, bool TAP>
 __global__ void __launch_bounds__(CP_WARPS * 32, 3) k_couple(DevCfg c, const DevCfg *__restrict__ cp, DevState s,
                                                           const int *__restrict__ start, const int *__restrict__ skey,
                                                           const DevGlobals *__restrict__ g,
@@ -1614,7 +1634,8 @@ __global__ void __launch_bounds__(CP_WARPS * 32, 3) k_couple(DevCfg c, const Dev
                                                           const float4 *__restrict__ P2, const float4 *__restrict__ DP,
                                                           const int *__restrict__ tg, const int4 *__restrict__ RC4,
                                                           const int4 *__restrict__ win, int win_cap,
-                                                          float *__restrict__ shep32) {
+                                                          float *__restrict__ shep32, TapTable tt,
+                                                          const int *__restrict__ tslot, int64_t n_all) {
     constexpr int Z = ND - 1;
     constexpr unsigned FULL = 0xffffffffu;
     __shared__ float4 s_pos[CP_WARPS][CP_CAP];
@@ -1654,6 +1675,17 @@ __global__ void __launch_bounds__(CP_WARPS * 32, 3) k_couple(DevCfg c, const Dev
         }
         const bool act = is_sph_or_sphb(ta);
         if (MODE == 1 && is_boundary(ta)) s.row(FD_POR)[a] = 1.0;
+        int ntap = 0, tag_a = 0, tlim = 0, js = 0;
+        int *tout = nullptr;
+        if (TAP) {
+            js = *tslot;
+            if (act) tag_a = s.irow(FI_TAG)[a];
+            if (MODE == 1 && act) {
+                const int2 o = tt.oc[(int64_t)js * n_all + tag_a];
+                tout = tt.nb + (int64_t)js * tt.cap + o.x;
+                tlim = o.y;
+            }
+        }
         int cc[3] = {0, 0, 0};
         decode<ND>(key, sdims, cc);
         const int col = key / zdim;
@@ -1740,6 +1772,10 @@ __global__ void __launch_bounds__(CP_WARPS * 32, 3) k_couple(DevCfg c, const Dev
                                                 ((shp >> 4) & 3) - 1, c.rc2, 1);
                         }
                         if (in) {
+                            if (TAP) {
+                                if (MODE == 1 && ntap < tlim) tout[ntap] = s.irow(FI_TAG)[id.x & B_MASK] | (id.x & ~B_MASK);
+                                ntap++;
+                            }
                             const float r = sqrtf(r2);
                             const float qq = r * two_over_rc;
                             wgt = c_ihn * wK32(qq, wcon);
@@ -1924,6 +1960,10 @@ __global__ void __launch_bounds__(CP_WARPS * 32, 3) k_couple(DevCfg c, const Dev
                 if (!more) break;
             }
         }
+        if (TAP && MODE == 0) {
+            const int64_t off = tap_reserve(ntap, tt.cnt + js);
+            if (act) tt.oc[(int64_t)js * n_all + tag_a] = make_int2((int)off, off + ntap <= tt.cap ? ntap : 0);
+        }
         if (!act) continue;
         if (MODE == 0) {
             s.row(FD_POR)[a] = por.s;
@@ -2054,7 +2094,7 @@ __device__ __forceinline__ int warp_range_src(int excl, int j) {
 /* One DEM-DEM contact in FP64 (calcDEMContacts, sph.h:1676-1706): the
  * overlap (Ra + Rb) - r cancels, so r and the spring-dashpot force are FP64 */
 template <int ND>
-__device__ __noinline__ void dem_contact(const DevCfg *__restrict__ cp, const DevState s, int a, int b,
+__device__ __noinline__ bool dem_contact(const DevCfg *__restrict__ cp, const DevState s, int a, int b,
                                          const int *sh, double *fc) {
     const double Ra = s.row(FD_RADIUS)[a] > 0 ? s.row(FD_RADIUS)[a] : cp->dem_radius;
     const double Rb = s.row(FD_RADIUS)[b] > 0 ? s.row(FD_RADIUS)[b] : cp->dem_radius;
@@ -2066,7 +2106,7 @@ __device__ __noinline__ void dem_contact(const DevCfg *__restrict__ cp, const De
     }
     r = sqrt(r);
     const double overlap = (Ra + Rb) - r;
-    if (!(overlap > 0.0)) return;
+    if (!(overlap > 0.0)) return false;
     const double ma = s.row(FD_MASS)[a];
     double odot = 0.0;
 #pragma unroll
@@ -2074,6 +2114,18 @@ __device__ __noinline__ void dem_contact(const DevCfg *__restrict__ cp, const De
     const double sN = cp->dem_k * overlap + cp->dem_gamma * odot;
 #pragma unroll
     for (int k = 0; k < ND; k++) fc[k] += (sN * (dx[k] / r)) / ma;
+    return true;
+}
+
+/* TAP: a warp's passing candidates of one round go to the owner's fixed
+ * slots (out, per of them) in lane order; every lane calls it once per
+ * round of the warp-uniform candidate loop */
+__device__ __forceinline__ void tap_flush(bool &hit, int &ent, int *out, int per, int &k) {
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    const int pos = k + __popc(m & ((1u << (threadIdx.x & 31)) - 1u));
+    if (hit && out && pos < per) out[pos] = ent;
+    k += __popc(m);
+    hit = false;
 }
 
 /* Update of DEM particle a from its warp-reduced FPI and contact sums
@@ -2151,14 +2203,18 @@ __device__ __noinline__ void dem_end_update(const DevCfg *__restrict__ cp, const
  * flat over the lanes; sums are reduced over the warp.  Contacts (the overlap
  * 2R - r cancels) and the state update are FP64; the Di Felice drag
  * coefficient is FP32. */
-template <int ND>
+/* TAP (adjoint replay only): the FPI partners and the contacts with positive
+ * overlap of each DEM particle also go to the tap tables tf / tct of step
+ * *tslot (DEM particle w of the DEM range owns slots w * per). */
+template <int ND, bool TAP>
 __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restrict__ cp, DevState s,
                                                  const int *__restrict__ start, const int *__restrict__ skey,
                                                  const DevGlobals *__restrict__ g, const float4 *__restrict__ P0,
                                                  const float4 *__restrict__ P1, const float4 *__restrict__ P2,
                                                  const float4 *__restrict__ Q0, const float4 *__restrict__ Q1,
                                                  const float4 *__restrict__ Q2, const int *__restrict__ tg,
-                                                 const float4 *__restrict__ DS) {
+                                                 const float4 *__restrict__ DS, TapTable tf, TapTable tct,
+                                                 const int *__restrict__ tslot, int64_t n_all) {
     constexpr int Z = ND - 1;
     constexpr unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
@@ -2182,6 +2238,16 @@ __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restr
         if ((tg[a] & 0xff) != T_DEM) continue;
         const float4 pa = P0[a];
         const float ha = pa.w;
+        /* tap state: this lane's pending entry, entries so far, owner slots */
+        bool thit = false;
+        int tent = 0, kf = 0, kc = 0, js = 0;
+        int *fout = nullptr, *cout = nullptr;
+        if (TAP) {
+            js = *tslot;
+            const int64_t w = a - dem0;
+            if ((w + 1) * tf.per <= tf.cap) fout = tf.nb + (int64_t)js * tf.cap + w * tf.per;
+            if ((w + 1) * tct.per <= tct.cap) cout = tct.nb + (int64_t)js * tct.cap + w * tct.per;
+        }
         /* FPI over the SPH candidates: this particle in its SPH bucket's frame */
         const float4 ds = DS[a];
         int cs[3] = {0, 0, 0};
@@ -2194,6 +2260,7 @@ __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restr
             int total = 0;
             const int excl = warp_excl_scan(re.cnt, lane, &total);
             for (int t = 0; t < total; t += 32) {
+                if (TAP) tap_flush(thit, tent, fout, tf.per, kf);
                 const int j = t + lane;
                 const int src = warp_range_src(excl, j);
                 const int b0 = __shfl_sync(FULL, re.b0, src), ex = __shfl_sync(FULL, excl, src);
@@ -2239,7 +2306,12 @@ __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restr
                 fvel[2] += dvW * vb.z;
                 por += dvW * xb.z;
                 sum += dvW;
+                if (TAP) {
+                    thit = true;
+                    tent = s.irow(FI_TAG)[b] | (shp << B_BITS);
+                }
             }
+            if (TAP) tap_flush(thit, tent, fout, tf.per, kf);
         }
         sum = warp_sum(sum);
         por = warp_sum(por);
@@ -2260,6 +2332,7 @@ __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restr
             int total = 0;
             const int excl = warp_excl_scan(re.cnt, lane, &total);
             for (int t = 0; t < total; t += 32) {
+                if (TAP) tap_flush(thit, tent, cout, tct.per, kc);
                 const int j = t + lane;
                 const int src = warp_range_src(excl, j);
                 const int b0 = __shfl_sync(FULL, re.b0, src), ex = __shfl_sync(FULL, excl, src);
@@ -2289,8 +2362,20 @@ __global__ void __launch_bounds__(BLK) k_dem_end(DevCfg c, const DevCfg *__restr
                 if (r2 >= T - band && !exact_pair<ND>(cp, s, a, b, sh[0], sh[1], sh[2], 0.0, 0)) continue;
                 if (shp != 0x15 && !img_ok<ND>(tgb >> 8, sh)) continue;
                 if ((Ra_f + P2[b].y) * 1.0001f - sqrtf(r2) <= 0.f) continue;
-                dem_contact<ND>(cp, s, a, b, sh, fc);
+                const bool touch = dem_contact<ND>(cp, s, a, b, sh, fc);
+                if (TAP && touch) {
+                    thit = true;
+                    tent = s.irow(FI_TAG)[b] | (shp << B_BITS);
+                }
             }
+            if (TAP) tap_flush(thit, tent, cout, tct.per, kc);
+        }
+        if (TAP && lane == 0) {
+            const int64_t w = a - dem0, at = (int64_t)js * n_all + s.irow(FI_TAG)[a];
+            tf.oc[at] = make_int2((int)(w * tf.per), fout && kf <= tf.per ? kf : 0);
+            if (!fout || kf > tf.per) atomicMax(tf.cnt + js, (int)tf.cap + 1);   /* marks the step overflowed */
+            tct.oc[at] = make_int2((int)(w * tct.per), cout && kc <= tct.per ? kc : 0);
+            if (!cout || kc > tct.per) atomicMax(tct.cnt + js, (int)tct.cap + 1);
         }
 #pragma unroll
         for (int k = 0; k < ND; k++)
@@ -2384,7 +2469,7 @@ int resident_blocks(int64_t particles) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_couple<ND, MODE>, CP_WARPS * 32, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_couple<ND, MODE, false>, CP_WARPS * 32, 0);
         resident = std::max(1, sms * per_sm);
     }
     const int64_t need = (particles + 32 * CP_WARPS - 1) / (32 * CP_WARPS);
@@ -2398,7 +2483,7 @@ int dem_end_blocks(int64_t particles) {
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dem_end<ND>, BLK, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_dem_end<ND, false>, BLK, 0);
         resident = std::max(1, sms * per_sm);
     }
     return std::max(1, std::min(resident, warp_blocks((int)std::min<int64_t>(particles, 1 << 22))));
@@ -2626,22 +2711,35 @@ void dddt(sphdem_ctx *c) {
 #undef LD_
 }
 
-void porosity(sphdem_ctx *c) {
+/* the porosity (MODE 0) or DEM -> SPH drag (MODE 1) pass; while the
+ * adjoint's replay graph is captured, the form that also writes the
+ * coupling tap table */
+template <int MODE>
+void couple(sphdem_ctx *c, const char *name) {
+    const TapTable tt = c->tap ? c->tap->cpl : TapTable{};
+    const int *ts = c->tap ? c->tap->slot : nullptr;
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "porosity32", (k_couple<ND, 0>), (std::max(1, resident_blocks<ND, 0>(c->n) / c->grid_div)), CP_WARPS * 32, 0, c->cfg,   \
-                  c->dcfg, c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg, c->mx_rc4, c->mx_win, c->mx_win_cap, c->mx_shep32)
+    do {                                                                                                        \
+        const int nb_ = std::max(1, resident_blocks<ND, MODE>(c->n) / c->grid_div);                             \
+        if (c->tap)                                                                                             \
+            SPHDEM_LAUNCH(c, name, (k_couple<ND, MODE, true>), nb_, CP_WARPS * 32, 0, c->cfg, c->dcfg, c->A,      \
+                          c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg,   \
+                          c->mx_rc4, c->mx_win, c->mx_win_cap, c->mx_shep32, tt, ts, c->n);                       \
+        else                                                                                                    \
+            SPHDEM_LAUNCH(c, name, (k_couple<ND, MODE, false>), nb_, CP_WARPS * 32, 0, c->cfg, c->dcfg, c->A,     \
+                          c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg,   \
+                          c->mx_rc4, c->mx_win, c->mx_win_cap, c->mx_shep32, tt, ts, c->n);                       \
+    } while (0)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }
 
+void porosity(sphdem_ctx *c) { couple<0>(c, "porosity32"); }
+
 void dem_drag(sphdem_ctx *c) {
     SPHDEM_LAUNCH(c, "pack_dem_drag32", k_pack_dem_drag, grid_for(c->n, 256), 256, 0, c->A, c->mx_shep32, c->mx_vel,
                   c->mx_dp, c->n);
-#define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "dem_drag32", (k_couple<ND, 1>), (std::max(1, resident_blocks<ND, 1>(c->n) / c->grid_div)), CP_WARPS * 32, 0, c->cfg,   \
-                  c->dcfg, c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_dp, c->mx_tg, c->mx_rc4, c->mx_win, c->mx_win_cap, c->mx_shep32)
-    SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
-#undef L_
+    couple<1>(c, "dem_drag32");
 }
 
 void dem_end(sphdem_ctx *c) {
@@ -2649,9 +2747,19 @@ void dem_end(sphdem_ctx *c) {
     /* one warp per DEM particle, grid-stride over the DEM range: one wave of
      * resident blocks (a grid sized by the particle count would launch
      * mostly empty warps) */
+    const TapTable tf = c->tap ? c->tap->fpi : TapTable{}, tct = c->tap ? c->tap->ct : TapTable{};
+    const int *ts = c->tap ? c->tap->slot : nullptr;
 #define L_(ND)                                                                                                  \
-    SPHDEM_LAUNCH(c, "dem_end32", k_dem_end<ND>, dem_end_blocks<ND>(c->n), BLK, 0, c->cfg, c->dcfg, c->A, c->buf.start, c->buf.skey,  \
-                  c->g, c->mx_pos, c->mx_vel, c->mx_aux, c->mx_q0, c->mx_q1, c->mx_q2, c->mx_tg, c->mx_ds)
+    do {                                                                                                        \
+        if (c->tap)                                                                                             \
+            SPHDEM_LAUNCH(c, "dem_end32", (k_dem_end<ND, true>), dem_end_blocks<ND>(c->n), BLK, 0, c->cfg,        \
+                          c->dcfg, c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_vel, c->mx_aux,        \
+                          c->mx_q0, c->mx_q1, c->mx_q2, c->mx_tg, c->mx_ds, tf, tct, ts, c->n);                   \
+        else                                                                                                    \
+            SPHDEM_LAUNCH(c, "dem_end32", (k_dem_end<ND, false>), dem_end_blocks<ND>(c->n), BLK, 0, c->cfg,       \
+                          c->dcfg, c->A, c->buf.start, c->buf.skey, c->g, c->mx_pos, c->mx_vel, c->mx_aux,        \
+                          c->mx_q0, c->mx_q1, c->mx_q2, c->mx_tg, c->mx_ds, tf, tct, ts, c->n);                   \
+    } while (0)
     SPHDEM_ND_DISPATCH(c->cfg.nd, L_);
 #undef L_
 }

@@ -248,6 +248,7 @@ class Library:
         L.sphdem_cell_ids_noalloc.argtypes = [H, C.POINTER(C.c_int32)]
         D = C.POINTER(C.c_double)
         L.sphdem_adjoint_forward.argtypes = [H, C.c_int, C.c_int]
+        L.sphdem_adjoint_set_tape_memory.argtypes = [H, C.c_int64]
         L.sphdem_output_vars.argtypes = [H, C.POINTER(SphDemOutputVars)]
         L.sphdem_adjoint_backward.argtypes = [H, D, D, D, C.POINTER(SphDemGrads), D, D, D]
         L.sphdem_batch_create.argtypes = [C.POINTER(H), C.c_int, C.POINTER(H)]
@@ -389,6 +390,11 @@ class Simulation:
         o = SphDemOutputVars()
         self.L.check(self.L.lib.sphdem_output_vars(self.h, C.byref(o)), self.h, "output_vars")
         return o.as_dict()
+
+    def adjoint_set_tape_memory(self, nbytes: int):
+        """Device memory for the tapes of checkpoint segments kept from the
+        forward pass (0: one segment's; < 0: half of the free memory)."""
+        self.L.check(self.L.lib.sphdem_adjoint_set_tape_memory(self.h, int(nbytes)), self.h, "set_tape_memory")
 
     def adjoint_forward(self, nsteps: int, ckpt_every: int):
         self.L.check(self.L.lib.sphdem_adjoint_forward(self.h, nsteps, ckpt_every), self.h, "adjoint_forward")

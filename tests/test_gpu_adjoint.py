@@ -296,6 +296,65 @@ def test_coupled_adjoint_vs_central_differences(lib, precision):
         assert abs(ad - fd) <= RTOL * abs(fd), f"DEM direction {k}: adjoint {ad} fd {fd}"
 
 
+def test_coupled_forward_taps_equal_scanned_tables(lib, monkeypatch):
+    """Mixed handles take the reverse sweep's coupling, FPI and contact tables
+    from the forward passes that evaluate those pairs (k_couple, k_dem_end);
+    scanning for them after each phase, as FP64 handles do, gives the same
+    gradients (the tables differ only in entry order and in zero-weight
+    pairs beyond the coupling radius)."""
+    case = moving_coupled()
+    out = {}
+    for scan in (False, True):
+        if scan:
+            monkeypatch.setenv("SPHDEM_ADJ_SCAN_TAPS", "1")
+        else:
+            monkeypatch.delenv("SPHDEM_ADJ_SCAN_TAPS", raising=False)
+        sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+        sim.adjoint_forward(CPL_STEPS, CPL_K)
+        L0, dr, dv = cpl_loss_and_seed(sim)
+        grads, dr0, dv0, _ = sim.adjoint_backward(dL_dr=dr, dL_dv=dv)
+        sim.close()
+        out[scan] = (grads, dr0, dv0)
+    (g1, r1, v1), (g2, r2, v2) = out[False], out[True]
+    for name in ("dem_k", "dem_gamma", "viscosity", "drag_scale"):
+        a, b = getattr(g1, name), getattr(g2, name)
+        print(name, a, b)
+        assert abs(a - b) <= 1e-6 * abs(b), f"{name}: forward taps {a}, scanned {b}"
+    for x, y in ((r1, r2), (v1, v2)):
+        assert np.abs(x - y).max() <= 1e-6 * np.abs(y).max()
+
+
+@pytest.mark.parametrize("family", ["fluid", "coupled"])
+def test_tape_store_equals_checkpoint_replay(lib, family):
+    """Keeping every checkpoint segment's tape from the forward pass
+    (sphdem_adjoint_set_tape_memory) gives the gradients of the classic form,
+    which keeps one segment's tape and replays the others from their
+    checkpoints; a second backward pass after the store was reused for a
+    replay still gives them."""
+    if family == "fluid":
+        case, steps, K, prec = moving_dambreak(), SPH_STEPS, SPH_K, cases.PREC_FP64
+        seed = lambda sim: dict(zip(("dL_dr", "dL_dv", "dL_dvhat"), sph_loss_and_seed(sim)[1:]))
+    else:
+        case, steps, K, prec = moving_coupled(), CPL_STEPS, CPL_K, cases.PREC_MIXED
+        seed = lambda sim: dict(zip(("dL_dr", "dL_dv"), cpl_loss_and_seed(sim)[1:]))
+    out = []
+    for mem in (0, 1 << 36):
+        sim = capi.Simulation(lib, case.cfg, case.particles, precision=prec)
+        sim.adjoint_set_tape_memory(mem)
+        sim.adjoint_forward(steps, K)
+        sd = seed(sim)
+        out.append(sim.adjoint_backward(**sd))
+        if mem:
+            out.append(sim.adjoint_backward(**sd))
+        sim.close()
+    g0, r0 = out[0][0], out[0][1]
+    for g, r, *_ in out[1:]:
+        for name in ("dem_k", "dem_gamma", "viscosity", "drag_scale"):
+            a, b = getattr(g, name), getattr(g0, name)
+            assert abs(a - b) <= 1e-6 * max(abs(b), 1e-300), f"{name}: {a} vs {b}"
+        assert np.abs(r - r0).max() <= 1e-6 * np.abs(r0).max()
+
+
 def test_adjoint_rejects_unsupported_fluid(lib):
     # damBreak's own options (Monaghan viscosity, anticlumping, h following
     # density) are outside the fluid adjoint
