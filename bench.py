@@ -356,8 +356,15 @@ def measure_adjoint(lib, capi, cases, nsteps=100, ckpt=10):
                                        tape_mem=-1)
     out["coupled_500"]["workload"] = ("as coupled, 500 steps, checkpoint every 50, segment tapes kept in "
                                       "device memory")
+    # the coupled configuration's own VAR_H_CORRECTION (h following density,
+    # the 1/Omega gradient correction): 100 steps, checkpoints every 50
+    cplv = cases.workload("sediment3d_adjoint_varh")
+    out["coupled_varh"] = _time_adjoint(lib, capi, cases, cplv, cpl_steps, cpl_ckpt, cpl_seed, precisions=("mixed",),
+                                        tape_mem=-1)
+    out["coupled_varh"]["workload"] = ("as coupled, with VAR_H_CORRECTION (h = 1.5 (m / rho)^(1/3), gradients "
+                                       "over Omega), segment tapes kept in device memory")
     out["ratio"] = max(out["dem"]["mixed"]["ratio"], out["fluid"]["mixed"]["ratio"],
-                       out["coupled"]["mixed"]["ratio"])
+                       out["coupled"]["mixed"]["ratio"], out["coupled_varh"]["mixed"]["ratio"])
     return out
 
 

@@ -1025,9 +1025,16 @@ std::string adjoint_supported(sphdem_ctx *c, int *mode) {
         if (!all_coupled)
             return "the coupled adjoint covers SPH, SPH-boundary and DEM particles (no repulsive boundary particles)";
         if (cfg.visc != SPHDEM_VISC_MORRIS) return "the coupled adjoint covers Morris viscosity only";
-        if (!(cfg.flags & SPHDEM_F_CONST_H)) return "the coupled adjoint needs a constant smoothing length";
         if (!(cfg.flags & SPHDEM_F_NO_ANTICLUMPING)) return "the coupled adjoint does not cover anticlumping";
-        if (cfg.var_h()) return "the coupled adjoint does not cover VAR_H_CORRECTION";
+        /* h constant, or following the density under VAR_H_CORRECTION (the
+         * sediment3D form; its reverse passes are the FP32 ones) */
+        if (cfg.var_h()) {
+            if (cfg.flags & SPHDEM_F_CONST_H) return "the coupled adjoint covers VAR_H_CORRECTION with h following density";
+            if (cfg.precision != SPHDEM_PREC_MIXED)
+                return "the coupled adjoint covers VAR_H_CORRECTION on mixed-precision handles";
+        } else if (!(cfg.flags & SPHDEM_F_CONST_H)) {
+            return "the coupled adjoint needs a constant smoothing length or VAR_H_CORRECTION";
+        }
         if (cfg.gamma != 7.0) return "the coupled adjoint covers the gamma = 7 equation of state";
         if (c->n > (4 << 20)) return "the coupled adjoint covers at most 4M particles";
         *mode = ADJ_MODE_COUPLED;

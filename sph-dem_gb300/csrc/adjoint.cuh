@@ -26,7 +26,7 @@ constexpr int ADJ_NGRAD = 5;       /* d/dk, d/dgamma, d/dalpha, d/dnu, d/d(drag 
 constexpr int CP_NACC = 24;        /* coupled step: accumulators per particle */
 constexpr int CP_NEND = 15;        /* coupled step: end-phase results per particle */
 constexpr int CP_NMID = 8;         /* coupled step: middle intermediates per particle */
-constexpr int CP_NREC32 = 8;       /* coupled step, mixed: float4 records per particle */
+constexpr int CP_NREC32 = 9;       /* coupled step, mixed: float4 records per particle */
 constexpr int CP_FPI_PER = 384;    /* FPI partners per DEM particle per step (3D fluid at rest: ~122) */
 
 /* one step's transposed pair table: (offset, count) per partner tag, the
@@ -108,6 +108,7 @@ struct AdjointData {
     /* one step's pair geometry per entry of the coupling / FPI tables: (d,
      * W'/r) and W, FP32 on mixed handles, FP64 on FP64 handles */
     void *g4_cpl = nullptr, *gw_cpl = nullptr, *g4_fpi = nullptr, *gw_fpi = nullptr;
+    double *hs = nullptr;           /* VAR_H_CORRECTION: the step's h_s per particle (tag order) */
 };
 
 /* G = (F(r, h_a) + F(r, h_b)) / 2 and dG/dr, F(r, h) = -10 C (2-q)^3 / h^(d+2)

@@ -91,7 +91,8 @@ enum : int {
     CA_FD0 = 17,    /* DEM: adjoint of the lagged drag fdrag0 */
     CA_SHEP = 20,   /* DEM: adjoint of the Shepard sum */
     CA_RHOS = 21,   /* fluid: total adjoint of rho_s */
-    CA_EBAR = 22    /* fluid: adjoint of e = 1 - eps (0 where clamped) */
+    CA_EBAR = 22,   /* fluid: adjoint of e = 1 - eps (0 where clamped) */
+    CA_HB = 23      /* fluid, VAR_H_CORRECTION: adjoint of h_s */
 };
 /* end-phase results (CP_NEND): total adjoint of r1, vh1, f1, fp, fv */
 enum : int { CE_R1 = 0, CE_VH1 = 3, CE_F = 6, CE_P = 9, CE_V = 12 };
@@ -347,8 +348,11 @@ __device__ __forceinline__ void wc_kernel(const DevCfg &c, double r, double &W, 
     Wp = c.c_ihn * c.wcon * (-10.0 * q * t2 * t) * c.two_over_rc;
 }
 
-/* intermediates: middle positions, vh_s (fluid) / vh_m (DEM), rho_s, 1/rho_s */
-__global__ void k_cp_pre(int64_t n, double dt, const double *s0, const double *rm, const int *typ, double *aux) {
+/* intermediates: middle positions, vh_s (fluid) / vh_m (DEM), rho_s, 1/rho_s;
+ * with hs (VAR_H_CORRECTION): the step's smoothing length h_s = hfac (m /
+ * rho_s)^(1/d) of the fluid (the start phase's update), hh of the rest */
+__global__ void k_cp_pre(int64_t n, double dt, const double *s0, const double *rm, const int *typ, double *aux,
+                         const double *mass, const double *hh, double *hs, double hfac, int nd) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double *x = s0 + i * ADJ_NC;
@@ -362,6 +366,7 @@ __global__ void k_cp_pre(int64_t n, double dt, const double *s0, const double *r
     }
     o[6] = x[AS_DENS] + hd * x[AS_DDDT];
     o[7] = is_fluid(t) ? 1.0 / o[6] : 0.0;
+    if (hs) hs[i] = is_fluid(t) ? hfac * pow(mass[i] * o[7], 1.0 / nd) : hh[i];
 }
 
 /* ---- pair geometry of the coupling and FPI tables -------------------------
@@ -391,6 +396,18 @@ template <> struct MT<double> {
     }
     static __device__ __forceinline__ double root(double x) { return sqrt(x); }
 };
+
+/* dW/dh(r, h) = -C h^-(d+1) (d K(q) + q K'(q)) */
+template <int ND, typename M>
+__device__ __forceinline__ M w_dh(M wcon, M r, M ih) {
+    const M q = r * ih;
+    if (q > (M)2) return (M)0;
+    const M t = (M)2 - q, t2 = t * t;
+    M ihd1 = ih;
+#pragma unroll
+    for (int d = 0; d < ND; d++) ihd1 *= ih;
+    return -wcon * ihd1 * (t2 * t * ((M)ND * t * ((M)1 + (M)2 * q) - (M)10 * q * q));
+}
 
 /* coupling pairs, one thread per fluid particle: d = r_a - r_i at the middle
  * positions, W = W_c(r) = C_c K(2r/Rc) and W_c'(r) / r (sph.h:1246-1256) */
@@ -678,10 +695,11 @@ __global__ void k_cp_fpi(DevCfg c, int n_dem, const int *dem_tags, double dt, co
  * partners (transposed FPI table), the adjoints of its density, porosity,
  * end position, velocity and force parts that the partners' normalised sums
  * give it */
-template <typename M>
+template <typename M, bool VH>
 __global__ void k_cp_fpi_fluid(int64_t n, int nd, const double *s1, const double *aux, const double *cmid,
                                const double *mass, const int *typ, const int *nbT, const int *ixT, const int2 *ocT,
-                               const typename MT<M>::V4 *g4, const M *gw, const double *coef, double *cacc) {
+                               const typename MT<M>::V4 *g4, const M *gw, const double *coef, double *cacc,
+                               const double *hp, double wcon) {
     using Acc = typename MT<M>::Acc;
     const int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (b >= n || !is_fluid(typ[b])) return;
@@ -696,7 +714,8 @@ __global__ void k_cp_fpi_fluid(int64_t n, int nd, const double *s1, const double
         fv[q] = (M)xb[AS_FV + q];
         vh[q] = (M)xb[AS_VH + q];
     }
-    Acc arho, aeps, ar[3], afp[3], afv[3], avh[3];
+    Acc arho, aeps, ar[3], afp[3], afv[3], avh[3], ahs;
+    const M ihb = VH ? (M)(1.0 / hp[b]) : (M)0, wc = (M)wcon;
     for (int k = 0; k < o.y; k++) {
         const int e = ixT[o.x + k];
         const M W = gw[e];
@@ -720,6 +739,15 @@ __global__ void k_cp_fpi_fluid(int64_t n, int nd, const double *s1, const double
         arho.add(-dvolb * dvol * irho);
         aeps.add(dvol * W * NporB);
         const M dd[3] = {gd.x, gd.y, gd.z};
+        if (VH) {
+            /* VAR_H_CORRECTION: W(r / h_b, h_b) follows the fluid particle's h */
+            const M r = MT<M>::root(dd[0] * dd[0] + dd[1] * dd[1] + dd[2] * dd[2]);
+            M wdh = 0;
+            if (nd == 3) wdh = w_dh<3, M>(wc, r, ihb);
+            else if (nd == 2) wdh = w_dh<2, M>(wc, r, ihb);
+            else wdh = w_dh<1, M>(wc, r, ihb);
+            ahs.add(Wb * wdh);
+        }
         for (int q3 = 0; q3 < nd; q3++) {
             ar[q3].add(-Wb * gd.w * dd[q3]);
             afp[q3].add(mb * W * cfp[q3]);
@@ -730,6 +758,7 @@ __global__ void k_cp_fpi_fluid(int64_t n, int nd, const double *s1, const double
     double *acc = cacc + b * CP_NACC;
     acc[CA_RHO] += arho.value();
     acc[CA_EPS] += aeps.value();
+    if (VH) acc[CA_HB] += ahs.value();
     for (int q = 0; q < nd; q++) {
         acc[CA_R1 + q] += ar[q].value();
         acc[CA_FP + q] += afp[q].value();
@@ -1291,7 +1320,7 @@ __global__ void k_cp_assemble(int64_t n, double dt, const int *typ, const double
  * (r1 lo, m), R_E2 = (vh1, adjoint of dddt1 + hd adjoint of rho1).  Pair
  * displacements come from the double-float positions; per-particle sums are
  * Kahan-compensated and land in the FP64 accumulators once. */
-enum { R_M0 = 0, R_M1, R_M2, R_M3, R_M4, R_E0, R_E1, R_E2 };
+enum { R_M0 = 0, R_M1, R_M2, R_M3, R_M4, R_E0, R_E1, R_E2, R_O };
 
 __global__ void k_cp_pack32(int64_t n, double dt, const double *aux, const double *cmid, const double *s1,
                             const double *adj, const double *mass, const double *hh, const int *typ, float4 *rec) {
@@ -1488,6 +1517,323 @@ __global__ void __launch_bounds__(128) k_cp_force32(DevCfg c, int64_t n, const i
     if ((threadIdx.x & 31) == 0 && gnu != 0.f) atomicAdd(&grads[3], (double)gnu);
 }
 
+
+/* ---- VAR_H_CORRECTION (mixed handles): h = hfac (m / rho_s)^(1/d) follows
+ * the density, and every gradient of a particle's sums carries 1 / Omega
+ * (calcOmega, sph.h:438-451; gradW, sph.h:331-332):
+ *
+ *   Omega_x = 1 + h_x S_x / (rho_x d),  S_x = sum_y m_y dW/dh(r_xy, h_x)  (self term included)
+ *   middle:  f_x += (1/Omega_x) sum_y [ -m_y (p_x F(r,h_x) + p_y F(r,h_y)) d
+ *                                       + c_xy phi_xy w ],
+ *            phi = r^2 M / (r^2 + 0.01 hav^2),  M = (F(r,h_x) + F(r,h_y)) / 2
+ *   end:     dddt_x = (1/Omega_x) sum_y m_y (w.d) F(r, h_x)
+ *   FPI:     W(r / h_b, h_b) with the fluid particle's h
+ *
+ * with the Wendland C2 kernel W = C h^-d K(q), K = (2-q)^4 (1+2q), and
+ * F(r, h) = W'/r = -10 C h^-(d+2) (2-q)^3.  Both phases use h_s and rho_s
+ * (the end tail updates them after the continuity pass).  The reverse sweep
+ * adds the adjoint of h_s per particle (CA_HB; from the end, middle and FPI
+ * sums, and from Omega's own dependence on h), and of Omega_x, which is
+ * -Dbar dddt / Omega (end) and -(Pbar.fp + Vbar.fv) / Omega (middle) per
+ * particle; its pair terms (dOmega/dr, dOmega/dh) ride in the same pair
+ * loops.  Finally rho_s's adjoint takes hbar dh/drho = -hbar h / (d rho). */
+template <int ND>
+struct KerVH {
+    float F, Fr, Fh, Whr, Whh;   /* F, dF/dr, dF/dh, d2W/dh dr, d2W/dh2 */
+};
+
+template <int ND>
+__device__ __forceinline__ KerVH<ND> ker_vh(float wcon, float r, float ih) {
+    KerVH<ND> k = {0.f, 0.f, 0.f, 0.f, 0.f};
+    const float q = r * ih;
+    if (q > 2.f) return k;
+    const float t = 2.f - q, t2 = t * t;
+    const float i2 = ipow_nd2<ND>(ih), i3 = i2 * ih;           /* ih^(d+2), ih^(d+3) */
+    k.F = -10.f * wcon * i2 * (t2 * t);
+    k.Fr = 30.f * wcon * i3 * t2;
+    k.Fh = 10.f * wcon * i3 * t2 * ((float)(ND + 2) * t - 3.f * q);
+    const float g = t2 * t * ((float)ND * t * (1.f + 2.f * q) - 10.f * q * q);
+    const float gp = q * t2 * (30.f * q - 10.f * (float)(ND + 2) * t);
+    k.Whr = -wcon * i2 * gp;
+    k.Whh = wcon * i2 * ((float)(ND + 1) * g + q * gp);
+    return k;
+}
+
+/* Omega of the middle and end pair sets of every fluid particle, and the
+ * end one's adjoint factor kappa_e = Omegabar_e h / (rho d), Omegabar_e =
+ * -Dbar dddt1 / Omega_e: record R_O = (Omega_m, Omega_e, kappa_m (set by
+ * k_cp_end32_vh), kappa_e) */
+template <int ND>
+__global__ void __launch_bounds__(128) k_cp_omega32(int64_t n, float wcon, const int *typ,
+                                                    const int *__restrict__ nbm, const int2 *__restrict__ ocm,
+                                                    const int *__restrict__ nbe, const int2 *__restrict__ oce,
+                                                    const DevCfg c, const double *s1, float4 *rec) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a >= n || !is_fluid(typ[a])) return;
+    float om[2];
+    for (int ph = 0; ph < 2; ph++) {
+        const float4 *X0 = rec + (ph ? R_E0 : R_M0) * n, *X1 = rec + (ph ? R_E1 : R_M1) * n;
+        const int *nb = ph ? nbe : nbm;
+        const int2 o = (ph ? oce : ocm)[a];
+        const float4 p0 = X0[a], p1 = X1[a];
+        const float ih = p0.w;
+        Kf S;
+        S.add(p1.w * w_dh<ND, float>(wcon, 0.f, ih));
+        for (int k = 0; k < o.y; k++) {
+            int sh[3];
+            const int b = table_entry(__ldg(nb + o.x + k), sh);
+            float img[3];
+            image32<ND>(c, sh, img);
+            const float4 q0 = X0[b], q1 = X1[b];
+            const float pa[3] = {p0.x, p0.y, p0.z}, la[3] = {p1.x, p1.y, p1.z};
+            const float pb[3] = {q0.x, q0.y, q0.z}, lb[3] = {q1.x, q1.y, q1.z};
+            float r2 = 0.f;
+#pragma unroll
+            for (int q = 0; q < ND; q++) {
+                const float dq = ((pa[q] - pb[q]) + (la[q] - lb[q])) - img[q];
+                r2 = fmaf(dq, dq, r2);
+            }
+            S.add(q1.w * w_dh<ND, float>(wcon, sqrtf(r2), ih));
+        }
+        const float rho = rec[R_M2 * n + a].w;
+        om[ph] = 1.f + (float)(S.value()) / (ih * rho * (float)ND);
+    }
+    const float rho = rec[R_M2 * n + a].w, h = 1.f / rec[R_M0 * n + a].w;
+    const float ombar_e = -rec[R_E2 * n + a].w * (float)s1[a * ADJ_NC + AS_DDDT] / om[1];
+    rec[R_O * n + a] = make_float4(om[0], om[1], 0.f, ombar_e * h / (rho * (float)ND));
+}
+
+/* k_cp_end32 under VAR_H_CORRECTION: continuity with F(r, h_a) / Omega_a and
+ * the end Omega's pair terms; then the totals, the adjoints of h_s (CA_HB)
+ * and rho_s (CA_RHO) that the end phase gives, and kappa_m */
+template <int ND>
+__global__ void __launch_bounds__(128) k_cp_end32_vh(DevCfg c, int64_t n, double dt, const int *typ,
+                                                     const int *__restrict__ nb, const int2 *__restrict__ oc,
+                                                     const double *adj, const double *s1, double *cacc, double *cend,
+                                                     float4 *rec) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (a >= n || !is_fluid(typ[a])) return;
+    const float4 *E0 = rec + R_E0 * n, *E1 = rec + R_E1 * n, *E2 = rec + R_E2 * n, *O = rec + R_O * n;
+    const float wcon = (float)c.wcon;
+    const float4 p0 = E0[a], p1 = E1[a], p2 = E2[a], oa = O[a];
+    const float pa[3] = {p0.x, p0.y, p0.z}, la[3] = {p1.x, p1.y, p1.z}, va[3] = {p2.x, p2.y, p2.z};
+    const float ma = p1.w, da = p2.w / oa.y, ka = oa.w;   /* delta_a = Dbar / Omega_e, kappa_e */
+    Kf rb[ND], wb[ND], hb;
+    const int2 o = oc[a];
+    for (int k = 0; k < o.y; k++) {
+        int sh[3];
+        const int b = table_entry(__ldg(nb + o.x + k), sh);
+        float img[3];
+        image32<ND>(c, sh, img);
+        const float4 q0 = E0[b], q1 = E1[b], q2 = E2[b], ob = O[b];
+        const float pb[3] = {q0.x, q0.y, q0.z}, lb[3] = {q1.x, q1.y, q1.z}, vb[3] = {q2.x, q2.y, q2.z};
+        float d[3], w[3], r2 = 0.f, wd = 0.f;
+#pragma unroll
+        for (int q = 0; q < ND; q++) {
+            d[q] = ((pa[q] - pb[q]) + (la[q] - lb[q])) - img[q];
+            w[q] = va[q] - vb[q];
+            r2 = fmaf(d[q], d[q], r2);
+            wd = fmaf(w[q], d[q], wd);
+        }
+        if (!(r2 > 0.f)) continue;
+        const float r = sqrtf(r2), ir = 1.f / r;
+        const KerVH<ND> ka_ = ker_vh<ND>(wcon, r, p0.w), kb_ = ker_vh<ND>(wcon, r, q0.w);
+        const float mb = q1.w, db = q2.w / ob.y, kb = ob.w;
+        const float cA = da * mb * ka_.F + db * ma * kb_.F;
+        const float cB = (da * mb * ka_.Fr + db * ma * kb_.Fr) * wd + (ka * mb * ka_.Whr + kb * ma * kb_.Whr);
+#pragma unroll
+        for (int q = 0; q < ND; q++) {
+            rb[q].add(cA * w[q] + cB * d[q] * ir);
+            wb[q].add(cA * d[q]);
+        }
+        hb.add(da * mb * wd * ka_.Fh + ka * mb * ka_.Whh);
+    }
+    const double hd = 0.5 * dt;
+    const double *aa = adj + a * ADJ_NC, *x1 = s1 + a * ADJ_NC;
+    double *ac = cacc + a * CP_NACC;
+    const bool sph = typ[a] == T_SPH;
+    double *ce = cend + a * CP_NEND;
+    /* Omega_e's own h and rho: Omega - 1 = h S / (rho d) */
+    const double rho = rec[R_M2 * n + a].w, ih = p0.w, h = 1.0 / ih;
+    const double ombar = (double)ka * rho * ND * ih;
+    ac[CA_HB] += hb.value() + ombar * ((double)oa.y - 1.0) * ih +
+                 (double)ka * ma * (double)ker_vh<ND>(wcon, 0.f, p0.w).Whh;
+    ac[CA_RHO] += -ombar * ((double)oa.y - 1.0) / rho;
+    float P[3] = {0.f, 0.f, 0.f}, V[3] = {0.f, 0.f, 0.f};
+    double pf = 0.0;   /* Pbar.fp + Vbar.fv of the middle forces */
+    for (int q = 0; q < 3; q++) {
+        const double rt = aa[AS_R + q] + ac[CA_R1 + q] + (q < ND ? rb[q].value() : 0.0);
+        const double vt = aa[AS_VH + q] + ac[CA_VH1 + q] + (q < ND ? wb[q].value() : 0.0) + hd * rt;
+        const double F = sph ? aa[AS_F + q] + dt * (vt + aa[AS_V + q]) : 0.0;
+        ce[CE_R1 + q] = rt;
+        ce[CE_VH1 + q] = vt;
+        ce[CE_F + q] = F;
+        ce[CE_P + q] = F + ac[CA_FP + q];
+        ce[CE_V + q] = sph ? F + ac[CA_FV + q] : 0.0;
+        pf += ce[CE_P + q] * x1[AS_FP + q] + ce[CE_V + q] * x1[AS_FV + q];
+        P[q] = (float)ce[CE_P + q];
+        V[q] = (float)ce[CE_V + q];
+    }
+    float4 *M3 = rec + R_M3 * n, *M4 = rec + R_M4 * n;
+    M3[a] = make_float4(P[0], P[1], P[2], M3[a].w);
+    M4[a] = make_float4(V[0], V[1], V[2], M4[a].w);
+    /* kappa_m = Omegabar_m h / (rho d), Omegabar_m = -(Pbar.fp + Vbar.fv) / Omega_m */
+    rec[R_O * n + a].z = (float)(-pf / (double)oa.x * h / (rho * ND));
+}
+
+/* one orientation (x, y) of the middle pair terms under VAR_H_CORRECTION,
+ * T = -m_y (p_x F_x + p_y F_y) d + c_xy phi w, against Px, Vx (the adjoints
+ * of x's pressure and viscous sums over Omega_x): dT/dd, dT/dw and the
+ * adjoints of rho, p and h of x and of y, and of nu */
+template <int ND>
+struct PairVH {
+    float Dd[3], Dw[3], Rx, Ry, Qx, Qy, Hx, Hy, nu;
+};
+
+template <int ND>
+__device__ __forceinline__ PairVH<ND> force_pair_vh(float nu, float rho0, const float *d, const float *w, float r,
+                                                    const KerVH<ND> &kx, const KerVH<ND> &ky, float hav,
+                                                    const float *Px, const float *Vx, float my, float rhox,
+                                                    float rhoy, float px, float py) {
+    PairVH<ND> o;
+    float Pd = 0.f, Vw = 0.f;
+#pragma unroll
+    for (int q = 0; q < ND; q++) {
+        Pd = fmaf(Px[q], d[q], Pd);
+        Vw = fmaf(Vx[q], w[q], Vw);
+    }
+    const float ir = 1.f / r, r2 = r * r;
+    const float sp = -my * (px * kx.F + py * ky.F), spr = -my * (px * kx.Fr + py * ky.Fr);
+    const float Mf = 0.5f * (kx.F + ky.F), Mr = 0.5f * (kx.Fr + ky.Fr);
+    const float eta2 = 0.01f * hav * hav, den = 1.f / (r2 + eta2);
+    const float phi = Mf * r2 * den;
+    const float dphi = Mr * r2 * den + Mf * 2.f * r * eta2 * den * den;
+    const float dphh = -Mf * r2 * den * den * 0.01f * hav;      /* dphi/dh through hav (either particle) */
+    const float cxy = 2.f * nu * rho0 * my / (rhox * rhoy);
+    const float VT = cxy * phi * Vw;
+    const float cd = (spr * Pd + cxy * Vw * dphi) * ir;
+#pragma unroll
+    for (int q = 0; q < ND; q++) {
+        o.Dd[q] = sp * Px[q] + cd * d[q];
+        o.Dw[q] = cxy * phi * Vx[q];
+    }
+    o.Rx = -VT / rhox;
+    o.Ry = -VT / rhoy;
+    o.Qx = -my * kx.F * Pd;
+    o.Qy = -my * ky.F * Pd;
+    o.Hx = -my * px * kx.Fh * Pd + cxy * Vw * (0.5f * kx.Fh * r2 * den + dphh);
+    o.Hy = -my * py * ky.Fh * Pd + cxy * Vw * (0.5f * ky.Fh * r2 * den + dphh);
+    o.nu = VT / nu;
+    return o;
+}
+
+/* k_cp_force32 under VAR_H_CORRECTION: the middle pair terms with F(r, h_x),
+ * F(r, h_y) and 1/Omega_x, Omega_m's pair terms, then the EOS and the
+ * adjoint of rho_s with h's and Omega_m's parts */
+template <int ND>
+__global__ void __launch_bounds__(128) k_cp_force32_vh(DevCfg c, int64_t n, const int *typ,
+                                                       const int *__restrict__ nb, const int2 *__restrict__ oc,
+                                                       const double *adj, const double *aux, const double *cend,
+                                                       const float4 *__restrict__ rec, double *cmid, double *cacc,
+                                                       double *grads) {
+    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    float gnu = 0.f;
+    if (a < n && is_fluid(typ[a])) {
+        const float4 *M0 = rec + R_M0 * n, *M1 = rec + R_M1 * n, *M2 = rec + R_M2 * n, *M3 = rec + R_M3 * n,
+                     *M4 = rec + R_M4 * n, *O = rec + R_O * n;
+        const float wcon = (float)c.wcon, nu = (float)c.viscosity, rho0 = (float)c.dens;
+        const float4 p0 = M0[a], p1 = M1[a], p2 = M2[a], p3 = M3[a], p4 = M4[a], oa = O[a];
+        const float pa[3] = {p0.x, p0.y, p0.z}, la[3] = {p1.x, p1.y, p1.z}, va[3] = {p2.x, p2.y, p2.z};
+        const float ioa = 1.f / oa.x;
+        const float Pa[3] = {p3.x * ioa, p3.y * ioa, p3.z * ioa}, Va[3] = {p4.x * ioa, p4.y * ioa, p4.z * ioa};
+        const bool own = p3.x != 0.f || p3.y != 0.f || p3.z != 0.f || p4.x != 0.f || p4.y != 0.f || p4.z != 0.f;
+        const float ma = p1.w, ka = oa.z;
+        Kf Db[ND], Wb[ND], Rb, Qb, Hb;
+        const int2 o = oc[a];
+        for (int k = 0; k < o.y; k++) {
+            int sh[3];
+            const int b = table_entry(__ldg(nb + o.x + k), sh);
+            float img[3];
+            image32<ND>(c, sh, img);
+            const float4 q0 = M0[b], q1 = M1[b], q2 = M2[b], q3 = M3[b], q4 = M4[b], ob = O[b];
+            const float pb[3] = {q0.x, q0.y, q0.z}, lb[3] = {q1.x, q1.y, q1.z}, vb[3] = {q2.x, q2.y, q2.z};
+            float d[3], w[3], md[3], mw[3], r2 = 0.f;
+#pragma unroll
+            for (int q = 0; q < ND; q++) {
+                d[q] = ((pa[q] - pb[q]) + (la[q] - lb[q])) - img[q];
+                w[q] = va[q] - vb[q];
+                md[q] = -d[q];
+                mw[q] = -w[q];
+                r2 = fmaf(d[q], d[q], r2);
+            }
+            if (!(r2 > 0.f)) continue;
+            const float r = sqrtf(r2), ir = 1.f / r;
+            const KerVH<ND> kA = ker_vh<ND>(wcon, r, p0.w), kB = ker_vh<ND>(wcon, r, q0.w);
+            const float hav = 0.5f * (p4.w + q4.w);
+            const float mb = q1.w;
+            if (own) {
+                const PairVH<ND> t = force_pair_vh<ND>(nu, rho0, d, w, r, kA, kB, hav, Pa, Va, mb, p2.w, q2.w, p3.w,
+                                                       q3.w);
+#pragma unroll
+                for (int q = 0; q < ND; q++) {
+                    Db[q].add(t.Dd[q]);
+                    Wb[q].add(t.Dw[q]);
+                }
+                Rb.add(t.Rx);
+                Qb.add(t.Qx);
+                Hb.add(t.Hx);
+                gnu += t.nu;
+            }
+            if (q3.x != 0.f || q3.y != 0.f || q3.z != 0.f || q4.x != 0.f || q4.y != 0.f || q4.z != 0.f) {
+                const float iob = 1.f / ob.x;
+                const float Pb_[3] = {q3.x * iob, q3.y * iob, q3.z * iob}, Vb_[3] = {q4.x * iob, q4.y * iob, q4.z * iob};
+                const PairVH<ND> t = force_pair_vh<ND>(nu, rho0, md, mw, r, kB, kA, hav, Pb_, Vb_, ma, q2.w, p2.w,
+                                                       q3.w, p3.w);
+#pragma unroll
+                for (int q = 0; q < ND; q++) {
+                    Db[q].add(-t.Dd[q]);
+                    Wb[q].add(-t.Dw[q]);
+                }
+                Rb.add(t.Ry);
+                Qb.add(t.Qy);
+                Hb.add(t.Hy);
+            }
+            /* Omega_m's pair terms */
+            const float cR = (ka * mb * kA.Whr + ob.z * ma * kB.Whr) * ir;
+#pragma unroll
+            for (int q = 0; q < ND; q++) Db[q].add(cR * d[q]);
+            Hb.add(ka * mb * kA.Whh);
+        }
+        const double rhoa = aux[a * ADJ_AUX + 6];
+        const double eps = cmid[a * CP_NMID + CM_EPS];
+        const double x = rhoa / (c.refd * eps), x2 = x * x, x7 = x2 * x2 * x2 * x;
+        const double dp_drho = c.prb * (5.0 * x7 + 2.0) / (rhoa * rhoa * rhoa);
+        const double dp_deps = -7.0 * c.prb * x7 / (eps * rhoa * rhoa);
+        double *ac = cacc + a * CP_NACC;
+        const double *aa = adj + a * ADJ_NC, *ea = cend + a * CP_NEND;
+        const double Qv = Qb.value();
+        /* Omega_m's own h and rho, then h = hfac (m / rho)^(1/d) */
+        const double ih = p0.w, h = 1.0 / ih;
+        const double ombar = (double)ka * (double)p2.w * ND * ih;
+        const double hbar = ac[CA_HB] + Hb.value() + ombar * ((double)oa.x - 1.0) * ih +
+                            (double)ka * ma * (double)ker_vh<ND>(wcon, 0.f, p0.w).Whh;
+        ac[CA_RHOS] = aa[AS_DENS] + ac[CA_RHO] + Rb.value() + Qv * dp_drho - ombar * ((double)oa.x - 1.0) / rhoa -
+                      hbar * h / (ND * rhoa);
+        const double epsb = ac[CA_EPS] + Qv * dp_deps;
+        ac[CA_EBAR] = cmid[a * CP_NMID + CM_CLAMP] != 0.0 ? 0.0 : -epsb;
+        for (int q = 0; q < 3; q++) {
+            ac[CA_RS + q] = ea[CE_R1 + q] + (q < ND ? Db[q].value() : 0.0);
+            cmid[a * CP_NMID + CM_VHS + q] = q < ND ? Wb[q].value() : 0.0;
+        }
+    }
+    gnu += __shfl_xor_sync(0xffffffffu, gnu, 16);
+    gnu += __shfl_xor_sync(0xffffffffu, gnu, 8);
+    gnu += __shfl_xor_sync(0xffffffffu, gnu, 4);
+    gnu += __shfl_xor_sync(0xffffffffu, gnu, 2);
+    gnu += __shfl_xor_sync(0xffffffffu, gnu, 1);
+    if ((threadIdx.x & 31) == 0 && gnu != 0.f) atomicAdd(&grads[3], (double)gnu);
+}
+
 }  // namespace
 
 void cpl_count_tables(sphdem_ctx *c, AdjointData *a) {
@@ -1539,6 +1885,7 @@ void cpl_alloc(sphdem_ctx *c, AdjointData *a) {
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->trw.tsum, (size_t)SC_THREADS * SC_SUMS_PER * sizeof(int)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->trw.tmp, (size_t)std::max(a->cpl.cap, a->fpi.cap) * sizeof(int2)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->coef, (size_t)n * CP_NCOEF * sizeof(double)));
+    if (c->cfg.var_h()) SPHDEM_CUDA_CHECK(cudaMalloc(&a->hs, (size_t)n * sizeof(double)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->ct.nb, (size_t)K * a->ct_cap * sizeof(int)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->ct.oc, (size_t)K * n * sizeof(int2)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->ct.cnt, (size_t)K * sizeof(int)));
@@ -1559,8 +1906,9 @@ void cpl_free(AdjointData *a) {
     for (int *p : {a->cplT.nb, a->cplT.ix, a->fpiT.nb, a->fpiT.ix, a->trw.cnt, a->trw.fill, a->trw.off, a->trw.tsum})
         cudaFree(p);
     for (void *p : {(void *)a->cplT.oc, (void *)a->fpiT.oc, (void *)a->trw.tmp, (void *)a->coef, a->g4_cpl, a->gw_cpl,
-                    a->g4_fpi, a->gw_fpi})
+                    a->g4_fpi, a->gw_fpi, (void *)a->hs})
         cudaFree(p);
+    a->hs = nullptr;
     a->g4_cpl = a->gw_cpl = a->g4_fpi = a->gw_fpi = nullptr;
     a->cplT = TrTable{};
     a->fpiT = TrTable{};
@@ -1640,7 +1988,7 @@ namespace {
 /* the coupling passes of the reverse step with pair math in M */
 template <typename M>
 void cpl_backward_coupling(sphdem_ctx *c, AdjointData *a, int sl, const double *s0, const double *s1, double dt,
-                           bool after_forces) {
+                           bool after_forces, const double *hp) {
     using V4 = typename MT<M>::V4;
     const int64_t n = c->n;
     const int nd = a->n_dem;
@@ -1656,15 +2004,21 @@ void cpl_backward_coupling(sphdem_ctx *c, AdjointData *a, int sl, const double *
         transpose<false>(c, a, nbc, occ, a->cplT);
         SPHDEM_LAUNCH(c, "adj_por", k_cp_por<M>, g, CB, 0, c->cfg, n, a->aux, a->typ, occ, gwc, a->cmid);
         if (nd == 0) return;
-        SPHDEM_LAUNCH(c, "adj_geo_fpi", k_cp_geo_fpi<M>, gd, CB, 0, c->cfg, nd, a->dem_tags, s1, a->hh, nbf, ocf, g4f,
+        SPHDEM_LAUNCH(c, "adj_geo_fpi", k_cp_geo_fpi<M>, gd, CB, 0, c->cfg, nd, a->dem_tags, s1, hp, nbf, ocf, g4f,
                       gwf);
         transpose<true>(c, a, nbf, ocf, a->fpiT);
         SPHDEM_LAUNCH(c, "adj_shep", k_cp_shep<M>, gd, CB, 0, nd, a->dem_tags, a->aux, a->mass, a->cplT.nb, a->cplT.ix,
                       a->cplT.oc, gwc, a->cmid);
         SPHDEM_LAUNCH(c, "adj_fpi_dem", k_cp_fpi<M>, gd, CB, 0, c->cfg, nd, a->dem_tags, dt, s1, a->aux, a->cmid,
                       a->mass, nbf, ocf, g4f, gwf, a->adj, a->cacc, a->coef, a->grads);
-        SPHDEM_LAUNCH(c, "adj_fpi_fluid", k_cp_fpi_fluid<M>, g, CB, 0, n, c->cfg.nd, s1, a->aux, a->cmid, a->mass,
-                      a->typ, a->fpiT.nb, a->fpiT.ix, a->fpiT.oc, g4f, gwf, a->coef, a->cacc);
+        if (c->cfg.var_h())
+            SPHDEM_LAUNCH(c, "adj_fpi_fluid", (k_cp_fpi_fluid<M, true>), g, CB, 0, n, c->cfg.nd, s1, a->aux, a->cmid,
+                          a->mass, a->typ, a->fpiT.nb, a->fpiT.ix, a->fpiT.oc, g4f, gwf, a->coef, a->cacc, hp,
+                          c->cfg.wcon);
+        else
+            SPHDEM_LAUNCH(c, "adj_fpi_fluid", (k_cp_fpi_fluid<M, false>), g, CB, 0, n, c->cfg.nd, s1, a->aux, a->cmid,
+                          a->mass, a->typ, a->fpiT.nb, a->fpiT.ix, a->fpiT.oc, g4f, gwf, a->coef, a->cacc, hp,
+                          c->cfg.wcon);
         return;
     }
     /* porosity, DEM -> fluid drag and Shepard terms, after the forces gave
@@ -1690,36 +2044,48 @@ void cpl_backward_step(sphdem_ctx *c, AdjointData *a, int j, double dt) {
     const int *nbm = a->nb_mid + (size_t)sl * a->pair_cap, *nbe = a->nb_end + (size_t)sl * a->pair_cap;
     const int2 *ocm = a->oc_mid + (size_t)sl * n, *oce = a->oc_end + (size_t)sl * n;
     const int g = grid_for(n, CB), g256 = grid_for(n, 256);
-    const bool mixed = a->crec != nullptr;
+    const bool mixed = a->crec != nullptr, vh = c->cfg.var_h();
+    /* the step's smoothing lengths: h_s under VAR_H_CORRECTION, else constant */
+    const double *hp = vh ? a->hs : a->hh;
     cudaStream_t st = c->stream;
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cacc, 0, (size_t)n * CP_NACC * sizeof(double), st));
     SPHDEM_CUDA_CHECK(cudaMemsetAsync(a->cmid, 0, (size_t)n * CP_NMID * sizeof(double), st));
-    SPHDEM_LAUNCH(c, "adj_pre", k_cp_pre, g256, 256, 0, n, dt, s0, rm, a->typ, a->aux);
-    if (mixed) cpl_backward_coupling<float>(c, a, sl, s0, s1, dt, false);
-    else cpl_backward_coupling<double>(c, a, sl, s0, s1, dt, false);
+    SPHDEM_LAUNCH(c, "adj_pre", k_cp_pre, g256, 256, 0, n, dt, s0, rm, a->typ, a->aux, a->mass, a->hh,
+                  vh ? a->hs : nullptr, c->cfg.hfac, c->cfg.nd);
+    if (mixed) cpl_backward_coupling<float>(c, a, sl, s0, s1, dt, false, hp);
+    else cpl_backward_coupling<double>(c, a, sl, s0, s1, dt, false, hp);
     SPHDEM_LAUNCH(c, "adj_contacts", k_cp_dem, g, CB, 0, c->cfg, n, dt, s1, a->aux, a->mass, a->rad, a->typ,
                   nbp(a->ct), ocp(a->ct), a->adj, a->cacc, a->grads);
     if (mixed) {
-        SPHDEM_LAUNCH(c, "adj_pack32", k_cp_pack32, g256, 256, 0, n, dt, a->aux, a->cmid, s1, a->adj, a->mass, a->hh,
+        SPHDEM_LAUNCH(c, "adj_pack32", k_cp_pack32, g256, 256, 0, n, dt, a->aux, a->cmid, s1, a->adj, a->mass, hp,
                       a->typ, a->crec);
 #define L_(ND)                                                                                                   \
     do {                                                                                                         \
-        SPHDEM_LAUNCH(c, "adj_end32", k_cp_end32<ND>, g, CB, 0, c->cfg, n, dt, a->typ, nbe, oce, a->adj, a->cacc, \
-                      a->cend, a->crec);                                                                         \
-        SPHDEM_LAUNCH(c, "adj_force32", k_cp_force32<ND>, g, CB, 0, c->cfg, n, a->typ, nbm, ocm, a->adj, a->aux,  \
-                      a->cend, a->crec, a->cmid, a->cacc, a->grads);                                             \
+        if (vh) {                                                                                                \
+            SPHDEM_LAUNCH(c, "adj_omega32", k_cp_omega32<ND>, g, CB, 0, n, (float)c->cfg.wcon, a->typ, nbm, ocm, \
+                          nbe, oce, c->cfg, s1, a->crec);                                                         \
+            SPHDEM_LAUNCH(c, "adj_end32", k_cp_end32_vh<ND>, g, CB, 0, c->cfg, n, dt, a->typ, nbe, oce, a->adj,   \
+                          s1, a->cacc, a->cend, a->crec);                                                         \
+            SPHDEM_LAUNCH(c, "adj_force32", k_cp_force32_vh<ND>, g, CB, 0, c->cfg, n, a->typ, nbm, ocm, a->adj,   \
+                          a->aux, a->cend, a->crec, a->cmid, a->cacc, a->grads);                                  \
+        } else {                                                                                                 \
+            SPHDEM_LAUNCH(c, "adj_end32", k_cp_end32<ND>, g, CB, 0, c->cfg, n, dt, a->typ, nbe, oce, a->adj,      \
+                          a->cacc, a->cend, a->crec);                                                             \
+            SPHDEM_LAUNCH(c, "adj_force32", k_cp_force32<ND>, g, CB, 0, c->cfg, n, a->typ, nbm, ocm, a->adj,      \
+                          a->aux, a->cend, a->crec, a->cmid, a->cacc, a->grads);                                  \
+        }                                                                                                        \
     } while (0)
         if (c->cfg.nd == 3) L_(3);
         else if (c->cfg.nd == 2) L_(2);
         else L_(1);
 #undef L_
-        cpl_backward_coupling<float>(c, a, sl, s0, s1, dt, true);
+        cpl_backward_coupling<float>(c, a, sl, s0, s1, dt, true, hp);
     } else {
         SPHDEM_LAUNCH(c, "adj_end", k_cp_end, g, CB, 0, c->cfg, n, dt, s1, a->mass, a->hh, a->typ, nbe, oce, a->adj,
                       a->cacc, a->cend);
         SPHDEM_LAUNCH(c, "adj_force", k_cp_force, g, CB, 0, c->cfg, n, a->aux, a->mass, a->hh, a->typ, nbm, ocm,
                       a->adj, a->cend, a->cmid, a->cacc, a->grads);
-        cpl_backward_coupling<double>(c, a, sl, s0, s1, dt, true);
+        cpl_backward_coupling<double>(c, a, sl, s0, s1, dt, true, hp);
     }
     SPHDEM_LAUNCH(c, "adj_assemble", k_cp_assemble, g256, 256, 0, n, dt, a->typ, a->cacc, a->cend, a->cmid, a->adj);
 }

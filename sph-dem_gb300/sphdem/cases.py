@@ -557,6 +557,9 @@ def workload(name: str, **kw) -> Case:
         # adjoint covers (three fixed sphBoundary floor layers, constant h)
         "sediment3d_adjoint": lambda: sediment3d(nx=37, n_dem=5000, nsteps=500, seed=4, floor="sphb3",
                                                  var_h=False),
+        # the same with the coupled configuration's VAR_H_CORRECTION
+        "sediment3d_adjoint_varh": lambda: sediment3d(nx=37, n_dem=5000, nsteps=500, seed=4, floor="sphb3",
+                                                      var_h=True),
         # small parity cases (seconds on one CPU core)
         "dambreak2d_small": lambda: dambreak2d(dx=0.05, nsteps=40),
         # damBreak's own options: Monaghan viscosity (nu = 1e-2), anticlumping,
@@ -596,6 +599,9 @@ def workload(name: str, **kw) -> Case:
                                                       reinit_every=4),
         "sediment3d_adjoint_small": lambda: sediment3d(nx=10, L=0.04, height=0.08, n_dem=60, nsteps=30,
                                                        floor="sphb3", var_h=False, viscosity=1e-4),
+        # the same with sediment3D's VAR_H_CORRECTION (h following density)
+        "sediment3d_adjoint_varh_small": lambda: sediment3d(nx=10, L=0.04, height=0.08, n_dem=60, nsteps=30,
+                                                            floor="sphb3", var_h=True, viscosity=1e-4),
     }
     if name not in table:
         raise KeyError(f"unknown workload {name!r}; known: {sorted(table)}")

@@ -296,6 +296,62 @@ def test_coupled_adjoint_vs_central_differences(lib, precision):
         assert abs(ad - fd) <= RTOL * abs(fd), f"DEM direction {k}: adjoint {ad} fd {fd}"
 
 
+def moving_coupled_varh():
+    """moving_coupled() with VAR_H_CORRECTION: h follows the density
+    (h = 1.5 (m / rho)^(1/3)) and the gradients carry 1/Omega."""
+    base = moving_coupled()
+    case = cases.workload("sediment3d_adjoint_varh_small")
+    for k in ("r", "v", "vhat"):
+        case.particles[k] = base.particles[k].copy()
+    return case
+
+
+def test_coupled_varh_adjoint_vs_central_differences(lib):
+    """The coupled adjoint under VAR_H_CORRECTION (mixed-precision handles)
+    against FP64 central differences: the four scalars, DEM positions and
+    fluid positions (whose pair terms carry the h and Omega derivatives)."""
+    case = moving_coupled_varh()
+    sim = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    sim.adjoint_forward(CPL_STEPS, CPL_K)
+    L0, dr, dv = cpl_loss_and_seed(sim)
+    grads, dr0, _, _ = sim.adjoint_backward(dL_dr=dr, dL_dv=dv)
+    sim.close()
+    want = (capi.GRAD_DEM_K | capi.GRAD_DEM_GAMMA | capi.GRAD_VISCOSITY | capi.GRAD_DRAG_SCALE
+            | capi.GRAD_POSITIONS)
+    assert grads.valid & want == want
+    for name, rel in (("dem_k", 1e-6), ("dem_gamma", 1e-6), ("viscosity", 1e-4), ("drag_scale", 1e-4)):
+        base = case.cfg.get(name, 1.0)
+        eps = rel * base
+        cp, cm = dict(case.cfg), dict(case.cfg)
+        cp[name], cm[name] = base + eps, base - eps
+        fd = (cpl_run_loss(lib, case, cfg=cp) - cpl_run_loss(lib, case, cfg=cm)) / (2 * eps)
+        ad = getattr(grads, name)
+        print("varh", name, "adjoint", ad, "fd", fd)
+        assert abs(ad - fd) <= RTOL * abs(fd), f"{name}: adjoint {ad} fd {fd}"
+    rng = np.random.default_rng(11)
+    r0 = np.asarray(case.particles["r"], dtype=np.float64).copy()
+    iam = np.asarray(case.particles["iam"])
+    scale = np.abs(r0).max()
+    smooth = 0
+    for kind, mask in (("DEM", iam == cases.DEM), ("fluid", iam == cases.SPH)):
+        for k in range(4):
+            u = np.zeros_like(r0)
+            u[mask] = rng.normal(size=(mask.sum(), 3))
+            u /= np.linalg.norm(u)
+            ad = float((dr0 * u).sum())
+            fds = []
+            for e in (1e-6, 0.25e-6):
+                eps = e * scale
+                fds.append((cpl_run_loss(lib, case, r=r0 + eps * u) - cpl_run_loss(lib, case, r=r0 - eps * u))
+                           / (2 * eps))
+            print("varh", kind, "direction", k, "adjoint", ad, "fd", fds)
+            if abs(fds[0] - fds[1]) > RTOL * abs(fds[1]):
+                continue      # a discontinuity of the step inside the bracket
+            smooth += 1
+            assert abs(ad - fds[1]) <= RTOL * abs(fds[1]), f"{kind} direction {k}: adjoint {ad} fd {fds}"
+    assert smooth >= 6
+
+
 def test_coupled_forward_taps_equal_scanned_tables(lib, monkeypatch):
     """Mixed handles take the reverse sweep's coupling, FPI and contact tables
     from the forward passes that evaluate those pairs (k_couple, k_dem_end);
