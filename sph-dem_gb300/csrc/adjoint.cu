@@ -118,6 +118,7 @@ __global__ void k_save(DevState s, int64_t n, double *dst, const int *slot, int 
         o[AS_FP + d] = s.row(FD_FP + d)[k];
         o[AS_FV + d] = s.row(FD_FV + d)[k];
     }
+    o[AS_OME] = s.row(FD_OMEGA)[k];
 }
 
 __global__ void k_restore(DevState s, int64_t n, const double *src) {
@@ -938,7 +939,7 @@ int tape_blocks(sphdem_ctx *c, AdjointData *a, int nseg) {
                   K * (2 * a->pair_cap * (int64_t)sizeof(int) + 2 * n * (int64_t)sizeof(int2));
     if (a->mode == ADJ_MODE_COUPLED)
         blk += K * ((a->cpl.cap + a->fpi.cap + a->ct_cap) * (int64_t)sizeof(int) + 3 * n * (int64_t)sizeof(int2) +
-                    3 * (int64_t)sizeof(int) + n * 3 * (int64_t)sizeof(double));
+                    3 * (int64_t)sizeof(int) + n * RM_NC * (int64_t)sizeof(double));
     int64_t budget = c->adj_tape_mem;
     if (budget < 0) {   /* half of the device memory free now */
         size_t fr = 0, tot = 0;

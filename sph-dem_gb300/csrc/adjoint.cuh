@@ -11,13 +11,14 @@
 namespace sphdem {
 
 /* per-particle state record in tag order: r, v, vh, f, dens, dddt, fdrag
- * (the DEM drag the next middle phase spreads to the fluid), and the
- * pressure / viscous force parts fp, fv of the fluid (read by the end
- * phase's FPI) */
+ * (the DEM drag the next middle phase spreads to the fluid), the pressure /
+ * viscous force parts fp, fv of the fluid (read by the end phase's FPI),
+ * and Omega of the end phase's continuity pass (VAR_H_CORRECTION) */
 enum : int {
     AS_R = 0, AS_V = 3, AS_VH = 6, AS_F = 9, AS_DENS = 12, AS_DDDT = 13, AS_FDRAG = 14, AS_FP = 17, AS_FV = 20,
-    ADJ_NC = 23
+    AS_OME = 23, ADJ_NC = 24
 };
+constexpr int RM_NC = 4;           /* coupled: middle-phase record per particle, r and Omega of the force pass */
 constexpr int ADJ_MAX_CONTACTS = 32;
 constexpr int ADJ_AUX = 8;         /* SPH: r_s, vh_s, rho_s, pdr2_s */
 constexpr int ADJ_NREC = 7;        /* SPH, mixed: float4 records per particle */
@@ -93,7 +94,7 @@ struct AdjointData {
     PairTable fpi;                  /* DEM -> fluid pairs of calcFPI (end phase), by DEM particle */
     PairTable ct;                   /* DEM contacts (end phase), by DEM particle */
     int64_t ct_cap = 0;
-    double *rmid = nullptr;         /* positions after each step's middle phase, K x n x 3 */
+    double *rmid = nullptr;         /* r and Omega after each step's middle phase, K x n x RM_NC */
     double *cacc = nullptr;         /* CP_NACC accumulators per particle */
     double *cend = nullptr;         /* CP_NEND end-phase results per particle */
     double *cmid = nullptr;         /* CP_NMID middle intermediates per particle */

@@ -316,12 +316,14 @@ __global__ void k_cp_ct_table(DevCfg c, DevState s, const int *start, const DevG
     if (k > per) atomicMax(cnt + j, (int)cap + 1);
 }
 
-/* positions after the middle phase, tag order, at slot *slot */
+/* positions and Omega of the force pass after the middle phase, tag order,
+ * at slot *slot */
 __global__ void k_cp_tap_r(DevState s, int64_t n, double *rmid, const int *slot) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k >= n) return;
-    double *o = rmid + ((int64_t)(*slot) * n + s.irow(FI_TAG)[k]) * 3;
+    double *o = rmid + ((int64_t)(*slot) * n + s.irow(FI_TAG)[k]) * RM_NC;
     for (int d = 0; d < 3; d++) o[d] = s.row(FD_R + d)[k];
+    o[3] = s.row(FD_OMEGA)[k];
 }
 
 /* ---- reverse pass of one step ------------------------------------------ */
@@ -361,7 +363,7 @@ __global__ void k_cp_pre(int64_t n, double dt, const double *s0, const double *r
     const int t = typ[i];
     for (int d = 0; d < 3; d++) {
         /* DEM: the snapshot is r_m = r_s + hd vh0 in the middle rebuild's frame */
-        o[d] = t == T_DEM ? rm[i * 3 + d] - hd * x[AS_VH + d] : rm[i * 3 + d];
+        o[d] = t == T_DEM ? rm[i * RM_NC + d] - hd * x[AS_VH + d] : rm[i * RM_NC + d];
         o[3 + d] = (t == T_SPH || t == T_DEM) ? x[AS_VH + d] + hd * x[AS_F + d] : x[AS_VH + d];
     }
     o[6] = x[AS_DENS] + hd * x[AS_DDDT];
@@ -1322,8 +1324,12 @@ __global__ void k_cp_assemble(int64_t n, double dt, const int *typ, const double
  * Kahan-compensated and land in the FP64 accumulators once. */
 enum { R_M0 = 0, R_M1, R_M2, R_M3, R_M4, R_E0, R_E1, R_E2, R_O };
 
+/* rm (VAR_H_CORRECTION): the middle record, whose Omega with the end one
+ * gives R_O = (Omega_m, Omega_e, kappa_m (set by k_cp_end32_vh), kappa_e),
+ * kappa_e = Omegabar_e h / (rho d), Omegabar_e = -Dbar dddt1 / Omega_e */
 __global__ void k_cp_pack32(int64_t n, double dt, const double *aux, const double *cmid, const double *s1,
-                            const double *adj, const double *mass, const double *hh, const int *typ, float4 *rec) {
+                            const double *adj, const double *mass, const double *hh, const int *typ, float4 *rec,
+                            const double *rm, int nd) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n || !is_fluid(typ[i])) return;
     const double *x = aux + i * ADJ_AUX, *x1 = s1 + i * ADJ_NC, *aa = adj + i * ADJ_NC;
@@ -1339,8 +1345,13 @@ __global__ void k_cp_pack32(int64_t n, double dt, const double *aux, const doubl
     for (int d = 0; d < 3; d++) split2(x1[AS_R + d], hi[d], lo[d]);
     rec[R_E0 * n + i] = make_float4(hi[0], hi[1], hi[2], ih);
     rec[R_E1 * n + i] = make_float4(lo[0], lo[1], lo[2], m);
-    rec[R_E2 * n + i] = make_float4((float)x1[AS_VH], (float)x1[AS_VH + 1], (float)x1[AS_VH + 2],
-                                    (float)(aa[AS_DDDT] + hd * aa[AS_DENS]));
+    const double Db = aa[AS_DDDT] + hd * aa[AS_DENS];
+    rec[R_E2 * n + i] = make_float4((float)x1[AS_VH], (float)x1[AS_VH + 1], (float)x1[AS_VH + 2], (float)Db);
+    if (rm) {
+        const double ome = x1[AS_OME];
+        rec[R_O * n + i] = make_float4((float)rm[i * RM_NC + 3], (float)ome, 0.f,
+                                       (float)(-Db * x1[AS_DDDT] / ome * hh[i] / (x[6] * nd)));
+    }
 }
 
 template <int ND>
@@ -1557,50 +1568,6 @@ __device__ __forceinline__ KerVH<ND> ker_vh(float wcon, float r, float ih) {
     k.Whr = -wcon * i2 * gp;
     k.Whh = wcon * i2 * ((float)(ND + 1) * g + q * gp);
     return k;
-}
-
-/* Omega of the middle and end pair sets of every fluid particle, and the
- * end one's adjoint factor kappa_e = Omegabar_e h / (rho d), Omegabar_e =
- * -Dbar dddt1 / Omega_e: record R_O = (Omega_m, Omega_e, kappa_m (set by
- * k_cp_end32_vh), kappa_e) */
-template <int ND>
-__global__ void __launch_bounds__(128) k_cp_omega32(int64_t n, float wcon, const int *typ,
-                                                    const int *__restrict__ nbm, const int2 *__restrict__ ocm,
-                                                    const int *__restrict__ nbe, const int2 *__restrict__ oce,
-                                                    const DevCfg c, const double *s1, float4 *rec) {
-    const int64_t a = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (a >= n || !is_fluid(typ[a])) return;
-    float om[2];
-    for (int ph = 0; ph < 2; ph++) {
-        const float4 *X0 = rec + (ph ? R_E0 : R_M0) * n, *X1 = rec + (ph ? R_E1 : R_M1) * n;
-        const int *nb = ph ? nbe : nbm;
-        const int2 o = (ph ? oce : ocm)[a];
-        const float4 p0 = X0[a], p1 = X1[a];
-        const float ih = p0.w;
-        Kf S;
-        S.add(p1.w * w_dh<ND, float>(wcon, 0.f, ih));
-        for (int k = 0; k < o.y; k++) {
-            int sh[3];
-            const int b = table_entry(__ldg(nb + o.x + k), sh);
-            float img[3];
-            image32<ND>(c, sh, img);
-            const float4 q0 = X0[b], q1 = X1[b];
-            const float pa[3] = {p0.x, p0.y, p0.z}, la[3] = {p1.x, p1.y, p1.z};
-            const float pb[3] = {q0.x, q0.y, q0.z}, lb[3] = {q1.x, q1.y, q1.z};
-            float r2 = 0.f;
-#pragma unroll
-            for (int q = 0; q < ND; q++) {
-                const float dq = ((pa[q] - pb[q]) + (la[q] - lb[q])) - img[q];
-                r2 = fmaf(dq, dq, r2);
-            }
-            S.add(q1.w * w_dh<ND, float>(wcon, sqrtf(r2), ih));
-        }
-        const float rho = rec[R_M2 * n + a].w;
-        om[ph] = 1.f + (float)(S.value()) / (ih * rho * (float)ND);
-    }
-    const float rho = rec[R_M2 * n + a].w, h = 1.f / rec[R_M0 * n + a].w;
-    const float ombar_e = -rec[R_E2 * n + a].w * (float)s1[a * ADJ_NC + AS_DDDT] / om[1];
-    rec[R_O * n + a] = make_float4(om[0], om[1], 0.f, ombar_e * h / (rho * (float)ND));
 }
 
 /* k_cp_end32 under VAR_H_CORRECTION: continuity with F(r, h_a) / Omega_a and
@@ -1890,7 +1857,7 @@ void cpl_alloc(sphdem_ctx *c, AdjointData *a) {
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->ct.oc, (size_t)K * n * sizeof(int2)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->ct.cnt, (size_t)K * sizeof(int)));
     a->ct.cap = a->ct_cap;
-    SPHDEM_CUDA_CHECK(cudaMalloc(&a->rmid, (size_t)K * n * 3 * sizeof(double)));
+    SPHDEM_CUDA_CHECK(cudaMalloc(&a->rmid, (size_t)K * n * RM_NC * sizeof(double)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->cacc, (size_t)n * CP_NACC * sizeof(double)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->cend, (size_t)n * CP_NEND * sizeof(double)));
     SPHDEM_CUDA_CHECK(cudaMalloc(&a->cmid, (size_t)n * CP_NMID * sizeof(double)));
@@ -2038,7 +2005,7 @@ void cpl_backward_step(sphdem_ctx *c, AdjointData *a, int j, double dt) {
     const size_t stb = (size_t)a->blk * (a->K + 1);
     const double *s0 = a->seg + (stb + j - 1) * n * ADJ_NC, *s1 = a->seg + (stb + j) * n * ADJ_NC;
     const int sl = a->blk * a->K + j - 1;
-    const double *rm = a->rmid + (size_t)sl * n * 3;
+    const double *rm = a->rmid + (size_t)sl * n * RM_NC;
     auto nbp = [&](const PairTable &t) { return t.nb + (size_t)sl * t.cap; };
     auto ocp = [&](const PairTable &t) { return t.oc + (size_t)sl * n; };
     const int *nbm = a->nb_mid + (size_t)sl * a->pair_cap, *nbe = a->nb_end + (size_t)sl * a->pair_cap;
@@ -2058,12 +2025,10 @@ void cpl_backward_step(sphdem_ctx *c, AdjointData *a, int j, double dt) {
                   nbp(a->ct), ocp(a->ct), a->adj, a->cacc, a->grads);
     if (mixed) {
         SPHDEM_LAUNCH(c, "adj_pack32", k_cp_pack32, g256, 256, 0, n, dt, a->aux, a->cmid, s1, a->adj, a->mass, hp,
-                      a->typ, a->crec);
+                      a->typ, a->crec, vh ? rm : nullptr, c->cfg.nd);
 #define L_(ND)                                                                                                   \
     do {                                                                                                         \
         if (vh) {                                                                                                \
-            SPHDEM_LAUNCH(c, "adj_omega32", k_cp_omega32<ND>, g, CB, 0, n, (float)c->cfg.wcon, a->typ, nbm, ocm, \
-                          nbe, oce, c->cfg, s1, a->crec);                                                         \
             SPHDEM_LAUNCH(c, "adj_end32", k_cp_end32_vh<ND>, g, CB, 0, c->cfg, n, dt, a->typ, nbe, oce, a->adj,   \
                           s1, a->cacc, a->cend, a->crec);                                                         \
             SPHDEM_LAUNCH(c, "adj_force32", k_cp_force32_vh<ND>, g, CB, 0, c->cfg, n, a->typ, nbm, ocm, a->adj,   \

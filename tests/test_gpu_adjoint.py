@@ -435,8 +435,8 @@ def test_adjoint_rejects_unsupported_fluid(lib):
 CFG4_STEPS, CFG4_K = 20, 10
 
 
-def cfg4_case():
-    case = cases.workload("sediment3d_adjoint")
+def cfg4_case(var_h=False):
+    case = cases.workload("sediment3d_adjoint_varh" if var_h else "sediment3d_adjoint")
     iam = np.asarray(case.particles["iam"])
     rng = np.random.default_rng(10)
     # spheres in touching pairs (2 % overlap), so that the contacts act from
@@ -469,11 +469,13 @@ def cfg4_loss(lib, case, cfg=None, r=None):
     return L
 
 
-def test_config4_coupled_adjoint_vs_central_differences(lib):
-    case = cfg4_case()
+@pytest.mark.parametrize("var_h", [False, True], ids=["const_h", "var_h"])
+def test_config4_coupled_adjoint_vs_central_differences(lib, var_h):
+    """var_h: the coupled configuration's VAR_H_CORRECTION (mixed handles)."""
+    case = cfg4_case(var_h)
     assert case.notes["n_dem"] == 5000 and case.notes["n_fluid"] > 98000
     grads = {}
-    for prec in (cases.PREC_FP64, cases.PREC_MIXED):
+    for prec in ((cases.PREC_MIXED,) if var_h else (cases.PREC_FP64, cases.PREC_MIXED)):
         sim = capi.Simulation(lib, case.cfg, case.particles, precision=prec)
         sim.adjoint_forward(CFG4_STEPS, CFG4_K)
         L0, dr, dv = cpl_loss_and_seed(sim)
