@@ -11,6 +11,12 @@ particles), checked every 100 steps from the same input.
   of the coupled sedimentation workload with a single DEM sphere and a floor
   of three fixed sphBoundary layers: the bar holds at every checkpoint to
   step 1000.
+- The coupled workload at its full size (1,080,400 particles): every 100
+  steps along a 1000-step mixed run, an FP64 handle started from the mixed
+  handle's state takes the same step; the two agree to the bar in rho and f
+  at every checkpoint.  This bounds the mixed arithmetic's own error at each
+  point of the run, apart from the flow's amplification of earlier
+  differences (below).
 - The coupled workload as configured (the same sub-box with its 3,125 DEM
   spheres and the repulsive boundary floor): the bar holds at the first
   checkpoint, and the runs then separate at the rate the sedimenting
@@ -82,6 +88,50 @@ def test_dambreak_mixed_vs_fp64_1000_steps(lib):
     rows = _against_fp64(lib, case, {"mixed": (cases.PREC_MIXED, case.particles)})["mixed"]
     for s, e_rho, e_f in rows:
         assert e_rho <= TOL and e_f <= TOL, f"step {s}: {e_rho:.2e} {e_f:.2e}"
+
+
+# the state a step starts from: the fields creation takes, then the forces,
+# continuity rates, lagged DEM drag and energy rates, and the step globals
+STATE_INIT = ("iam", "r", "v", "vhat", "mass", "dens", "h", "radius", "norm1", "norm2", "norm3")
+STATE_SET = ("f", "fp", "fv", "fb", "dddt", "fdrag", "u", "e_visc", "dudt", "de_visc_dt")
+
+
+def _clone(lib, cfg, src, precision):
+    """A new handle of `precision` holding src's state, as an exact restart does."""
+    a = src.get(capi.FIELD_ALL)
+    dst = capi.Simulation(lib, cfg, {k: np.array(a[k]) for k in STATE_INIT}, precision=precision)
+    buf = dst.get(capi.FIELD_ALL)
+    for k in STATE_SET:
+        buf[k][...] = a[k]
+    dst.set(buf, capi.FIELD_F | capi.FIELD_DDDT | capi.FIELD_COUPLING | capi.FIELD_ENERGY)
+    dst.set_globals(src.globals())
+    return dst
+
+
+def test_coupled_full_size_one_step_error_along_1000_steps(lib):
+    """The 1.08M coupled workload: at every 100th step of a 1000-step mixed
+    run, one step from the mixed state in FP64 against the mixed step."""
+    case = cases.workload("sediment3d")
+    rho0 = case.cfg["dens"]
+    m = capi.Simulation(lib, case.cfg, case.particles, precision=cases.PREC_MIXED)
+    worst = (0.0, 0.0)
+    try:
+        for c in range(NSTEPS // EVERY):
+            m.step(EVERY - 1)
+            f = _clone(lib, case.cfg, m, cases.PREC_FP64)
+            try:
+                m.step(1)
+                f.step(1)
+                e_rho, e_f = _err(m.get(MASK), f.get(MASK), rho0)
+            finally:
+                f.close()
+            print(f"step {EVERY * (c + 1)}: one step mixed vs FP64 from the same state: "
+                  f"max|drho|/rho0 {e_rho:.2e}  max|df|/max|f| {e_f:.2e}")
+            worst = (max(worst[0], e_rho), max(worst[1], e_f))
+            assert e_rho <= TOL and e_f <= TOL, f"step {EVERY * (c + 1)}: {e_rho:.2e} {e_f:.2e}"
+    finally:
+        m.close()
+    print(f"worst over the run: {worst[0]:.2e} {worst[1]:.2e}")
 
 
 def _coupled_box(floor="boundary", n_dem=3125):
