@@ -1353,6 +1353,61 @@ int oracle_get(void *h, SphDemParticles *o) {
     return 0;
 }
 
+/* Write the fields the mask selects (the SPHDEM_FIELD_* groups of
+ * sphdem_set_fields), container order; as a case hook writes them between
+ * phases through the façade's host mirror. */
+int oracle_set(void *h, uint32_t mask, const SphDemParticles *in) {
+    Sim *s = static_cast<Sim *>(h);
+    const int n = s->ps.size();
+    if (in->n != n) return SPHDEM_ERR_INVALID;
+    for (int k = 0; k < n; k++) {
+        Part &p = s->ps[k];
+        auto get3 = [&](double *dst, const double *src) {
+            if (src) for (int i = 0; i < 3; i++) dst[i] = src[3 * k + i];
+        };
+        auto get1 = [&](double &dst, const double *src) { if (src) dst = src[k]; };
+        if (mask & SPHDEM_FIELD_R) get3(p.r, in->r);
+        if (mask & SPHDEM_FIELD_V) get3(p.v, in->v);
+        if (mask & SPHDEM_FIELD_VHAT) get3(p.vhat, in->vhat);
+        if (mask & SPHDEM_FIELD_MASS) get1(p.mass, in->mass);
+        if (mask & SPHDEM_FIELD_DENS) get1(p.dens, in->dens);
+        if (mask & SPHDEM_FIELD_H) get1(p.h, in->h);
+        if (mask & SPHDEM_FIELD_F) {
+            get3(p.f, in->f); get3(p.fp, in->fp); get3(p.fv, in->fv); get3(p.fb, in->fb);
+        }
+        if (mask & SPHDEM_FIELD_DDDT) get1(p.dddt, in->dddt);
+        if (mask & SPHDEM_FIELD_PRESS) {
+            get1(p.press, in->press); get1(p.pdr2, in->pdr2);
+        }
+        if (mask & SPHDEM_FIELD_COUPLING) {
+            get1(p.porosity, in->porosity); get1(p.dpordt, in->dporositydt); get1(p.shep, in->shep_sum);
+            get3(p.fdrag, in->fdrag); get3(p.fvel, in->fvel); get3(p.gradPor, in->grad_porosity);
+        }
+        if (mask & SPHDEM_FIELD_OMEGA) get1(p.omega, in->omega);
+        if (mask & SPHDEM_FIELD_V0) {
+            get3(p.v0, in->v0); get3(p.vhat0, in->vhat0);
+        }
+        if (mask & SPHDEM_FIELD_NORMALS) {
+            get3(p.norm1, in->norm1); get3(p.norm2, in->norm2); get3(p.norm3, in->norm3);
+        }
+        if (mask & SPHDEM_FIELD_RADIUS) get1(p.radius, in->radius);
+        if (mask & SPHDEM_FIELD_ENERGY) {
+            get1(p.u, in->u); get1(p.dudt, in->dudt); get1(p.eViscF, in->e_visc); get1(p.deViscFdt, in->de_visc_dt);
+        }
+    }
+    return 0;
+}
+
+/* time, dt, maxdt and the step count, as sphdem_set_globals sets them */
+int oracle_set_globals(void *h, const SphDemGlobals *g) {
+    Sim *s = static_cast<Sim *>(h);
+    s->time = g->time;
+    s->dt = g->dt;
+    s->maxdt = g->maxdt;
+    s->step = g->sph_step;
+    return 0;
+}
+
 int oracle_output_vars(void *h, SphDemOutputVars *o) {
     static_cast<Sim *>(h)->output_vars(*o);
     return 0;

@@ -23,7 +23,9 @@ def zlib_flags() -> list:
     return ["-lz"] if probe.returncode == 0 else []
 
 
-def build_case(case_dir: str, out: str, extra=()) -> str:
+def build_case(case_dir: str, out: str, extra=(), libdir: str = LIBDIR) -> str:
+    """libdir: the directory of the libsphdem.so to link (the device library
+    by default)."""
     case_dir = os.path.abspath(case_dir)
     srcs = [os.path.join(HERE, "run_facade.cpp"), os.path.join(HERE, "io_data_vtk.cpp")]
     for f in ("customSim.cpp", "customOutput.cpp"):
@@ -31,7 +33,7 @@ def build_case(case_dir: str, out: str, extra=()) -> str:
         if os.path.exists(p):
             srcs.append(p)
     cmd = ["g++", "-std=gnu++17", "-O2", "-w", f"-I{case_dir}", f"-I{os.path.join(HERE, 'include')}",
-           *srcs, f"-L{LIBDIR}", "-lsphdem", f"-Wl,-rpath,{LIBDIR}", "-o", out, *zlib_flags(), *extra]
+           *srcs, f"-L{libdir}", "-lsphdem", f"-Wl,-rpath,{libdir}", "-o", out, *zlib_flags(), *extra]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError("case build failed:\n" + res.stderr[-6000:])

@@ -50,6 +50,86 @@ def test_reference_case_sources_build_unchanged(tmp_path):
     assert os.path.exists(out)
 
 
+ORACLE_ABI = os.path.join(REPO, "tests", "facade_oracle", "sphdem_oracle_abi.cpp")
+PORT_SRC = os.path.join(REPO, "oracle", "port", "sphdem_oracle.cpp")
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_CASE), reason="reference sources not present")
+def test_reference_case_hooks_run_unchanged(tmp_path):
+    """The reference's own sediment3D customSim.cpp / customOutput.cpp,
+    unmodified, run end to end through the façade: the host mirror pulled and
+    pushed around every hook, the case's constants as the configuration, the
+    step loop of run.cpp.  The GPU machines carry no reference sources, so the
+    step phases come from the CPU oracle port through the same C ABI
+    (tests/facade_oracle links it in place of the device library).  After
+    four steps (adaptive dt) the state equals the oracle port's with its
+    built-in hooks, which are sediment3D's: gravity on the fluid before the
+    middle phase; gravity on the spheres, the floor wall and freezing
+    (before TIME_DROP_PARTICLE) before the end phase; freezing after it."""
+    libdir = tmp_path / "oracle_abi"
+    libdir.mkdir()
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+                    "-I" + os.path.join(REPO, "include"), ORACLE_ABI, PORT_SRC, "-o", str(libdir / "libsphdem.so")],
+                   check=True, capture_output=True, text=True)
+    exe = build_case(REF_CASE, str(tmp_path / "run_sediment3D"), libdir=str(libdir))
+
+    # the configuration the case's constants give (a one-particle run dumps it)
+    probe = cases.dambreak2d(dx=0.1, nsteps=1)
+    one = {k: np.asarray(v)[:1] for k, v in probe.particles.items()}
+    one["r"] = np.array([[1e-3, 1e-3, 1e-3]])
+    state.write_state(str(tmp_path / "one.spdm"), one)
+    cfg_path = tmp_path / "cfg.bin"
+    res = subprocess.run([exe, str(tmp_path / "one.spdm"), "0", str(tmp_path / "one.bin"), "--dump-config",
+                          str(cfg_path)], capture_output=True, text=True, timeout=120)
+    assert res.returncode == 0, res.stderr[-2000:]
+    cfg = capi.SphDemConfig.from_buffer_copy(cfg_path.read_bytes())
+    assert cfg.ndim == 3 and cfg.flags & cases.F_LIQ_DEM and cfg.flags & cases.F_VAR_H_CORRECTION
+
+    # a sedimentation state inside the case's box: fluid lattice on the case's
+    # spacing over a repulsive floor layer, spheres of the case's radius
+    L, height = cfg.rmax[0] - cfg.rmin[0], cfg.rmax[2] - cfg.rmin[2]
+    nx = int(round(L / cfg.psep))
+    gen = cases.sediment3d(nx=nx, L=L, height=height, n_dem=150, dem_radius_factor=cfg.dem_radius / cfg.psep,
+                           rho_s=cfg.dem_dens, viscosity=cfg.viscosity, seed=12, nsteps=4)
+    parts = {k: np.array(v) for k, v in gen.particles.items()}
+    parts["h"][parts["iam"] == cases.DEM] = cfg.dem_search_radius
+    init = tmp_path / "init.spdm"
+    state.write_state(str(init), parts)
+    nsteps = 4
+    final = tmp_path / "final.bin"
+    res = subprocess.run([exe, str(init), str(nsteps), str(final)], capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stderr[-2000:]
+    a = read_final(str(final))
+
+    # the oracle port with the built-in hooks
+    import ctypes as C
+    from oracle import port_api
+    hooks = capi.SphDemConfig.from_buffer_copy(cfg_path.read_bytes())
+    hooks.gravity_sph = capi.D3(0.0, 0.0, -9.81)
+    hooks.gravity_dem = capi.D3(0.0, 0.0, -9.81)
+    hooks.n_walls = 1
+    hooks.walls[0].point = capi.D3(cfg.rmin[0], cfg.rmin[1], cfg.rmin[2])
+    hooks.walls[0].normal = capi.D3(0.0, 0.0, 1.0)
+    hooks.freeze_dem_until = cfg.time_drop_particle
+    lib = port_api.lib()
+    buf = capi.ParticleBuffers(len(parts["iam"]), parts)
+    h = C.c_void_p()
+    assert lib.oracle_create(C.byref(hooks), buf.ref(), C.byref(h)) == 0, lib.oracle_last_error()
+    try:
+        assert lib.oracle_step(h, nsteps) == 0, lib.oracle_last_error()
+        out = capi.ParticleBuffers(len(parts["iam"]))
+        lib.oracle_get(h, out.ref())
+    finally:
+        lib.oracle_destroy(h)
+    fl = parts["iam"] == cases.SPH
+    assert np.abs(out["vhat"][fl]).max() > 0.0          # the fluid moved under gravity
+    for k in ("r", "v", "vhat", "f", "dens", "h"):
+        scale = max(np.abs(out[k]).max(), 1e-300)
+        err = np.abs(a[k] - out[k]).max() / scale
+        print("reference sediment3D hooks vs built-in hooks", k, err)
+        assert err <= 1e-12, f"{k}: {err:.3e}"
+
+
 def read_final(path):
     with open(path, "rb") as fh:
         buf = fh.read()
