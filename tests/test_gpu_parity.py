@@ -113,7 +113,7 @@ MIXED_TOL = {"dens": 1e-5, "r": 1e-6, "f": 1e-3}
 # gradient by the inverse moment matrix, whose condition number at particles
 # of the free surface (few neighbours) amplifies the FP32 rounding of the pair
 # offsets; with density re-initialisation every step (a summation over those
-# positions) the run keeps the spec bar of 1e-4 on density, not 1e-5
+# positions) the run keeps the mixed-precision bar of 1e-4 on density, not 1e-5
 MIXED_TOL_BY_CASE = {"dambreak2d_own_small": {"dens": 1e-4, "r": 1e-5, "f": 1e-3}}
 
 
