@@ -4,7 +4,7 @@ The checker build (oracle/ref/build_ref.py), the golden-fixture script and
 the tests that read the reference's shipped case files take the reference
 root from the SPHDEM_REFERENCE_ROOT environment variable, defaulting to the
 read-only checkout this recipe was written against.  Where the directory is
-absent (the GPU machines), those steps are skipped.
+absent, those steps are skipped.
 """
 import os
 

@@ -144,7 +144,7 @@ bool decode_array(const std::string &body, const std::string &type, bool compres
         }
 #else
         (void)rd;
-        err = "the file is zlib-compressed and this build has no zlib";
+        err = "the file is zlib-compressed and the reader was built without zlib";
         return false;
 #endif
     } else {

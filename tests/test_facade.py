@@ -59,9 +59,10 @@ def test_reference_case_hooks_run_unchanged(tmp_path):
     """The reference's own sediment3D customSim.cpp / customOutput.cpp,
     unmodified, run end to end through the façade: the host mirror pulled and
     pushed around every hook, the case's constants as the configuration, the
-    step loop of run.cpp.  The GPU machines carry no reference sources, so the
-    step phases come from the CPU oracle port through the same C ABI
-    (tests/facade_oracle links it in place of the device library).  After
+    step loop of run.cpp.  The test runs where the reference's sources are
+    present, on the CPU: the step phases come from the CPU oracle port through
+    the same C ABI (tests/facade_oracle links it in place of the device
+    library).  After
     four steps (adaptive dt) the state equals the oracle port's with its
     built-in hooks, which are sediment3D's: gravity on the fluid before the
     middle phase; gravity on the spheres, the floor wall and freezing
