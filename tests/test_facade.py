@@ -81,7 +81,7 @@ def test_reference_case_hooks_run_unchanged(tmp_path):
     state.write_state(str(tmp_path / "one.spdm"), one)
     cfg_path = tmp_path / "cfg.bin"
     res = subprocess.run([exe, str(tmp_path / "one.spdm"), "0", str(tmp_path / "one.bin"), "--dump-config",
-                          str(cfg_path)], capture_output=True, text=True, timeout=120)
+                          str(cfg_path)], capture_output=True, text=True, timeout=120, cwd=str(tmp_path))
     assert res.returncode == 0, res.stderr[-2000:]
     cfg = capi.SphDemConfig.from_buffer_copy(cfg_path.read_bytes())
     assert cfg.ndim == 3 and cfg.flags & cases.F_LIQ_DEM and cfg.flags & cases.F_VAR_H_CORRECTION
@@ -98,7 +98,9 @@ def test_reference_case_hooks_run_unchanged(tmp_path):
     state.write_state(str(init), parts)
     nsteps = 4
     final = tmp_path / "final.bin"
-    res = subprocess.run([exe, str(init), str(nsteps), str(final)], capture_output=True, text=True, timeout=600)
+    # the case's output code writes its own files into the working directory
+    res = subprocess.run([exe, str(init), str(nsteps), str(final)], capture_output=True, text=True, timeout=600,
+                         cwd=str(tmp_path))
     assert res.returncode == 0, res.stderr[-2000:]
     a = read_final(str(final))
 
