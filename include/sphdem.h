@@ -372,6 +372,8 @@ int sphdem_batch_time_steps(sphdem_batch b, int nsteps, double *ms);
  * 8 x (steps_per_trial + 1) steps.  `chosen` (optional, 3 ints per member)
  * receives block size, grid divisor and staged tiles (0 / 1). */
 int sphdem_batch_tune(sphdem_batch b, int steps_per_trial, int *chosen);
+/* Text of b's last failure; with b == NULL, of the calling thread's last
+ * failed sphdem_batch_create ("no batch" if there was none). */
 int sphdem_batch_last_error(sphdem_batch b, char *buf, size_t len);
 
 /* Largest particle count sphdem_cell_ids_noalloc accepts. */
@@ -406,6 +408,9 @@ int sphdem_time_steps(sphdem_handle h, int nsteps, double *ms);
 int sphdem_alloc_host(size_t bytes, void **ptr);
 int sphdem_free_host(void *ptr);
 
+/* Text of h's last failure; with h == NULL, of the calling thread's last
+ * failed sphdem_create ("no handle" if there was none).  The reference
+ * prints to cerr and exits instead (dataLL.cpp:207-211). */
 int sphdem_last_error(sphdem_handle h, char *buf, size_t len);
 const char *sphdem_version(void);
 

@@ -128,31 +128,40 @@ int check_members(sphdem_batch_ctx *b) {
 
 extern "C" {
 
+/* text of the calling thread's last failed sphdem_batch_create */
+static thread_local std::string g_batch_create_err;
+
 int sphdem_batch_create(const sphdem_handle *members, int n, sphdem_batch *out) {
-    if (!out || !members || n <= 0) return SPHDEM_ERR_INVALID;
+    auto bad = [](int code, const std::string &msg) {
+        g_batch_create_err = msg;
+        return code;
+    };
+    if (!out) return bad(SPHDEM_ERR_INVALID, "null output pointer");
     *out = nullptr;
+    if (!members || n <= 0) return bad(SPHDEM_ERR_INVALID, "no members");
     for (int i = 0; i < n; i++)
-        if (!members[i]) return SPHDEM_ERR_INVALID;
+        if (!members[i]) return bad(SPHDEM_ERR_INVALID, "member " + std::to_string(i) + " is a null handle");
     for (int i = 0; i < n; i++)
         for (int j = 0; j < i; j++)
-            if (members[i] == members[j]) return SPHDEM_ERR_INVALID;
+            if (members[i] == members[j])
+                return bad(SPHDEM_ERR_INVALID,
+                           "members " + std::to_string(j) + " and " + std::to_string(i) + " are the same handle");
     /* a density re-initialisation step rebuilds once more than the others,
      * which one shared graph per step cannot follow */
     for (int i = 0; i < n; i++)
-        if (sphdem::reinit_configured(members[i]->host_cfg)) return SPHDEM_ERR_UNSUPPORTED;
+        if (sphdem::reinit_configured(members[i]->host_cfg))
+            return bad(SPHDEM_ERR_UNSUPPORTED,
+                       "member " + std::to_string(i) + " re-initialises its density (reinit_dens_every / reinit_dens_at)");
     sphdem_batch_ctx *b = new sphdem_batch_ctx;
     b->members.assign(members, members + n);
     b->ev_join.assign(n, nullptr);
-    if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess) {
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming);
+    for (int i = 0; i < n && e == cudaSuccess; i++) e = cudaEventCreateWithFlags(&b->ev_join[i], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
         sphdem_batch_destroy(b);
-        return SPHDEM_ERR_CUDA;
+        return bad(SPHDEM_ERR_CUDA, std::string("CUDA: ") + cudaGetErrorString(e));
     }
-    for (int i = 0; i < n; i++)
-        if (cudaEventCreateWithFlags(&b->ev_join[i], cudaEventDisableTiming) != cudaSuccess) {
-            sphdem_batch_destroy(b);
-            return SPHDEM_ERR_CUDA;
-        }
     *out = b;
     return SPHDEM_OK;
 }
@@ -299,7 +308,8 @@ int sphdem_batch_tune(sphdem_batch b, int steps_per_trial, int *chosen) {
 
 int sphdem_batch_last_error(sphdem_batch b, char *buf, size_t len) {
     if (!buf || !len) return SPHDEM_ERR_INVALID;
-    std::snprintf(buf, len, "%s", b ? b->err.c_str() : "no batch");
+    const std::string e = b ? b->err : (g_batch_create_err.empty() ? std::string("no batch") : g_batch_create_err);
+    std::snprintf(buf, len, "%s", e.c_str());
     return SPHDEM_OK;
 }
 

@@ -404,14 +404,16 @@ extern "C" {
 
 const char *sphdem_version(void) { return "sphdem-gb300 0.1 (sm_103a)"; }
 
+/* text of the calling thread's last failed sphdem_create (no handle exists
+ * to hold it) */
+static thread_local std::string g_create_err;
+
 int sphdem_last_error(sphdem_handle h, char *buf, size_t len) {
     if (!buf || !len) return SPHDEM_ERR_INVALID;
-    const std::string &e = h ? h->err : std::string("no handle");
+    const std::string e = h ? h->err : (g_create_err.empty() ? std::string("no handle") : g_create_err);
     std::snprintf(buf, len, "%s", e.c_str());
     return SPHDEM_OK;
 }
-
-static thread_local std::string g_create_err;
 
 int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init, int64_t capacity, sphdem_handle *out) {
     if (!out) return SPHDEM_ERR_INVALID;

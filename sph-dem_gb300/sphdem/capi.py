@@ -441,9 +441,8 @@ class Batch:
         arr = (C.c_void_p * len(self.sims))(*[s.h.value for s in self.sims])
         h = C.c_void_p()
         rc = lib.lib.sphdem_batch_create(arr, len(self.sims), C.byref(h))
-        if rc:
-            raise SphDemError(f"sphdem_batch_create: {ERR_NAMES.get(rc, rc)}")
         self.h = h
+        self._check(rc, "sphdem_batch_create")
 
     def _check(self, rc, what):
         if rc:
