@@ -298,16 +298,18 @@ int sphdem_cell_ids(sphdem_handle h, int32_t *cell_xyz);
  * reference, which has no derivatives.  Covers, with fixed dt and no
  * damping:
  *  - handles whose particles are all DEM (LIQ_DEM without fluid, no
- *    freezing): gradients dem_k, dem_gamma and the initial state;
+ *    freezing; at most 67,108,863 particles): gradients dem_k, dem_gamma
+ *    and the initial state;
  *  - fluid handles of SPH and SPH-boundary particles (no LIQ_DEM) with
  *    artificial viscosity, CONST_H, NO_ANTICLUMPING, no VAR_H_CORRECTION and
- *    no periodic axes (the dam break): gradients `viscosity` =
- *    dL/d(alpha_artificial) and the initial state;
+ *    no periodic axes (the dam break; at most 4M particles): gradients
+ *    `viscosity` = dL/d(alpha_artificial) and the initial state;
  *  - coupled LIQ_DEM handles of SPH, SPH-boundary and DEM particles with
- *    Morris viscosity, CONST_H, NO_ANTICLUMPING, no VAR_H_CORRECTION, gamma
- *    = 7 (periodic axes allowed; sedimentation): gradients dem_k, dem_gamma,
- *    `viscosity` = dL/d(kinematic viscosity), drag_scale and the initial
- *    state.
+ *    Morris viscosity, NO_ANTICLUMPING, gamma = 7 and either CONST_H or, on
+ *    mixed-precision handles, VAR_H_CORRECTION with h following the density
+ *    (periodic axes allowed; sedimentation; at most 4M particles):
+ *    gradients dem_k, dem_gamma, `viscosity` = dL/d(kinematic viscosity),
+ *    drag_scale and the initial state.
  * Other handles get SPHDEM_ERR_UNSUPPORTED.
  *
  * sphdem_adjoint_forward runs nsteps ordinary steps from the current state,

@@ -55,6 +55,7 @@
  * result does not depend on the launch order.
  */
 #include <algorithm>
+#include <climits>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -1020,6 +1021,8 @@ std::string adjoint_supported(sphdem_ctx *c, int *mode) {
     if (cfg.liq_dem()) {
         if (cfg.freeze_until >= 0) return "the adjoint does not cover freezing";
         if (all_dem) {
+            /* the contact tables hold ADJ_MAX_CONTACTS * n entries, an int */
+            if (c->n > INT_MAX / ADJ_MAX_CONTACTS) return "the DEM adjoint covers at most 67,108,863 particles";
             *mode = ADJ_MODE_DEM;
             return "";
         }
