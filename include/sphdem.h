@@ -1,8 +1,8 @@
 /*
  * sphdem.h -- C ABI of the GB300-native SPH-DEM per-step particle hot path.
  *
- * One handle = one simulation (or one ensemble of independent simulations)
- * resident in the HBM of one GPU.  Every entry point returns an int status
+ * One handle = one simulation resident in the HBM of one GPU; a batch
+ * (sphdem_batch_*) steps an ensemble of independent handles together.  Every entry point returns an int status
  * (SPHDEM_OK == 0); no C++ exception crosses this boundary.  Text for the last
  * failure is available from sphdem_last_error().
  *
@@ -64,7 +64,7 @@ extern "C" {
 #define SPHDEM_F_FIXED_DT         (1u << 4)  /* dt == maxdt every step          */
 #define SPHDEM_F_DEM_ONLY_CONTACT (1u << 5)  /* reserved                        */
 #define SPHDEM_F_CORRECTED_GRADIENT (1u << 6) /* CORRECTED_GRADIENT (calcInvM, sph.h:394-434);
-                                                 FP64 precision, no LIQ_DEM */
+                                                 both precisions, no LIQ_DEM */
 #define SPHDEM_F_DEM_BLOCK        (1u << 7)  /* DEM_BLOCK: every DEM particle takes the mean
                                                  DEM force before the end kick
                                                  (sphIncompress.cpp:231-238); needs LIQ_DEM */
@@ -87,7 +87,7 @@ typedef struct SphDemWall {
 /* All case constants the reference takes from customConstants.h /
  * demConstants.h at compile time, passed at run time instead. */
 typedef struct SphDemConfig {
-    int32_t  ndim;                 /* NDIM: 2 or 3                                */
+    int32_t  ndim;                 /* NDIM: 1, 2 or 3 (the tests run 2 and 3)     */
     int32_t  visc_model;           /* SPHDEM_VISC_*                               */
     uint32_t flags;                /* SPHDEM_F_*                                  */
     int32_t  precision;            /* SPHDEM_PREC_*                               */
