@@ -30,6 +30,11 @@ const double VISCOSITY = 1e-06;
 const double BFAC = 1.0;
 const int OUTSTEP = 10;
 const double MAXTIME = 5.986414282632196e-05 * OUTSTEP;
+const int RESTART_EVERY_N_STEPS = 5;
+#define TIME_OVERIDE 0
+#define START_TIME 0
+#define NSTEP_OVERIDE 0
+#define START_NSTEP 0
 const double DAMPTIME = 0.0;
 const int MAX_NUM_PARTICLES_PER_CPU = 2456;
 const int REINIT_DENS_EVERY_N_STEPS = 50000000;

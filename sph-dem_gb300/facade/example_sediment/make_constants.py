@@ -50,6 +50,11 @@ def constants(name: str = "sediment3d_small") -> str:
         f"const double BFAC = {r(c['bfac'])};",
         f"const int OUTSTEP = {outstep};",
         f"const double MAXTIME = {r(c['maxdt'])} * OUTSTEP;",
+        "const int RESTART_EVERY_N_STEPS = 5;",
+        "#define TIME_OVERIDE 0",
+        "#define START_TIME 0",
+        "#define NSTEP_OVERIDE 0",
+        "#define START_NSTEP 0",
         f"const double DAMPTIME = {r(c['damptime'])};",
         f"const int MAX_NUM_PARTICLES_PER_CPU = {case.n + 256};",
         f"const int REINIT_DENS_EVERY_N_STEPS = {int(c['reinit_dens_every']) or 50000000};",

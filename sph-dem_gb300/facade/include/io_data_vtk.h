@@ -38,6 +38,20 @@ class Cio_data_vtk {
     void writeRestart(int timestep, particleContainer &ps, CglobalVars *globals);
     void writeOutput(int timestep, particleContainer &ps, CglobalVars *globals);
 
+    /* <filename>Globals<rank>.dat (CioGlobals, ioGlobals.cpp:4-139): one
+     * row per output step.  readGlobals reads the rows up to the one of
+     * outStep into g (none for outStep 0); writeGlobals keeps the rows up
+     * to outStep - 1 and writes g as the row of outStep, creating the file
+     * with the reference's header line.  Numbers are written to full
+     * precision. */
+    void readGlobals(int outStep, CglobalVars *g);
+    void writeGlobals(int outStep, CglobalVars *g);
+    /* <filename>Domain<rank>.dat (CioDomain, ioDomain.cpp:3-40): rank,
+     * procDomain[2 NDIM], procNeighbrs[3^NDIM]; readDomain returns false
+     * when the file cannot be read */
+    bool readDomain(int outStep, CglobalVars *g);
+    void writeDomain(int outStep, CglobalVars *g);
+
     /* one piece by path; readPiece returns false (with a message on stderr)
      * when the file cannot be read */
     static bool readPiece(const std::string &path, particleContainer &ps);

@@ -50,7 +50,7 @@ inline SphDemConfig sphdem_case_config(int precision, bool fixed_dt) {
     c.flags |= SPHDEM_F_LIQ_DEM;
 #endif
 #ifdef CORRECTED_GRADIENT
-    c.flags |= SPHDEM_F_CORRECTED_GRADIENT; /* FP64 precision only */
+    c.flags |= SPHDEM_F_CORRECTED_GRADIENT; /* both precisions; not with LIQ_DEM */
 #endif
 #if defined(LIQ_DEM) && defined(DEM_BLOCK)
     c.flags |= SPHDEM_F_DEM_BLOCK;

@@ -451,3 +451,114 @@ void Cio_data_vtk::writeOutput(int timestep, particleContainer &ps, CglobalVars 
     writePiece(piece, ps, exactPoints);
     writeIndex(stem + ".pvtu", std::vector<std::string>(1, piece), exactPoints);
 }
+
+/* ---- Globals and Domain files ------------------------------------------ */
+
+namespace {
+
+std::string rank_file(const std::string &base, const char *what, int rank) {
+    return base + what + std::to_string(rank) + ".dat";
+}
+
+/* one data row of a Globals file into g (CioGlobals::myGetLine,
+ * ioGlobals.cpp:25-37: the columns it reads, the custom ones not); the row's
+ * OutStep, or -1 for a line that is not a row */
+int parse_globals_row(const std::string &line, CglobalVars *g) {
+    std::istringstream ss(line);
+    int step = -1;
+    if (!(ss >> step)) return -1;
+    double lin1 = 0, wt;
+    ss >> g->sphStep >> g->time >> g->linMom[0] >> lin1 >> g->angMom >> g->eKE >> g->eBForce >> g->eElast >>
+        g->eElastExact >> g->eViscF >> g->eViscB >> g->eFF >> g->eTotal;
+    for (int k = 0; k < 6; k++) ss >> wt; /* wall-clock columns */
+    ss >> g->maxV >> g->aveDens >> g->varDens >> g->aveDensFromMass >> g->n >> g->nSph >> g->maxF >> g->maxFF >>
+        g->rmsFF >> g->edElastdt >> g->edViscFdt >> g->edFFdt;
+    if (NDIM > 1) g->linMom[NDIM > 1 ? 1 : 0] = lin1;
+    return step;
+}
+
+std::string num(double v) {
+    char b[32];
+    std::snprintf(b, sizeof b, "%.17g", v);
+    return b;
+}
+
+const char GLOBALS_HEADER[] =
+    "# OutStep SPHStep Time linMomX linMomY angMom KE eBForce eElast eElastExact eViscF eViscB eFF eTotal "
+    "wtTotalStep wtTotalForceCalc wtTotalDddtCalc wtTotalReset wtTotalUpdateDomain wtTotalMPI maxV aveDens varDens "
+    "aveDensFromMass n nSph maxF maxFF rmsFF edElastdt edViscFdt edFFdt";
+
+}  // namespace
+
+void Cio_data_vtk::readGlobals(int outStep, CglobalVars *g) {
+    std::ifstream in(rank_file(filename, "Globals", g->mpiRank).c_str());
+    if (!in || outStep <= 0) return; /* ioGlobals.cpp:62: no row for step 0 */
+    std::string line;
+    std::getline(in, line); /* the header */
+    while (std::getline(in, line)) {
+        const int step = parse_globals_row(line, g);
+        if (step >= outStep) break;
+    }
+}
+
+void Cio_data_vtk::writeGlobals(int outStep, CglobalVars *g) {
+    const std::string path = rank_file(filename, "Globals", g->mpiRank);
+    std::vector<std::string> lines;
+    {
+        std::ifstream in(path.c_str());
+        std::string line;
+        while (std::getline(in, line)) lines.push_back(line);
+    }
+    if (lines.empty()) lines.push_back(GLOBALS_HEADER);
+    /* the write position of openAndSeekToStep(outStep - 1) (ioGlobals.cpp:48-73):
+     * right after the header for outStep - 1 <= 0, after the row of outStep - 1
+     * if the rows reach it, else at the end */
+    size_t keep = lines.size();
+    if (outStep - 1 <= 0) {
+        keep = 1;
+    } else {
+        CglobalVars scratch;
+        for (size_t i = 1; i < lines.size(); i++) {
+            const int step = parse_globals_row(lines[i], &scratch);
+            if (step >= outStep - 1) {
+                if (step == outStep - 1) keep = i + 1;
+                break;
+            }
+        }
+    }
+    lines.resize(keep);
+    std::ostringstream row;
+    row << outStep << ' ' << g->sphStep << ' ' << num(g->time) << ' ' << num(g->linMom[0]) << ' '
+        << num(NDIM > 1 ? g->linMom[NDIM > 1 ? 1 : 0] : 0.0) << ' ' << num(g->angMom) << ' ' << num(g->eKE) << ' '
+        << num(g->eBForce) << ' ' << num(g->eElast) << ' ' << num(g->eElastExact) << ' ' << num(g->eViscF) << ' '
+        << num(g->eViscB) << ' ' << num(g->eFF) << ' ' << num(g->eTotal);
+    for (int k = 0; k < 6; k++) row << " 0"; /* wall-clock columns: not measured here */
+    row << ' ' << num(g->maxV) << ' ' << num(g->aveDens) << ' ' << num(g->varDens) << ' ' << num(g->aveDensFromMass)
+        << ' ' << g->n << ' ' << g->nSph << ' ' << num(g->maxF) << ' ' << num(g->maxFF) << ' ' << num(g->rmsFF) << ' '
+        << num(g->edElastdt) << ' ' << num(g->edViscFdt) << ' ' << num(g->edFFdt);
+    for (int k = 0; k < GLOBAL_CUSTOM_BUFFER_SIZE; k++) row << ' ' << num(g->custom[k]);
+    lines.push_back(row.str());
+    std::ofstream out(path.c_str(), std::ios::trunc);
+    for (const std::string &l : lines) out << l << '\n';
+}
+
+bool Cio_data_vtk::readDomain(int, CglobalVars *g) {
+    std::ifstream in(rank_file(filename, "Domain", g->mpiRank).c_str());
+    int rank = 0;
+    if (!(in >> rank)) return false;
+    for (int i = 0; i < 2 * NDIM; i++)
+        if (!(in >> g->procDomain[i])) return false;
+    for (int k = 0; k < SPHDEM_FACADE_NEIGHBOURS; k++)
+        if (!(in >> g->procNeighbrs[k])) return false;
+    g->mpiRank = rank;
+    g->procNeighbrs[SPHDEM_FACADE_NEIGHBOURS / 2] = -1; /* the process itself (ioDomain.cpp:16-17) */
+    return true;
+}
+
+void Cio_data_vtk::writeDomain(int, CglobalVars *g) {
+    std::ofstream out(rank_file(filename, "Domain", g->mpiRank).c_str(), std::ios::trunc);
+    out << g->mpiRank << ' ';
+    for (int i = 0; i < 2 * NDIM; i++) out << num(g->procDomain[i]) << ' ';
+    for (int k = 0; k < SPHDEM_FACADE_NEIGHBOURS; k++) out << g->procNeighbrs[k] << ' ';
+    out << '\n';
+}

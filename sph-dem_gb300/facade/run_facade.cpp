@@ -1,24 +1,38 @@
 /*
- * Driver of a case directory on the device (the step loop of run.cpp:80-170):
+ * Driver of a case directory on the device (the step loop of run.cpp:15-170):
  * compiled together with the case's customConstants.h, customSim.cpp and
  * customOutput.cpp against the façade headers (include/), linked with
- * libsphdem.so.
+ * libsphdem.so.  Two command lines:
+ *
+ *   run_case <inbase> <intimestep> <outbase> [--mixed] [--fixed-dt]
+ *
+ * is run.cpp's own (used when <inbase> is not a file): the Domain, Globals
+ * row and restart piece of output step <intimestep> are read from
+ * <inbase>Domain0.dat, <inbase>Globals0.dat and
+ * <inbase>Restart%07d_0.vtu; then, as run.cpp does, the case's hooks and
+ * the device phases step while time <= MAXTIME and the output step <=
+ * OUTSTEP, with maxdt = MAXTIME / OUTSTEP, and every MAXTIME / OUTSTEP of
+ * simulated time come the output-step diagnostics, the case's calcOutput,
+ * <outbase>%07d output pieces and a Globals row, and every
+ * RESTART_EVERY_N_STEPS output steps a restart and a Domain file.
+ * TIME_OVERIDE / START_TIME, NSTEP_OVERIDE / START_NSTEP and
+ * START_WRITE_TIME apply as in run.cpp when the case defines them.
  *
  *   run_case <initial state> <nsteps> <final state out> [--mixed] [--fixed-dt]
  *            [--restart-out <base>] [--dump-config <file>]
  *
- * The initial state is a restart piece or index the case's setup writes
+ * runs a fixed number of steps from a state file: a restart piece or index
  * (<base>Restart0000000_0.vtu / .pvtu, read as Cio_data_vtk::readRestart
- * reads it) or an SPDMST01 state file.  --restart-out writes the final state
- * as <base>Restart%07d (the step count) with Float64 points;
+ * reads it) or an SPDMST01 state file, with calcOutput every OUTSTEP steps.
+ * The final state is written as r, v, vhat, f, dens, h per particle (tag
+ * order) after a 16-byte header ("SPDMFAC1", n).  --restart-out writes it
+ * also as <base>Restart%07d (the step count) with Float64 points;
  * --dump-config writes the SphDemConfig the case's constants give (raw
  * struct bytes).
  *
  * Every step calls the case's beforeStart / beforeMiddle / beforeEnd /
  * afterEnd hooks on the host mirror between the device phases
- * (SPHDEM_PHASE_START / MIDDLE / END), and calcOutput every OUTSTEP steps.
- * The final state is written as r, v, vhat, f, dens, h per particle (tag
- * order) after a 16-byte header ("SPDMFAC1", n).
+ * (SPHDEM_PHASE_START / MIDDLE / END).
  */
 #include <algorithm>
 #include <cstdint>
@@ -29,6 +43,8 @@
 #include <iostream>
 #include <string>
 #include <vector>
+
+#include <sys/stat.h>
 
 #include "customConstants.h"
 #include "customOutput.h"
@@ -42,6 +58,9 @@ bool ends_with(const std::string &s, const char *suf) {
     const size_t k = std::strlen(suf);
     return s.size() >= k && s.compare(s.size() - k, k, suf) == 0;
 }
+
+/* the SphDemParticles view of particles read from a restart, in tag order */
+void soa_of(particleContainer &ps, SphDemParticles &p, std::vector<std::vector<char> > &keep);
 
 /* a .vtu piece or a .pvtu index (its pieces in order) -> particles, then the
  * SphDemParticles view of them, in tag order */
@@ -61,6 +80,11 @@ bool read_vtk_state(const std::string &path, SphDemParticles &p, std::vector<std
     } else if (!Cio_data_vtk::readPiece(path, ps)) {
         return false;
     }
+    soa_of(ps, p, keep);
+    return true;
+}
+
+void soa_of(particleContainer &ps, SphDemParticles &p, std::vector<std::vector<char> > &keep) {
     std::stable_sort(ps.begin(), ps.end(), [](const Cparticle &a, const Cparticle &b) { return a.tag < b.tag; });
     const int64_t n = (int64_t)ps.size();
     auto f64 = [&](size_t k) {
@@ -105,7 +129,6 @@ bool read_vtk_state(const std::string &path, SphDemParticles &p, std::vector<std
         p.h[i] = q.h;
         p.radius[i] = q.radius;
     }
-    return true;
 }
 
 bool read_state(const char *path, SphDemParticles &p, std::vector<std::vector<char> > &keep) {
@@ -159,11 +182,153 @@ void write_final(const char *path, const particleContainer &ps) {
     }
 }
 
+void fail_exit(sphdem_handle h, const char *what) {
+    char msg[512];
+    sphdem_last_error(h, msg, sizeof msg);
+    std::cerr << what << ": " << msg << std::endl;
+    std::exit(-1);
+}
+
+void phase(sphdem_handle h, int p, const char *what) {
+    if (sphdem_phase(h, p) != SPHDEM_OK) fail_exit(h, what);
+}
+
+/* one step of run.cpp:102-118: the case's hooks on the host mirror between
+ * the device phases */
+void hooked_step(sphdem_handle h, CdataLL &data, CcustomSim &customSim) {
+    CglobalVars &globals = data.globals;
+    phase(h, SPHDEM_HOOK_BEFORE_START, "step"); /* globals.sphStep++ (run.cpp:104) */
+    data.pull();
+    customSim.beforeStart(globals.time);
+    data.push();
+    phase(h, SPHDEM_PHASE_START, "start");
+    data.pull();
+    customSim.beforeMiddle(globals.time);
+    data.push();
+    phase(h, SPHDEM_PHASE_MIDDLE, "middle");
+    data.pull();
+    customSim.beforeEnd(globals.time);
+    data.push();
+    phase(h, SPHDEM_PHASE_END, "end");
+    data.pull();
+    customSim.afterEnd(globals.time);
+    data.push();
+}
+
+/* sph.calcOutputVars() (sphIncompress.h:274-319, run.cpp:131): the
+ * output-step quantities into the globals */
+void output_vars(sphdem_handle h, CglobalVars &g) {
+    SphDemOutputVars ov;
+    if (sphdem_output_vars(h, &ov) != SPHDEM_OK) fail_exit(h, "sphdem_output_vars");
+    for (int d = 0; d < NDIM; d++) g.linMom[d] = ov.lin_mom[d];
+    g.angMom = ov.ang_mom;
+    g.eKE = ov.e_ke;
+    g.eElast = ov.e_elast;
+    g.eElastExact = ov.e_elast_exact;
+    g.edElastdt = ov.ed_elast_dt;
+    g.eViscF = ov.e_visc_f;
+    g.edViscFdt = ov.ed_visc_f_dt;
+    g.eFF = ov.e_ff;
+    g.edFFdt = ov.ed_ff_dt;
+    g.eViscB = ov.e_visc_b;
+    g.eBForce = ov.e_b_force;
+    g.eTotal = ov.e_total;
+    g.maxV = ov.max_v;
+    g.maxF = ov.max_f;
+    g.maxFF = ov.max_ff;
+    g.rmsFF = ov.rms_ff;
+    g.aveDens = ov.ave_dens;
+    g.varDens = ov.var_dens;
+    g.aveDensFromMass = ov.ave_dens_from_mass;
+    g.n = (int)ov.n;
+    g.nSph = (int)ov.n_sph;
+}
+
+bool is_file(const char *path) {
+    struct stat st;
+    return stat(path, &st) == 0 && S_ISREG(st.st_mode);
+}
+
+/* run.cpp:15-170 on one process: read the Domain, Globals row and restart of
+ * output step intimestep under inbase, then step and write outputs under
+ * outbase until MAXTIME or OUTSTEP */
+int run_reference_loop(const std::string &inbase, int intimestep, const std::string &outbase, bool mixed,
+                       bool fixed_dt) {
+    CglobalVars globals;
+    Cio_data_vtk io_data(inbase, &globals);
+    if (!io_data.readDomain(intimestep, &globals))
+        std::cout << "no Domain file under " << inbase << ": the domain is RMIN..RMAX" << std::endl;
+    io_data.readGlobals(intimestep, &globals);
+    particleContainer ps0;
+    io_data.readRestart(intimestep, &ps0, &globals);
+    int outstep = intimestep;
+#if defined(TIME_OVERIDE) && defined(START_TIME)
+    if (TIME_OVERIDE) globals.time = START_TIME;
+#endif
+#if defined(NSTEP_OVERIDE) && defined(START_NSTEP)
+    if (NSTEP_OVERIDE) outstep = START_NSTEP;
+#endif
+    io_data.setFilename(outbase, &globals);
+
+    SphDemParticles init;
+    std::vector<std::vector<char> > keep;
+    soa_of(ps0, init, keep);
+    SphDemConfig cfg = sphdem_case_config(mixed ? SPHDEM_PREC_MIXED : SPHDEM_PREC_FP64, fixed_dt);
+    for (int d = 0; d < NDIM; d++) {
+        /* the binning domain is the process's domain (dataLL.cpp:13-14) */
+        cfg.domain_min[d] = globals.procDomain[2 * d];
+        cfg.domain_max[d] = globals.procDomain[2 * d + 1];
+    }
+    sphdem_handle h = nullptr;
+    const int64_t capacity = std::max<int64_t>(init.n, MAX_NUM_PARTICLES_PER_CPU);
+    if (sphdem_create(&cfg, &init, capacity, &h) != SPHDEM_OK) fail_exit(nullptr, "sphdem_create");
+    /* the time and step count of the Globals row, maxdt of run.cpp:87 */
+    SphDemGlobals dg;
+    if (sphdem_get_globals(h, &dg) != SPHDEM_OK) fail_exit(h, "sphdem_get_globals");
+    dg.time = globals.time;
+    dg.sph_step = globals.sphStep;
+    dg.maxdt = MAXTIME / OUTSTEP;
+    if (sphdem_set_globals(h, &dg) != SPHDEM_OK) fail_exit(h, "sphdem_set_globals");
+
+    particleContainer ps((size_t)init.n);
+    CdataLL data(ps, globals, h);
+    data.pull();
+    CcustomSim customSim(&data, globals.time);
+    CcustomOutput customOutput(&data);
+#ifndef START_WRITE_TIME
+    double nextWriteTime = globals.time + MAXTIME / OUTSTEP;
+#else
+    double nextWriteTime = START_WRITE_TIME;
+#endif
+    while (globals.time <= MAXTIME && outstep <= OUTSTEP) {
+        hooked_step(h, data, customSim);
+        if (globals.time >= nextWriteTime) {
+            outstep++;
+            globals.outstep = outstep;
+            output_vars(h, globals);
+            customOutput.calcOutput(outstep, &customSim, &io_data);
+            io_data.writeOutput(outstep, ps, &globals);
+            io_data.writeGlobals(outstep, &globals);
+            if (outstep % RESTART_EVERY_N_STEPS == 0) {
+                io_data.writeRestart(outstep, ps, &globals);
+                io_data.writeDomain(outstep, &globals);
+            }
+            nextWriteTime = globals.time + MAXTIME / OUTSTEP;
+            globals.maxdt = MAXTIME / OUTSTEP;
+        }
+    }
+    sphdem_destroy(h);
+    return 0;
+}
+
 }  // namespace
 
 int main(int argc, char *argv[]) {
     if (argc < 4) {
-        std::cout << "Usage: run_case <initial state> <nsteps> <final state> [--mixed] [--fixed-dt]" << std::endl;
+        std::cout << "Usage: run_case <inbase> <intimestep> <outbase> [--mixed] [--fixed-dt]\n"
+                     "       run_case <initial state> <nsteps> <final state> [--mixed] [--fixed-dt]"
+                     " [--restart-out <base>] [--dump-config <file>]"
+                  << std::endl;
         return -1;
     }
     bool mixed = false, fixed_dt = false;
@@ -174,6 +339,8 @@ int main(int argc, char *argv[]) {
         if (!std::strcmp(argv[i], "--restart-out") && i + 1 < argc) restart_out = argv[++i];
         if (!std::strcmp(argv[i], "--dump-config") && i + 1 < argc) dump_config = argv[++i];
     }
+    /* run.cpp's command line: a base name, not a file */
+    if (!is_file(argv[1])) return run_reference_loop(argv[1], std::atoi(argv[2]), argv[3], mixed, fixed_dt);
     SphDemParticles init;
     std::vector<std::vector<char> > keep;
     const std::string in_path = argv[1];
@@ -191,10 +358,7 @@ int main(int argc, char *argv[]) {
     sphdem_handle h = nullptr;
     /* room for the particles the case's hooks insert (dataLL.cpp:241) */
     const int64_t capacity = std::max<int64_t>(init.n, MAX_NUM_PARTICLES_PER_CPU);
-    if (sphdem_create(&cfg, &init, capacity, &h) != SPHDEM_OK) {
-        std::cerr << "sphdem_create failed" << std::endl;
-        return -1;
-    }
+    if (sphdem_create(&cfg, &init, capacity, &h) != SPHDEM_OK) fail_exit(nullptr, "sphdem_create");
     CglobalVars globals;
     particleContainer ps((size_t)init.n);
     CdataLL data(ps, globals, h);
@@ -202,32 +366,9 @@ int main(int argc, char *argv[]) {
     CcustomSim customSim(&data, globals.time);
     CcustomOutput customOutput(&data);
     Cio_data_vtk io(std::string(argv[3]), &globals);
-    auto phase = [&](int p, const char *what) {
-        if (sphdem_phase(h, p) != SPHDEM_OK) {
-            char msg[512];
-            sphdem_last_error(h, msg, sizeof msg);
-            std::cerr << what << ": " << msg << std::endl;
-            std::exit(-1);
-        }
-    };
     int outstep = 0;
     for (int s = 0; s < nsteps; s++) {
-        phase(SPHDEM_HOOK_BEFORE_START, "step");   /* globals.sphStep++ (run.cpp:104) */
-        data.pull();
-        customSim.beforeStart(globals.time);
-        data.push();
-        phase(SPHDEM_PHASE_START, "start");
-        data.pull();
-        customSim.beforeMiddle(globals.time);
-        data.push();
-        phase(SPHDEM_PHASE_MIDDLE, "middle");
-        data.pull();
-        customSim.beforeEnd(globals.time);
-        data.push();
-        phase(SPHDEM_PHASE_END, "end");
-        data.pull();
-        customSim.afterEnd(globals.time);
-        data.push();
+        hooked_step(h, data, customSim);
         if ((s + 1) % OUTSTEP == 0) {
             data.pull();
             customOutput.calcOutput(++outstep, &customSim, &io);

@@ -294,7 +294,11 @@ int main(int argc, char **argv) {
 def _vtk_tool(tmp_path, ndim):
     d = tmp_path / f"tool{ndim}"
     d.mkdir(exist_ok=True)
-    (d / "customConstants.h").write_text(f"#ifndef CC_H\n#define CC_H\nconst int NDIM = {ndim};\n#endif\n")
+    # the constants every case defines that the I/O headers read
+    box = ", ".join(["0.0"] * ndim), ", ".join(["1.0"] * ndim)
+    (d / "customConstants.h").write_text(f"#ifndef CC_H\n#define CC_H\nconst int NDIM = {ndim};\n"
+                                         f"const double RMIN[NDIM] = {{{box[0]}}};\n"
+                                         f"const double RMAX[NDIM] = {{{box[1]}}};\n#endif\n")
     (d / "vtk_tool.cpp").write_text(VTK_TOOL)
     sys.path.insert(0, FACADE)
     from build_case import zlib_flags
@@ -398,3 +402,94 @@ def test_case_runs_from_a_restart_piece(tmp_path):
             assert np.abs(o[k] - outs[0][k]).max() <= 1e-12 * scale, k
     d = io_vtk.read_vtu(str(tmp_path / "outRestart0000004_0.vtu"))
     np.testing.assert_array_equal(d["points"], outs[-1]["r"])
+
+
+def _oracle_abi(libdir):
+    """The oracle-backed C-ABI library of tests/facade_oracle in libdir."""
+    os.makedirs(libdir, exist_ok=True)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fPIC", "-shared",
+                    "-I" + os.path.join(REPO, "include"), ORACLE_ABI, PORT_SRC, "-o",
+                    os.path.join(libdir, "libsphdem.so")], check=True, capture_output=True, text=True)
+    return str(libdir)
+
+
+def test_run_loop_of_the_reference_command_line(tmp_path):
+    """run_case <inbase> <intimestep> <outbase>, run.cpp's own command line
+    and loop (run.cpp:15-170), on the CPU through the oracle-backed C ABI.
+    From the Domain file and restart a case's setup writes, the loop steps
+    the example case's hooks until time passes MAXTIME (fixed dt = MAXTIME /
+    OUTSTEP) and writes, every MAXTIME / OUTSTEP of simulated time, an output
+    piece and a Globals row, and every RESTART_EVERY_N_STEPS (5) output steps
+    a restart and a Domain file.  The state it writes at an output step
+    equals the fixed-step command's after as many steps; the Globals row
+    carries that step's count, time and output-step quantities.  Started
+    again from the restart of output step 5 (its Globals row gives time and
+    step count), the loop continues the output steps, overwriting the rows
+    after step 5 of the same Globals file as CioGlobals does."""
+    from sphdem import io_vtk
+    lib = _oracle_abi(str(tmp_path / "oracle_abi"))
+    exe = build_case(os.path.join(FACADE, "example_sediment"), str(tmp_path / "run_example"), libdir=lib)
+    case = cases.workload("sediment3d_small")
+    ps = dict(case.particles)
+    ps["tag"] = np.arange(1, case.n + 1, dtype=np.int32)
+    io_vtk.write_restart(str(tmp_path / "init"), 0, ps, 3, exact=True)
+    # the domain the case's constants give, so both command lines bin alike
+    res = subprocess.run([exe, str(tmp_path / "initRestart0000000_0.vtu"), "0", str(tmp_path / "probe.bin"),
+                          "--dump-config", str(tmp_path / "cfg.bin")], capture_output=True, text=True, timeout=120,
+                         cwd=str(tmp_path))
+    assert res.returncode == 0, res.stderr[-2000:]
+    cfg = capi.SphDemConfig.from_buffer_copy((tmp_path / "cfg.bin").read_bytes())
+    dom = [x for d in range(3) for x in (cfg.domain_min[d], cfg.domain_max[d])]
+    io_vtk.write_domain(str(tmp_path / "initDomain0.dat"), 3, dom)
+
+    res = subprocess.run([exe, "init", "0", "out", "--fixed-dt"], capture_output=True, text=True, timeout=600,
+                         cwd=str(tmp_path))
+    assert res.returncode == 0, res.stderr[-2000:]
+    rows = io_vtk.read_globals(str(tmp_path / "outGlobals0.dat"))
+    dt = cfg.maxdt
+    maxtime = dt * 10  # the example case: OUTSTEP 10, MAXTIME = 10 maxdt
+    assert [int(r["OutStep"]) for r in rows] == list(range(1, len(rows) + 1))
+    assert len(rows) >= 8
+    steps = [int(r["SPHStep"]) for r in rows]
+    assert steps == sorted(steps) and len(set(steps)) == len(steps)
+    for r in rows:
+        assert abs(r["Time"] - r["SPHStep"] * dt) <= 1e-9 * dt * r["SPHStep"]
+        assert int(r["n"]) == case.n
+    # the loop ended on time > MAXTIME, as run.cpp's does
+    assert rows[-1]["Time"] > maxtime and rows[-2]["Time"] <= maxtime
+    for k in range(1, len(rows) + 1):
+        assert (tmp_path / f"out{k:07d}_0.vtu").exists() and (tmp_path / f"out{k:07d}.pvtu").exists()
+    assert (tmp_path / "outRestart0000005_0.vtu").exists() and not (tmp_path / "outRestart0000004_0.vtu").exists()
+    assert io_vtk.read_domain(str(tmp_path / "outDomain0.dat"), 3)["proc_domain"] == dom
+
+    # output step 5 against the fixed-step command after as many steps
+    row5 = rows[4]
+    n5 = int(row5["SPHStep"])
+    final = tmp_path / "final.bin"
+    res = subprocess.run([exe, str(tmp_path / "initRestart0000000_0.vtu"), str(n5), str(final), "--fixed-dt"],
+                         capture_output=True, text=True, timeout=600, cwd=str(tmp_path))
+    assert res.returncode == 0, res.stderr[-2000:]
+    a = read_final(str(final))
+    d = io_vtk.read_vtu(str(tmp_path / "outRestart0000005_0.vtu"))
+    for k in ("v", "vhat"):
+        np.testing.assert_array_equal(d["arrays"][k], a[k])
+    for k in ("dens", "h"):
+        np.testing.assert_array_equal(d["arrays"][k], a[k])
+    np.testing.assert_array_equal(d["points"], a["r"].astype(np.float32).astype(np.float64))
+    # the row's output-step quantities are the oracle's calcOutputVars of that state
+    iam, m, vh = d["arrays"]["iam"], d["arrays"]["mass"], d["arrays"]["vhat"]
+    ke = 0.5 * float(np.sum(m[iam == cases.SPH] * np.sum(vh[iam == cases.SPH] ** 2, axis=1)))
+    assert abs(row5["KE"] - ke) <= 1e-12 * ke
+    assert int(row5["nSph"]) == int(np.sum(iam == cases.SPH))
+
+    # continued from output step 5 into the same files
+    res = subprocess.run([exe, "out", "5", "out", "--fixed-dt"], capture_output=True, text=True, timeout=600,
+                         cwd=str(tmp_path))
+    assert res.returncode == 0, res.stderr[-2000:]
+    again = io_vtk.read_globals(str(tmp_path / "outGlobals0.dat"))
+    assert [int(r["OutStep"]) for r in again] == list(range(1, len(again) + 1))
+    assert again[:5] == rows[:5]
+    # time and step count carry on from the row of step 5
+    assert int(again[5]["SPHStep"]) > n5
+    for r in again[5:]:
+        assert abs(r["Time"] - r["SPHStep"] * dt) <= 1e-9 * dt * r["SPHStep"]
