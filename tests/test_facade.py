@@ -291,23 +291,28 @@ int main(int argc, char **argv) {
 """
 
 
-def _vtk_tool(tmp_path, ndim):
-    d = tmp_path / f"tool{ndim}"
+def _facade_tool(tmp_path, ndim, name, source):
+    """A small program over the façade's I/O (io_data_vtk.cpp) for NDIM = ndim."""
+    d = tmp_path / f"{name}{ndim}"
     d.mkdir(exist_ok=True)
     # the constants every case defines that the I/O headers read
     box = ", ".join(["0.0"] * ndim), ", ".join(["1.0"] * ndim)
     (d / "customConstants.h").write_text(f"#ifndef CC_H\n#define CC_H\nconst int NDIM = {ndim};\n"
                                          f"const double RMIN[NDIM] = {{{box[0]}}};\n"
                                          f"const double RMAX[NDIM] = {{{box[1]}}};\n#endif\n")
-    (d / "vtk_tool.cpp").write_text(VTK_TOOL)
+    (d / f"{name}.cpp").write_text(source)
     sys.path.insert(0, FACADE)
     from build_case import zlib_flags
-    exe = str(d / "vtk_tool")
+    exe = str(d / name)
     res = subprocess.run(["g++", "-std=gnu++17", "-O1", f"-I{d}", f"-I{os.path.join(FACADE, 'include')}",
-                          str(d / "vtk_tool.cpp"), os.path.join(FACADE, "io_data_vtk.cpp"), "-o", exe,
+                          str(d / f"{name}.cpp"), os.path.join(FACADE, "io_data_vtk.cpp"), "-o", exe,
                           *zlib_flags()], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr[-3000:]
     return exe
+
+
+def _vtk_tool(tmp_path, ndim):
+    return _facade_tool(tmp_path, ndim, "vtk_tool", VTK_TOOL)
 
 
 @pytest.mark.parametrize("name", ["dambreak2d_small", "sediment3d_small"])
@@ -493,3 +498,73 @@ def test_run_loop_of_the_reference_command_line(tmp_path):
     assert int(again[5]["SPHStep"]) > n5
     for r in again[5:]:
         assert abs(r["Time"] - r["SPHStep"] * dt) <= 1e-9 * dt * r["SPHStep"]
+
+
+GD_TOOL = r"""
+#include <cstdio>
+#include <cstdlib>
+#include "io_data_vtk.h"
+/* gd_tool <inbase> <outbase>: prints the Domain file of inbase (rank,
+ * procDomain, procNeighbrs); writes Globals rows 1, 2, 3 and then 2 again
+ * under outbase and prints what readGlobals(2) reads back */
+int main(int argc, char **argv) {
+    CglobalVars g;
+    Cio_data_vtk in(argv[1], &g);
+    if (!in.readDomain(0, &g)) return 1;
+    std::printf("%d", g.mpiRank);
+    for (int i = 0; i < 2 * NDIM; i++) std::printf(" %.17g", g.procDomain[i]);
+    for (int k = 0; k < SPHDEM_FACADE_NEIGHBOURS; k++) std::printf(" %d", g.procNeighbrs[k]);
+    std::printf("\n");
+    Cio_data_vtk out(argv[2], &g);
+    for (int step : {1, 2, 3, 2}) {
+        g.sphStep = 10 * step + (step == 2 ? 7 : 0);
+        g.time = 0.1 * step + 1e-13;
+        g.eKE = 1.0 / 3.0 * step;
+        g.n = 100 + step;
+        g.custom[0] = -step;
+        out.writeGlobals(step, &g);
+    }
+    CglobalVars r;
+    out.readGlobals(2, &r);
+    std::printf("%d %.17g %.17g %d\n", r.sphStep, r.time, r.eKE, r.n);
+    return 0;
+}
+"""
+
+
+@pytest.mark.skipif(not os.path.isfile(os.path.join(REF_ROOT, "damBreak", "initDataGlobals0.dat")),
+                    reason="reference files not present")
+def test_cpp_globals_and_domain_files_in_the_reference_layout(tmp_path):
+    """The façade's C++ Globals and Domain files against the files the
+    reference wrote for damBreak (2D): the Globals header line is the
+    reference's own, and its Domain line (rank, procDomain[4], procNeighbrs[9],
+    ioDomain.cpp:3-23) reads back value for value.  Rows written for steps 1,
+    2, 3 and then 2 again leave rows 1 and 2, as CioGlobals's
+    openAndSeekToStep(outStep - 1) places the write (ioGlobals.cpp:48-73,
+    111-139), and readGlobals(2) reads row 2 back to full precision."""
+    from sphdem import io_vtk
+    ref_dir = os.path.join(REF_ROOT, "damBreak")
+    # one process: the single-rank line of the Domain file, under the rank's name
+    line = open(os.path.join(ref_dir, "initDataDomain.dat")).readline()
+    (tmp_path / "initDomain0.dat").write_text(line)
+    exe = _facade_tool(tmp_path, 2, "gd_tool", GD_TOOL)
+    res = subprocess.run([exe, str(tmp_path / "init"), str(tmp_path / "out")], capture_output=True, text=True,
+                         timeout=60)
+    assert res.returncode == 0, res.stderr
+    dom, back = res.stdout.splitlines()
+    want = line.split()
+    got = dom.split()
+    assert int(got[0]) == int(want[0])
+    assert [float(x) for x in got[1:5]] == [float(x) for x in want[1:5]]
+    nb = [int(x) for x in want[5:14]]
+    nb[4] = -1  # the process itself (ioDomain.cpp:16-17)
+    assert [int(x) for x in got[5:14]] == nb
+
+    ours = open(tmp_path / "outGlobals0.dat").read().splitlines()
+    theirs = open(os.path.join(ref_dir, "initDataGlobals0.dat")).read().splitlines()
+    assert ours[0] == theirs[0]
+    rows = io_vtk.read_globals(str(tmp_path / "outGlobals0.dat"))
+    assert [int(r["OutStep"]) for r in rows] == [1, 2]
+    assert rows[1]["SPHStep"] == 27 and rows[1]["custom"][0] == -2.0
+    step, time, eke, n = back.split()
+    assert (int(step), float(time), float(eke), int(n)) == (27, 0.2 + 1e-13, 2.0 / 3.0, 102)
