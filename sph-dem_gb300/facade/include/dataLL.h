@@ -22,6 +22,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <iostream>
 #include <string>
 #include <vector>
@@ -87,12 +88,110 @@ class CdataLL {
             if (Iffunct(ps[i])) Thefunct(ps[i], nbrs[i], globals);
     }
 
+    /* the remaining traverse forms of dataLL.h:125-142 */
+    template <class T, void Thefunct(Cparticle &, CglobalVars &, T &)>
+    void traverse(T &a) {
+        for (size_t i = 0; i < ps.size(); i++) Thefunct(ps[i], globals, a);
+    }
+    template <class T, void Thefunct(Cparticle &, CglobalVars &, T &), bool Iffunct(Cparticle &)>
+    void traverse(T &a) {
+        for (size_t i = 0; i < ps.size(); i++)
+            if (Iffunct(ps[i])) Thefunct(ps[i], globals, a);
+    }
+    template <void Thefunct(Cparticle &, CglobalVars &, double, double)>
+    void traverse(double a, double b) {
+        for (size_t i = 0; i < ps.size(); i++) Thefunct(ps[i], globals, a, b);
+    }
+    template <void Thefunct(Cparticle &, CglobalVars &, double, double), bool Iffunct(Cparticle &)>
+    void traverse(double a, double b) {
+        for (size_t i = 0; i < ps.size(); i++)
+            if (Iffunct(ps[i])) Thefunct(ps[i], globals, a, b);
+    }
+    template <void Thefunct(Cparticle &, CglobalVars &, double, double, double), bool Iffunct(Cparticle &)>
+    void traverse(double a, double b, double c) {
+        for (size_t i = 0; i < ps.size(); i++)
+            if (Iffunct(ps[i])) Thefunct(ps[i], globals, a, b, c);
+    }
+
+    /* every (particle, neighbour) pair, in both orders (dataLL.impl.h:181-216) */
+    template <void Thefunct(Cparticle &, Cparticle &, CglobalVars &)>
+    void neighbours() {
+        lists();
+        for (size_t i = 0; i < ps.size(); i++)
+            for (Cparticle *pn : nbrs[i]) Thefunct(ps[i], *pn, globals);
+    }
+    template <void Thefunct(Cparticle &, Cparticle &, CglobalVars &), bool Iffunct(Cparticle &)>
+    void neighbours() {
+        lists();
+        for (size_t i = 0; i < ps.size(); i++)
+            if (Iffunct(ps[i]))
+                for (Cparticle *pn : nbrs[i]) Thefunct(ps[i], *pn, globals);
+    }
+    template <class T, void Thefunct(Cparticle &, vector<Cparticle *> &, CglobalVars &, T &), bool Iffunct(Cparticle &)>
+    void neighboursGroup(T &a) {
+        lists();
+        for (size_t i = 0; i < ps.size(); i++)
+            if (Iffunct(ps[i])) Thefunct(ps[i], nbrs[i], globals, a);
+    }
+
+    /* neighbours of particles that are not in the simulation, e.g. points of
+     * an output grid (dataLL.impl.h:282-306): the simulation's particles of
+     * the query's relation (DEM for a DEM query, else the others) within
+     * 2 max(h) of it, periodic images as ghost copies.  A search over all
+     * particles per query, for output steps. */
+    template <void Thefunct(Cparticle &, Cparticle &, CglobalVars &)>
+    void neighboursUsing(vector<Cparticle> &qs) {
+        for (Cparticle &q : qs) {
+            vector<Cparticle *> found;
+            search(q, -1.0, found);
+            for (Cparticle *pn : found) Thefunct(q, *pn, globals);
+        }
+    }
+    template <void Thefunct(Cparticle &, vector<Cparticle *> &, CglobalVars &)>
+    void neighboursUsing(vector<Cparticle> &qs) {
+        for (Cparticle &q : qs) {
+            vector<Cparticle *> found;
+            search(q, -1.0, found);
+            Thefunct(q, found, globals);
+        }
+    }
+    /* neighbours within a given radius (dataLL.impl.h:244-255), searched as
+     * neighboursUsing searches */
+    template <void Thefunct(Cparticle &, vector<Cparticle *> &, CglobalVars &), bool Iffunct(Cparticle &)>
+    void neighboursGroupAtRadius(const double radius) {
+        for (size_t i = 0; i < ps.size(); i++)
+            if (Iffunct(ps[i])) {
+                vector<Cparticle *> found;
+                search(ps[i], radius, found);
+                Thefunct(ps[i], found, globals);
+            }
+    }
+
+    int numParticles() { return (int)ps.size(); }
+    /* CdataLL::reset (dataLL.cpp:140-236) from case code: the mirror's state
+     * goes to the device, which rebuilds its buckets and lists there, and
+     * comes back */
+    void reset() {
+        push();
+        check(sphdem_rebuild(h), "sphdem_rebuild");
+        pull();
+    }
+    /* CdataLL::sumOverProcs (dataLL.cpp:790-830): one process holds every
+     * particle, so the sums are the values themselves */
+    void sumOverProcs(vect *, int) {}
+    void sumOverProcs(double *, int) {}
+
    private:
     particleContainer &ps;
     sphdem_handle h;
     vector<Cparticle> pending_insert;
     vector<vector<Cparticle *> > nbrs;
+    /* periodic images of neighbours: copies with the position shifted by a
+     * period, as the reference's ghost particles are (dataLL.cpp:648-660);
+     * pointers stay valid while the deque grows */
+    std::deque<Cparticle> ghosts;
     bool lists_valid = false;
+    vector<double> vu, vdudt, vev, vdev;
     vector<double> vr, vv, vvh, vv0, vvh0, vf, vfp, vfv, vfb, vfd, vfvel, vgp, vn1, vn2, vn3;
     vector<double> vm, vd, vh, vrad, vdddt, vpress, vpdr2, vpor, vdpor, vshep, vom;
     vector<int32_t> viam, vtag;
@@ -107,6 +206,8 @@ class CdataLL {
     }
     void soa(SphDemParticles &p);
     void lists();
+    Cparticle *image_of(Cparticle &q, Cparticle &b);
+    void search(Cparticle &q, double radius, vector<Cparticle *> &found);
 };
 
 inline void CdataLL::soa(SphDemParticles &p) {
@@ -128,6 +229,7 @@ inline void CdataLL::soa(SphDemParticles &p) {
     p.mass = v1(vm); p.dens = v1(vd); p.h = v1(vh); p.radius = v1(vrad); p.dddt = v1(vdddt);
     p.press = v1(vpress); p.pdr2 = v1(vpdr2); p.porosity = v1(vpor); p.dporositydt = v1(vdpor);
     p.shep_sum = v1(vshep); p.omega = v1(vom);
+    p.u = v1(vu); p.dudt = v1(vdudt); p.e_visc = v1(vev); p.de_visc_dt = v1(vdev);
 }
 
 inline void CdataLL::pull() {
@@ -146,6 +248,7 @@ inline void CdataLL::pull() {
         q.mass = vm[i]; q.dens = vd[i]; q.h = vh[i]; q.radius = vrad[i]; q.dddt = vdddt[i];
         q.press = vpress[i]; q.pdr2 = vpdr2[i]; q.porosity = vpor[i]; q.dporositydt = vdpor[i];
         q.shepSum = vshep[i]; q.omega = vom[i];
+        q.u = vu[i]; q.dudt = vdudt[i]; q.eViscF = vev[i]; q.deViscFdt = vdev[i];
         q.iam = (iamTypes)viam[i];
         q.tag = vtag[i];
         q.concave = vconc[i] != 0;
@@ -230,15 +333,81 @@ inline void CdataLL::push() {
 inline void CdataLL::lists() {
     if (lists_valid) return;
     const size_t n = ps.size();
-    vector<int64_t> offs(n + 1);
-    int64_t np = 0;
-    check(sphdem_pairs(h, SPHDEM_PAIRS_SPH, offs.data(), nullptr, 0, &np), "sphdem_pairs");
-    vector<int32_t> idx((size_t)np);
-    check(sphdem_pairs(h, SPHDEM_PAIRS_SPH, offs.data(), idx.data(), np, &np), "sphdem_pairs");
+    /* calcNeighbours (dataLL.cpp:1026-1075): DEM particles take the DEM
+     * relation, the others the SPH one; each row comes from one of the two */
+    vector<int64_t> offs[2] = {vector<int64_t>(n + 1), vector<int64_t>(n + 1)};
+    vector<int32_t> idx[2];
+    const int kinds[2] = {SPHDEM_PAIRS_SPH, SPHDEM_PAIRS_DEM};
+    for (int k = 0; k < 2; k++) {
+        int64_t np = 0;
+        check(sphdem_pairs(h, kinds[k], offs[k].data(), nullptr, 0, &np), "sphdem_pairs");
+        idx[k].resize((size_t)np);
+        check(sphdem_pairs(h, kinds[k], offs[k].data(), idx[k].data(), np, &np), "sphdem_pairs");
+    }
+    ghosts.clear();
     nbrs.assign(n, vector<Cparticle *>());
-    for (size_t i = 0; i < n; i++)
-        for (int64_t k = offs[i]; k < offs[i + 1]; k++) nbrs[i].push_back(&ps[idx[k]]);
+    for (size_t i = 0; i < n; i++) {
+        const int k = ps[i].iam == dem ? 1 : 0;
+        for (int64_t e = offs[k][i]; e < offs[k][i + 1]; e++) nbrs[i].push_back(image_of(ps[i], ps[idx[k][e]]));
+    }
     lists_valid = true;
+}
+
+/* b itself, or, where b is p's neighbour across a periodic boundary, the
+ * ghost copy of b at its periodic image nearest p: r = RMIN - RMAX + r or
+ * RMAX - RMIN + r on that axis, as dataLL.cpp:648-660 places ghosts.  A
+ * periodic axis spans at least three buckets of 2 h_max, so the nearest
+ * image is the neighbour. */
+inline Cparticle *CdataLL::image_of(Cparticle &p, Cparticle &b) {
+    int shift[NDIM];
+    bool any = false;
+    for (int d = 0; d < NDIM; d++) {
+        shift[d] = 0;
+        if (!PERIODIC[d]) continue;
+        const double half = 0.5 * (RMAX[d] - RMIN[d]);
+        const double dx = p.r[d] - b.r[d];
+        if (dx > half) shift[d] = 1;
+        if (dx < -half) shift[d] = -1;
+        any = any || shift[d] != 0;
+    }
+    if (!any) return &b;
+    ghosts.push_back(b);
+    Cparticle &g = ghosts.back();
+    for (int d = 0; d < NDIM; d++) {
+        if (shift[d] > 0) g.r[d] = RMAX[d] - RMIN[d] + b.r[d];
+        if (shift[d] < 0) g.r[d] = RMIN[d] - RMAX[d] + b.r[d];
+    }
+    return &g;
+}
+
+/* every particle of q's relation (DEM for a DEM query, else the others)
+ * whose nearest image lies within 2 max(h) of q (radius < 0) or within
+ * radius, the image as a ghost copy where it is not the particle itself */
+inline void CdataLL::search(Cparticle &q, double radius, vector<Cparticle *> &found) {
+    const bool dem_q = q.iam == dem;
+    for (size_t j = 0; j < ps.size(); j++) {
+        Cparticle &b = ps[j];
+        if (&b == &q || (b.iam == dem) != dem_q || (int)b.iam < 0) continue;
+        vect r = b.r;
+        for (int d = 0; d < NDIM; d++) {
+            if (!PERIODIC[d]) continue;
+            const double half = 0.5 * (RMAX[d] - RMIN[d]);
+            const double dx = q.r[d] - b.r[d];
+            if (dx > half) r[d] = RMAX[d] - RMIN[d] + b.r[d];
+            if (dx < -half) r[d] = RMIN[d] - RMAX[d] + b.r[d];
+        }
+        const double lim2 = radius < 0 ? std::pow(2.0 * (q.h > b.h ? q.h : b.h), 2) : radius * radius;
+        if (len2(q.r - r) > lim2) continue;
+        bool same = true;
+        for (int d = 0; d < NDIM; d++) same = same && r[d] == b.r[d];
+        if (same) {
+            found.push_back(&b);
+        } else {
+            ghosts.push_back(b);
+            ghosts.back().r = r;
+            found.push_back(&ghosts.back());
+        }
+    }
 }
 
 #endif

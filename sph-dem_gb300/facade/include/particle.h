@@ -7,6 +7,7 @@
 #ifndef SPHDEM_FACADE_PARTICLE_H
 #define SPHDEM_FACADE_PARTICLE_H
 
+#include <cmath>
 #include <fstream>
 #include <iostream>
 #include <string>
@@ -34,6 +35,21 @@ class Cparticle {
     enum iamTypes iam = sph;
     int tag = 0;
     bool concave = true;
+    /* calcEnergies integrals per unit mass (sphIncompress.h:769-781): u, dudt,
+     * eViscF and deViscFdt are mirrored from the device; the other three
+     * pairs are zero on the device path, as on the reference's */
+    double u = 0, dudt = 0;
+    double eViscF = 0, deViscFdt = 0, eViscB = 0, deViscBdt = 0, eBForce = 0, deBForcedt = 0, eFF = 0, deFFdt = 0;
+    /* members the reference's particle carries for case and output code
+     * (particle.h:262-316); host-only here */
+    vect fg, vort, origPos;
+    double tmp = 0, minDt = 0, colour = 0;
+    int gHead = 0;
+
+    /* the neighbour predicate (particle.h:236-238), Wendland support 2h */
+    bool is_neighbr(Cparticle &p) {
+        return (&p != this) && len2(r - p.r) <= std::pow(2.0 * (h > p.h ? h : p.h), 2);
+    }
 };
 
 typedef vector<Cparticle> particleContainer;

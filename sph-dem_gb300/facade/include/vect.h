@@ -8,6 +8,8 @@
 #define SPHDEM_FACADE_VECT_H
 
 #include <cmath>
+#include <iomanip>
+#include <ostream>
 
 #include "customConstants.h"
 
@@ -29,6 +31,10 @@ class TVect {
     TVect(T a, T b, T c) {
         const T v[3] = {a, b, c};
         for (int i = 0; i < N; i++) x[i] = i < 3 ? v[i] : T(0);
+    }
+    /* `vect v = ARRAY;` from a case constant such as RMIN[NDIM] */
+    TVect(const T (&a)[N]) {
+        for (int i = 0; i < N; i++) x[i] = a[i];
     }
     T &operator[](int i) { return x[i]; }
     const T &operator[](int i) const { return x[i]; }
@@ -97,6 +103,32 @@ template <typename T, int N>
 inline T len2(const TVect<T, N> &a) { return dot(a, a); }
 template <typename T, int N>
 inline T len(const TVect<T, N> &a) { return std::sqrt(len2(a)); }
+
+/* element-wise product and quotient, as blitz's TinyVector arithmetic */
+template <typename T, int N>
+inline TVect<T, N> operator*(TVect<T, N> a, const TVect<T, N> &b) {
+    for (int i = 0; i < N; i++) a.x[i] *= b.x[i];
+    return a;
+}
+template <typename T, int N>
+inline TVect<T, N> operator/(TVect<T, N> a, const TVect<T, N> &b) {
+    for (int i = 0; i < N; i++) a.x[i] /= b.x[i];
+    return a;
+}
+
+/* the text blitz writes for a TinyVector (its tinyvecio.cc layout): the
+ * length, then the components in fields of width 10 between brackets, a line
+ * break after every seventh */
+template <typename T, int N>
+inline std::ostream &operator<<(std::ostream &os, const TVect<T, N> &a) {
+    os << N << " [ ";
+    for (int i = 0; i < N; i++) {
+        os << std::setw(10) << a.x[i];
+        if ((i + 1) % 7 == 0) os << std::endl << "  ";
+    }
+    os << " ]";
+    return os;
+}
 
 typedef TVect<double, NDIM> vect;
 typedef TVect<int, NDIM> vectInt;

@@ -24,6 +24,7 @@ int oracle_pairs(void *h, int kind, int64_t *offs, int32_t *idx, int64_t cap, in
 int oracle_insert(void *h, const SphDemParticles *in, int64_t *out_idx);
 int oracle_mark_for_deletion(void *h, const int64_t *idx, int64_t k);
 int oracle_output_vars(void *h, SphDemOutputVars *o);
+int oracle_rebuild(void *h);
 const char *oracle_last_error(void);
 }
 
@@ -107,6 +108,11 @@ int sphdem_insert_particles(sphdem_handle h, const SphDemParticles *in, int64_t 
 
 int sphdem_mark_for_deletion(sphdem_handle h, const int64_t *idx, int64_t k) {
     const int rc = oracle_mark_for_deletion(h->o, idx, k);
+    return rc ? fail(h, rc) : SPHDEM_OK;
+}
+
+int sphdem_rebuild(sphdem_handle h) {
+    const int rc = oracle_rebuild(h->o);
     return rc ? fail(h, rc) : SPHDEM_OK;
 }
 

@@ -568,3 +568,144 @@ def test_cpp_globals_and_domain_files_in_the_reference_layout(tmp_path):
     assert rows[1]["SPHStep"] == 27 and rows[1]["custom"][0] == -2.0
     step, time, eke, n = back.split()
     assert (int(step), float(time), float(eke), int(n)) == (27, 0.2 + 1e-13, 2.0 / 3.0, 102)
+
+
+NEIGHBOUR_OUTPUT = r"""
+#include <fstream>
+#include <iomanip>
+
+#include "customOutput.h"
+#include "dataLL.impl.h"
+#include "sph.h"
+#include "sphIncompress.h"
+
+namespace {
+struct Tally {
+    double mass = 0;
+};
+inline void addMass(Cparticle &p, CglobalVars &, Tally &t) { t.mass += p.mass; }
+inline void countPair(Cparticle &, Cparticle &, CglobalVars &g) { g.custom[0] += 1.0; }
+inline void countGroup(Cparticle &, vector<Cparticle *> &nb, CglobalVars &g) { g.custom[1] += nb.size(); }
+inline void countAt(Cparticle &, vector<Cparticle *> &nb, CglobalVars &g) { g.custom[2] += nb.size(); }
+inline void countUsing(Cparticle &, vector<Cparticle *> &nb, CglobalVars &g) { g.custom[3] += nb.size(); }
+inline void countAgain(Cparticle &, vector<Cparticle *> &nb, CglobalVars &g) { g.custom[4] += nb.size(); }
+inline void mark2(Cparticle &p, CglobalVars &, double a, double b) { p.colour = a + b; }
+inline void mark3(Cparticle &p, CglobalVars &, double a, double b, double c) { p.tmp = a + b + c; }
+}  // namespace
+
+/* the SPH density summation over neighbour groups with periodic images, then
+ * the other CdataLL forms, each tallied into the globals */
+void CcustomOutput::calcOutput(int outstep, CcustomSim *, Cio_data_vtk *io) {
+    CglobalVars &g = data->globals;
+    for (int k = 0; k < 5; k++) g.custom[k] = 0;
+    data->neighboursGroup<Nsph::calcDensity, Nsph::ifSphOrSphBoundary>();
+    particleContainer &ps = data->getParticles();
+    {
+        std::ofstream out((io->filename + ".dens").c_str(), std::ios::binary);
+        for (Cparticle &p : ps) {
+            const double rec[7] = {p.r[0], p.r[1], p.r[2], p.mass, p.h, p.dens, (double)p.iam};
+            out.write(reinterpret_cast<const char *>(rec), sizeof rec);
+        }
+    }
+    data->neighbours<countPair, Nsph::ifSphOrSphBoundary>();
+    data->neighboursGroup<countGroup, Nsph::ifSphOrSphBoundary>();
+    Tally t;
+    data->traverse<Tally, addMass, Nsph::ifSph>(t);
+    data->traverse<mark2, Nsph::ifSph>(1.0, 2.0);
+    data->traverse<mark3, Nsph::ifSph>(1.0, 2.0, 3.0);
+    data->neighboursGroupAtRadius<countAt, Nsph::ifSph>(0.005);
+    vector<Cparticle> qs(ps.begin(), ps.begin() + 50);
+    data->neighboursUsing<countUsing>(qs);
+    data->reset();
+    data->neighboursGroup<countAgain, Nsph::ifSphOrSphBoundary>();
+    double colour = 0, tmp = 0;
+    for (Cparticle &p : ps)
+        if (p.iam == sph) {
+            colour = p.colour;
+            tmp = p.tmp;
+            break;
+        }
+    std::ofstream s((io->filename + ".stats").c_str());
+    s << std::setprecision(17) << g.custom[0] << ' ' << g.custom[1] << ' ' << t.mass << ' ' << data->numParticles()
+      << ' ' << colour << ' ' << tmp << ' ' << g.custom[2] << ' ' << g.custom[3] << ' ' << g.custom[4] << '\n';
+}
+"""
+
+
+def test_neighbour_forms_with_periodic_images(tmp_path):
+    """The façade's neighbour forms on the CPU through the oracle-backed C
+    ABI, with a case whose output code uses them (the example case's
+    constants and hooks: periodic x and y).  Over neighbour groups,
+    Nsph::calcDensity (sph.h:1149-1190) gives the SPH density summation with
+    each neighbour at its nearest periodic image, as the reference's ghost
+    copies place it; it matches a brute-force minimum-image summation.  The
+    pair, group, at-radius and external-query forms count the pairs a
+    brute-force search counts; the traverse forms with a state object and
+    with two and three constants reach every particle; reset() keeps the
+    lists."""
+    lib = _oracle_abi(str(tmp_path / "oracle_abi"))
+    case_dir = tmp_path / "case"
+    case_dir.mkdir()
+    src = os.path.join(FACADE, "example_sediment")
+    for f in ("customConstants.h", "customSim.h", "customSim.cpp", "customOutput.h"):
+        (case_dir / f).write_text(open(os.path.join(src, f)).read())
+    (case_dir / "customOutput.cpp").write_text(NEIGHBOUR_OUTPUT)
+    exe = build_case(str(case_dir), str(tmp_path / "run_case"), libdir=lib)
+    case = cases.workload("sediment3d_small")
+    init = tmp_path / "init.spdm"
+    state.write_state(str(init), case.particles)
+    out = tmp_path / "final.bin"
+    res = subprocess.run([exe, str(init), "10", str(out), "--fixed-dt"], capture_output=True, text=True,
+                         timeout=600, cwd=str(tmp_path))
+    assert res.returncode == 0, res.stderr[-2000:]
+    rec = np.fromfile(str(out) + ".dens", dtype="<f8").reshape(-1, 7)
+    r, m, h, dens, iam = rec[:, 0:3], rec[:, 3], rec[:, 4], rec[:, 5], rec[:, 6].astype(int)
+    cfg = case.cfg
+    L = np.array(cfg["rmax"]) - np.array(cfg["rmin"])
+    per = np.array(cfg["periodic"], bool)
+    n = len(m)
+    fluid = (iam == cases.SPH) | (iam == cases.SPH_BOUNDARY)
+    nondem = iam != cases.DEM
+    # nearest images, as the reference places its ghosts: RMIN - RMAX + r or RMAX - RMIN + r
+    rmin, rmax = np.array(cfg["rmin"]), np.array(cfg["rmax"])
+    d = r[:, None, :] - r[None, :, :]
+    img = np.broadcast_to(r[None, :, :], d.shape).copy()
+    for a in range(3):
+        if per[a]:
+            hi, lo = d[:, :, a] > 0.5 * L[a], d[:, :, a] < -0.5 * L[a]
+            img[:, :, a] = np.where(hi, (rmax[a] - rmin[a]) + r[None, :, a], img[:, :, a])
+            img[:, :, a] = np.where(lo, (rmin[a] - rmax[a]) + r[None, :, a], img[:, :, a])
+    dx = r[:, None, :] - img
+    d2 = (dx[:, :, 0] * dx[:, :, 0] + dx[:, :, 1] * dx[:, :, 1]) + dx[:, :, 2] * dx[:, :, 2]
+    lim2 = (2.0 * np.maximum(h[:, None], h[None, :])) ** 2
+    off = ~np.eye(n, dtype=bool)
+    crossing = (np.abs(r[:, None, :] - r[None, :, :]) > 0.5 * L).any(axis=2) & (d2 <= lim2) & off
+    assert crossing[fluid][:, nondem].sum() > 0  # the summation does use periodic images
+
+    def wendland(q, hh):
+        c = 21.0 / (256.0 * cfg["pi"])  # the case's PI (3.14159265 in the reference's cases)
+        return np.where(q <= 2.0, c * (2.0 - q) ** 4 * (1.0 + 2.0 * q), 0.0) / hh ** 3
+
+    pair = (d2 <= lim2) & off & nondem[None, :] & fluid[None, :]
+    q = np.sqrt(d2) / h[:, None]
+    want = m * wendland(0.0, h) + np.sum(np.where(pair, m[None, :] * wendland(q, h[:, None]), 0.0), axis=1)
+    err = np.abs(dens[fluid] - want[fluid]).max() / np.abs(want[fluid]).max()
+    assert err <= 1e-12, err
+
+    stats = open(str(out) + ".stats").read().split()
+    pairs, groups, mass_sph, count, colour, tmp, at_r, using, again = (float(x) for x in stats)
+    # ties at exactly 2 max(h) may fall either way: bracket the brute-force counts
+    tie = np.abs(d2 - lim2) <= 1e-12 * lim2
+    grp = off & nondem[None, :] & fluid[:, None]
+    lo_n, hi_n = (grp & (d2 <= lim2) & ~tie).sum(), (grp & ((d2 <= lim2) | tie)).sum()
+    assert lo_n <= groups <= hi_n and pairs == groups and again == groups
+    assert abs(mass_sph - m[iam == cases.SPH].sum()) <= 1e-12 * mass_sph
+    assert int(count) == n and colour == 3.0 and tmp == 6.0
+    sphq = iam == cases.SPH
+    at = off & nondem[None, :] & sphq[:, None] & (d2 <= 0.005 ** 2)
+    assert at.sum() - (np.abs(d2 - 0.005 ** 2) <= 1e-12 * 0.005 ** 2).sum() <= at_r <= at.sum() + (np.abs(d2 - 0.005 ** 2) <= 1e-12 * 0.005 ** 2).sum()
+    # external queries: copies of the first 50 particles find their originals too
+    rel = np.where(iam[:50, None] == cases.DEM, iam[None, :] == cases.DEM, iam[None, :] != cases.DEM)
+    u_lo = (rel & (d2[:50] <= lim2[:50]) & ~tie[:50]).sum()
+    u_hi = (rel & ((d2[:50] <= lim2[:50]) | tie[:50])).sum()
+    assert u_lo <= using <= u_hi
