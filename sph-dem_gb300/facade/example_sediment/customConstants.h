@@ -18,6 +18,8 @@ const double PI = 3.14159265;
 const double RMIN[NDIM] = {0.0, 0.0, 0.0};
 const double RMAX[NDIM] = {0.04, 0.04, 0.08};
 const int PERIODIC[NDIM] = {1, 1, 0};
+const int GHOST[2*NDIM] = {0, 0, 0, 0, 0, 0};
+const double DENS_DROP[NDIM] = {0.0, 0.0, 0.0};
 const double PSEP = 0.004;
 const double HFAC = 1.5;
 const double H = 0.006;

@@ -38,6 +38,8 @@ def constants(name: str = "sediment3d_small") -> str:
         f"const double RMIN[NDIM] = {{{', '.join(r(v) for v in c['rmin'])}}};",
         f"const double RMAX[NDIM] = {{{', '.join(r(v) for v in c['rmax'])}}};",
         f"const int PERIODIC[NDIM] = {{{', '.join(str(int(v)) for v in c['periodic'])}}};",
+        "const int GHOST[2*NDIM] = {0, 0, 0, 0, 0, 0};",
+        "const double DENS_DROP[NDIM] = {0.0, 0.0, 0.0};",
         f"const double PSEP = {r(c['psep'])};",
         f"const double HFAC = {r(c['hfac'])};",
         f"const double H = {r(c['h'])};",

@@ -17,9 +17,53 @@
 #if !defined(WENDLAND)
 #error "the device path implements the Wendland C2 kernel only (#define WENDLAND)"
 #endif
-#if defined(LUBRICATION) || defined(HERTZ) || defined(HERTZ_KUWABARA) || defined(REINIT_DENS_MLS)
-#error "option not implemented by the device path"
+/* Options of the reference's step (sph.h, sphIncompress.h/.cpp, dataLL.cpp)
+ * that the device path does not implement: a case that defines one would
+ * step differently, so it does not build.  Options that only add fields or
+ * checks (CHECK_FOR_NAN, SAVE_VHALF, TEST_VISC, HACK_TO_SAVE_MEM,
+ * DEFORMATION_MATRIX) and LIQ_DEM_CUSTOM_WALL_CONTACTS (without it the
+ * reference looks for wall particles in the DEM lists, which hold DEM
+ * particles only) do not change the step. */
+#if defined(LUBRICATION) || defined(HERTZ) || defined(HERTZ_KUWABARA)
+#error "DEM contact law not implemented by the device path (LINEAR only)"
 #endif
+#if defined(REINIT_DENS_MLS) || defined(SMOOTHED_VISC_VELOCITY) || defined(SMOOTHED_VISC_VELOCITY_MLS) || \
+    defined(SMOOTHED_VISC_VELOCITY_HAT) || defined(SMOOTHING) || defined(SPH_SMOOTHING) || \
+    defined(DIRECT_SMOOTHING) || defined(GRID_SMOOTHING) || defined(AVE_VELOCITY)
+#error "MLS re-initialisation and velocity smoothing are not implemented by the device path"
+#endif
+#if defined(LIQ_DEM_SEPARATE_DRAGS) || defined(LIQ_DEM_SIMPLE_DRAG) || defined(LIQ_DEM_ERGUN_DRAG) || \
+    defined(ERGUN) || defined(LIQ_DEM_LIFT) || defined(LIQ_DEM_ADDED_MASS) || defined(LIQ_DEM_ONE_WAY_COUPLE) || \
+    defined(LIQ_DEM_TEST) || defined(LIQ_DEM_DENS_NORMAL) || defined(LIQ_DEM_DDDT_VER2) || \
+    defined(LIQ_DEM_VARIABLE_TIMESTEP) || defined(_2D_DEM)
+#error "SPH-DEM coupling variant not implemented by the device path (Di Felice drag, porosity-weighted continuity)"
+#endif
+#if defined(FIXED_DEM) || defined(NO_DEM_CONTACTS)
+#error "FIXED_DEM / NO_DEM_CONTACTS are not implemented by the device path (freeze DEM particles in a hook)"
+#endif
+#if defined(SLK) || defined(VAR_H_CORRECTION2) || defined(MY_VAR_RES) || defined(DDENS_VARIANT) || \
+    defined(DENS_DIFFUSE) || defined(DENS_DIFFUSE_PRESS) || defined(BACKGROUND_PRESSURE_FORCE) || \
+    defined(INCL_THERM_ENERGY) || defined(HALF_COURANT)
+#error "SPH step variant not implemented by the device path"
+#endif
+#if defined(VISC_CLEARY) || defined(MORRIS_SPH_BOUNDARY) || defined(SLIP_BOUNDARIES) || defined(RADIAL_BOUNDARY) || \
+    defined(MODIFY_BFORCE_WITH_STILL_LEVEL) || defined(BORE_SOLITON)
+#error "viscosity or boundary variant not implemented by the device path"
+#endif
+
+/* The two per-axis constants of the reference's ghost particles
+ * (dataLL.cpp:648-683) that the device path does not implement: mirror
+ * ghosts at GHOST[] walls, and a density offset DENS_DROP on crossing a
+ * periodic boundary.  They are arrays, so the check runs at start-up:
+ * the reason a case cannot run, or nullptr. */
+inline const char *sphdem_case_unsupported() {
+    for (int i = 0; i < 2 * NDIM; i++)
+        if (GHOST[i] != 0) return "GHOST[] mirror boundaries are not implemented by the device path";
+    for (int d = 0; d < NDIM; d++)
+        if (PERIODIC[d] && DENS_DROP[d] != 0.0)
+            return "DENS_DROP across a periodic boundary is not implemented by the device path";
+    return nullptr;
+}
 
 inline SphDemConfig sphdem_case_config(int precision, bool fixed_dt) {
     SphDemConfig c;

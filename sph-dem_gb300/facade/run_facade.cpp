@@ -339,6 +339,10 @@ int main(int argc, char *argv[]) {
         if (!std::strcmp(argv[i], "--restart-out") && i + 1 < argc) restart_out = argv[++i];
         if (!std::strcmp(argv[i], "--dump-config") && i + 1 < argc) dump_config = argv[++i];
     }
+    if (const char *why = sphdem_case_unsupported()) {
+        std::cerr << "this case cannot run on the device path: " << why << std::endl;
+        return -1;
+    }
     /* run.cpp's command line: a base name, not a file */
     if (!is_file(argv[1])) return run_reference_loop(argv[1], std::atoi(argv[2]), argv[3], mixed, fixed_dt);
     SphDemParticles init;

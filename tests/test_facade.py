@@ -43,18 +43,28 @@ REF_CASE = os.path.join(REF_ROOT, "sediment3D")
 
 
 @pytest.mark.skipif(not os.path.isdir(REF_CASE), reason="reference sources not present")
-@pytest.mark.parametrize("name", ["sediment3D", "cell3D", "solitonPeriodic"])
-def test_reference_case_sources_build_unchanged(tmp_path, name):
-    """Reference case directories' own hooks and output code, unmodified:
-    sediment3D, cell3D (particle insertion, vect constants, vect output) and
-    solitonPeriodic (traverse with a state object, the wider predicate set,
-    periodic neighbour groups).  Of the reference's case directories that
-    compile against its own headers, the others stop on a kernel other than
-    Wendland C2, on constants the reference's step no longer finds, or on
-    GSL in their output analysis."""
+def test_reference_case_sources_build_unchanged(tmp_path):
+    """The reference's own sediment3D hooks and output code, unmodified."""
     _need_lib()
-    out = build_case(os.path.join(REF_ROOT, name), str(tmp_path / f"run_{name}"))
+    out = build_case(REF_CASE, str(tmp_path / "run_sediment3D"))
     assert os.path.exists(out)
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_CASE), reason="reference sources not present")
+@pytest.mark.parametrize("name,option", [("cell3D", "SPH-DEM coupling variant"),
+                                         ("porosityJump", "SPH-DEM coupling variant"),
+                                         ("solitonPeriodic", "viscosity or boundary variant"),
+                                         ("couette", "Wendland C2 kernel only")])
+def test_reference_cases_with_options_the_device_lacks_do_not_build(tmp_path, name, option):
+    """Reference case directories that compile against the reference's own
+    headers but ask for step options the device path does not implement
+    (cell3D and porosityJump: LIQ_DEM_SEPARATE_DRAGS, LIQ_DEM_VARIABLE_TIMESTEP;
+    solitonPeriodic: a boundary variant; couette: a kernel other than
+    Wendland C2) stop at compile time with the reason, instead of stepping
+    differently from the reference."""
+    _need_lib()
+    with pytest.raises(RuntimeError, match=option):
+        build_case(os.path.join(REF_ROOT, name), str(tmp_path / f"run_{name}"))
 
 
 ORACLE_ABI = os.path.join(REPO, "tests", "facade_oracle", "sphdem_oracle_abi.cpp")
@@ -716,3 +726,26 @@ def test_neighbour_forms_with_periodic_images(tmp_path):
     u_lo = (rel & (d2[:50] <= lim2[:50]) & ~tie[:50]).sum()
     u_hi = (rel & ((d2[:50] <= lim2[:50]) | tie[:50])).sum()
     assert u_lo <= using <= u_hi
+
+
+def test_case_with_mirror_ghosts_is_refused_at_start(tmp_path):
+    """A case whose GHOST[] asks for mirror boundaries (dataLL.cpp:664-683),
+    which the device path does not implement, builds but stops at start-up
+    with the reason."""
+    lib = _oracle_abi(str(tmp_path / "oracle_abi"))
+    case_dir = tmp_path / "case"
+    case_dir.mkdir()
+    src = os.path.join(FACADE, "example_sediment")
+    for f in ("customSim.h", "customSim.cpp", "customOutput.h", "customOutput.cpp"):
+        (case_dir / f).write_text(open(os.path.join(src, f)).read())
+    consts = open(os.path.join(src, "customConstants.h")).read()
+    assert "const int GHOST[2*NDIM] = {0, 0, 0, 0, 0, 0};" in consts
+    (case_dir / "customConstants.h").write_text(
+        consts.replace("const int GHOST[2*NDIM] = {0, 0, 0, 0, 0, 0};", "const int GHOST[2*NDIM] = {0, 0, 0, 0, 1, 0};"))
+    exe = build_case(str(case_dir), str(tmp_path / "run_case"), libdir=lib)
+    case = cases.workload("sediment3d_small")
+    init = tmp_path / "init.spdm"
+    state.write_state(str(init), case.particles)
+    res = subprocess.run([exe, str(init), "1", str(tmp_path / "final.bin")], capture_output=True, text=True,
+                         timeout=120, cwd=str(tmp_path))
+    assert res.returncode != 0 and "GHOST[] mirror boundaries" in res.stderr, res.stderr
