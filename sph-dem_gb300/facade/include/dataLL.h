@@ -25,6 +25,7 @@
 #include <deque>
 #include <iostream>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../../include/sphdem.h"
@@ -190,6 +191,7 @@ class CdataLL {
      * period, as the reference's ghost particles are (dataLL.cpp:648-660);
      * pointers stay valid while the deque grows */
     std::deque<Cparticle> ghosts;
+    std::unordered_map<long long, Cparticle *> ghost_of; /* (particle, shift) -> its ghost */
     bool lists_valid = false;
     vector<double> vu, vdudt, vev, vdev;
     vector<double> vr, vv, vvh, vv0, vvh0, vf, vfp, vfv, vfb, vfd, vfvel, vgp, vn1, vn2, vn3;
@@ -207,6 +209,7 @@ class CdataLL {
     void soa(SphDemParticles &p);
     void lists();
     Cparticle *image_of(Cparticle &q, Cparticle &b);
+    Cparticle *ghost(Cparticle &b, const int *shift);
     void search(Cparticle &q, double radius, vector<Cparticle *> &found);
 };
 
@@ -262,7 +265,10 @@ inline void CdataLL::pull() {
     globals.demDt = g.dem_dt;
     globals.sphStep = (int)g.sph_step;
     globals.n = (int)ps.size();
+    /* neighbour lists and ghost copies follow the new state */
     lists_valid = false;
+    ghosts.clear();
+    ghost_of.clear();
 }
 
 inline void CdataLL::push() {
@@ -345,6 +351,7 @@ inline void CdataLL::lists() {
         check(sphdem_pairs(h, kinds[k], offs[k].data(), idx[k].data(), np, &np), "sphdem_pairs");
     }
     ghosts.clear();
+    ghost_of.clear();
     nbrs.assign(n, vector<Cparticle *>());
     for (size_t i = 0; i < n; i++) {
         const int k = ps[i].iam == dem ? 1 : 0;
@@ -370,13 +377,24 @@ inline Cparticle *CdataLL::image_of(Cparticle &p, Cparticle &b) {
         if (dx < -half) shift[d] = -1;
         any = any || shift[d] != 0;
     }
-    if (!any) return &b;
+    return any ? ghost(b, shift) : &b;
+}
+
+/* the ghost copy of particle b shifted by whole periods (shift[d] in
+ * {-1, 0, 1}), one per particle and shift, as the reference keeps one ghost
+ * particle per image */
+inline Cparticle *CdataLL::ghost(Cparticle &b, const int *shift) {
+    long long key = (long long)(&b - &ps[0]);
+    for (int d = 0; d < NDIM; d++) key = 3 * key + (shift[d] + 1);
+    auto it = ghost_of.find(key);
+    if (it != ghost_of.end()) return it->second;
     ghosts.push_back(b);
     Cparticle &g = ghosts.back();
     for (int d = 0; d < NDIM; d++) {
         if (shift[d] > 0) g.r[d] = RMAX[d] - RMIN[d] + b.r[d];
         if (shift[d] < 0) g.r[d] = RMIN[d] - RMAX[d] + b.r[d];
     }
+    ghost_of[key] = &g;
     return &g;
 }
 
@@ -388,25 +406,9 @@ inline void CdataLL::search(Cparticle &q, double radius, vector<Cparticle *> &fo
     for (size_t j = 0; j < ps.size(); j++) {
         Cparticle &b = ps[j];
         if (&b == &q || (b.iam == dem) != dem_q || (int)b.iam < 0) continue;
-        vect r = b.r;
-        for (int d = 0; d < NDIM; d++) {
-            if (!PERIODIC[d]) continue;
-            const double half = 0.5 * (RMAX[d] - RMIN[d]);
-            const double dx = q.r[d] - b.r[d];
-            if (dx > half) r[d] = RMAX[d] - RMIN[d] + b.r[d];
-            if (dx < -half) r[d] = RMIN[d] - RMAX[d] + b.r[d];
-        }
+        Cparticle *img = image_of(q, b);
         const double lim2 = radius < 0 ? std::pow(2.0 * (q.h > b.h ? q.h : b.h), 2) : radius * radius;
-        if (len2(q.r - r) > lim2) continue;
-        bool same = true;
-        for (int d = 0; d < NDIM; d++) same = same && r[d] == b.r[d];
-        if (same) {
-            found.push_back(&b);
-        } else {
-            ghosts.push_back(b);
-            ghosts.back().r = r;
-            found.push_back(&ghosts.back());
-        }
+        if (len2(q.r - img->r) <= lim2) found.push_back(img);
     }
 }
 
