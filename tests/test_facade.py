@@ -749,3 +749,63 @@ def test_case_with_mirror_ghosts_is_refused_at_start(tmp_path):
     res = subprocess.run([exe, str(init), "1", str(tmp_path / "final.bin")], capture_output=True, text=True,
                          timeout=120, cwd=str(tmp_path))
     assert res.returncode != 0 and "GHOST[] mirror boundaries" in res.stderr, res.stderr
+
+
+def test_case_hook_insertion_and_deletion_on_the_oracle(tmp_path):
+    """insertNewParticle / markForDeletion in a case hook through the façade,
+    on the CPU through the oracle-backed C ABI, against the same changes made
+    directly on the oracle port (the device form of this test runs with -m
+    gpu)."""
+    import ctypes as C
+    import shutil
+    from oracle import port_api
+    lib = _oracle_abi(str(tmp_path / "oracle_abi"))
+    src = os.path.join(FACADE, "example_sediment")
+    case_dir = tmp_path / "case"
+    shutil.copytree(src, case_dir, ignore=shutil.ignore_patterns("__pycache__"))
+    (case_dir / "customSim.h").write_text(HOOK_H)
+    with open(case_dir / "customSim.cpp", "a") as fh:
+        fh.write(HOOK_CPP)
+    exe = build_case(str(case_dir), str(tmp_path / "run_case"), libdir=lib)
+    case = cases.workload("sediment3d_small")
+    init = tmp_path / "init.spdm"
+    state.write_state(str(init), case.particles)
+    final = tmp_path / "final.bin"
+    res = subprocess.run([exe, str(init), "5", str(final), "--fixed-dt", "--dump-config", str(tmp_path / "cfg.bin")],
+                         capture_output=True, text=True, timeout=300, cwd=str(tmp_path))
+    assert res.returncode == 0, res.stderr[-2000:]
+    a = read_final(str(final))
+
+    cfg = capi.SphDemConfig.from_buffer_copy((tmp_path / "cfg.bin").read_bytes())
+    # the example case's hooks as the port's built-in ones
+    cfg.gravity_sph = capi.D3(0.0, 0.0, -9.81)
+    cfg.gravity_dem = capi.D3(0.0, 0.0, -9.81)
+    cfg.n_walls = 1
+    cfg.walls[0].point = capi.D3(cfg.rmin[0], cfg.rmin[1], cfg.rmin[2])
+    cfg.walls[0].normal = capi.D3(0.0, 0.0, 1.0)
+    port = port_api.lib()
+    buf = capi.ParticleBuffers(case.n, case.particles)
+    h = C.c_void_p()
+    assert port.oracle_create(C.byref(cfg), buf.ref(), C.byref(h)) == 0, port.oracle_last_error()
+    try:
+        assert port.oracle_step(h, 2) == 0
+        fluid = np.nonzero(case.particles["iam"] == cases.SPH)[0][::50].astype(np.int64)
+        assert port.oracle_mark_for_deletion(h, fluid.ctypes.data_as(C.POINTER(C.c_int64)), len(fluid)) == 0
+        R = cfg.dem_radius
+        blk = {"iam": np.full(3, cases.DEM, np.int32),
+               "r": np.array([[0.01 * (j + 1), 0.02, 0.072] for j in range(3)]),
+               "mass": np.full(3, cfg.dem_vol * cfg.dem_dens), "dens": np.full(3, cfg.dem_dens),
+               "h": np.full(3, R), "radius": np.full(3, R)}
+        ins = capi.ParticleBuffers(3, blk)
+        idx = (C.c_int64 * 3)()
+        assert port.oracle_insert(h, ins.ref(), idx) == 0, port.oracle_last_error()
+        assert list(idx) == [case.n, case.n + 1, case.n + 2]
+        assert port.oracle_step(h, 3) == 0
+        out = capi.ParticleBuffers(case.n + 3)
+        port.oracle_get(h, out.ref())
+    finally:
+        port.oracle_destroy(h)
+    live = out["iam"] >= 0
+    assert (~live).sum() == fluid.size and a["r"].shape[0] == case.n + 3
+    for k in ("r", "vhat", "dens"):
+        np.testing.assert_array_equal(a[k][live], out[k][live], err_msg=k)
