@@ -809,3 +809,115 @@ def test_case_hook_insertion_and_deletion_on_the_oracle(tmp_path):
     assert (~live).sum() == fluid.size and a["r"].shape[0] == case.n + 3
     for k in ("r", "vhat", "dens"):
         np.testing.assert_array_equal(a[k][live], out[k][live], err_msg=k)
+
+
+def _constants_2d(case, outstep=10):
+    """customConstants.h of a 2D fluid case (no LIQ_DEM) from a workload of
+    sphdem.cases: the dam break's constants in the reference's form."""
+    c = case.cfg
+    r = lambda v: repr(float(v))  # noqa: E731
+    assert c["ndim"] == 2 and not c["flags"] & cases.F_LIQ_DEM
+    flags = c["flags"]
+    lines = ["#ifndef CUSTOMCONSTANTS_H", "#define CUSTOMCONSTANTS_H", "#include <cmath>", "#define _2D_",
+             "#define NDIM 2", "#define WENDLAND", "#define VISC_ARTIFICIAL"]
+    if flags & 1:
+        lines.append("#define CONST_H")
+    if flags & 2:
+        lines.append("#define NO_ANTICLUMPING")
+    lines += [
+        f"const double PI = {r(c['pi'])};",
+        f"const double RMIN[NDIM] = {{{r(c['rmin'][0])}, {r(c['rmin'][1])}}};",
+        f"const double RMAX[NDIM] = {{{r(c['rmax'][0])}, {r(c['rmax'][1])}}};",
+        "const int PERIODIC[NDIM] = {0, 0};", "const int GHOST[2*NDIM] = {0, 0, 0, 0};",
+        "const double DENS_DROP[NDIM] = {0.0, 0.0};",
+        f"const double PSEP = {r(c['psep'])};", f"const double HFAC = {r(c['hfac'])};",
+        f"const double H = {r(c['h'])};", f"const double DENS = {r(c['dens'])};",
+        f"const double REFD = {r(c['refd'])};", f"const double GAMMA = {r(c['gamma'])};",
+        f"const double PRB = {r(c['prb'])};", f"const double SPSOUND = {r(c['spsound'])};",
+        f"const double VISCOSITY = {r(c['viscosity'])};",
+        f"const double ALPHA_ARTIFICIAL = {r(c['alpha_artificial'])};", f"const double BFAC = {r(c['bfac'])};",
+        f"const int OUTSTEP = {outstep};", f"const double MAXTIME = {r(c['maxdt'])} * OUTSTEP;",
+        "const int RESTART_EVERY_N_STEPS = 5;", f"const double DAMPTIME = {r(c['damptime'])};",
+        f"const int MAX_NUM_PARTICLES_PER_CPU = {case.n + 16};",
+        "const int REINIT_DENS_EVERY_N_STEPS = 50000000;", "const int REINIT_DENS_AT_N_STEPS = 50000000;",
+        "#endif", ""]
+    return "\n".join(lines)
+
+
+CASE_2D_SIM_H = """#ifndef CUSTOMSIM_H
+#define CUSTOMSIM_H
+#include "customConstants.h"
+#include "customSimBase.h"
+#include "dataLL.h"
+#include "sph.h"
+class CcustomSim : public CcustomSimBase {
+   public:
+    CcustomSim(CdataLL *_data, double _time) : CcustomSimBase(_data, _time) {}
+    void beforeMiddle(double newTime);
+};
+#endif
+"""
+CASE_2D_SIM_CPP = """#include "customSim.h"
+#include "dataLL.impl.h"
+namespace {
+inline void gravity(Cparticle &p, CglobalVars &g) { p.f[1] -= 9.81; }
+}
+void CcustomSim::beforeMiddle(double newTime) { data->traverse<gravity, Nsph::ifSph>(); }
+"""
+CASE_2D_OUT_H = """#ifndef CUSTOMOUTPUT_H
+#define CUSTOMOUTPUT_H
+#include "customOutputBase.h"
+#include "customSim.h"
+class CcustomOutput : public CcustomOutputBase {
+   public:
+    CcustomOutput(CdataLL *_data) : CcustomOutputBase(_data) {}
+    void calcOutput(int outstep, CcustomSim *custSim, Cio_data_vtk *io) {}
+};
+#endif
+"""
+
+
+def test_2d_fluid_case_through_the_facade_on_the_oracle(tmp_path):
+    """A 2D fluid case without LIQ_DEM (the dam break's configuration:
+    Wendland C2, artificial viscosity, CONST_H, walls of boundary particles)
+    built against the façade and stepped through its hooks (gravity on the
+    fluid before the middle phase) on the CPU oracle, against the oracle
+    port with the same gravity as its built-in hook: equal bit for bit."""
+    import ctypes as C
+    from oracle import port_api
+    lib = _oracle_abi(str(tmp_path / "oracle_abi"))
+    case = cases.workload("dambreak2d_small")
+    case_dir = tmp_path / "case"
+    case_dir.mkdir()
+    (case_dir / "customConstants.h").write_text(_constants_2d(case))
+    (case_dir / "customSim.h").write_text(CASE_2D_SIM_H)
+    (case_dir / "customSim.cpp").write_text(CASE_2D_SIM_CPP)
+    (case_dir / "customOutput.h").write_text(CASE_2D_OUT_H)
+    exe = build_case(str(case_dir), str(tmp_path / "run_case"), libdir=lib)
+    init = tmp_path / "init.spdm"
+    state.write_state(str(init), case.particles)
+    nsteps = 20
+    final = tmp_path / "final.bin"
+    res = subprocess.run([exe, str(init), str(nsteps), str(final), "--fixed-dt", "--dump-config",
+                          str(tmp_path / "cfg.bin")], capture_output=True, text=True, timeout=300, cwd=str(tmp_path))
+    assert res.returncode == 0, res.stderr[-2000:]
+    a = read_final(str(final))
+    cfg = capi.SphDemConfig.from_buffer_copy((tmp_path / "cfg.bin").read_bytes())
+    assert cfg.ndim == 2 and cfg.visc_model == cases.VISC_ARTIFICIAL
+    for k in ("domain_min", "domain_max"):
+        assert list(getattr(cfg, k))[:2] == list(case.cfg[k])[:2], k
+    cfg.gravity_sph = capi.D3(0.0, -9.81, 0.0)
+    port = port_api.lib()
+    buf = capi.ParticleBuffers(case.n, case.particles)
+    h = C.c_void_p()
+    assert port.oracle_create(C.byref(cfg), buf.ref(), C.byref(h)) == 0, port.oracle_last_error()
+    try:
+        assert port.oracle_step(h, nsteps) == 0
+        out = capi.ParticleBuffers(case.n)
+        port.oracle_get(h, out.ref())
+    finally:
+        port.oracle_destroy(h)
+    assert np.abs(out["vhat"]).max() > 0.0
+    for k in ("r", "v", "vhat", "f", "dens", "h"):
+        np.testing.assert_array_equal(a[k][:, :2] if a[k].ndim == 2 else a[k],
+                                      out[k][:, :2] if out[k].ndim == 2 else out[k], err_msg=k)
