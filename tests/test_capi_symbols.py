@@ -49,3 +49,23 @@ def test_config_struct_layout_matches_header():
     ours = [f for f, _ in capi.SphDemConfig._fields_]
     for m in members:
         assert m in ours, m
+
+
+def test_integration_binding_compiles(tmp_path):
+    """The reference-side binding INTEGRATION.md shows (its first C++ block)
+    compiles against include/sphdem.h, with a case's constants and the
+    façade's framework headers standing in for the reference's."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no C++ compiler")
+    text = open(os.path.join(REPO, "INTEGRATION.md")).read()
+    block = re.search(r"```cpp\n(.*?)```", text, flags=re.S).group(1)
+    src = tmp_path / "run_gpu.cpp"
+    src.write_text("#include <cstdlib>\n#include <iostream>\n#include <vector>\n" + block)
+    facade = os.path.join(REPO, "sph-dem_gb300", "facade")
+    res = subprocess.run([gxx, "-std=c++17", "-fsyntax-only", "-I" + os.path.join(REPO, "include"),
+                          "-I" + os.path.join(facade, "example_sediment"), "-I" + os.path.join(facade, "include"),
+                          str(src)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr[-3000:]
