@@ -52,8 +52,8 @@ def test_config_struct_layout_matches_header():
 
 
 def test_integration_binding_compiles(tmp_path):
-    """The reference-side binding INTEGRATION.md shows (its first C++ block)
-    compiles against include/sphdem.h, with a case's constants and the
+    """The reference-side binding of the integration notes (their first C++
+    block) compiles against include/sphdem.h, with a case's constants and the
     façade's framework headers standing in for the reference's."""
     import shutil
     import subprocess
