@@ -43,7 +43,8 @@ class CdataLL {
 
     CglobalVars &globals;
 
-    particleContainer &getParticles() { return ps; }
+    /* the particle container, as a pointer as the reference returns it (dataLL.h:237-238) */
+    particleContainer *getParticles() { return &ps; }
     sphdem_handle handle() const { return h; }
 
     /* device -> mirror (all fields, globals); neighbour lists on demand */

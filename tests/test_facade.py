@@ -214,7 +214,7 @@ HOOK_CPP = """
 void CcustomSim::afterEnd(double newTime) {
     static int step = 0;
     if (++step != 2) return;
-    particleContainer &ps = data->getParticles();
+    particleContainer &ps = *data->getParticles();
     int k = 0;
     for (size_t i = 0; i < ps.size(); i++)
         if (ps[i].iam == sph && (k++ % 50) == 0) data->markForDeletion(ps[i]);
@@ -616,7 +616,7 @@ void CcustomOutput::calcOutput(int outstep, CcustomSim *, Cio_data_vtk *io) {
     CglobalVars &g = data->globals;
     for (int k = 0; k < 5; k++) g.custom[k] = 0;
     data->neighboursGroup<Nsph::calcDensity, Nsph::ifSphOrSphBoundary>();
-    particleContainer &ps = data->getParticles();
+    particleContainer &ps = *data->getParticles();
     {
         std::ofstream out((io->filename + ".dens").c_str(), std::ios::binary);
         for (Cparticle &p : ps) {
