@@ -211,6 +211,8 @@ typedef struct sphdem_ctx *sphdem_handle;
  * particle count the handle will ever hold (>= init->n). */
 int sphdem_create(const SphDemConfig *cfg, const SphDemParticles *init,
                   int64_t capacity, sphdem_handle *out);
+/* Release the handle's device memory (the reference's particle container and
+ * CdataLL live until the process ends, run.cpp:163-164). */
 int sphdem_destroy(sphdem_handle h);
 
 /* Run one phase or built-in hook point (SPHDEM_PHASE_* / SPHDEM_HOOK_*).
@@ -220,10 +222,16 @@ int sphdem_destroy(sphdem_handle h);
  * would apply at that point.  A host-side hook instead uses get/set_fields. */
 int sphdem_phase(sphdem_handle h, int phase);
 
-/* nsteps full steps: sph_step++, then the seven phases/hooks in run.cpp order.
- * Consecutive calls replay one captured CUDA graph of a step. */
+/* nsteps full steps of the run loop (run.cpp:102-118): sph_step++, then the
+ * seven phases/hooks in run.cpp order.  Consecutive calls replay one captured
+ * CUDA graph of a step. */
 int sphdem_step(sphdem_handle h, int nsteps);
 
+/* Read / write the fields `mask` selects, in tag order: what hook and output
+ * code reads and writes on the reference's particle container
+ * (data->getParticles(), dataLL.h:237-238; the Cparticle members,
+ * particle.h:262-316).  set_fields writes r, v, vhat, f (f, fp, fv, fb),
+ * dens, h, normals, radius, coupling, energy and dddt groups. */
 int sphdem_get_fields(sphdem_handle h, uint32_t mask, SphDemParticles *out);
 int sphdem_set_fields(sphdem_handle h, uint32_t mask, const SphDemParticles *in);
 /* sphdem_get_fields without waiting (no counterpart in the reference, whose
@@ -235,8 +243,12 @@ int sphdem_set_fields(sphdem_handle h, uint32_t mask, const SphDemParticles *in)
  * overlap; a third waits on the device for the first to finish.  Integer
  * fields (iam, tag) are not copied by this call. */
 int sphdem_get_fields_async(sphdem_handle h, uint32_t mask, const SphDemParticles *out);
+/* Wait for the handle's sphdem_get_fields_async copies (no counterpart). */
 int sphdem_fields_wait(sphdem_handle h);
+/* The step globals of CglobalVars (globalVars.h:196-220): time, dt, new dt,
+ * maxdt, DEM dt, sphStep; set_globals writes time, dt, maxdt and sphStep. */
 int sphdem_get_globals(sphdem_handle h, SphDemGlobals *out);
+/* Sizes of the current rebuild (no counterpart; for reporting). */
 int sphdem_get_stats(sphdem_handle h, SphDemStats *out);
 int sphdem_set_globals(sphdem_handle h, const SphDemGlobals *in);
 
@@ -264,7 +276,9 @@ int sphdem_mark_for_deletion(sphdem_handle h, const int64_t *idx, int64_t k);
  * bin, sort by cell, permute. */
 int sphdem_rebuild(sphdem_handle h);
 
-/* Export one neighbour relation as CSR over tag order.  `offsets` has n+1
+/* Export one neighbour relation as CSR over tag order: calcNeighbours
+ * (dataLL.cpp:1026-1075) for SPHDEM_PAIRS_SPH / _DEM, calcNeighboursCoupling
+ * (dataLL.cpp:1104-1192) for the two coupling directions.  `offsets` has n+1
  * entries, `idx` holds neighbour tags' positions (tag order index).  Pass
  * idx == NULL to query the pair count in *n_pairs. */
 int sphdem_pairs(sphdem_handle h, int kind, int64_t *offsets, int32_t *idx,
@@ -286,6 +300,7 @@ typedef struct SphDemOutputVars {
     int64_t n, n_sph;
 } SphDemOutputVars;
 
+/* CsphIncompress::calcOutputVars (sphIncompress.h:274-319) on the device */
 int sphdem_output_vars(sphdem_handle h, SphDemOutputVars *out);
 
 /* Bucket index of every particle (tag order) in the reference's own maps:
@@ -332,6 +347,7 @@ typedef struct SphDemGrads {
     uint32_t valid;             /* SPHDEM_GRAD_* bits of the entries computed */
 } SphDemGrads;
 
+/* Adjoint forward pass (no counterpart in the reference, see above). */
 int sphdem_adjoint_forward(sphdem_handle h, int nsteps, int ckpt_every);
 /* Device memory the adjoint may use to keep checkpoint segments' tapes (the
  * per-step states and pair tables the reverse sweep reads) from the forward
@@ -342,6 +358,7 @@ int sphdem_adjoint_forward(sphdem_handle h, int nsteps, int ckpt_every);
  * sphdem_adjoint_forward.  Applies from the next sphdem_adjoint_forward.
  * All-DEM handles always keep one segment's tape. */
 int sphdem_adjoint_set_tape_memory(sphdem_handle h, int64_t bytes);
+/* Adjoint backward pass (no counterpart in the reference, see above). */
 int sphdem_adjoint_backward(sphdem_handle h, const double *dL_dr, const double *dL_dv,
                             const double *dL_dvhat, SphDemGrads *grads,
                             double *dL_dr0, double *dL_dv0, double *dL_dvhat0);
@@ -357,6 +374,8 @@ int sphdem_adjoint_backward(sphdem_handle h, const double *dL_dr, const double *
  * (reinit_dens_every / reinit_dens_at) gives SPHDEM_ERR_UNSUPPORTED. */
 typedef struct sphdem_batch_ctx *sphdem_batch;
 
+/* Batches have no counterpart in the reference, which runs one simulation
+ * per process (run.cpp:16-164). */
 int sphdem_batch_create(const sphdem_handle *members, int n, sphdem_batch *out);
 int sphdem_batch_destroy(sphdem_batch b);
 /* nsteps full steps of every member (hooks on the device, as sphdem_step) */
@@ -395,13 +414,16 @@ int sphdem_batch_last_error(sphdem_batch b, char *buf, size_t len);
 int sphdem_cell_ids_noalloc(sphdem_handle h, int32_t *cell_xyz);
 
 /* Per-kernel device time accumulated with CUDA events since the last reset
- * (names separated by '\n' in `names`, times in ms, launch counts). */
+ * (names separated by '\n' in `names`, times in ms, launch counts).  No
+ * counterpart: the reference times whole phases with gettimeofday
+ * (run.cpp:96-100, globalVars.h:163-188). */
 int sphdem_kernel_times(sphdem_handle h, char *names, size_t names_len,
                         double *ms, int64_t *launches, int max_kernels,
                         int *n_kernels);
 int sphdem_kernel_times_reset(sphdem_handle h, int enable);
 
-/* Time `nsteps` full steps on the handle's stream with CUDA events. */
+/* Time `nsteps` full steps on the handle's stream with CUDA events (no
+ * counterpart). */
 int sphdem_time_steps(sphdem_handle h, int nsteps, double *ms);
 
 /* Page-locked host buffers for get/set_fields: transfers from and to them run

@@ -1,5 +1,5 @@
 /*
- * Driver of a case directory on the device (the step loop of run.cpp:15-170):
+ * Driver of a case directory on the device (the step loop of run.cpp:16-164):
  * compiled together with the case's customConstants.h, customSim.cpp and
  * customOutput.cpp against the façade headers (include/), linked with
  * libsphdem.so.  Two command lines:
@@ -249,7 +249,7 @@ bool is_file(const char *path) {
     return stat(path, &st) == 0 && S_ISREG(st.st_mode);
 }
 
-/* run.cpp:15-170 on one process: read the Domain, Globals row and restart of
+/* run.cpp:16-164 on one process: read the Domain, Globals row and restart of
  * output step intimestep under inbase, then step and write outputs under
  * outbase until MAXTIME or OUTSTEP */
 int run_reference_loop(const std::string &inbase, int intimestep, const std::string &outbase, bool mixed,

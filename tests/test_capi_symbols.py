@@ -69,3 +69,25 @@ def test_integration_binding_compiles(tmp_path):
                           "-I" + os.path.join(facade, "example_sediment"), "-I" + os.path.join(facade, "include"),
                           str(src)], capture_output=True, text=True)
     assert res.returncode == 0, res.stderr[-3000:]
+
+
+def test_every_entry_point_cites_the_reference():
+    """Each declaration of include/sphdem.h sits in a block (back to the
+    previous blank line) that cites the reference interface it replaces
+    (file:line) or states that it has no counterpart there."""
+    lines = open(os.path.join(REPO, "include", "sphdem.h")).read().splitlines()
+    decl = re.compile(r"^(int|const char \*)\s+(sphdem_\w+)\(")
+    missing = []
+    for i, line in enumerate(lines):
+        m = decl.match(line)
+        if not m:
+            continue
+        j = i - 1
+        block = []
+        while j >= 0 and lines[j].strip():
+            block.append(lines[j])
+            j -= 1
+        text = " ".join(block)
+        if not (re.search(r"\w+\.(h|cpp):\d+", text) or "counterpart" in text):
+            missing.append(m.group(2))
+    assert not missing, missing

@@ -437,7 +437,7 @@ def _oracle_abi(libdir):
 
 def test_run_loop_of_the_reference_command_line(tmp_path):
     """run_case <inbase> <intimestep> <outbase>, run.cpp's own command line
-    and loop (run.cpp:15-170), on the CPU through the oracle-backed C ABI.
+    and loop (run.cpp:16-164), on the CPU through the oracle-backed C ABI.
     From the Domain file and restart a case's setup writes, the loop steps
     the example case's hooks until time passes MAXTIME (fixed dt = MAXTIME /
     OUTSTEP) and writes, every MAXTIME / OUTSTEP of simulated time, an output
