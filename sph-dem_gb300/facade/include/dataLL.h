@@ -115,7 +115,7 @@ class CdataLL {
             if (Iffunct(ps[i])) Thefunct(ps[i], globals, a, b, c);
     }
 
-    /* every (particle, neighbour) pair, in both orders (dataLL.impl.h:181-216) */
+    /* every (particle, neighbour) pair, in both orders (dataLL.impl.h:182-216) */
     template <void Thefunct(Cparticle &, Cparticle &, CglobalVars &)>
     void neighbours() {
         lists();
@@ -137,7 +137,7 @@ class CdataLL {
     }
 
     /* neighbours of particles that are not in the simulation, e.g. points of
-     * an output grid (dataLL.impl.h:282-306): the simulation's particles of
+     * an output grid (dataLL.impl.h:283-306): the simulation's particles of
      * the query's relation (DEM for a DEM query, else the others) within
      * 2 max(h) of it, periodic images as ghost copies.  A search over all
      * particles per query, for output steps. */

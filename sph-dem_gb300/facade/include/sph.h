@@ -1,11 +1,11 @@
 /*
  * Nsph helpers case hook and output code calls (sph.h): the particle-type
- * predicates (sph.h:1827-1897, with the reference's bodies, including
+ * predicates (sph.h:1827-1889, with the reference's bodies, including
  * ifDemOrDemBoundary testing dem only and ifSphOrSphBoundaryOrImmersedDem
  * testing sph and sphBoundary only), the Wendland C2 kernel K, W and its
- * gradient factor F (sph.h:71-76, 199-205, 306-308, written as the
+ * gradient factor F (sph.h:74-80, 199-205, 306-308, written as the
  * reference writes them so that hook arithmetic rounds alike), gradW
- * (sph.h:321-342), calcHFromDens and calcDensity (sph.h:1149-1190, 1822-1824)
+ * (sph.h:322-342), calcHFromDens and calcDensity (sph.h:1149-1190, 1823-1825)
  * and the linear DEM normal force (LINEAR, sph.h:1495-1516).  The device
  * implements the step itself.
  */

@@ -551,7 +551,7 @@ bool Cio_data_vtk::readDomain(int, CglobalVars *g) {
     for (int k = 0; k < SPHDEM_FACADE_NEIGHBOURS; k++)
         if (!(in >> g->procNeighbrs[k])) return false;
     g->mpiRank = rank;
-    g->procNeighbrs[SPHDEM_FACADE_NEIGHBOURS / 2] = -1; /* the process itself (ioDomain.cpp:16-17) */
+    g->procNeighbrs[SPHDEM_FACADE_NEIGHBOURS / 2] = -1; /* the process itself (ioDomain.cpp:14-15) */
     return true;
 }
 

@@ -314,7 +314,7 @@ def write_domain(path: str, ndim: int, proc_domain, rank: int = 0, neighbours=No
     (one process: every neighbour is the process itself)."""
     if neighbours is None:
         neighbours = [rank] * 3 ** ndim
-        neighbours[(3 ** ndim) // 2] = -1  # the centre is -1, as readDomain sets it (ioDomain.cpp:16-17)
+        neighbours[(3 ** ndim) // 2] = -1  # the centre is -1, as readDomain sets it (ioDomain.cpp:14-15)
     vals = [rank] + [repr(float(x)) for x in proc_domain[:2 * ndim]] + list(neighbours)
     with open(path, "w") as fh:
         fh.write(" ".join(str(v) for v in vals) + " \n")

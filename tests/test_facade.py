@@ -574,7 +574,7 @@ def test_cpp_globals_and_domain_files_in_the_reference_layout(tmp_path):
     assert int(got[0]) == int(want[0])
     assert [float(x) for x in got[1:5]] == [float(x) for x in want[1:5]]
     nb = [int(x) for x in want[5:14]]
-    nb[4] = -1  # the process itself (ioDomain.cpp:16-17)
+    nb[4] = -1  # the process itself (ioDomain.cpp:14-15)
     assert [int(x) for x in got[5:14]] == nb
 
     ours = open(tmp_path / "outGlobals0.dat").read().splitlines()
@@ -729,7 +729,7 @@ def test_neighbour_forms_with_periodic_images(tmp_path):
 
 
 def test_case_with_mirror_ghosts_is_refused_at_start(tmp_path):
-    """A case whose GHOST[] asks for mirror boundaries (dataLL.cpp:664-683),
+    """A case whose GHOST[] asks for mirror boundaries (dataLL.cpp:667-686),
     which the device path does not implement, builds but stops at start-up
     with the reason."""
     lib = _oracle_abi(str(tmp_path / "oracle_abi"))
