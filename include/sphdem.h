@@ -111,8 +111,8 @@ typedef struct SphDemConfig {
     double   dem_search_radius;    /* DEM_SEARCH_RADIUS                           */
     double   dem_vol;              /* DEM_VOL                                     */
     double   coupling_radius;      /* LIQ_DEM_COUPLING_RADIUS                     */
-    double   dem_timestep;         /* DEM_TIMESTEP (demConstants.h:159)            */
-    double   liq_dem_timestep;     /* LIQ_DEM_TIMESTEP (demConstants.h:172)        */
+    double   dem_timestep;         /* DEM_TIMESTEP (demConstants.h:6)              */
+    double   liq_dem_timestep;     /* LIQ_DEM_TIMESTEP (demConstants.h:19)         */
     double   time_drop_particle;   /* TIME_DROP_PARTICLE                          */
     double   freeze_dem_until;     /* built-in hook: DEM frozen while time <= this */
     double   gravity_sph[3];       /* built-in beforeMiddle hook, type sph only    */

@@ -267,7 +267,7 @@ def dem_settling3d(lattice=(25, 25, 80), box=(0.1, 0.1, 0.3), radius: float = 1e
 
 
 def _dem_timesteps(cfg: dict) -> None:
-    """DEM_TIMESTEP and LIQ_DEM_TIMESTEP exactly as demConstants.h:159,172."""
+    """DEM_TIMESTEP and LIQ_DEM_TIMESTEP exactly as demConstants.h:6, 19."""
     pi = cfg["pi"]
     vol = (4.0 / 3.0) * pi * cfg["dem_radius"] ** 3
     mass = vol * cfg["dem_dens"]
