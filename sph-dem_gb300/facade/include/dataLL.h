@@ -169,6 +169,19 @@ class CdataLL {
             }
     }
 
+#ifdef LIQ_DEM
+    /* the coupling neighbours (dataLL.impl.h:257-268, calcNeighboursCoupling
+     * dataLL.cpp:1104-1192): a fluid particle's DEM particles under the
+     * reference's coupling bucket rule, a DEM particle's SPH-grid neighbours,
+     * periodic partners as ghost copies at their nearest image */
+    template <void Thefunct(Cparticle &, vector<Cparticle *> &, CglobalVars &), bool Iffunct(Cparticle &)>
+    void neighboursGroupCoupling() {
+        coupling_lists();
+        for (size_t i = 0; i < ps.size(); i++)
+            if (Iffunct(ps[i])) Thefunct(ps[i], cnbrs[i], globals);
+    }
+#endif
+
     int numParticles() { return (int)ps.size(); }
     /* CdataLL::reset (dataLL.cpp:140-236) from case code: the mirror's state
      * goes to the device, which rebuilds its buckets and lists there, and
@@ -187,13 +200,13 @@ class CdataLL {
     particleContainer &ps;
     sphdem_handle h;
     vector<Cparticle> pending_insert;
-    vector<vector<Cparticle *> > nbrs;
+    vector<vector<Cparticle *> > nbrs, cnbrs;
     /* periodic images of neighbours: copies with the position shifted by a
      * period, as the reference's ghost particles are (dataLL.cpp:648-660);
      * pointers stay valid while the deque grows */
     std::deque<Cparticle> ghosts;
     std::unordered_map<long long, Cparticle *> ghost_of; /* (particle, shift) -> its ghost */
-    bool lists_valid = false;
+    bool lists_valid = false, clists_valid = false;
     vector<double> vu, vdudt, vev, vdev;
     vector<double> vr, vv, vvh, vv0, vvh0, vf, vfp, vfv, vfb, vfd, vfvel, vgp, vn1, vn2, vn3;
     vector<double> vm, vd, vh, vrad, vdddt, vpress, vpdr2, vpor, vdpor, vshep, vom;
@@ -209,6 +222,9 @@ class CdataLL {
     }
     void soa(SphDemParticles &p);
     void lists();
+    void coupling_lists();
+    /* one relation of the device as CSR over tag order */
+    void relation(int kind, vector<int64_t> &offs, vector<int32_t> &idx);
     Cparticle *image_of(Cparticle &q, Cparticle &b);
     Cparticle *ghost(Cparticle &b, const int *shift);
     void search(Cparticle &q, double radius, vector<Cparticle *> &found);
@@ -268,6 +284,7 @@ inline void CdataLL::pull() {
     globals.n = (int)ps.size();
     /* neighbour lists and ghost copies follow the new state */
     lists_valid = false;
+    clists_valid = false;
     ghosts.clear();
     ghost_of.clear();
 }
@@ -333,7 +350,11 @@ inline void CdataLL::push() {
         ps.resize(n);
         for (size_t j = 0; j < k; j++) ps[slot[j]] = pending_insert[j];
         pending_insert.clear();
+        /* the container may have moved: lists and ghosts are rebuilt on use */
         lists_valid = false;
+        clists_valid = false;
+        ghosts.clear();
+        ghost_of.clear();
     }
 }
 
@@ -342,23 +363,41 @@ inline void CdataLL::lists() {
     const size_t n = ps.size();
     /* calcNeighbours (dataLL.cpp:1026-1075): DEM particles take the DEM
      * relation, the others the SPH one; each row comes from one of the two */
-    vector<int64_t> offs[2] = {vector<int64_t>(n + 1), vector<int64_t>(n + 1)};
+    vector<int64_t> offs[2];
     vector<int32_t> idx[2];
-    const int kinds[2] = {SPHDEM_PAIRS_SPH, SPHDEM_PAIRS_DEM};
-    for (int k = 0; k < 2; k++) {
-        int64_t np = 0;
-        check(sphdem_pairs(h, kinds[k], offs[k].data(), nullptr, 0, &np), "sphdem_pairs");
-        idx[k].resize((size_t)np);
-        check(sphdem_pairs(h, kinds[k], offs[k].data(), idx[k].data(), np, &np), "sphdem_pairs");
-    }
-    ghosts.clear();
-    ghost_of.clear();
+    relation(SPHDEM_PAIRS_SPH, offs[0], idx[0]);
+    relation(SPHDEM_PAIRS_DEM, offs[1], idx[1]);
     nbrs.assign(n, vector<Cparticle *>());
     for (size_t i = 0; i < n; i++) {
         const int k = ps[i].iam == dem ? 1 : 0;
         for (int64_t e = offs[k][i]; e < offs[k][i + 1]; e++) nbrs[i].push_back(image_of(ps[i], ps[idx[k][e]]));
     }
     lists_valid = true;
+}
+
+inline void CdataLL::relation(int kind, vector<int64_t> &offs, vector<int32_t> &idx) {
+    offs.assign(ps.size() + 1, 0);
+    int64_t np = 0;
+    check(sphdem_pairs(h, kind, offs.data(), nullptr, 0, &np), "sphdem_pairs");
+    idx.resize((size_t)np);
+    check(sphdem_pairs(h, kind, offs.data(), idx.data(), np, &np), "sphdem_pairs");
+}
+
+inline void CdataLL::coupling_lists() {
+    if (clists_valid) return;
+    const size_t n = ps.size();
+    /* fluid -> DEM rows of sph / sphBoundary particles, DEM -> fluid rows of
+     * DEM particles; each row comes from one of the two relations */
+    vector<int64_t> offs[2];
+    vector<int32_t> idx[2];
+    relation(SPHDEM_PAIRS_COUPLE_SD, offs[0], idx[0]);
+    relation(SPHDEM_PAIRS_COUPLE_DS, offs[1], idx[1]);
+    cnbrs.assign(n, vector<Cparticle *>());
+    for (size_t i = 0; i < n; i++) {
+        const int k = ps[i].iam == dem ? 1 : 0;
+        for (int64_t e = offs[k][i]; e < offs[k][i + 1]; e++) cnbrs[i].push_back(image_of(ps[i], ps[idx[k][e]]));
+    }
+    clists_valid = true;
 }
 
 /* b itself, or, where b is p's neighbour across a periodic boundary, the

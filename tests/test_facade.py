@@ -606,6 +606,11 @@ inline void countGroup(Cparticle &, vector<Cparticle *> &nb, CglobalVars &g) { g
 inline void countAt(Cparticle &, vector<Cparticle *> &nb, CglobalVars &g) { g.custom[2] += nb.size(); }
 inline void countUsing(Cparticle &, vector<Cparticle *> &nb, CglobalVars &g) { g.custom[3] += nb.size(); }
 inline void countAgain(Cparticle &, vector<Cparticle *> &nb, CglobalVars &g) { g.custom[4] += nb.size(); }
+inline void countSD(Cparticle &p, vector<Cparticle *> &nb, CglobalVars &g) {
+    g.custom[5] += nb.size();
+    for (Cparticle *pn : nb) g.custom[7] = std::max(g.custom[7], len(p.r - pn->r));
+}
+inline void countDS(Cparticle &, vector<Cparticle *> &nb, CglobalVars &g) { g.custom[6] += nb.size(); }
 inline void mark2(Cparticle &p, CglobalVars &, double a, double b) { p.colour = a + b; }
 inline void mark3(Cparticle &p, CglobalVars &, double a, double b, double c) { p.tmp = a + b + c; }
 }  // namespace
@@ -614,7 +619,7 @@ inline void mark3(Cparticle &p, CglobalVars &, double a, double b, double c) { p
  * the other CdataLL forms, each tallied into the globals */
 void CcustomOutput::calcOutput(int outstep, CcustomSim *, Cio_data_vtk *io) {
     CglobalVars &g = data->globals;
-    for (int k = 0; k < 5; k++) g.custom[k] = 0;
+    for (int k = 0; k < 8; k++) g.custom[k] = 0;
     data->neighboursGroup<Nsph::calcDensity, Nsph::ifSphOrSphBoundary>();
     particleContainer &ps = *data->getParticles();
     {
@@ -633,6 +638,8 @@ void CcustomOutput::calcOutput(int outstep, CcustomSim *, Cio_data_vtk *io) {
     data->neighboursGroupAtRadius<countAt, Nsph::ifSph>(0.005);
     vector<Cparticle> qs(ps.begin(), ps.begin() + 50);
     data->neighboursUsing<countUsing>(qs);
+    data->neighboursGroupCoupling<countSD, Nsph::ifSphOrSphBoundary>();
+    data->neighboursGroupCoupling<countDS, Nsph::ifDem>();
     data->reset();
     data->neighboursGroup<countAgain, Nsph::ifSphOrSphBoundary>();
     double colour = 0, tmp = 0;
@@ -644,7 +651,8 @@ void CcustomOutput::calcOutput(int outstep, CcustomSim *, Cio_data_vtk *io) {
         }
     std::ofstream s((io->filename + ".stats").c_str());
     s << std::setprecision(17) << g.custom[0] << ' ' << g.custom[1] << ' ' << t.mass << ' ' << data->numParticles()
-      << ' ' << colour << ' ' << tmp << ' ' << g.custom[2] << ' ' << g.custom[3] << ' ' << g.custom[4] << '\n';
+      << ' ' << colour << ' ' << tmp << ' ' << g.custom[2] << ' ' << g.custom[3] << ' ' << g.custom[4] << ' '
+      << g.custom[5] << ' ' << g.custom[6] << ' ' << g.custom[7] << '\n';
 }
 """
 
@@ -710,7 +718,7 @@ def test_neighbour_forms_with_periodic_images(tmp_path):
     assert err <= 1e-12, err
 
     stats = open(str(out) + ".stats").read().split()
-    pairs, groups, mass_sph, count, colour, tmp, at_r, using, again = (float(x) for x in stats)
+    pairs, groups, mass_sph, count, colour, tmp, at_r, using, again, sd, ds, sd_max = (float(x) for x in stats)
     # ties at exactly 2 max(h) may fall either way: bracket the brute-force counts
     tie = np.abs(d2 - lim2) <= 1e-12 * lim2
     grp = off & nondem[None, :] & fluid[:, None]
@@ -726,6 +734,31 @@ def test_neighbour_forms_with_periodic_images(tmp_path):
     u_lo = (rel & (d2[:50] <= lim2[:50]) & ~tie[:50]).sum()
     u_hi = (rel & ((d2[:50] <= lim2[:50]) | tie[:50])).sum()
     assert u_lo <= using <= u_hi
+    # coupling groups: the port's two coupling relations at the same state
+    # (the example hooks are the port's built-in ones), partners at their
+    # nearest image within the coupling radius
+    import ctypes as C
+    from oracle import port_api
+    pcfg = capi.config_struct(case.cfg)
+    port = port_api.lib()
+    pbuf = capi.ParticleBuffers(case.n, case.particles)
+    ph = C.c_void_p()
+    assert port.oracle_create(C.byref(pcfg), pbuf.ref(), C.byref(ph)) == 0, port.oracle_last_error()
+    try:
+        assert port.oracle_step(ph, 10) == 0
+        tot = []
+        for kind in (2, 3):
+            offs = (C.c_int64 * (n + 1))()
+            npairs = C.c_int64(0)
+            assert port.oracle_pairs(ph, kind, offs, None, 0, C.byref(npairs)) == 0
+            tot.append(npairs.value)
+        chk = capi.ParticleBuffers(case.n)
+        port.oracle_get(ph, chk.ref())
+    finally:
+        port.oracle_destroy(ph)
+    np.testing.assert_array_equal(chk["r"], r)  # the same state
+    assert (sd, ds) == (tot[0], tot[1]) and sd > 0 and ds > 0
+    assert sd_max < cfg["coupling_radius"]
 
 
 def test_case_with_mirror_ghosts_is_refused_at_start(tmp_path):
