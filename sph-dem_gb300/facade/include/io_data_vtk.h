@@ -36,6 +36,9 @@ class Cio_data_vtk {
     /* the reference's entry points (rank = globals->mpiRank) */
     void readRestart(int timestep, particleContainer *outPs, CglobalVars *globals);
     void writeRestart(int timestep, particleContainer &ps, CglobalVars *globals);
+    /* the output pieces <base>%07d in the restart layout above; the
+     * reference's visualisation output (io_data_vtk.cpp:413-720: Float32
+     * press, porosity, shepSum, fdrag, force parts, ...) is not written */
     void writeOutput(int timestep, particleContainer &ps, CglobalVars *globals);
 
     /* <filename>Globals<rank>.dat (CioGlobals, ioGlobals.cpp:4-139): one
