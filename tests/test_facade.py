@@ -954,3 +954,32 @@ def test_2d_fluid_case_through_the_facade_on_the_oracle(tmp_path):
     for k in ("r", "v", "vhat", "f", "dens", "h"):
         np.testing.assert_array_equal(a[k][:, :2] if a[k].ndim == 2 else a[k],
                                       out[k][:, :2] if out[k].ndim == 2 else out[k], err_msg=k)
+
+
+@pytest.mark.parametrize("macro,reason", [
+    ("LUBRICATION", "DEM contact law"),
+    ("SMOOTHED_VISC_VELOCITY", "velocity smoothing"),
+    ("LIQ_DEM_SEPARATE_DRAGS", "SPH-DEM coupling variant"),
+    ("LIQ_DEM_VARIABLE_TIMESTEP", "SPH-DEM coupling variant"),
+    ("FIXED_DEM", "FIXED_DEM / NO_DEM_CONTACTS"),
+    ("VAR_H_CORRECTION2", "SPH step variant"),
+    ("MORRIS_SPH_BOUNDARY", "viscosity or boundary variant"),
+])
+def test_constants_bridge_refuses_options_the_device_lacks(tmp_path, macro, reason):
+    """sphdem_case_config.h stops the build of a case that defines a step
+    option of the reference the device path does not implement."""
+    src = tmp_path / "probe.cpp"
+    src.write_text(f'#define {macro}\n#include "sphdem_case_config.h"\nint main() {{ return 0; }}\n')
+    res = subprocess.run(["g++", "-std=gnu++17", "-fsyntax-only",
+                          "-I" + os.path.join(FACADE, "example_sediment"), "-I" + os.path.join(FACADE, "include"),
+                          str(src)], capture_output=True, text=True)
+    assert res.returncode != 0 and reason in res.stderr, res.stderr[-1500:]
+
+
+def test_constants_bridge_accepts_the_example_case(tmp_path):
+    src = tmp_path / "probe.cpp"
+    src.write_text('#include "sphdem_case_config.h"\nint main() { return sphdem_case_unsupported() ? 1 : 0; }\n')
+    res = subprocess.run(["g++", "-std=gnu++17", "-fsyntax-only",
+                          "-I" + os.path.join(FACADE, "example_sediment"), "-I" + os.path.join(FACADE, "include"),
+                          str(src)], capture_output=True, text=True)
+    assert res.returncode == 0, res.stderr[-1500:]
