@@ -290,6 +290,9 @@ inline void CdataLL::pull() {
 }
 
 inline void CdataLL::push() {
+    /* buffers sized for the mirror first (it grows at insertions) */
+    SphDemParticles p;
+    soa(p);
     for (size_t i = 0; i < ps.size(); i++) {
         const Cparticle &q = ps[i];
         for (int d = 0; d < NDIM; d++) {
@@ -299,8 +302,6 @@ inline void CdataLL::push() {
         vd[i] = q.dens;
         vh[i] = q.h;
     }
-    SphDemParticles p;
-    soa(p);
     check(sphdem_set_fields(h, SPHDEM_FIELD_R | SPHDEM_FIELD_V | SPHDEM_FIELD_VHAT | SPHDEM_FIELD_F |
                                    SPHDEM_FIELD_DENS | SPHDEM_FIELD_H, &p),
           "sphdem_set_fields");
