@@ -544,6 +544,12 @@ int main(int argc, char **argv) {
     CglobalVars r;
     out.readGlobals(2, &r);
     std::printf("%d %.17g %.17g %d\n", r.sphStep, r.time, r.eKE, r.n);
+    if (argc > 3) {  /* a Globals file written elsewhere: its row 2 */
+        CglobalVars q;
+        Cio_data_vtk other(argv[3], &q);
+        other.readGlobals(2, &q);
+        std::printf("%d %.17g %.17g %d\n", q.sphStep, q.time, q.eKE, q.n);
+    }
     return 0;
 }
 """
@@ -565,10 +571,20 @@ def test_cpp_globals_and_domain_files_in_the_reference_layout(tmp_path):
     line = open(os.path.join(ref_dir, "initDataDomain.dat")).readline()
     (tmp_path / "initDomain0.dat").write_text(line)
     exe = _facade_tool(tmp_path, 2, "gd_tool", GD_TOOL)
-    res = subprocess.run([exe, str(tmp_path / "init"), str(tmp_path / "out")], capture_output=True, text=True,
-                         timeout=60)
+    # rows written by the Python writer, read back by the C++ reader
+    ov = {"lin_mom": [0.0, 0.0, 0.0], "ang_mom": 0.0, "e_ke": 0.0, "e_b_force": 0.0, "e_elast": 0.0,
+          "e_elast_exact": 0.0, "e_visc_f": 0.0, "e_visc_b": 0.0, "e_ff": 0.0, "e_total": 0.0, "max_v": 0.0,
+          "ave_dens": 0.0, "var_dens": 0.0, "ave_dens_from_mass": 0.0, "n": 0, "n_sph": 0, "max_f": 0.0,
+          "max_ff": 0.0, "rms_ff": 0.0, "ed_elast_dt": 0.0, "ed_visc_f_dt": 0.0, "ed_ff_dt": 0.0}
+    for k in (1, 2, 3):
+        io_vtk.append_globals(str(tmp_path / "pyGlobals0.dat"), k, 5 * k, 0.7 * k + 1e-14,
+                              dict(ov, e_ke=1.0 / 7.0 * k, n=200 + k))
+    res = subprocess.run([exe, str(tmp_path / "init"), str(tmp_path / "out"), str(tmp_path / "py")],
+                         capture_output=True, text=True, timeout=60)
     assert res.returncode == 0, res.stderr
-    dom, back = res.stdout.splitlines()
+    dom, back, py = res.stdout.splitlines()
+    step, time, eke, n = py.split()
+    assert (int(step), float(time), float(eke), int(n)) == (10, 1.4 + 1e-14, 2.0 / 7.0, 202)
     want = line.split()
     got = dom.split()
     assert int(got[0]) == int(want[0])
